@@ -1,0 +1,24 @@
+"""GB300-native finite-difference hot path of liaman/Geophysics.
+
+The compute lives in libgeofd.so (CUDA kernels for sm_103a behind a C ABI,
+include/geofd.h).  This package is the host-side mirror of the reference's
+entry points:
+
+  GPU_vti2dfd, CPU_vti2dfd, GPU_vti3dfd   file-based drop-ins (same arguments)
+  fd2d_shot, FD3DPlan, fd3d_shot          array-level forward modelling
+  rtm2d_batch                             batched 2D RTM (MPI-program semantics)
+  laplace2d, laplace3d                    adjoint Laplacian image filter
+  read_par                                `key= value` par files
+
+Arrays: numpy arrays are host buffers; torch CUDA tensors are device
+buffers and run on torch's current CUDA stream.
+"""
+from ._lib import (GEO_MEM_DEVICE, GEO_MEM_HOST, GEO_MODE_EXACT, GEO_MODE_FAST, GEO_VARIANT_CPU,
+                   GEO_VARIANT_GPU, GEO_VARIANT_MPI, GeoError, lib)
+from .api import (CPU_vti2dfd, FD3DPlan, GPU_vti2dfd, GPU_vti3dfd, fd2d_shot, fd3d_shot, laplace2d, laplace3d,
+                  launch_count, read_par, rtm2d_batch, version)
+
+__all__ = ["GPU_vti2dfd", "CPU_vti2dfd", "GPU_vti3dfd", "fd2d_shot", "FD3DPlan", "fd3d_shot", "rtm2d_batch",
+           "laplace2d", "laplace3d", "read_par", "launch_count", "version", "lib", "GeoError",
+           "GEO_MEM_HOST", "GEO_MEM_DEVICE", "GEO_VARIANT_CPU", "GEO_VARIANT_GPU", "GEO_VARIANT_MPI",
+           "GEO_MODE_EXACT", "GEO_MODE_FAST"]

@@ -1,0 +1,276 @@
+"""Array-level and file-level entry points over libgeofd.
+
+Inputs may be numpy arrays (host memory) or torch CUDA tensors (device
+memory, run on torch's current stream); outputs come back as the same kind.
+Array layouts are the reference's: 2D models (nx, nz), 3D models (ny, nx, nz),
+shot records (ntraces, nt).
+"""
+import ctypes as C
+
+import numpy as np
+
+from ._lib import (FD2DDesc, FD3DDesc, GEO_MEM_DEVICE, GEO_MEM_HOST, GEO_MODE_EXACT, GEO_MODE_FAST,
+                   GEO_VARIANT_CPU, GEO_VARIANT_GPU, GEO_VARIANT_MPI, RTM2DDesc, check, lib)
+
+_VARIANTS = {"cpu": GEO_VARIANT_CPU, "gpu": GEO_VARIANT_GPU, "mpi": GEO_VARIANT_MPI}
+_MODES = {"exact": GEO_MODE_EXACT, "fast": GEO_MODE_FAST}
+
+
+def _torch():
+    try:
+        import torch
+        return torch
+    except ImportError:  # pragma: no cover - torch is part of the image
+        return None
+
+
+def _is_dev(a):
+    t = _torch()
+    return t is not None and isinstance(a, t.Tensor) and a.is_cuda
+
+
+class _Bufs:
+    """Pointer marshalling for one call: all arrays host or all device."""
+
+    def __init__(self, *arrays):
+        devs = {_is_dev(a) for a in arrays if a is not None}
+        if len(devs) > 1:
+            raise ValueError("mix of host and device arrays")
+        self.dev = devs.pop() if devs else False
+        self.keep = []
+
+    @property
+    def mem(self):
+        return GEO_MEM_DEVICE if self.dev else GEO_MEM_HOST
+
+    def stream(self):
+        if not self.dev:
+            return None
+        return C.c_void_p(_torch().cuda.current_stream().cuda_stream)
+
+    def inp(self, a):
+        if a is None:
+            return None
+        if self.dev:
+            t = _torch()
+            a = a.to(t.float32).contiguous()
+            self.keep.append(a)
+            return C.c_void_p(a.data_ptr())
+        a = np.ascontiguousarray(a, dtype=np.float32)
+        self.keep.append(a)
+        return C.c_void_p(a.ctypes.data)
+
+    def out(self, shape, like=None):
+        if self.dev:
+            t = _torch()
+            o = t.empty(shape, dtype=t.float32, device=like.device if like is not None else "cuda")
+            return o, C.c_void_p(o.data_ptr())
+        o = np.empty(shape, np.float32)
+        return o, C.c_void_p(o.ctypes.data)
+
+
+def version():
+    return lib().geo_version().decode()
+
+
+def launch_count():
+    """Kernel launches issued by the library since it was loaded."""
+    return int(lib().geo_launch_count())
+
+
+def fd2d_shot(v, e, d, *, npd, nt, dx, dz, dt, favg, fs, zs, pfac=10.0, ds=0.0, is_=1, variant="cpu", sv=0,
+              wtype=1, rec_iz=None, rec_scale=None, mute_tt=0, snap_every=0):
+    """One 2D shot; returns the record (nx, nt) [and padded P snapshots].
+
+    variant: "cpu" (CPU_vti2dfd), "gpu" (GPU_vti2dfd) or "mpi" (the MPI
+    RTM program's forward modelling)."""
+    b = _Bufs(v, e, d)
+    nx, nz = v.shape
+    var = _VARIANTS[variant] if isinstance(variant, str) else int(variant)
+    desc = FD2DDesc(nx=nx, nz=nz, npd=npd, nt=nt, dx=dx, dz=dz, dt=dt, favg=favg, pfac=pfac, wtype=wtype,
+                    fs=fs, ds=ds, zs=zs, is_=is_, variant=var, sv=sv,
+                    rec_iz=npd if rec_iz is None else rec_iz,
+                    rec_scale=(2.0 if var == GEO_VARIANT_CPU else 1.0) if rec_scale is None else rec_scale,
+                    mute_tt=mute_tt)
+    pv, pe, pd = b.inp(v), b.inp(e), b.inp(d)
+    shot, ps = b.out((nx, nt), v)
+    snaps, psn = (None, None)
+    if snap_every:
+        snaps, psn = b.out(((nt - 1) // snap_every + 1, nx + 2 * npd, nz + 2 * npd), v)
+    check(lib().geo_fd2d_shot(C.byref(desc), pv, pe, pd, ps, psn, snap_every, b.mem, b.stream()), "geo_fd2d_shot")
+    return (shot, snaps) if snap_every else shot
+
+
+class FD3DPlan:
+    """Device state for repeated 3D shots on one grid (geo_fd3d_plan_*)."""
+
+    def __init__(self, *, nx, ny, nz, npd, nt, dx, dy, dz, dt, favg, fsx, fsy, fsz, pfac=10.0, wtype=1, sv=0,
+                 mode="fast", dsx=0, dsy=0, dsz=0, rec_iz=None, rx0=0, drx=1, nrx=None, ry0=0, dry=1, nry=None,
+                 mute_tt=0):
+        self.desc = FD3DDesc(nx=nx, ny=ny, nz=nz, npd=npd, nt=nt, dx=dx, dy=dy, dz=dz, dt=dt, favg=favg, pfac=pfac,
+                             wtype=wtype, sv=sv, mode=_MODES[mode] if isinstance(mode, str) else int(mode),
+                             fsx=fsx, fsy=fsy, fsz=fsz, dsx=dsx, dsy=dsy, dsz=dsz,
+                             rec_iz=npd if rec_iz is None else rec_iz, rx0=rx0, drx=drx,
+                             nrx=nx if nrx is None else nrx, ry0=ry0, dry=dry, nry=ny if nry is None else nry,
+                             mute_tt=mute_tt)
+        self._p = C.c_void_p()
+        check(lib().geo_fd3d_plan_create(C.byref(self._p), C.byref(self.desc)), "geo_fd3d_plan_create")
+        self.padded = (ny + 2 * npd, nx + 2 * npd, nz + 2 * npd)
+
+    def set_model(self, v, e, d):
+        b = _Bufs(v, e, d)
+        check(lib().geo_fd3d_set_model(self._p, b.inp(v), b.inp(e), b.inp(d), b.mem, b.stream()),
+              "geo_fd3d_set_model")
+
+    def run_shot(self, is_=0, device=None):
+        """Shot `is_` (0-based); returns (nry, nrx, nt), on the GPU if device."""
+        D = self.desc
+        shape = (D.nry, D.nrx, D.nt)
+        if device:
+            t = _torch()
+            out = t.empty(shape, dtype=t.float32, device=device)
+            check(lib().geo_fd3d_run_shot(self._p, is_, C.c_void_p(out.data_ptr()), GEO_MEM_DEVICE,
+                                          C.c_void_p(t.cuda.current_stream().cuda_stream)), "geo_fd3d_run_shot")
+            return out
+        out = np.empty(shape, np.float32)
+        check(lib().geo_fd3d_run_shot(self._p, is_, C.c_void_p(out.ctypes.data), GEO_MEM_HOST, None),
+              "geo_fd3d_run_shot")
+        return out
+
+    def time_steps(self, n, stream=None):
+        """Device time (ms) of n bare time steps on the current state."""
+        ms = C.c_float()
+        check(lib().geo_fd3d_time_steps(self._p, n, C.byref(ms), stream), "geo_fd3d_time_steps")
+        return ms.value
+
+    def fields(self):
+        P = np.empty(self.padded, np.float32)
+        Q = np.empty(self.padded, np.float32)
+        check(lib().geo_fd3d_get_fields(self._p, C.c_void_p(P.ctypes.data), C.c_void_p(Q.ctypes.data),
+                                        GEO_MEM_HOST, None), "geo_fd3d_get_fields")
+        return P, Q
+
+    def close(self):
+        if self._p:
+            lib().geo_fd3d_plan_destroy(self._p)
+            self._p = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def fd3d_shot(v, e, d, is_=0, **kw):
+    """One-call 3D shot (create plan, set model, run, destroy)."""
+    ny, nx, nz = v.shape
+    plan = FD3DPlan(nx=nx, ny=ny, nz=nz, **kw)
+    try:
+        plan.set_model(v, e, d)
+        return plan.run_shot(is_, device=v.device if _is_dev(v) else None)
+    finally:
+        plan.close()
+
+
+def rtm2d_batch(v, e, d, *, npd, nt, dx, dz, dt_ms, favg, pfac, zs, shot_x, shot_nxs, laplace=True,
+                per_shot=False, tile_x=0):
+    """Batched 2D RTM with the MPI program's semantics; returns the stacked
+    (Laplacian-filtered) image (nx, nz) [and the per-shot images]."""
+    b = _Bufs(v, e, d)
+    nx, nz = v.shape
+    ns = len(shot_x)
+    sx = (C.c_int * ns)(*[int(k) for k in shot_x])
+    sw = (C.c_int * ns)(*[int(k) for k in shot_nxs])
+    desc = RTM2DDesc(nx=nx, nz=nz, npd=npd, nt=nt, dx=dx, dz=dz, dt_ms=dt_ms, favg=favg, pfac=pfac, zs=zs, ns=ns,
+                     shot_x=sx, shot_nxs=sw, laplace=1 if laplace else 0, tile_z=0, tile_x=tile_x)
+    pv, pe, pd = b.inp(v), b.inp(e), b.inp(d)
+    img, pi = b.out((nx, nz), v)
+    shots = pshots = None
+    if per_shot:
+        shots, pshots = b.out((int(sum(int(w) for w in shot_nxs)) * nz,), v)
+    check(lib().geo_rtm2d_batch(C.byref(desc), pv, pe, pd, pi, pshots, b.mem, b.stream()), "geo_rtm2d_batch")
+    if per_shot:
+        out, o = [], 0
+        for w in shot_nxs:
+            out.append(shots[o:o + int(w) * nz].reshape(int(w), nz))
+            o += int(w) * nz
+        return img, out
+    return img
+
+
+def laplace2d(img):
+    """Adjoint first-difference Laplacian (laplac2_lop adj=1) of (nx, nz)."""
+    b = _Bufs(img)
+    nx, nz = img.shape
+    pi = b.inp(img)
+    out, po = b.out((nx, nz), img)
+    check(lib().geo_laplace2d(nx, nz, pi, po, b.mem, b.stream()), "geo_laplace2d")
+    return out
+
+
+def laplace3d(img):
+    """3D adjoint first-difference Laplacian of (ny, nx, nz)."""
+    b = _Bufs(img)
+    ny, nx, nz = img.shape
+    pi = b.inp(img)
+    out, po = b.out((ny, nx, nz), img)
+    check(lib().geo_laplace3d(nx, ny, nz, pi, po, b.mem, b.stream()), "geo_laplace3d")
+    return out
+
+
+def _s(x):
+    return x.encode() if isinstance(x, str) else x
+
+
+def GPU_vti2dfd(nx, nz, dx, dz, npd, SV, FNv, FNe, FNd, favg, ns, fs, ds, zs, FNshot, FNsnap, nt, dt, run_count=1):
+    """Drop-in for GPU_vti2dfd_kernels.cu:301 (files in, files out)."""
+    lib().GPU_vti2dfd(nx, nz, dx, dz, npd, SV, _s(FNv), _s(FNe), _s(FNd), favg, ns, fs, ds, zs, _s(FNshot),
+                      _s(FNsnap), nt, dt, run_count)
+
+
+def CPU_vti2dfd(nx, nz, dx, dz, npd, SV, FNv, FNe, FNd, favg, ns, fs, ds, zs, FNshot, FNsnap, nt, dt, run_count=1):
+    """Drop-in for CPU_vti2dfd_kernels.c:366 (CPU semantics, computed on the GPU)."""
+    lib().CPU_vti2dfd(nx, nz, dx, dz, npd, SV, _s(FNv), _s(FNe), _s(FNd), favg, ns, fs, ds, zs, _s(FNshot),
+                      _s(FNsnap), nt, dt, run_count)
+
+
+def GPU_vti3dfd(nx, ny, nz, dx, dy, dz, npml, SV, FNv, FNe, FNd, favg, ns, fsx, dsx, fsy, dsy, fsz, dsz, FNshot,
+                FNsnap, nt, dt, run_count=1):
+    """Drop-in for GPU_vti3dfd_kernels.cu:371."""
+    lib().GPU_vti3dfd(nx, ny, nz, dx, dy, dz, npml, SV, _s(FNv), _s(FNe), _s(FNd), favg, ns, fsx, dsx, fsy, dsy,
+                      fsz, dsz, _s(FNshot), _s(FNsnap), nt, dt, run_count)
+
+
+class Par:
+    """A `key= value` par file read by geo_par_load."""
+
+    def __init__(self, path):
+        self._p = C.c_void_p()
+        check(lib().geo_par_load(_s(path), C.byref(self._p)), "geo_par_load")
+
+    def int(self, key):
+        x = C.c_int()
+        check(lib().geo_par_get_int(self._p, _s(key), C.byref(x)), "geo_par_get_int")
+        return x.value
+
+    def float(self, key):
+        x = C.c_float()
+        check(lib().geo_par_get_float(self._p, _s(key), C.byref(x)), "geo_par_get_float")
+        return x.value
+
+    def str(self, key):
+        buf = C.create_string_buffer(1024)
+        check(lib().geo_par_get_string(self._p, _s(key), buf, 1024), "geo_par_get_string")
+        return buf.value.decode()
+
+    def __del__(self):
+        try:
+            if self._p:
+                lib().geo_par_free(self._p)
+        except Exception:
+            pass
+
+
+def read_par(path):
+    return Par(path)

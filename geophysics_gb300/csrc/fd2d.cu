@@ -1,0 +1,267 @@
+// 2D VTI staggered-grid kernels, batched over shots.
+//
+// One launch updates every shot of a batch: the grid is persistent (a
+// multiple of the SM count) and walks the list of (shot, tile) work items,
+// so uneven aperture windows share one launch.  A tile is 32 z-points (one
+// warp, z contiguous in memory) by `blockDim.y` x-columns.
+//
+// Arithmetic keeps the reference's operation order exactly (the library is
+// compiled with contraction off), so results are bit-identical to the
+// reference CPU code and to the oracle:
+//   velocity  CPU_vti2dfd_kernels.c:79-106 / GPU_vti2dfd_kernels.cu:209-238
+//   stress    CPU_vti2dfd_kernels.c:108-177 / GPU_vti2dfd_kernels.cu:240-299
+//             MPI program Toa_rtm_vti_adcig_cdp.c:1227-1327 (rho*vp^2 form,
+//             pz/qx chains in double after pow(1+2del, 0.5))
+#include "geo_internal.h"
+
+namespace geo {
+
+__constant__ float c_fd[4] = {1.196289f, -0.0797526f, 0.009570313f, -0.0006975447f};
+// exp(-x^2-z^2) on the 7x7 source window, x,z in [-3,3] (ptsource,
+// CPU_vti2dfd_kernels.c:72); filled from the host's exp() at load.
+__constant__ double c_gauss[49];
+
+static bool g_gauss_ready = false;
+static int ensure_gauss() {
+    if (g_gauss_ready) return GEO_OK;
+    double g[49];
+    for (int x = -3; x <= 3; x++)
+        for (int z = -3; z <= 3; z++) g[(x + 3) * 7 + (z + 3)] = std::exp((double)(-z * z - x * x));
+    GEO_CUDA(cudaMemcpyToSymbol(c_gauss, g, sizeof g));
+    g_gauss_ready = true;
+    return GEO_OK;
+}
+
+struct Tile2D {
+    const Shot2D *sh;
+    int ix, iz;
+};
+
+__device__ __forceinline__ bool locate(const Shot2D *shots, const int *item_shot, int item, Tile2D &t) {
+    const int s = item_shot[item];
+    const Shot2D *sh = shots + s;
+    const int tile = item - sh->tile_base;
+    const int tz = tile % sh->ntz, tx = tile / sh->ntz;
+    t.sh = sh;
+    t.iz = tz * 32 + threadIdx.x;
+    t.ix = tx * blockDim.y + threadIdx.y;
+    return t.ix >= 4 && t.ix < sh->nnx - 4 && t.iz >= 4 && t.iz < sh->nnz - 4;
+}
+
+// P/Q read for the velocity update.  The GPU-form source (P,Q += amp at one
+// cell before the velocity update, GPU_vti2dfd_kernels.cu:423) is applied on
+// the fly to the taps that touch the source cell.
+template <bool PT_SRC>
+__device__ __forceinline__ float tap(const float *a, long idx, long src, float amp) {
+    float v = a[idx];
+    if (PT_SRC && idx == src) v = v + amp;
+    return v;
+}
+
+template <int VARIANT>
+__global__ void __launch_bounds__(256) k_vel2d(const Shot2D *__restrict__ shots, const int *__restrict__ item_shot,
+                                               int nitems, Step2D st) {
+    for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
+        Tile2D t;
+        if (!locate(shots, item_shot, item, t)) continue;
+        const Shot2D &sh = *t.sh;
+        const int nnz = sh.nnz;
+        const long id = (long)t.ix * nnz + t.iz;
+        const bool pt_src = VARIANT == V_GPU && st.src_on;
+        const long src = (long)sh.ixs * nnz + sh.izs;
+        const bool near = pt_src && ((t.iz == sh.izs && abs(t.ix - sh.ixs) <= 4) || (t.ix == sh.ixs && abs(t.iz - sh.izs) <= 4));
+        for (int f = 0; f < st.nf; f++) {
+            const float *P = sh.P[f], *Q = sh.Q[f];
+            float xx = 0.0f, zz = 0.0f;
+            if (near) {
+#pragma unroll
+                for (int im = 0; im < 4; im++) {
+                    xx += c_fd[im] * (tap<true>(P, id + (im + 1) * nnz, src, st.amp) - tap<true>(P, id - im * nnz, src, st.amp));
+                    zz += c_fd[im] * (tap<true>(Q, id + im + 1, src, st.amp) - tap<true>(Q, id - im, src, st.amp));
+                }
+            } else {
+#pragma unroll
+                for (int im = 0; im < 4; im++) {
+                    xx += c_fd[im] * (__ldg(P + id + (im + 1) * nnz) - __ldg(P + id - im * nnz));
+                    zz += c_fd[im] * (__ldg(Q + id + im + 1) - __ldg(Q + id - im));
+                }
+            }
+            float *u = sh.u[f], *w = sh.w[f];
+            // u1 = coffx2*u0 - coffx1*dtx*xx (the MPI copy's extra *rho is *1.0f)
+            u[id] = sh.cx2[t.ix] * u[id] - sh.cx1[t.ix] * sh.dtx * xx;
+            w[id] = sh.cz2[t.iz] * w[id] - sh.cz1[t.iz] * sh.dtz * zz;
+        }
+    }
+}
+
+template <int VARIANT, int PHASE>
+__global__ void __launch_bounds__(256) k_stress2d(const Shot2D *__restrict__ shots, const int *__restrict__ item_shot,
+                                                  int nitems, Step2D st) {
+    for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
+        Tile2D t;
+        if (!locate(shots, item_shot, item, t)) continue;
+        const Shot2D &sh = *t.sh;
+        const int nnz = sh.nnz, ix = t.ix, iz = t.iz;
+        const long id = (long)ix * nnz + iz;
+        const float vp = __ldg(sh.vp + id);
+        float e2 = __ldg(sh.e2 + id), d2 = 0.0f;
+        double pw = 0.0;
+        if (VARIANT == V_MPI) pw = __ldg(sh.pw + id);
+        else d2 = __ldg(sh.d2 + id);
+        if (st.taper) {
+            const int bx = ix - sh.tx0, bz = iz - sh.tz0;
+            if (bx >= 0 && bx < kTB && bz >= 0 && bz < kTB) {
+                e2 = sh.te2[bx * kTB + bz];
+                if (VARIANT == V_MPI) pw = sh.tpw[bx * kTB + bz];
+                else d2 = sh.td2[bx * kTB + bz];
+            }
+        }
+        const float ax1 = sh.ax1[ix], ax2 = sh.ax2[ix], az1 = sh.az1[iz], az2 = sh.az2[iz];
+        // Gaussian source window value (CPU/MPI forward), added after the split sum.
+        float s = 0.0f;
+        if ((VARIANT == V_CPU || VARIANT == V_MPI) && PHASE == PH_FWD && st.src_on) {
+            const int rx = ix - sh.ixs, rz = iz - sh.izs;
+            if (rx >= -3 && rx <= 3 && rz >= -3 && rz <= 3)
+                s = (float)((double)st.amp * c_gauss[(rx + 3) * 7 + (rz + 3)]);
+        }
+        float Pn[2], Qn[2];
+        for (int f = 0; f < st.nf; f++) {
+            const float *u = sh.u[f], *w = sh.w[f];
+            float xx = 0.0f, zz = 0.0f;
+#pragma unroll
+            for (int im = 0; im < 4; im++) {
+                xx += c_fd[im] * (__ldg(u + id + im * nnz) - __ldg(u + id - (im + 1) * nnz));
+                zz += c_fd[im] * (__ldg(w + id + im) - __ldg(w + id - im - 1));
+            }
+            float px = sh.px[f][id], pz = sh.pz[f][id], qx = sh.qx[f][id], qz = sh.qz[f][id];
+            if (VARIANT == V_MPI) {
+                px = ax2 * px - ax1 * vp * e2 * sh.dtx * xx;
+                pz = (float)((double)(az2 * pz) - (double)(az1 * vp) * pw * (double)sh.dtz * (double)zz);
+                qx = (float)((double)(ax2 * qx) - (double)(ax1 * vp) * pw * (double)sh.dtx * (double)xx);
+                qz = az2 * qz - az1 * vp * sh.dtz * zz;
+            } else {
+                px = ax2 * px - ax1 * vp * vp * e2 * sh.dtx * xx;
+                pz = az2 * pz - az1 * vp * vp * d2 * sh.dtz * zz;
+                qx = ax2 * qx - ax1 * vp * vp * d2 * sh.dtx * xx;
+                qz = az2 * qz - az1 * vp * vp * sh.dtz * zz;
+            }
+            sh.px[f][id] = px; sh.pz[f][id] = pz; sh.qx[f][id] = qx; sh.qz[f][id] = qz;
+            float P, Q;
+            if ((VARIANT == V_CPU || VARIANT == V_MPI) && PHASE == PH_FWD) {
+                P = px + pz + s;
+                Q = qx + qz + s;
+            } else {
+                P = px + pz;
+                Q = qx + qz;
+            }
+            sh.P[f][id] = P;
+            sh.Q[f][id] = Q;
+            Pn[f] = P; Qn[f] = Q;
+        }
+        const int gx = ix - sh.npd, gz = iz - sh.npd;
+        if (PHASE == PH_FWD) {
+            // receiver gather at rec_iz, time-major
+            if (iz == sh.rec_iz && gx >= 0 && gx < sh.nx) {
+                const float r = sh.rec_scale == 2.0f ? Pn[0] + Pn[0] : Pn[0] * sh.rec_scale;
+                sh.rec_p[(long)st.it * sh.nx + gx] = r;
+                if (sh.rec_q) sh.rec_q[(long)st.it * sh.nx + gx] = Qn[0];
+            }
+            // interior-edge lines for the boundary-driven reconstruction
+            // (Toa_rtm_vti_adcig_cdp.c:668-683): top, bottom, left, right
+            if (sh.edge_p && gx >= 0 && gx < sh.nx && gz >= 0 && gz < sh.nz) {
+                const long L = 2L * sh.nx + 2L * sh.nz, b = (long)st.it * L;
+                if (gz == 0) { sh.edge_p[b + gx] = Pn[0]; sh.edge_q[b + gx] = Qn[0]; }
+                if (gz == sh.nz - 1) { sh.edge_p[b + sh.nx + gx] = Pn[0]; sh.edge_q[b + sh.nx + gx] = Qn[0]; }
+                if (gx == 0) { sh.edge_p[b + 2 * sh.nx + gz] = Pn[0]; sh.edge_q[b + 2 * sh.nx + gz] = Qn[0]; }
+                if (gx == sh.nx - 1) { sh.edge_p[b + 2 * sh.nx + sh.nz + gz] = Pn[0]; sh.edge_q[b + 2 * sh.nx + sh.nz + gz] = Qn[0]; }
+            }
+        } else if (st.nf == 2 && gx >= 0 && gx < sh.nx && gz >= 0 && gz < sh.nz) {
+            // zero-lag cross-correlation image and source illumination
+            // (Toa_rtm_vti_adcig_cdp.c:1067-1076): the illumination sum is
+            // formed in double, as pow() returns it, and a zero becomes 1
+            const long o = (long)gx * sh.nz + gz;
+            const float sv = Pn[0];
+            float ill = (float)((double)sh.ill[o] + (double)sv * (double)sv);
+            if (ill == 0.0f) ill = 1.0f;
+            sh.ill[o] = ill;
+            sh.mig[o] = sh.mig[o] + Pn[1] * sv;
+        }
+    }
+}
+
+// Boundary-driven reconstruction and receiver injection before step it of
+// the backward pass (Toa_rtm_vti_adcig_cdp.c:914-927 and 953-957): the saved
+// interior-edge lines go into the source-side P,Q (corners end with the
+// left/right values, as the reference's loop order leaves them) and the
+// muted surface records into the receiver-side P,Q at the surface row.
+__global__ void k_inject2d(const Shot2D *__restrict__ shots, int maxline, int it) {
+    const Shot2D &sh = shots[blockIdx.y];
+    const int nx = sh.nx, nz = sh.nz, npd = sh.npd, nnz = sh.nnz;
+    const long L = 2L * nx + 2L * nz;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < L; k += gridDim.x * blockDim.x) {
+        int ix, iz;
+        if (k < nx) { ix = npd + k; iz = npd; if (k == 0 || k == nx - 1) goto rec; }
+        else if (k < 2 * nx) { ix = npd + k - nx; iz = npd + nz - 1; if (k - nx == 0 || k - nx == nx - 1) goto rec; }
+        else if (k < 2 * nx + nz) { ix = npd; iz = npd + k - 2 * nx; }
+        else { ix = npd + nx - 1; iz = npd + k - 2 * nx - nz; }
+        {
+            const long id = (long)ix * nnz + iz;
+            sh.P[0][id] = sh.edge_p[(long)it * L + k];
+            sh.Q[0][id] = sh.edge_q[(long)it * L + k];
+        }
+    rec:
+        if (k < nx) {
+            const long id = (long)(npd + k) * nnz + npd;
+            sh.P[1][id] = sh.rec_p[(long)it * nx + k];
+            sh.Q[1][id] = sh.rec_q[(long)it * nx + k];
+        }
+    }
+    (void)maxline;
+}
+
+template <int V>
+static void vel_dispatch(const Shot2D *d_shots, const int *d_item_shot, int nitems, dim3 grid, dim3 block,
+                         Step2D st, cudaStream_t s) {
+    k_vel2d<V><<<grid, block, 0, s>>>(d_shots, d_item_shot, nitems, st);
+}
+
+int launch_vel2d(int variant, const Shot2D *d_shots, const int *d_item_shot, int nitems, int by, int grid,
+                 Step2D st, cudaStream_t s) {
+    dim3 block(32, by), g(grid);
+    switch (variant) {
+        case V_CPU: vel_dispatch<V_CPU>(d_shots, d_item_shot, nitems, g, block, st, s); break;
+        case V_GPU: vel_dispatch<V_GPU>(d_shots, d_item_shot, nitems, g, block, st, s); break;
+        default: vel_dispatch<V_MPI>(d_shots, d_item_shot, nitems, g, block, st, s); break;
+    }
+    return check_launch("vel2d");
+}
+
+int launch_stress2d(int variant, int phase, const Shot2D *d_shots, const int *d_item_shot, int nitems, int by,
+                    int grid, Step2D st, cudaStream_t s) {
+    GEO_TRY(ensure_gauss());
+    dim3 block(32, by), g(grid);
+#define GEO_STRESS(V, PH) k_stress2d<V, PH><<<g, block, 0, s>>>(d_shots, d_item_shot, nitems, st)
+    if (phase == PH_FWD) {
+        switch (variant) {
+            case V_CPU: GEO_STRESS(V_CPU, PH_FWD); break;
+            case V_GPU: GEO_STRESS(V_GPU, PH_FWD); break;
+            default: GEO_STRESS(V_MPI, PH_FWD); break;
+        }
+    } else {
+        switch (variant) {
+            case V_CPU: GEO_STRESS(V_CPU, PH_BWD); break;
+            case V_GPU: GEO_STRESS(V_GPU, PH_BWD); break;
+            default: GEO_STRESS(V_MPI, PH_BWD); break;
+        }
+    }
+#undef GEO_STRESS
+    return check_launch("stress2d");
+}
+
+int launch_inject2d(const Shot2D *d_shots, int nshots, int maxline, int it, cudaStream_t s) {
+    dim3 g((maxline + 255) / 256, nshots);
+    k_inject2d<<<g, 256, 0, s>>>(d_shots, maxline, it);
+    return check_launch("inject2d");
+}
+
+}  // namespace geo

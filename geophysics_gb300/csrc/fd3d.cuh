@@ -1,0 +1,36 @@
+// Device-side views of a 3D grid, shared by the 3D kernels.
+#pragma once
+#include <cuda_runtime.h>
+
+struct geo_fd3d_plan;
+
+namespace geo {
+
+struct Grid3D {
+    int nnx, nny, nnz, ldz;     // padded extents; ldz = z stride (== nnz)
+    long sxy;                   // y stride
+    int npd, nx, ny, nz;        // sponge width and interior extents
+    float dtx, dty, dtz;        // dt/dx etc. (float division, as the reference)
+    const float *cx1, *cx2, *ax1, *ax2, *cy1, *cy2, *ay1, *ay2, *cz1, *cz2, *az1, *az2;
+    const float *vp, *e2, *d2;  // vp, 1+2eps, sqrtf(1+2del)
+    float *u, *v, *w, *P, *Q;
+    float *px, *py, *pz, *qx, *qy, *qz;
+};
+
+struct StepArgs3D {
+    int it;
+    int src_on;
+    float amp;
+    int ixs, iys, izs;
+    long src;                   // linear source index (or -1)
+    float *rec;                 // time-major record (nt x nrx*nry) or null
+    int rec_iz, rx0, drx, nrx, ry0, dry, nry;
+};
+
+Grid3D make_grid(const geo_fd3d_plan *p);
+int run_shot_3d(geo_fd3d_plan *p, int is, cudaStream_t s, int (*on_step)(void *, int), void *ctx);
+const float *plan3d_P(const geo_fd3d_plan *p);
+int fetch_shot_3d(geo_fd3d_plan *p, float *shot, int mem, cudaStream_t s);
+int plan3d_dims(const geo_fd3d_plan *p, int *nnx, int *nny, int *nnz);
+
+}  // namespace geo

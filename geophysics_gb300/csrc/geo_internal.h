@@ -1,0 +1,135 @@
+// Internal declarations of libgeofd: host-side setup helpers, device
+// descriptors and kernel launchers shared by the translation units.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdio>
+#include <cstdint>
+#include <vector>
+#include <string>
+#include "../../include/geofd.h"
+
+namespace geo {
+
+// ------------------------------------------------------------ error plumbing
+extern thread_local char g_last_error[256];
+int fail(int code, const char *fmt, ...);
+
+#define GEO_CUDA(call)                                                            \
+    do {                                                                          \
+        cudaError_t e_ = (call);                                                  \
+        if (e_ != cudaSuccess)                                                    \
+            return ::geo::fail(GEO_ERR_CUDA, "%s:%d %s: %s", __FILE__, __LINE__,  \
+                               #call, cudaGetErrorString(e_));                    \
+    } while (0)
+#define GEO_TRY(expr)                  \
+    do {                               \
+        int s_ = (expr);               \
+        if (s_ != GEO_OK) return s_;   \
+    } while (0)
+
+void count_launch(long long n = 1);
+long long launches_so_far();
+int check_launch(const char *what);
+
+// RAII device buffer (cudaMalloc/cudaFree).
+struct DevBuf {
+    void *p = nullptr;
+    size_t bytes = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf &) = delete;
+    DevBuf &operator=(const DevBuf &) = delete;
+    ~DevBuf() { release(); }
+    int alloc(size_t n);
+    int zero(cudaStream_t s);
+    void release();
+    template <class T> T *as() const { return static_cast<T *>(p); }
+};
+
+// ------------------------------------------------------------ host setup
+// Reference program whose arithmetic a run follows.
+enum Variant { V_CPU = GEO_VARIANT_CPU, V_GPU = GEO_VARIANT_GPU, V_MPI = GEO_VARIANT_MPI };
+
+// pi as each reference program spells it.
+constexpr double kPiGui = 3.141592653;      // CPU_vti2dfd_kernels.c:27, GPU_vti*_kernels.cu:31
+constexpr double kPiMpi = 3.1415926535898;  // Toa_rtm_vti_adcig_cdp.c:39
+
+// Edge-replicate an nx*nz model into its padded (nx+2npd)*(nz+2npd) form.
+void pad_model_2d(int nx, int nz, int npd, const float *in, float *out);
+// Same for 3D, reference layout iz + nz*(ix + nx*iy).
+void pad_model_3d(int nx, int ny, int nz, int npd, const float *in, float *out);
+
+float sponge_d0(Variant v, int dims, float vpmax, float vcenter, int npd, float dx, float dy, float dz);
+// coff1/coff2 on half cells (velocities), acoff1/acoff2 on integer cells
+// (stresses); arrays of n+2npd.
+void sponge_profiles(Variant v, int n, int npd, float dt, float d0, float *coff1, float *coff2,
+                     float *acoff1, float *acoff2);
+// pfac*w(t_it) per step and whether the source is still on.
+void source_amplitudes(Variant v, int nt, float dt, float favg, float pfac, int wtype,
+                       std::vector<float> &amp, std::vector<uint8_t> &on);
+// Tapered (eps, del) near the source for the SV-suppression circle.
+struct Taper2D {
+    int x0 = 0, z0 = 0, n = 0;            // box origin (padded) and size
+    std::vector<float> e, d;              // tapered values on the box
+};
+void sv_taper_2d(Variant v, int nnx, int nnz, int npd, int ixs_center, int izs_center,
+                 const float *e_pad, const float *d_pad, Taper2D &out);
+
+// Per-trace direct-wave mute window [lo, hi) of samples to zero.
+void mute_window_gpu2d(int nx, int nt, float dt, float favg, float dx, float dz, int fs, int ds,
+                       int zs, int is, float mu_v, int tt, std::vector<int> &lo, std::vector<int> &hi);
+void mute_window_mpi(int nx, int nt, float dt_ms, float favg, float dx, float dz, int fs, int ds,
+                     int zs, int is, float mu_v, int tt, std::vector<int> &lo, std::vector<int> &hi);
+void mute_window_3d(int nx, int ny, int nt, float dt, float favg, float dx, float dy, float dz,
+                    int fsx, int fsy, int dsx, int dsy, int fsz, int is, float vp1, float eps1, int tt,
+                    std::vector<int> &hi);
+
+// Model sanity: finite, velocity > 0.
+int check_model(const float *v, const float *e, const float *d, size_t n);
+
+// ------------------------------------------------------------ 2D device side
+constexpr int kTB = 31;  // taper box edge (circle radius 15)
+
+// Per-shot descriptor read by the batched 2D kernels (device memory).
+struct Shot2D {
+    int nnx, nnz, npd, nx, nz;
+    float dtx, dtz;
+    const float *cx1, *cx2, *cz1, *cz2, *ax1, *ax2, *az1, *az2;
+    const float *vp, *e2, *d2;      // vp (or rho*vp^2), 1+2eps, sqrtf(1+2del)
+    const double *pw;               // pow(1+2del, 0.5) (MPI form)
+    int tx0, tz0;                   // taper box origin; te2/td2/tpw on kTB*kTB
+    const float *te2, *td2;
+    const double *tpw;
+    int ixs, izs;                   // source cell (padded)
+    float *u[2], *w[2], *P[2], *Q[2], *px[2], *pz[2], *qx[2], *qz[2];
+    int rec_iz;                     // receiver row
+    float rec_scale;
+    float *rec_p, *rec_q;           // time-major records nt x nx
+    float *edge_p, *edge_q;         // time-major edge lines nt x (2nx+2nz)
+    float *mig, *ill;               // image and source illumination nx*nz
+    int tile_base, ntz;             // first work item, tiles along z
+};
+
+struct Step2D {
+    int it;
+    float amp;        // pfac*w(t) this step (0 when off)
+    int src_on;       // source active this step
+    int taper;        // use the taper box for eps/del
+    int nf;           // fields updated (1: s only, 2: s and g)
+};
+
+enum Phase2D { PH_FWD = 0, PH_BWD = 1 };
+
+int launch_vel2d(int variant, const Shot2D *d_shots, const int *d_item_shot, int nitems, int by,
+                 int grid, Step2D st, cudaStream_t s);
+int launch_stress2d(int variant, int phase, const Shot2D *d_shots, const int *d_item_shot, int nitems,
+                    int by, int grid, Step2D st, cudaStream_t s);
+int launch_inject2d(const Shot2D *d_shots, int nshots, int maxline, int it, cudaStream_t s);
+int launch_mute_records(float *rec, int nx, int nt, const int *lo, const int *hi, cudaStream_t s);
+int launch_transpose_records(const float *tm, float *out, int ntr, int nt, cudaStream_t s);
+int launch_normalize_image(float *mig, const float *ill, size_t n, cudaStream_t s);
+int launch_stack_image(float *full, int nz, const float *const *imgs, const int *offsets,
+                       const int *widths, int nshots, int nx, cudaStream_t s);
+int launch_laplace2d(int nx, int nz, const float *in, float *out, cudaStream_t s);
+int launch_laplace3d(int nx, int ny, int nz, const float *in, float *out, cudaStream_t s);
+
+}  // namespace geo

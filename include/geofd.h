@@ -1,0 +1,193 @@
+/*
+ * geofd.h -- C ABI of the GB300 finite-difference library (libgeofd.so).
+ *
+ * Everything here is plain C: ints, floats, pointers and sizes.  Arrays use
+ * the reference's layouts:
+ *   2D model / image   a[ix*nz + iz]                  (x-major, z fastest)
+ *   3D model / image   a[iz + nz*(ix + nx*iy)]        (z fastest)
+ *   shot records       shot[it + nt*trace]            (trace-major)
+ *   3D traces          trace = irx + nrx*iry
+ * Units follow the reference's drop-in entry points where noted (dx in m,
+ * dt in microseconds, favg in Hz); the geo_* descriptors take SI floats.
+ *
+ * Memory: every geo_* call that takes a `mem` argument reads its inputs from
+ * and writes its outputs to host memory (GEO_MEM_HOST) or device memory of
+ * the current CUDA device (GEO_MEM_DEVICE).  Work buffers are allocated by the
+ * library unless stated otherwise.  `stream` is a cudaStream_t (NULL = the
+ * legacy default stream); calls are synchronous with respect to the host.
+ */
+#ifndef GEOFD_H
+#define GEOFD_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define GEO_OK            0
+#define GEO_ERR_ARG       1   /* bad size, position or flag                   */
+#define GEO_ERR_CUDA      2   /* a CUDA runtime call failed                   */
+#define GEO_ERR_IO        3   /* a file could not be opened/read/written      */
+#define GEO_ERR_MODEL     4   /* NaN/Inf or non-positive velocity in a model  */
+#define GEO_ERR_CFL       5   /* stability check failed                       */
+#define GEO_ERR_WINDOW    6   /* RTM aperture window leaves the model         */
+#define GEO_ERR_NOMEM     7   /* device allocation failed                     */
+#define GEO_ERR_NAN       8   /* wavefield watchdog saw NaN/Inf               */
+
+#define GEO_MEM_HOST   0
+#define GEO_MEM_DEVICE 1
+
+/* Semantic variants: which reference program the arithmetic follows.     */
+#define GEO_VARIANT_CPU    0  /* CPU_vti2dfd (GUI CPU, 7x7 Gaussian source
+                                 after the stress update, acoff2 from coff1,
+                                 2*P receivers)                              */
+#define GEO_VARIANT_GPU    1  /* GPU_vti2dfd / GPU_vti3dfd (point source
+                                 before the velocity update)                 */
+#define GEO_VARIANT_MPI    2  /* the MPI CPU RTM program (rho*vp^2 form,
+                                 t = it*dt, SV taper always on)              */
+
+/* 3D stress formulation */
+#define GEO_MODE_EXACT 0      /* split sponge fields everywhere (bit-exact
+                                 with the reference's arithmetic)            */
+#define GEO_MODE_FAST  1      /* P,Q unsplit inside the physical box         */
+
+const char *geo_version(void);
+const char *geo_strerror(int status);
+/* Number of kernel launches the library issued since load (all kinds). */
+long long geo_launch_count(void);
+
+/* ======================================================================
+ * Drop-in entry points: identical signatures and file formats to the
+ * reference's C ABI.  They return void like the originals and report a
+ * failure on stderr (the originals printf and exit(0)).
+ * ====================================================================== */
+
+/* 2D VTI FD with the GUI GPU program's semantics.
+ * Replaces GPU_vti2dfd, 2D-3D-vti-fd-cuda-gtk-GUI/GPU_vti2dfd_kernels.cu:301-304. */
+void GPU_vti2dfd(int nx, int nz, int dx, int dz, int npd, int SV,
+                 const char FNv[], const char FNe[], const char FNd[],
+                 int favg, int ns, int fs, int ds, int zs,
+                 const char FNshot[], const char FNsnap[], int nt, int dt, int run_count);
+
+/* 2D VTI FD with the GUI CPU program's semantics, computed on the GPU.
+ * Replaces CPU_vti2dfd, 2D-3D-vti-fd-cuda-gtk-GUI/CPU_vti2dfd_kernels.c:366-367. */
+void CPU_vti2dfd(int nx, int nz, int dx, int dz, int npd, int SV,
+                 const char FNv[], const char FNe[], const char FNd[],
+                 int favg, int ns, int fs, int ds, int zs,
+                 const char FNshot[], const char FNsnap[], int nt, int dt, int run_count);
+
+/* 3D VTI FD with the GUI GPU program's semantics.
+ * Replaces GPU_vti3dfd, 2D-3D-vti-fd-cuda-gtk-GUI/GPU_vti3dfd_kernels.cu:371-374. */
+void GPU_vti3dfd(int nx, int ny, int nz, int dx, int dy, int dz, int npml, int SV,
+                 const char FNv[], const char FNe[], const char FNd[],
+                 int favg, int ns, int fsx, int dsx, int fsy, int dsy, int fsz, int dsz,
+                 const char FNshot[], const char FNsnap[], int nt, int dt, int run_count);
+
+/* ======================================================================
+ * Status-returning API
+ * ====================================================================== */
+
+/* 2D forward modelling of one shot.  Mirrors the reference's per-shot loop
+ * (CPU_vti2dfd_kernels.c:465-510, GPU_vti2dfd_kernels.cu:404-444): zero the
+ * state, nt steps of source + velocity + stress + receiver gather. */
+typedef struct geo_fd2d_desc {
+    int   nx, nz, npd, nt;
+    float dx, dz, dt;        /* m, m, s                                      */
+    float favg, pfac;        /* Hz, source gain                              */
+    int   wtype;             /* 1 Ricker, 2/3 Gaussian derivatives           */
+    float fs, ds, zs;        /* source x (1-based), shot step, source z      */
+    int   is;                /* shot number, 1-based                         */
+    int   variant;           /* GEO_VARIANT_*                                */
+    int   sv;                /* SV-suppression taper around the source       */
+    int   rec_iz;            /* receiver row, padded index (npd = surface)   */
+    float rec_scale;         /* 1, or 2 for CPU_vti2dfd's P+P record         */
+    int   mute_tt;           /* >0: apply the GPU-form direct-wave mute      */
+} geo_fd2d_desc;
+
+/* v,e,d: nx*nz model; shot: nt*nx record.  snap (optional, may be NULL):
+ * receives the padded P every snap_every steps ((nt-1)/snap_every+1 frames
+ * of (nx+2npd)*(nz+2npd)). */
+int geo_fd2d_shot(const geo_fd2d_desc *desc, const float *v, const float *e, const float *d,
+                  float *shot, float *snap, int snap_every, int mem, void *stream);
+
+/* 3D forward modelling of one shot (GPU_vti3dfd semantics).
+ * Replaces the per-shot body of GPU_vti3dfd_kernels.cu:113-160. */
+typedef struct geo_fd3d_desc {
+    int   nx, ny, nz, npd, nt;
+    float dx, dy, dz, dt;
+    float favg, pfac;
+    int   wtype, sv, mode;   /* mode: GEO_MODE_EXACT / GEO_MODE_FAST         */
+    int   fsx, fsy, fsz, dsx, dsy, dsz;   /* source, 1-based grid cells      */
+    int   rec_iz;            /* receiver depth, padded index                 */
+    int   rx0, drx, nrx;     /* receiver x: npd+rx0+irx*drx                  */
+    int   ry0, dry, nry;     /* receiver y: npd+ry0+iry*dry                  */
+    int   mute_tt;           /* >0: mute_directwave3d with this tt           */
+} geo_fd3d_desc;
+
+typedef struct geo_fd3d_plan geo_fd3d_plan;
+
+/* A plan owns the device state of one 3D grid (model, wavefields, sponge
+ * profiles, record buffer) so repeated shots reuse it. */
+int geo_fd3d_plan_create(geo_fd3d_plan **plan, const geo_fd3d_desc *desc);
+int geo_fd3d_plan_destroy(geo_fd3d_plan *plan);
+/* v,e,d: nx*ny*nz model in the reference layout. */
+int geo_fd3d_set_model(geo_fd3d_plan *plan, const float *v, const float *e, const float *d,
+                       int mem, void *stream);
+/* Shot number `is` (0-based, as the reference's loop): shot is nt*nrx*nry. */
+int geo_fd3d_run_shot(geo_fd3d_plan *plan, int is, float *shot, int mem, void *stream);
+/* Runs nsteps bare time steps (no source or receivers) on the current
+ * state and returns their device time in ms -- used to time the stencil. */
+int geo_fd3d_time_steps(geo_fd3d_plan *plan, int nsteps, float *ms, void *stream);
+/* Copies the padded P (and Q) of the current state out. */
+int geo_fd3d_get_fields(geo_fd3d_plan *plan, float *P, float *Q, int mem, void *stream);
+/* One-call convenience: create, set model, run, destroy. */
+int geo_fd3d_shot(const geo_fd3d_desc *desc, int is, const float *v, const float *e, const float *d,
+                  float *shot, int mem, void *stream);
+
+/* 2D RTM with the MPI CPU program's semantics on per-shot aperture windows
+ * (2D-vti-fd+rtm-mpi/Toa_rtm_vti_adcig_cdp.c:295-392 with
+ * model_vti_get_boundry :483 and RTM_corr_adcig :739).  All shots run
+ * together: each time step is one persistent launch over every shot's
+ * tiles, and the time loop is replayed from a CUDA graph.  The stacked image
+ * is formed in shot order and optionally passed through the adjoint
+ * Laplacian (laplac2_lop adj=1). */
+typedef struct geo_rtm2d_desc {
+    int   nx, nz, npd, nt;   /* full model                                   */
+    float dx, dz, dt_ms;     /* dt in milliseconds, as that program takes it */
+    float favg, pfac;
+    int   zs;                /* source depth (1-based, zs_sxd)               */
+    int   ns;                /* number of shots                              */
+    const int *shot_x;       /* ns source x positions k (1-based), host      */
+    const int *shot_nxs;     /* ns odd window widths, host                   */
+    int   laplace;           /* apply the adjoint Laplacian to the stack     */
+    int   tile_z, tile_x;    /* 0 = autotuned                                */
+} geo_rtm2d_desc;
+
+/* v,e,d: nx*nz; image: nx*nz stacked (Laplacian-filtered if asked).
+ * per_shot (optional): ns images concatenated, shot s of size nxs_s*nz. */
+int geo_rtm2d_batch(const geo_rtm2d_desc *desc, const float *v, const float *e, const float *d,
+                    float *image, float *per_shot, int mem, void *stream);
+
+/* Adjoint first-difference Laplacian (laplac2_lop adj=1,
+ * utils-Laplacian-filter/laplace.c:9-53; the in-program copy
+ * Toa_gpu2DvtiFdRtmAdcigsLaplace.cu:150-202 clears `out` first, as this does). */
+int geo_laplace2d(int nx, int nz, const float *in, float *out, int mem, void *stream);
+/* 3D form (laplace_3d_filter, 3D-vti-fd+rtm-cuda/
+ * Toa_gpu_3dvti_rtm_adcigs_1orderfunction.cu:555-616). */
+int geo_laplace3d(int nx, int ny, int nz, const float *in, float *out, int mem, void *stream);
+
+/* ---- par file -------------------------------------------------------- */
+/* `key= value` lines (the reference's .par format, e.g.
+ * 2D-ISO-tomography-inversion-c-0.0/tomo-1.par) with the reference's
+ * parameter names.  geo_par_get* look a key up after geo_par_load. */
+typedef struct geo_par geo_par;
+int geo_par_load(const char *path, geo_par **par);
+int geo_par_get_int(const geo_par *par, const char *key, int *out);
+int geo_par_get_float(const geo_par *par, const char *key, float *out);
+int geo_par_get_string(const geo_par *par, const char *key, char *out, int cap);
+void geo_par_free(geo_par *par);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GEOFD_H */

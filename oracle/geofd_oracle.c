@@ -1,0 +1,811 @@
+/*
+ * geofd_oracle.c -- CPU restatement of the reference's FP32 staggered-grid
+ * VTI finite-difference hot path.  TEST INFRASTRUCTURE ONLY: it is the
+ * checker for the CUDA library (tests/, __graft_entry__.smoke() and the CPU
+ * baseline leg of bench.py load it); the product never links or calls it.
+ *
+ * Compiled twice by oracle/Makefile:
+ *   liborc32.so  REAL=float   -- follows the reference's FP32 arithmetic op
+ *                               by op (same operand order, no contraction,
+ *                               the same double-precision intermediates), so
+ *                               a GPU kernel that keeps the order is
+ *                               bit-exact against it;
+ *   liborc64.so  REAL=double  -- the same algorithm in FP64, used to state
+ *                               every FP32 result's error against FP64.
+ *
+ * Parity pinning: the FP32 build is checked against the reference's own CPU
+ * code compiled unmodified from the reference tree (oracle/_ref, see
+ * oracle/Makefile and tests/test_oracle_pin.py):
+ *   - 2D FD, CPU variant  == CPU_vti2dfd        (2D-3D-vti-fd-cuda-gtk-GUI/CPU_vti2dfd_kernels.c:366)
+ *   - 2D RTM, MPI variant == model_vti_get_boundry + RTM_corr_adcig
+ *                            (2D-vti-fd+rtm-mpi/Toa_rtm_vti_adcig_cdp.c:483,739)
+ *   - Laplacian          == laplac2_lop(adj=1) (utils-Laplacian-filter/laplace.c:9)
+ * The 3D VTI and 2D TTI paths have no CPU code in the reference; they follow
+ * the reference's CUDA kernels (2D-3D-vti-fd-cuda-gtk-GUI/GPU_vti3dfd_kernels.cu:53-201,
+ * 2D-tti-fd+rtm-cuda/Toa_gpu_2dtti_fd_1orderfunction.cu:81-183) and are
+ * "parity unpinned" against the reference itself.
+ *
+ * Layouts follow the reference: 2D id = ix*nnz + iz, 3D id = iz + nnz*(ix + nnx*iy)
+ * (z fastest); shot records are trace-major, shot[it + nt*trace].
+ */
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+#ifndef REAL
+#define REAL float
+#endif
+
+#if defined(ORC_FP64)
+#define RSQRT(x) sqrt(x)
+#else
+#define RSQRT(x) sqrtf(x)
+#endif
+
+/* variant codes (which reference program's semantics) */
+#define ORC_V_CPU    0   /* CPU_vti2dfd            (GUI CPU, C)          */
+#define ORC_V_GPU    1   /* GPU_vti2dfd/GPU_vti3dfd (GUI GPU, CUDA)       */
+#define ORC_V_MPI    2   /* Toa_rtm_vti_adcig_cdp.c (MPI CPU RTM)         */
+#define ORC_V_GPURTM 3   /* Toa_gpu2DvtiFdRtmAdcigsLaplace.cu (GPU RTM)   */
+
+/* pi literals differ between reference programs */
+#define PI_GUI 3.141592653        /* CPU_vti2dfd_kernels.c:27, GPU_vti2dfd_kernels.cu:31 */
+#define PI_MPI 3.1415926535898    /* Toa_rtm_vti_adcig_cdp.c:39 */
+
+static const float C8[4] = {1.196289f, -0.0797526f, 0.009570313f, -0.0006975447f};
+/* The 8th-order staggered coefficients (CPU_vti2dfd_kernels.c:334-343). */
+
+/* ---------------------------------------------------------------- setup */
+
+/* Edge replication into the sponge (CPU_vti2dfd_kernels.c:221-246; the
+ * 3D form GPU_vti3dfd_kernels.cu:208-255).  `a` is the padded array. */
+void orc_pad2d(int nx, int nz, int npd, REAL *a)
+{
+    int nnx = nx + 2 * npd, nnz = nz + 2 * npd, ix, iz;
+    for (ix = 0; ix < nnx; ix++)
+        for (iz = 0; iz < nnz; iz++) {
+            if (ix < npd) a[ix * nnz + iz] = a[npd * nnz + iz];
+            else if (ix >= nnx - npd) a[ix * nnz + iz] = a[(nnx - npd - 1) * nnz + iz];
+        }
+    for (ix = 0; ix < nnx; ix++)
+        for (iz = 0; iz < nnz; iz++) {
+            if (iz < npd) a[ix * nnz + iz] = a[ix * nnz + npd];
+            else if (iz >= nnz - npd) a[ix * nnz + iz] = a[ix * nnz + nnz - npd - 1];
+        }
+}
+
+void orc_pad3d(int nx, int ny, int nz, int npd, REAL *a)
+{
+    long nnx = nx + 2 * npd, nny = ny + 2 * npd, nnz = nz + 2 * npd, ix, iy, iz;
+    for (iy = 0; iy < nny; iy++) for (ix = 0; ix < nnx; ix++) for (iz = 0; iz < nnz; iz++) {
+        long id = iz + ix * nnz + iy * nnz * nnx;
+        if (ix < npd) a[id] = a[iz + npd * nnz + iy * nnz * nnx];
+        else if (ix >= nnx - npd) a[id] = a[iz + (nnx - npd - 1) * nnz + iy * nnz * nnx];
+    }
+    for (iy = 0; iy < nny; iy++) for (ix = 0; ix < nnx; ix++) for (iz = 0; iz < nnz; iz++) {
+        long id = iz + ix * nnz + iy * nnz * nnx;
+        if (iy < npd) a[id] = a[iz + ix * nnz + npd * nnz * nnx];
+        else if (iy >= nny - npd) a[id] = a[iz + ix * nnz + (nny - npd - 1) * nnz * nnx];
+    }
+    for (iy = 0; iy < nny; iy++) for (ix = 0; ix < nnx; ix++) for (iz = 0; iz < nnz; iz++) {
+        long id = iz + ix * nnz + iy * nnz * nnx;
+        if (iz < npd) a[id] = a[npd + ix * nnz + iy * nnz * nnx];
+        else if (iz >= nnz - npd) a[id] = a[nnz - npd - 1 + ix * nnz + iy * nnz * nnx];
+    }
+}
+
+/* Sponge damping constant d0.
+ *  CPU/MPI: 3*vpmax*ln(1e5)/(2*npd*dx)            CPU_vti2dfd_kernels.c:192, Toa_rtm_vti_adcig_cdp.c:1346
+ *  GPU 2D : 10*vp[nnx*nnz/2]*ln(1e5)/(2*npd*(dx+dz)/2)   GPU_vti2dfd_kernels.cu:105
+ *  GPU 3D : 10*vp[n/2]*ln(1e5)/(2*npd*(dx+dy+dz)/3)      GPU_vti3dfd_kernels.cu:205
+ * `vpmax` is the interior maximum (the CPU loop's scan over the padded
+ * array sees only replicated edge values outside the interior). */
+float orc_d0(int variant, int dims, float vpmax, float vcenter, int npd, float dx, float dy, float dz)
+{
+    if (variant == ORC_V_CPU || variant == ORC_V_MPI)
+        return (float)(3.0 * vpmax * log(100000.0) / (2.0 * npd * dx));
+    if (dims == 2)
+        return (float)(10.0 * vcenter * log(100000.0) / (2.0 * npd * ((dx + dz) / 2.0)));
+    return (float)(10.0 * vcenter * log(100000.0) / (2.0 * npd * ((dx + dy + dz) / 3.0)));
+}
+
+/* 1D sponge profiles along one axis with n interior cells (nn = n + 2*npd).
+ *  CPU  : CPU_vti2dfd_kernels.c:271-332 (acoff2 is built from coff1, and the
+ *         far side uses (1+i-n-npd)/npd)
+ *  MPI  : Toa_rtm_vti_adcig_cdp.c:1455-1525 (acoff2 from acoff1)
+ *  GPU  : GPU_vti2dfd_kernels.cu:108-139 (far side (i-n-npd)/npd) */
+void orc_sponge(int variant, int n, int npd, float dt, float d0,
+                float *coff1, float *coff2, float *acoff1, float *acoff2)
+{
+    int i, nn = n + 2 * npd;
+    for (i = 0; i < nn; i++) { coff1[i] = coff2[i] = acoff1[i] = acoff2[i] = 1.0f; }
+    if (variant == ORC_V_GPU || variant == ORC_V_GPURTM) {
+        for (i = 0; i < nn; i++) {
+            if (i < npd) {
+                coff1[i] = (float)(1.0 / (1.0 + (dt * d0 * pow((npd - 0.5 - i) / npd, 2.0)) / 2.0));
+                coff2[i] = (float)(coff1[i] * (1.0 - (dt * d0 * pow((npd - 0.5 - i) / npd, 2.0)) / 2.0));
+                acoff1[i] = (float)(1.0 / (1.0 + (dt * d0 * pow(((npd - i) * 1.0) / npd, 2.0)) / 2.0));
+                acoff2[i] = (float)(acoff1[i] * (1.0 - (dt * d0 * pow(((npd - i) * 1.0) / npd, 2.0)) / 2.0));
+            } else if (i >= npd + n) {
+                coff1[i] = (float)(1.0 / (1.0 + (dt * d0 * pow((0.5 + i - n - npd) / npd, 2.0)) / 2.0));
+                coff2[i] = (float)(coff1[i] * (1.0 - (dt * d0 * pow((0.5 + i - n - npd) / npd, 2.0)) / 2.0));
+                acoff1[i] = (float)(1.0 / (1.0 + (dt * d0 * pow(((i - n - npd) * 1.0) / npd, 2.0)) / 2.0));
+                acoff2[i] = (float)(acoff1[i] * (1.0 - (dt * d0 * pow(((i - n - npd) * 1.0) / npd, 2.0)) / 2.0));
+            }
+        }
+        return;
+    }
+    /* CPU and MPI: identical except where acoff2 takes its leading factor */
+    for (i = 0; i < npd; i++) {
+        coff1[i] = 1 / (1 + (dt * d0 * pow((npd - 0.5 - i) / npd, 2)) / 2);
+        coff2[i] = coff1[i] * (1 - (dt * d0 * pow((npd - 0.5 - i) / npd, 2)) / 2);
+    }
+    for (i = npd + n; i < n + 2 * npd; i++) {
+        coff1[i] = 1 / (1 + (dt * d0 * pow((0.5 + i - n - npd) / npd, 2)) / 2);
+        coff2[i] = coff1[i] * (1 - (dt * d0 * pow((0.5 + i - n - npd) / npd, 2)) / 2);
+    }
+    for (i = 0; i < npd; i++) {
+        acoff1[i] = 1 / (1 + (dt * d0 * pow(((npd - i) * 1.0) / npd, 2)) / 2);
+        acoff2[i] = (variant == ORC_V_CPU ? coff1[i] : acoff1[i]) * (1 - (dt * d0 * pow(((npd - i) * 1.0) / npd, 2)) / 2);
+    }
+    for (i = npd + n; i < n + 2 * npd; i++) {
+        acoff1[i] = 1 / (1 + (dt * d0 * pow(((1 + i - n - npd) * 1.0) / npd, 2)) / 2);
+        acoff2[i] = (variant == ORC_V_CPU ? coff1[i] : acoff1[i]) * (1 - (dt * d0 * pow(((1 + i - n - npd) * 1.0) / npd, 2)) / 2);
+    }
+}
+
+/* Wavelet (CPU_vti2dfd_kernels.c:30-48 get_wavelet; same formula inlined in
+ * add_source2d GPU_vti2dfd_kernels.cu:176-207).  Returns the float the
+ * reference stores: the expression is evaluated in double. */
+static float orc_wavelet(float ts, float favg, int wtype, double pi_)
+{
+    float x, xx, source = 0.0f;
+    if (wtype == 1) { x = favg * ts; xx = x * x; source = (float)((1 - 2 * pi_ * pi_ * (xx)) * exp(-(pi_ * pi_ * xx))); }
+    else if (wtype == 2) { double y = (-4) * favg * favg * pi_ * pi_ / log(0.1); source = (float)((-2) * pi_ * pi_ * ts * exp(-y * ts * ts)); }
+    else if (wtype == 3) { double y = (-1) * favg * favg * pi_ * pi_ / log(0.1); source = (float)exp(-y * ts * ts); }
+    return source;
+}
+
+/* Per-step source amplitude pfac*w(t) (0 once t > 2/favg), with the
+ * reference's float time accumulation: t starts at dt (CPU/GPU variants,
+ * CPU_vti2dfd_kernels.c:478) or at 0 (MPI, Toa_rtm_vti_adcig_cdp.c:654) and
+ * advances by repeated float addition.  amp[it] is what the GPU variant adds
+ * at one cell; the CPU/MPI variants multiply it by exp(-x^2-z^2) on a 7x7
+ * window (ptsource CPU_vti2dfd_kernels.c:50-76). */
+void orc_source_amp(int variant, int nt, float dt, float favg, float pfac, int wtype, float *amp, unsigned char *active)
+{
+    double pi_ = (variant == ORC_V_MPI) ? PI_MPI : PI_GUI;
+    float t = (variant == ORC_V_MPI) ? 0.0f : dt, tdelay = (float)(1.0 / favg), ts;
+    int it;
+    for (it = 0; it < nt; it++, t += dt) {
+        ts = t - tdelay;
+        active[it] = (t <= 2 * tdelay);
+        amp[it] = active[it] ? pfac * orc_wavelet(ts, favg, wtype, pi_) : 0.0f;
+    }
+}
+
+/* SV-suppression taper: returns the tapered epsilon/delta near the source.
+ *  CPU: CPU_vti2dfd_kernels.c:136-156 (CR=15, inner CR*CR/16, centre at the
+ *       source cell ixs,izs, double cos/pow)
+ *  MPI: Toa_rtm_vti_adcig_cdp.c:1258-1274 (same form, its own pi, always on)
+ *  GPU: GPU_vti2dfd_kernels.cu:260-278 (R=15,r=4; centre (fs+(is-1)ds+npd,
+ *       zs+npd); sqrtf of the radius), GPU RTM R=18,r=7
+ *       (Toa_gpu2DvtiFdRtmAdcigsLaplace.cu:342-382).
+ * The taper is applied in place to padded e,d (2D). */
+void orc_sv_taper2d(int variant, int nnx, int nnz, int npd, float fs, float ds, float zs, int is,
+                    const float *e_in, const float *d_in, float *e_out, float *d_out)
+{
+    int ix, iz;
+    if (variant == ORC_V_CPU || variant == ORC_V_MPI) {
+        double pi_ = (variant == ORC_V_MPI) ? PI_MPI : PI_GUI;
+        float f = fs + (is - 1) * ds;
+        int ixs = (int)(f + 0.5) + npd - 1, izs = (int)(zs + 0.5) + npd - 1, CR = 15;
+        for (ix = 0; ix < nnx; ix++) for (iz = 0; iz < nnz; iz++) {
+            int id = ix * nnz + iz, rx = ix - ixs, rz = iz - izs;
+            if ((rx * rx + rz * rz) <= CR * CR) {
+                if ((rx * rx + rz * rz) <= (CR * CR / 16)) { e_out[id] = 0.0f; d_out[id] = 0.0f; }
+                else {
+                    double g = 0.5 * (1 - cos(pi_ * ((pow((rx * rx + rz * rz), 0.5) - CR / 4.0) * 4.0 / (CR * 3.0 - 1))));
+                    e_out[id] = (float)(g * e_in[id]);
+                    d_out[id] = (float)(g * d_in[id]);
+                }
+            } else { e_out[id] = e_in[id]; d_out[id] = d_in[id]; }
+        }
+    } else {
+        int R = (variant == ORC_V_GPURTM) ? 18 : 15, r = (variant == ORC_V_GPURTM) ? 7 : 4;
+        int cx = (int)fs + (is - 1) * (int)ds + npd, cz = (int)zs + npd;
+        for (ix = 0; ix < nnx; ix++) for (iz = 0; iz < nnz; iz++) {
+            int id = ix * nnz + iz, rx = ix - cx, rz = iz - cz;
+            if ((rx * rx + rz * rz) <= R * R) {
+                if ((rx * rx + rz * rz) <= r * r) { e_out[id] = 0.0f; d_out[id] = 0.0f; }
+                else {
+                    double g = 0.5 * (1 - cos(PI_GUI * ((sqrtf((float)(rx * rx + rz * rz)) - r) * 4.0 / (R * 3.0 - 1))));
+                    e_out[id] = (float)(g * e_in[id]);
+                    d_out[id] = (float)(g * d_in[id]);
+                }
+            } else { e_out[id] = e_in[id]; d_out[id] = d_in[id]; }
+        }
+    }
+}
+
+/* ------------------------------------------------------------- 2D state */
+
+typedef struct {
+    int nnx, nnz, npd, variant;
+    REAL dtx, dtz;
+    const float *cx1, *cx2, *cz1, *cz2, *ax1, *ax2, *az1, *az2;
+    const REAL *vp;     /* vp (CPU/GPU) or rho*vp^2 (MPI) */
+    const REAL *e2;     /* 1+2*eps after the SV taper */
+    const REAL *d2;     /* sqrtf(1+2*del) (CPU/GPU) */
+    const double *pw;   /* pow(1+2*del,0.5) in double (MPI) */
+} orc_st2d;
+
+/* Velocity update (CPU_vti2dfd_kernels.c:79-106; the MPI copy
+ * Toa_rtm_vti_adcig_cdp.c:1200-1225 multiplies by rho == 1). */
+static void vel2d(const orc_st2d *s, REAL *u, REAL *w, const REAL *P, const REAL *Q)
+{
+    int ix, iz, im, nnz = s->nnz;
+    for (ix = 4; ix < s->nnx - 4; ix++)
+        for (iz = 4; iz < nnz - 4; iz++) {
+            int id = ix * nnz + iz;
+            REAL xx = 0, zz = 0;
+            for (im = 0; im < 4; im++) {
+                xx += (REAL)C8[im] * (P[id + (im + 1) * nnz] - P[id - im * nnz]);
+                zz += (REAL)C8[im] * (Q[id + im + 1] - Q[id - im]);
+            }
+            if (s->variant == ORC_V_MPI) {
+                u[id] = s->cx2[ix] * u[id] - s->cx1[ix] * s->dtx * (REAL)1.0 * xx;
+                w[id] = s->cz2[iz] * w[id] - s->cz1[iz] * s->dtz * (REAL)1.0 * zz;
+            } else {
+                u[id] = s->cx2[ix] * u[id] - s->cx1[ix] * s->dtx * xx;
+                w[id] = s->cz2[iz] * w[id] - s->cz1[iz] * s->dtz * zz;
+            }
+        }
+}
+
+/* Stress update with split sponge fields (CPU_vti2dfd_kernels.c:108-177,
+ * GPU_vti2dfd_kernels.cu:240-299, MPI Toa_rtm_vti_adcig_cdp.c:1227-1327).
+ * src (may be NULL) is added into P and Q after the split sum (CPU/MPI). */
+static void stress2d(const orc_st2d *s, const REAL *u, const REAL *w, REAL *P, REAL *Q,
+                     REAL *px, REAL *pz, REAL *qx, REAL *qz, const REAL *src)
+{
+    int ix, iz, im, nnz = s->nnz;
+    for (ix = 4; ix < s->nnx - 4; ix++)
+        for (iz = 4; iz < nnz - 4; iz++) {
+            int id = ix * nnz + iz;
+            REAL xx = 0, zz = 0, vp = s->vp[id];
+            for (im = 0; im < 4; im++) {
+                xx += (REAL)C8[im] * (u[id + im * nnz] - u[id - (im + 1) * nnz]);
+                zz += (REAL)C8[im] * (w[id + im] - w[id - im - 1]);
+            }
+            if (s->variant == ORC_V_MPI) {
+                /* the pow() factor turns the pz/qx chains into double */
+                px[id] = s->ax2[ix] * px[id] - s->ax1[ix] * vp * s->e2[id] * s->dtx * xx;
+                pz[id] = (REAL)(s->az2[iz] * pz[id] - s->az1[iz] * vp * s->pw[id] * s->dtz * zz);
+                qx[id] = (REAL)(s->ax2[ix] * qx[id] - s->ax1[ix] * vp * s->pw[id] * s->dtx * xx);
+                qz[id] = s->az2[iz] * qz[id] - s->az1[iz] * vp * s->dtz * zz;
+            } else {
+                px[id] = s->ax2[ix] * px[id] - s->ax1[ix] * vp * vp * s->e2[id] * s->dtx * xx;
+                pz[id] = s->az2[iz] * pz[id] - s->az1[iz] * vp * vp * s->d2[id] * s->dtz * zz;
+                qx[id] = s->ax2[ix] * qx[id] - s->ax1[ix] * vp * vp * s->d2[id] * s->dtx * xx;
+                qz[id] = s->az2[iz] * qz[id] - s->az1[iz] * vp * vp * s->dtz * zz;
+            }
+            if (src) { P[id] = px[id] + pz[id] + src[id]; Q[id] = qx[id] + qz[id] + src[id]; }
+            else     { P[id] = px[id] + pz[id];           Q[id] = qx[id] + qz[id]; }
+        }
+}
+
+/* Fill the 7x7 Gaussian source window (ptsource, CPU_vti2dfd_kernels.c:50-76;
+ * Toa_rtm_vti_adcig_cdp.c:1141-1174): s = (pfac*w) * exp(-x^2-z^2). */
+static void gauss_src2d(int nnz, int ixs, int izs, float amp, int active, REAL *s, int nnx)
+{
+    int i, j;
+    memset(s, 0, sizeof(REAL) * (size_t)nnx * nnz);
+    if (!active) return;
+    for (j = izs - 3; j <= izs + 3; j++)
+        for (i = ixs - 3; i <= ixs + 3; i++) {
+            int x = i - ixs, z = j - izs;
+            s[i * nnz + j] = (REAL)(amp * exp(-z * z - x * x));
+        }
+}
+
+typedef struct {
+    int nx, nz, npd, nt, variant, sv, wtype;
+    float dx, dz, dt, favg, pfac, fs, ds, zs;
+    int is;          /* shot number, 1-based as in the reference loops */
+    int rec_iz;      /* receiver row (padded z index) */
+    float rec_scale; /* 2 for CPU_vti2dfd's P+P record */
+} orc_fd2d_desc;
+
+/* Allocated working set for one 2D propagation. */
+typedef struct {
+    orc_st2d st;
+    REAL *u, *w, *P, *Q, *px, *pz, *qx, *qz, *s, *vp, *e2, *d2; double *pw;
+    float *cx1, *cx2, *cz1, *cz2, *ax1, *ax2, *az1, *az2;
+    float *amp; unsigned char *active;
+    int ixs, izs;
+} orc_prop2d;
+
+static void prop2d_free(orc_prop2d *p)
+{
+    free(p->u); free(p->w); free(p->P); free(p->Q); free(p->px); free(p->pz); free(p->qx); free(p->qz);
+    free(p->s); free(p->vp); free(p->e2); free(p->d2); free(p->pw);
+    free(p->cx1); free(p->cx2); free(p->cz1); free(p->cz2); free(p->ax1); free(p->ax2); free(p->az1); free(p->az2);
+    free(p->amp); free(p->active);
+}
+
+static void prop2d_zero_state(orc_prop2d *p)
+{
+    size_t n = (size_t)p->st.nnx * p->st.nnz * sizeof(REAL);
+    memset(p->u, 0, n); memset(p->w, 0, n); memset(p->P, 0, n); memset(p->Q, 0, n);
+    memset(p->px, 0, n); memset(p->pz, 0, n); memset(p->qx, 0, n); memset(p->qz, 0, n);
+}
+
+/* Build the propagator from an unpadded (nx x nz, x-major) model.  `taper`
+ * selects whether the SV taper is applied (the MPI backward passes use the
+ * untapered model, inv_update_stress Toa_rtm_vti_adcig_cdp.c:1293-1327). */
+static void prop2d_init(orc_prop2d *p, const orc_fd2d_desc *d, const float *v, const float *e,
+                        const float *dl, int taper)
+{
+    int nx = d->nx, nz = d->nz, npd = d->npd, nnx = nx + 2 * npd, nnz = nz + 2 * npd, ix, iz;
+    size_t n = (size_t)nnx * nnz;
+    float *vv = calloc(n, 4), *ee = calloc(n, 4), *dd = calloc(n, 4), *e1 = calloc(n, 4), *d1 = calloc(n, 4);
+    float vpmax, d0, dtf = d->dt;
+    memset(p, 0, sizeof(*p));
+    for (ix = 0; ix < nx; ix++) for (iz = 0; iz < nz; iz++) {
+        size_t id = (size_t)(ix + npd) * nnz + iz + npd;
+        vv[id] = v[ix * nz + iz]; ee[id] = e[ix * nz + iz]; dd[id] = dl[ix * nz + iz];
+    }
+    /* pad in float (the pad is a pure copy) */
+    {
+        REAL *tmp = malloc(n * sizeof(REAL)); size_t k;
+        float *arrs[3] = {ee, dd, vv};
+        int a;
+        for (a = 0; a < 3; a++) {
+            for (k = 0; k < n; k++) tmp[k] = arrs[a][k];
+            orc_pad2d(nx, nz, npd, tmp);
+            for (k = 0; k < n; k++) arrs[a][k] = (float)tmp[k];
+        }
+        free(tmp);
+    }
+    vpmax = vv[npd * nnz + npd];
+    for (ix = npd; ix < npd + nx; ix++) for (iz = npd; iz < npd + nz; iz++)
+        if (vpmax < vv[ix * nnz + iz]) vpmax = vv[ix * nnz + iz];
+    d0 = orc_d0(d->variant, 2, vpmax, vv[nnx * nnz / 2], npd, d->dx, d->dx, d->dz);
+
+    p->cx1 = malloc(nnx * 4); p->cx2 = malloc(nnx * 4); p->ax1 = malloc(nnx * 4); p->ax2 = malloc(nnx * 4);
+    p->cz1 = malloc(nnz * 4); p->cz2 = malloc(nnz * 4); p->az1 = malloc(nnz * 4); p->az2 = malloc(nnz * 4);
+    orc_sponge(d->variant, nx, npd, dtf, d0, p->cx1, p->cx2, p->ax1, p->ax2);
+    orc_sponge(d->variant, nz, npd, dtf, d0, p->cz1, p->cz2, p->az1, p->az2);
+
+    if (taper) orc_sv_taper2d(d->variant, nnx, nnz, npd, d->fs, d->ds, d->zs, d->is, ee, dd, e1, d1);
+    else { memcpy(e1, ee, n * 4); memcpy(d1, dd, n * 4); }
+
+    p->vp = malloc(n * sizeof(REAL)); p->e2 = malloc(n * sizeof(REAL)); p->d2 = malloc(n * sizeof(REAL));
+    p->pw = malloc(n * sizeof(double));
+    for (size_t k = 0; k < n; k++) {
+        if (d->variant == ORC_V_MPI) p->vp[k] = (REAL)1 * ((REAL)vv[k] * (REAL)vv[k]);  /* rho*vp^2, rho==1 */
+        else p->vp[k] = vv[k];
+        p->e2[k] = (REAL)1 + (REAL)2 * (REAL)e1[k];
+        p->d2[k] = RSQRT((REAL)1 + (REAL)2 * (REAL)d1[k]);
+        p->pw[k] = pow((1 + 2 * d1[k]), 0.5);
+    }
+    p->u = calloc(n, sizeof(REAL)); p->w = calloc(n, sizeof(REAL)); p->P = calloc(n, sizeof(REAL)); p->Q = calloc(n, sizeof(REAL));
+    p->px = calloc(n, sizeof(REAL)); p->pz = calloc(n, sizeof(REAL)); p->qx = calloc(n, sizeof(REAL)); p->qz = calloc(n, sizeof(REAL));
+    p->s = calloc(n, sizeof(REAL));
+    p->amp = malloc(d->nt * 4); p->active = malloc(d->nt);
+    orc_source_amp(d->variant, d->nt, dtf, d->favg, d->pfac, d->wtype, p->amp, p->active);
+    {
+        float f = d->fs + (d->is - 1) * d->ds;
+        p->ixs = (int)(f + 0.5) + npd - 1;
+        p->izs = (int)(d->zs + 0.5) + npd - 1;
+    }
+    p->st.nnx = nnx; p->st.nnz = nnz; p->st.npd = npd; p->st.variant = d->variant;
+    p->st.dtx = (REAL)(dtf / d->dx); p->st.dtz = (REAL)(dtf / d->dz);
+    p->st.cx1 = p->cx1; p->st.cx2 = p->cx2; p->st.cz1 = p->cz1; p->st.cz2 = p->cz2;
+    p->st.ax1 = p->ax1; p->st.ax2 = p->ax2; p->st.az1 = p->az1; p->st.az2 = p->az2;
+    p->st.vp = p->vp; p->st.e2 = p->e2; p->st.d2 = p->d2; p->st.pw = p->pw;
+    free(vv); free(ee); free(dd); free(e1); free(d1);
+}
+
+/* One forward time step it of the chosen variant.  CPU/MPI: Gaussian source
+ * enters after the stress update (CPU_vti2dfd_kernels.c:483-486).  GPU:
+ * point source added to P,Q before the velocity update
+ * (GPU_vti2dfd_kernels.cu:423-427). */
+static void prop2d_step(orc_prop2d *p, int it)
+{
+    if (p->st.variant == ORC_V_CPU || p->st.variant == ORC_V_MPI) {
+        gauss_src2d(p->st.nnz, p->ixs, p->izs, p->amp[it], p->active[it], p->s, p->st.nnx);
+        vel2d(&p->st, p->u, p->w, p->P, p->Q);
+        stress2d(&p->st, p->u, p->w, p->P, p->Q, p->px, p->pz, p->qx, p->qz, p->s);
+    } else {
+        if (p->active[it]) {
+            size_t id = (size_t)p->ixs * p->st.nnz + p->izs;
+            p->P[id] += (REAL)p->amp[it];
+            p->Q[id] += (REAL)p->amp[it];
+        }
+        vel2d(&p->st, p->u, p->w, p->P, p->Q);
+        stress2d(&p->st, p->u, p->w, p->P, p->Q, p->px, p->pz, p->qx, p->qz, NULL);
+    }
+}
+
+/* 2D forward modelling of one shot.  shot (nt*nx, trace-major) receives
+ * rec_scale*P at row rec_iz; snap (optional) receives the padded P every
+ * `snap_every` steps (CPU_vti2dfd_kernels.c:488-506).  Returns 0. */
+int orc_fd2d(const orc_fd2d_desc *d, const float *v, const float *e, const float *dl,
+             float *shot, float *snap, int snap_every)
+{
+    orc_prop2d p;
+    int it, ix, nnz = d->nz + 2 * d->npd;
+    size_t n = (size_t)(d->nx + 2 * d->npd) * nnz;
+    prop2d_init(&p, d, v, e, dl, d->variant == ORC_V_MPI ? 1 : d->sv);
+    for (it = 0; it < d->nt; it++) {
+        prop2d_step(&p, it);
+        for (ix = 0; ix < d->nx; ix++) {
+            REAL val = p.P[(size_t)(ix + d->npd) * nnz + d->rec_iz];
+            shot[it + (size_t)d->nt * ix] = (d->rec_scale == 2.0f) ? (float)(val + val) : (float)(val * d->rec_scale);
+        }
+        if (snap && snap_every > 0 && it % snap_every == 0) {
+            size_t k; float *dst = snap + (size_t)(it / snap_every) * n;
+            for (k = 0; k < n; k++) dst[k] = (float)p.P[k];
+        }
+    }
+    prop2d_free(&p);
+    return 0;
+}
+
+/* Direct-wave mute of a (nx traces x nt) record.
+ *  GPU form (GPU_vti2dfd_kernels.cu:151-174): zero (t0/dt - tt, t0/dt+2/(dt f)+tt)
+ *    with t0 = offset/(vp[1]*sqrt(1+2 eps[1])) from the padded model;
+ *  MPI form (Toa_rtm_vti_adcig_cdp.c:1587-1605): zero [0, mu_nt), dt in ms. */
+void orc_mute2d(int form, int nx, int nt, float dt, float favg, float dx, float dz,
+                int fs, int ds, int zs, int is, float mu_v, int tt, float *shot)
+{
+    int ix, it;
+    for (ix = 0; ix < nx; ix++) {
+        if (form == 0) { /* GPU */
+            float mu_x = dx * abs(ix - fs - (is - 1) * ds), mu_z = dz * zs;
+            float mu_t0 = sqrtf((float)(pow(mu_x, 2) + pow(mu_z, 2))) / mu_v;
+            int mu_t = (int)(2.0 / (dt * favg));
+            int mu_nt = (int)(mu_t0 / dt) + mu_t + tt;
+            for (it = 0; it < nt; it++)
+                if ((it > (int)(mu_t0 / dt) - tt) && it < mu_nt) shot[ix * nt + it] = 0.0f;
+        } else {        /* MPI, dt in ms */
+            float mu_x = dx * abs(ix - fs - (is - 1) * ds), mu_z = dz * zs;
+            float mu_t0 = sqrtf((float)(pow(mu_x, 2) + pow(mu_z, 2))) / mu_v;
+            int mu_t = (int)(2.0 / (dt / 1000 * favg));
+            int mu_nt = (int)(mu_t0 / dt * 1000) + mu_t + tt;
+            for (it = 0; it < mu_nt && it < nt; it++) shot[ix * nt + it] = 0.0f;
+        }
+    }
+}
+
+/* ------------------------------------------------------------ 2D RTM */
+
+/* One shot of the MPI CPU RTM (model_vti_get_boundry + RTM_corr_adcig,
+ * Toa_rtm_vti_adcig_cdp.c:483-737, 739-1139, driven as main() drives them
+ * :295-392) on the shot's aperture window:
+ *   nxs  odd window width; the window is centred on k = fs_sxd+(is-1)*ds_sxd
+ *        (1-based), window column c <-> padded global column npd+c+k-nxs/2;
+ *   forward with Gaussian source, SV taper always on (CR=15), receivers
+ *        txx,tzz at row npd+hsx-1 (hsx=1) and the four interior-edge lines;
+ *   mute both records (tt=285);
+ *   backward from a zero state: inject saved edges into s_txx0/s_tzz0,
+ *        vel + inv_update_stress; inject the muted records into g_*0 at
+ *        row npd, vel + inv_update_stress; image mig += g_txx*s_txx and
+ *        source_x = (float)((double)source_x + pow(s_txx,2)), 0 -> 1;
+ *   mig /= source_x.
+ * Output: mig_is (nxs*nz, x-major) and the stacking offset of column 0 in the
+ * full image (the reference adds column c at c + k - nxs/2 - 1, :1102-1104).
+ * The full model is nx*nz unpadded. */
+int orc_rtm2d_mpi_shot(int nx, int nz, int npd, int nt, float dx, float dz, float dt_ms,
+                       float favg, float pfac, int fs_sxd, int ds_sxd, int zs_sxd, int is, int nxs,
+                       const float *v, const float *e, const float *dl,
+                       float *mig_is, int *stack_offset, float *p_cal_x_out)
+{
+    int nnzs = nz + 2 * npd, nnxs = nxs + 2 * npd, k = fs_sxd + (is - 1) * ds_sxd;
+    int c, iz, it, i, j;
+    float *vs = malloc((size_t)nxs * nz * 4), *es = malloc((size_t)nxs * nz * 4), *ds_ = malloc((size_t)nxs * nz * 4);
+    /* padded full model to read the window from (edge replicated) */
+    int nnx = nx + 2 * npd;
+    REAL *vfull = calloc((size_t)nnx * nnzs, sizeof(REAL)), *efull = calloc((size_t)nnx * nnzs, sizeof(REAL)),
+         *dfull = calloc((size_t)nnx * nnzs, sizeof(REAL));
+    for (i = 0; i < nx; i++) for (j = 0; j < nz; j++) {
+        size_t id = (size_t)(i + npd) * nnzs + j + npd;
+        vfull[id] = v[i * nz + j]; efull[id] = e[i * nz + j]; dfull[id] = dl[i * nz + j];
+    }
+    orc_pad2d(nx, nz, npd, vfull); orc_pad2d(nx, nz, npd, efull); orc_pad2d(nx, nz, npd, dfull);
+    for (c = 0; c < nxs; c++) for (iz = 0; iz < nz; iz++) {
+        size_t g = (size_t)(npd + c + k - nxs / 2) * nnzs + iz + npd;
+        vs[c * nz + iz] = (float)vfull[g]; es[c * nz + iz] = (float)efull[g]; ds_[c * nz + iz] = (float)dfull[g];
+    }
+    free(vfull); free(efull); free(dfull);
+
+    orc_fd2d_desc d;
+    memset(&d, 0, sizeof d);
+    d.nx = nxs; d.nz = nz; d.npd = npd; d.nt = nt; d.variant = ORC_V_MPI; d.sv = 1; d.wtype = 1;
+    d.dx = dx; d.dz = dz; d.dt = dt_ms / 1000; d.favg = favg; d.pfac = pfac;
+    d.fs = (float)(nxs / 2 + 1); d.ds = 0; d.zs = (float)zs_sxd; d.is = is;
+
+    orc_prop2d fw, sr, rc;
+    prop2d_init(&fw, &d, vs, es, ds_, 1);
+    float mu_v = (float)(vs[1 * nz + 1] * sqrtf((1 + 2 * es[1 * nz + 1])));
+    size_t ntx = (size_t)nt * nxs, ntz = (size_t)nt * nz;
+    float *pcx = calloc(ntx, 4), *pcz = calloc(ntx, 4), *tx = calloc(ntx, 4), *bx = calloc(ntx, 4),
+          *tz = calloc(ntx, 4), *bz = calloc(ntx, 4), *lx = calloc(ntz, 4), *rx = calloc(ntz, 4),
+          *lz = calloc(ntz, 4), *rz = calloc(ntz, 4);
+    for (it = 0; it < nt; it++) {
+        prop2d_step(&fw, it);
+        for (i = npd; i < npd + nxs; i++) {
+            size_t col = (size_t)i * nnzs;
+            pcx[(size_t)(i - npd) * nt + it] = (float)fw.P[col + npd];
+            pcz[(size_t)(i - npd) * nt + it] = (float)fw.Q[col + npd];
+            tx[(size_t)(i - npd) * nt + it] = (float)fw.P[col + npd];
+            bx[(size_t)(i - npd) * nt + it] = (float)fw.P[col + npd + nz - 1];
+            tz[(size_t)(i - npd) * nt + it] = (float)fw.Q[col + npd];
+            bz[(size_t)(i - npd) * nt + it] = (float)fw.Q[col + npd + nz - 1];
+        }
+        for (j = npd; j < npd + nz; j++) {
+            lx[(size_t)(j - npd) * nt + it] = (float)fw.P[(size_t)npd * nnzs + j];
+            rx[(size_t)(j - npd) * nt + it] = (float)fw.P[(size_t)(npd + nxs - 1) * nnzs + j];
+            lz[(size_t)(j - npd) * nt + it] = (float)fw.Q[(size_t)npd * nnzs + j];
+            rz[(size_t)(j - npd) * nt + it] = (float)fw.Q[(size_t)(npd + nxs - 1) * nnzs + j];
+        }
+    }
+    prop2d_free(&fw);
+    orc_mute2d(1, nxs, nt, dt_ms, favg, dx, dz, nxs / 2 + 1, 0, zs_sxd, is, mu_v, 285, pcx);
+    orc_mute2d(1, nxs, nt, dt_ms, favg, dx, dz, nxs / 2 + 1, 0, zs_sxd, is, mu_v, 285, pcz);
+    if (p_cal_x_out) memcpy(p_cal_x_out, pcx, ntx * 4);
+
+    /* backward: both passes use the untapered model (inv_update_stress) */
+    prop2d_init(&sr, &d, vs, es, ds_, 0);
+    prop2d_init(&rc, &d, vs, es, ds_, 0);
+    float *srcx = calloc((size_t)nxs * nz, 4);
+    memset(mig_is, 0, (size_t)nxs * nz * 4);
+    for (it = nt - 1; it >= 0; it--) {
+        for (i = 0; i < nxs; i++) {
+            sr.P[(size_t)(npd + i) * nnzs + npd] = (REAL)tx[(size_t)i * nt + it];
+            sr.P[(size_t)(npd + i) * nnzs + npd + nz - 1] = (REAL)bx[(size_t)i * nt + it];
+            sr.Q[(size_t)(npd + i) * nnzs + npd] = (REAL)tz[(size_t)i * nt + it];
+            sr.Q[(size_t)(npd + i) * nnzs + npd + nz - 1] = (REAL)bz[(size_t)i * nt + it];
+        }
+        for (j = 0; j < nz; j++) {
+            sr.P[(size_t)npd * nnzs + npd + j] = (REAL)lx[(size_t)j * nt + it];
+            sr.P[(size_t)(npd + nxs - 1) * nnzs + npd + j] = (REAL)rx[(size_t)j * nt + it];
+            sr.Q[(size_t)npd * nnzs + npd + j] = (REAL)lz[(size_t)j * nt + it];
+            sr.Q[(size_t)(npd + nxs - 1) * nnzs + npd + j] = (REAL)rz[(size_t)j * nt + it];
+        }
+        vel2d(&sr.st, sr.u, sr.w, sr.P, sr.Q);
+        stress2d(&sr.st, sr.u, sr.w, sr.P, sr.Q, sr.px, sr.pz, sr.qx, sr.qz, NULL);
+        for (i = 0; i < nxs; i++) {
+            rc.P[(size_t)(npd + i) * nnzs + npd] = (REAL)pcx[(size_t)i * nt + it];
+            rc.Q[(size_t)(npd + i) * nnzs + npd] = (REAL)pcz[(size_t)i * nt + it];
+        }
+        vel2d(&rc.st, rc.u, rc.w, rc.P, rc.Q);
+        stress2d(&rc.st, rc.u, rc.w, rc.P, rc.Q, rc.px, rc.pz, rc.qx, rc.qz, NULL);
+        for (i = npd; i < nxs + npd; i++)
+            for (j = npd; j < nz + npd; j++) {
+                size_t id = (size_t)i * nnzs + j, o = (size_t)(i - npd) * nz + (j - npd);
+                REAL sv = sr.P[id];
+                srcx[o] = (float)((double)srcx[o] + pow((double)sv, 2));
+                if (srcx[o] == 0) srcx[o] = 1.0f;
+                mig_is[o] = (float)(mig_is[o] + (REAL)rc.P[id] * sv);
+            }
+    }
+    for (size_t o = 0; o < (size_t)nxs * nz; o++) mig_is[o] = mig_is[o] / srcx[o];
+    *stack_offset = k - nxs / 2 - 1;
+    prop2d_free(&sr); prop2d_free(&rc);
+    free(srcx); free(pcx); free(pcz); free(tx); free(bx); free(tz); free(bz); free(lx); free(rx); free(lz); free(rz);
+    free(vs); free(es); free(ds_);
+    return 0;
+}
+
+/* Stack per-shot images into the full image in shot order
+ * (Toa_rtm_vti_adcig_cdp.c:1102-1104; single-rank MPI_Reduce is a copy). */
+void orc_stack2d(int nz, int nxs, int offset, const float *mig_is, float *mig_full)
+{
+    int c, j;
+    for (c = 0; c < nxs; c++)
+        for (j = 0; j < nz; j++)
+            mig_full[(size_t)(c + offset) * nz + j] += mig_is[(size_t)c * nz + j];
+}
+
+/* Adjoint Laplacian (laplac2_lop adj=1, utils-Laplacian-filter/laplace.c:9-53;
+ * in-program copy Toa_gpu2DvtiFdRtmAdcigsLaplace.cu:150-202 zeroes `out`). */
+void orc_laplace2d_adj(int nz, int nx, const float *in, float *out)
+{
+    int iz, ix, j;
+    for (j = 0; j < nx * nz; j++) out[j] = 0.0f;
+    for (ix = 0; ix < nx; ix++)
+        for (iz = 0; iz < nz; iz++) {
+            j = iz + ix * nz;
+            if (iz > 0) { out[j - 1] -= in[j]; out[j] += in[j]; }
+            if (iz < nz - 1) { out[j + 1] -= in[j]; out[j] += in[j]; }
+            if (ix > 0) { out[j - nz] -= in[j]; out[j] += in[j]; }
+            if (ix < nx - 1) { out[j + nz] -= in[j]; out[j] += in[j]; }
+        }
+}
+
+/* 3D adjoint Laplacian, the same first-difference operator along z, x, y
+ * (the 3D RTM's laplace_3d_filter, 3D-vti-fd+rtm-cuda/
+ * Toa_gpu_3dvti_rtm_adcigs_1orderfunction.cu:555-616), out zeroed first. */
+void orc_laplace3d_adj(int nz, int nx, int ny, const float *in, float *out)
+{
+    long iz, ix, iy, j, nxz = (long)nx * nz, n = nxz * ny;
+    for (j = 0; j < n; j++) out[j] = 0.0f;
+    for (iy = 0; iy < ny; iy++)
+        for (ix = 0; ix < nx; ix++)
+            for (iz = 0; iz < nz; iz++) {
+                j = iz + ix * nz + iy * nxz;
+                if (iz > 0) { out[j - 1] -= in[j]; out[j] += in[j]; }
+                if (iz < nz - 1) { out[j + 1] -= in[j]; out[j] += in[j]; }
+                if (ix > 0) { out[j - nz] -= in[j]; out[j] += in[j]; }
+                if (ix < nx - 1) { out[j + nz] -= in[j]; out[j] += in[j]; }
+                if (iy > 0) { out[j - nxz] -= in[j]; out[j] += in[j]; }
+                if (iy < ny - 1) { out[j + nxz] -= in[j]; out[j] += in[j]; }
+            }
+}
+
+/* ------------------------------------------------------------------ 3D */
+
+typedef struct {
+    int nx, ny, nz, npd, nt, sv, wtype;
+    int mode;          /* 0: split sponge fields everywhere (the reference's
+                          arithmetic); 1: P,Q unsplit inside the physical box
+                          (the production fast path) */
+    float dx, dy, dz, dt, favg, pfac;
+    int fsx, fsy, fsz, dsx, dsy, dsz, is;   /* is 0-based (GPU_vti3dfd_kernels.cu:113) */
+    int rec_iz, rx0, drx, nrx, ry0, dry, nry;
+} orc_fd3d_desc;
+
+/* 3D VTI forward modelling of one shot with the GUI GPU program's semantics
+ * (GPU_vti3dfd_kernels.cu): point Ricker source added to P,Q before the
+ * velocity update (:53-88), velocity (:90-129) and split-sponge stress
+ * (:131-201) updates on [4, nn-4) in every axis, optional SV taper (R=15,
+ * r=4, centre fs+is*ds+npml-1), sponge profiles of the GPU form, d0 from the
+ * centre velocity (:203-206).  shot is (nt x nrx*nry) trace-major,
+ * shot[it + nt*(irx + nrx*iry)] = P[rec_iz, npd+rx0+irx*drx, npd+ry0+iry*dry].
+ * final_fields (optional) receives the padded P, Q at the end. */
+int orc_fd3d(const orc_fd3d_desc *d, const float *v, const float *e, const float *dl,
+             float *shot, float *final_P, float *final_Q)
+{
+    const int npd = d->npd;
+    const long nnx = d->nx + 2 * npd, nny = d->ny + 2 * npd, nnz = d->nz + 2 * npd, nxz = nnx * nnz;
+    const long n = nxz * nny;
+    long ix, iy, iz;
+    float *vv = calloc(n, 4), *ee = calloc(n, 4), *dd = calloc(n, 4);
+    REAL *tmp = malloc(n * sizeof(REAL));
+    for (iy = 0; iy < d->ny; iy++) for (ix = 0; ix < d->nx; ix++) for (iz = 0; iz < d->nz; iz++) {
+        long g = (iz + npd) + nnz * (ix + npd) + nxz * (iy + npd), s = iz + (long)d->nz * (ix + (long)d->nx * iy);
+        vv[g] = v[s]; ee[g] = e[s]; dd[g] = dl[s];
+    }
+    {
+        float *arrs[3] = {ee, dd, vv}; int a; long k;
+        for (a = 0; a < 3; a++) {
+            for (k = 0; k < n; k++) tmp[k] = arrs[a][k];
+            orc_pad3d(d->nx, d->ny, d->nz, npd, tmp);
+            for (k = 0; k < n; k++) arrs[a][k] = (float)tmp[k];
+        }
+    }
+    free(tmp);
+    if (d->sv) {
+        int R = 15, r = 4;
+        long cx = d->fsx + d->is * d->dsx + npd - 1, cy = d->fsy + d->is * d->dsy + npd - 1, cz = d->fsz + d->is * d->dsz + npd - 1;
+        for (iy = 0; iy < nny; iy++) for (ix = 0; ix < nnx; ix++) for (iz = 0; iz < nnz; iz++) {
+            int rx = (int)(ix - cx), ry = (int)(iy - cy), rz = (int)(iz - cz);
+            long id = iz + nnz * ix + nxz * iy;
+            int r2 = rx * rx + ry * ry + rz * rz;
+            if (r2 <= R * R) {
+                if (r2 <= r * r) { ee[id] = 0.0f; dd[id] = 0.0f; }
+                else {
+                    double g = 0.5 * (1 - cos(PI_GUI * ((sqrtf((float)r2) - r) * 4.0 / (R * 3.0 - 1))));
+                    ee[id] = (float)(g * ee[id]); dd[id] = (float)(g * dd[id]);
+                }
+            }
+        }
+    }
+    float d0 = orc_d0(ORC_V_GPU, 3, 0.0f, vv[nny * nnx * nnz / 2], npd, d->dx, d->dy, d->dz);
+    float *cx1 = malloc(nnx * 4), *cx2 = malloc(nnx * 4), *ax1 = malloc(nnx * 4), *ax2 = malloc(nnx * 4);
+    float *cy1 = malloc(nny * 4), *cy2 = malloc(nny * 4), *ay1 = malloc(nny * 4), *ay2 = malloc(nny * 4);
+    float *cz1 = malloc(nnz * 4), *cz2 = malloc(nnz * 4), *az1 = malloc(nnz * 4), *az2 = malloc(nnz * 4);
+    orc_sponge(ORC_V_GPU, d->nx, npd, d->dt, d0, cx1, cx2, ax1, ax2);
+    orc_sponge(ORC_V_GPU, d->ny, npd, d->dt, d0, cy1, cy2, ay1, ay2);
+    orc_sponge(ORC_V_GPU, d->nz, npd, d->dt, d0, cz1, cz2, az1, az2);
+
+    REAL *vp = malloc(n * sizeof(REAL)), *e2 = malloc(n * sizeof(REAL)), *d2 = malloc(n * sizeof(REAL));
+    long k;
+    for (k = 0; k < n; k++) {
+        vp[k] = vv[k];
+        e2[k] = (REAL)1 + (REAL)2 * (REAL)ee[k];
+        d2[k] = RSQRT((REAL)1 + (REAL)2 * (REAL)dd[k]);
+    }
+    free(vv); free(ee); free(dd);
+    REAL *u = calloc(n, sizeof(REAL)), *vv_ = calloc(n, sizeof(REAL)), *w = calloc(n, sizeof(REAL));
+    REAL *P = calloc(n, sizeof(REAL)), *Q = calloc(n, sizeof(REAL));
+    REAL *px = calloc(n, sizeof(REAL)), *py = calloc(n, sizeof(REAL)), *pz = calloc(n, sizeof(REAL));
+    REAL *qx = calloc(n, sizeof(REAL)), *qy = calloc(n, sizeof(REAL)), *qz = calloc(n, sizeof(REAL));
+    float *amp = malloc(d->nt * 4); unsigned char *act = malloc(d->nt);
+    orc_source_amp(ORC_V_GPU, d->nt, d->dt, d->favg, d->pfac, d->wtype, amp, act);
+    const long ixs = d->fsx + d->is * d->dsx + npd - 1, iys = d->fsy + d->is * d->dsy + npd - 1,
+               izs = d->fsz + d->is * d->dsz + npd - 1;
+    const long src = izs + ixs * nnz + iys * nxz;
+    const REAL dtx = (REAL)(d->dt / d->dx), dty = (REAL)(d->dt / d->dy), dtz = (REAL)(d->dt / d->dz);
+    int it;
+    for (it = 0; it < d->nt; it++) {
+        REAL P_src0 = P[src], Q_src0 = Q[src];
+        if (act[it]) { P[src] += (REAL)amp[it]; Q[src] += (REAL)amp[it]; }
+#pragma omp parallel for schedule(static) private(ix, iz)
+        for (iy = 4; iy < nny - 4; iy++)
+            for (ix = 4; ix < nnx - 4; ix++)
+                for (iz = 4; iz < nnz - 4; iz++) {
+                    long id = iz + ix * nnz + iy * nxz; int im;
+                    REAL xx = 0, yy = 0, zz = 0;
+                    for (im = 0; im < 4; im++) {
+                        yy += (REAL)C8[im] * (P[id + (im + 1) * nxz] - P[id - im * nxz]);
+                        xx += (REAL)C8[im] * (P[id + (im + 1) * nnz] - P[id - im * nnz]);
+                        zz += (REAL)C8[im] * (Q[id + im + 1] - Q[id - im]);
+                    }
+                    u[id] = cx2[ix] * u[id] - cx1[ix] * dtx * xx;
+                    vv_[id] = cy2[iy] * vv_[id] - cy1[iy] * dty * yy;
+                    w[id] = cz2[iz] * w[id] - cz1[iz] * dtz * zz;
+                }
+#pragma omp parallel for schedule(static) private(ix, iz)
+        for (iy = 4; iy < nny - 4; iy++)
+            for (ix = 4; ix < nnx - 4; ix++)
+                for (iz = 4; iz < nnz - 4; iz++) {
+                    long id = iz + ix * nnz + iy * nxz; int im;
+                    REAL xx = 0, yy = 0, zz = 0, c = vp[id];
+                    for (im = 0; im < 4; im++) {
+                        yy += (REAL)C8[im] * (vv_[id + im * nxz] - vv_[id - (im + 1) * nxz]);
+                        xx += (REAL)C8[im] * (u[id + im * nnz] - u[id - (im + 1) * nnz]);
+                        zz += (REAL)C8[im] * (w[id + im] - w[id - im - 1]);
+                    }
+                    int inside = d->mode == 1 && ix >= npd && ix < npd + d->nx && iy >= npd && iy < npd + d->ny
+                                 && iz >= npd && iz < npd + d->nz;
+                    if (inside) {
+                        REAL p0 = (id == src) ? P_src0 : P[id], q0 = (id == src) ? Q_src0 : Q[id];
+                        P[id] = p0 - c * c * e2[id] * dtx * xx - c * c * e2[id] * dty * yy - c * c * d2[id] * dtz * zz;
+                        Q[id] = q0 - c * c * d2[id] * dtx * xx - c * c * d2[id] * dty * yy - c * c * dtz * zz;
+                    } else {
+                        px[id] = ax2[ix] * px[id] - ax1[ix] * c * c * e2[id] * dtx * xx;
+                        py[id] = ay2[iy] * py[id] - ay1[iy] * c * c * e2[id] * dty * yy;
+                        pz[id] = az2[iz] * pz[id] - az1[iz] * c * c * d2[id] * dtz * zz;
+                        qx[id] = ax2[ix] * qx[id] - ax1[ix] * c * c * d2[id] * dtx * xx;
+                        qy[id] = ay2[iy] * qy[id] - ay1[iy] * c * c * d2[id] * dty * yy;
+                        qz[id] = az2[iz] * qz[id] - az1[iz] * c * c * dtz * zz;
+                        P[id] = px[id] + py[id] + pz[id];
+                        Q[id] = qx[id] + qy[id] + qz[id];
+                    }
+                }
+        {
+            int irx, iry;
+            for (iry = 0; iry < d->nry; iry++)
+                for (irx = 0; irx < d->nrx; irx++) {
+                    long gx = npd + d->rx0 + (long)irx * d->drx, gy = npd + d->ry0 + (long)iry * d->dry;
+                    shot[it + (long)d->nt * (irx + (long)d->nrx * iry)] = (float)P[d->rec_iz + nnz * gx + nxz * gy];
+                }
+        }
+    }
+    if (final_P) for (k = 0; k < n; k++) final_P[k] = (float)P[k];
+    if (final_Q) for (k = 0; k < n; k++) final_Q[k] = (float)Q[k];
+    free(cx1); free(cx2); free(ax1); free(ax2); free(cy1); free(cy2); free(ay1); free(ay2);
+    free(cz1); free(cz2); free(az1); free(az2);
+    free(vp); free(e2); free(d2); free(u); free(vv_); free(w); free(P); free(Q);
+    free(px); free(py); free(pz); free(qx); free(qy); free(qz); free(amp); free(act);
+    return 0;
+}
+
+/* Direct-wave mute of a 3D record (mute_directwave3d, GPU_vti3dfd_kernels.cu:342-369):
+ * zero it < mu_nt with t0 = |offset|/(vp[1]*sqrtf(1+2 eps[1])) (padded index 1). */
+void orc_mute3d(int nx, int ny, int nt, float dt, float favg, float dx, float dy, float dz,
+                int fsx, int fsy, int dsx, int dsy, int fsz, int is, float vp1, float eps1, int tt, float *shot)
+{
+    int ix, iy, it;
+    for (iy = 0; iy < ny; iy++) for (ix = 0; ix < nx; ix++) {
+        float mu_x = dx * abs(ix - fsx - is * dsx), mu_y = dy * abs(iy - fsy - is * dsy), mu_z = dz * fsz;
+        float mu_t0 = sqrtf((float)(pow(mu_x, 2) + pow(mu_y, 2) + pow(mu_z, 2))) / (vp1 * sqrtf(1 + 2 * eps1));
+        int mu_t = (int)(2.0 / (dt * favg));
+        int mu_nt = (int)(mu_t0 / dt) + mu_t + tt;
+        for (it = 0; it < nt && it < mu_nt; it++) shot[it + (long)ix * nt + (long)iy * nx * nt] = 0.0f;
+    }
+}

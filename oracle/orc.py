@@ -1,0 +1,202 @@
+"""ctypes bindings of the CPU oracle (liborc32/liborc64) and of the
+reference's own CPU code built into oracle/_ref.
+
+Test infrastructure only: imported by tests/, __graft_entry__.smoke() and the
+CPU-baseline leg of bench.py, never by the library.
+"""
+import ctypes as C
+import os
+import subprocess
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+V_CPU, V_GPU, V_MPI, V_GPURTM = 0, 1, 2, 3
+
+_f = np.float32
+_P = np.ctypeslib.ndpointer
+
+
+def build(with_ref=None):
+    """Compile the oracle (and the reference pin when its tree exists)."""
+    target = [] if with_ref is None else (["all"] if with_ref else ["oracle"])
+    subprocess.run(["make", "-s", "-C", HERE] + target, check=True)
+
+
+def _fp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_float)) if a is not None else None
+
+
+class FD2DDesc(C.Structure):
+    _fields_ = [(n, C.c_int) for n in ("nx", "nz", "npd", "nt", "variant", "sv", "wtype")] + \
+               [(n, C.c_float) for n in ("dx", "dz", "dt", "favg", "pfac", "fs", "ds", "zs")] + \
+               [("is_", C.c_int), ("rec_iz", C.c_int), ("rec_scale", C.c_float)]
+
+
+class FD3DDesc(C.Structure):
+    _fields_ = [(n, C.c_int) for n in ("nx", "ny", "nz", "npd", "nt", "sv", "wtype", "mode")] + \
+               [(n, C.c_float) for n in ("dx", "dy", "dz", "dt", "favg", "pfac")] + \
+               [(n, C.c_int) for n in ("fsx", "fsy", "fsz", "dsx", "dsy", "dsz", "is_",
+                                       "rec_iz", "rx0", "drx", "nrx", "ry0", "dry", "nry")]
+
+
+_libs = {}
+
+
+def lib(prec=32):
+    key = "orc%d" % prec
+    if key not in _libs:
+        path = os.path.join(HERE, "liborc%d.so" % prec)
+        if not os.path.exists(path):
+            build(with_ref=False)
+        L = C.CDLL(path)
+        L.orc_fd2d.argtypes = [C.POINTER(FD2DDesc)] + [C.POINTER(C.c_float)] * 5 + [C.c_int]
+        L.orc_fd3d.argtypes = [C.POINTER(FD3DDesc)] + [C.POINTER(C.c_float)] * 6
+        L.orc_rtm2d_mpi_shot.argtypes = [C.c_int] * 4 + [C.c_float] * 5 + [C.c_int] * 5 + \
+            [C.POINTER(C.c_float)] * 4 + [C.POINTER(C.c_int), C.POINTER(C.c_float)]
+        L.orc_laplace2d_adj.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_float), C.POINTER(C.c_float)]
+        L.orc_laplace3d_adj.argtypes = [C.c_int] * 3 + [C.POINTER(C.c_float)] * 2
+        L.orc_stack2d.argtypes = [C.c_int, C.c_int, C.c_int, C.POINTER(C.c_float), C.POINTER(C.c_float)]
+        L.orc_mute2d.argtypes = [C.c_int, C.c_int, C.c_int] + [C.c_float] * 4 + [C.c_int] * 4 + \
+            [C.c_float, C.c_int, C.POINTER(C.c_float)]
+        L.orc_mute3d.argtypes = [C.c_int] * 3 + [C.c_float] * 5 + [C.c_int] * 6 + [C.c_float] * 2 + \
+            [C.c_int, C.POINTER(C.c_float)]
+        _libs[key] = L
+    return _libs[key]
+
+
+def c32(a):
+    return np.ascontiguousarray(a, dtype=_f)
+
+
+def fd2d(v, e, d, *, npd, nt, dx, dz, dt, favg, pfac, fs, zs, ds=0.0, is_=1, variant=V_CPU,
+         sv=0, wtype=1, rec_iz=None, rec_scale=None, snap_every=0, prec=32):
+    """2D forward modelling of one shot; returns shot (nx, nt) [and snaps]."""
+    v, e, d = c32(v), c32(e), c32(d)
+    nx, nz = v.shape
+    desc = FD2DDesc(nx=nx, nz=nz, npd=npd, nt=nt, variant=variant, sv=sv, wtype=wtype,
+                    dx=dx, dz=dz, dt=dt, favg=favg, pfac=pfac, fs=fs, ds=ds, zs=zs, is_=is_,
+                    rec_iz=npd if rec_iz is None else rec_iz,
+                    rec_scale=(2.0 if variant == V_CPU else 1.0) if rec_scale is None else rec_scale)
+    shot = np.zeros((nx, nt), _f)
+    snaps = None
+    if snap_every:
+        nn = (nx + 2 * npd) * (nz + 2 * npd)
+        snaps = np.zeros(((nt - 1) // snap_every + 1, nx + 2 * npd, nz + 2 * npd), _f)
+    lib(prec).orc_fd2d(C.byref(desc), _fp(v), _fp(e), _fp(d), _fp(shot), _fp(snaps), snap_every)
+    return (shot, snaps) if snap_every else shot
+
+
+def fd3d(v, e, d, *, npd, nt, dx, dy, dz, dt, favg, pfac, fsx, fsy, fsz, dsx=0, dsy=0, dsz=0,
+         is_=0, sv=0, wtype=1, mode=0, rec_iz=None, rx0=0, drx=1, nrx=None, ry0=0, dry=1, nry=None,
+         final=False, prec=32):
+    """3D forward modelling (GUI GPU semantics); v,e,d shaped (ny, nx, nz)."""
+    v, e, d = c32(v), c32(e), c32(d)
+    ny, nx, nz = v.shape
+    nrx = nx if nrx is None else nrx
+    nry = ny if nry is None else nry
+    desc = FD3DDesc(nx=nx, ny=ny, nz=nz, npd=npd, nt=nt, sv=sv, wtype=wtype, mode=mode,
+                    dx=dx, dy=dy, dz=dz, dt=dt, favg=favg, pfac=pfac, fsx=fsx, fsy=fsy, fsz=fsz,
+                    dsx=dsx, dsy=dsy, dsz=dsz, is_=is_, rec_iz=npd if rec_iz is None else rec_iz,
+                    rx0=rx0, drx=drx, nrx=nrx, ry0=ry0, dry=dry, nry=nry)
+    shot = np.zeros((nry, nrx, nt), _f)
+    fp = fq = None
+    if final:
+        shape = (ny + 2 * npd, nx + 2 * npd, nz + 2 * npd)
+        fp, fq = np.zeros(shape, _f), np.zeros(shape, _f)
+    lib(prec).orc_fd3d(C.byref(desc), _fp(v), _fp(e), _fp(d), _fp(shot), _fp(fp), _fp(fq))
+    return (shot, fp, fq) if final else shot
+
+
+def rtm2d_mpi_shot(v, e, d, *, npd, nt, dx, dz, dt_ms, favg, pfac, fs_sxd, ds_sxd, zs_sxd, is_, nxs,
+                   prec=32):
+    """One MPI-semantics RTM shot; returns (mig_is (nxs,nz), offset, p_cal_x (nxs,nt))."""
+    v, e, d = c32(v), c32(e), c32(d)
+    nx, nz = v.shape
+    mig = np.zeros((nxs, nz), _f)
+    pcal = np.zeros((nxs, nt), _f)
+    off = C.c_int(0)
+    lib(prec).orc_rtm2d_mpi_shot(nx, nz, npd, nt, dx, dz, dt_ms, favg, pfac, fs_sxd, ds_sxd, zs_sxd,
+                                 is_, nxs, _fp(v), _fp(e), _fp(d), _fp(mig), C.byref(off), _fp(pcal))
+    return mig, off.value, pcal
+
+
+def stack2d(full, mig_is, offset):
+    lib().orc_stack2d(full.shape[1], mig_is.shape[0], offset, _fp(c32(mig_is)), _fp(full))
+
+
+def laplace2d_adj(img):
+    img = c32(img)
+    out = np.zeros_like(img)
+    nx, nz = img.shape
+    lib().orc_laplace2d_adj(nz, nx, _fp(img), _fp(out))
+    return out
+
+
+def laplace3d_adj(img):
+    img = c32(img)
+    out = np.zeros_like(img)
+    ny, nx, nz = img.shape
+    lib().orc_laplace3d_adj(nz, nx, ny, _fp(img), _fp(out))
+    return out
+
+
+# ------------------------------------------------------------- the reference
+REF = os.path.join(HERE, "_ref")
+
+
+def ref_available():
+    return os.path.exists(os.path.join(REF, "librefcpu2d.so"))
+
+
+def ref_cpu_vti2dfd(v, e, d, *, npd, nt, dx, dz, dt_us, favg, fs, zs, ns=1, ds=0, sv=0):
+    """Run the reference's CPU_vti2dfd (unmodified) through its file interface.
+
+    Returns (shots (ns, nx, nt), snaps (k, nnx, nnz)) -- snapshots are the
+    padded P of shot 1 every 50 steps, as the reference writes them."""
+    L = C.CDLL(os.path.join(REF, "librefcpu2d.so"))
+    L.CPU_vti2dfd.restype = None
+    v, e, d = c32(v), c32(e), c32(d)
+    nx, nz = v.shape
+    with tempfile.TemporaryDirectory() as td:
+        names = {}
+        for k, a in (("v", v), ("e", e), ("d", d)):
+            names[k] = os.path.join(td, k + ".bin").encode()
+            a.tofile(names[k].decode())
+        fshot = os.path.join(td, "shot.bin").encode()
+        fsnap = os.path.join(td, "snap.bin").encode()
+        L.CPU_vti2dfd(C.c_int(nx), C.c_int(nz), C.c_int(int(dx)), C.c_int(int(dz)), C.c_int(npd), C.c_int(sv),
+                      names["v"], names["e"], names["d"], C.c_int(int(favg)), C.c_int(ns), C.c_int(fs),
+                      C.c_int(ds), C.c_int(zs), fshot, fsnap, C.c_int(nt), C.c_int(int(dt_us)), C.c_int(1))
+        shots = np.fromfile(fshot.decode(), _f).reshape(ns, nx, nt)
+        snaps = np.fromfile(fsnap.decode(), _f).reshape(-1, nx + 2 * npd, nz + 2 * npd)
+    return shots, snaps
+
+
+def ref_rtm_mpi_shot(v, e, d, acc, *, npd, nt, dx, dz, dt_ms, favg, pfac, fs_sxd, ds_sxd, zs_sxd, is_, nxs):
+    """The reference MPI RTM for one shot; stacks into `acc` (nx,nz) in place."""
+    L = C.CDLL(os.path.join(REF, "librefrtm.so"))
+    L.ref_rtm_mpi_shot.argtypes = [C.c_int] * 4 + [C.c_float] * 5 + [C.c_int] * 5 + [C.POINTER(C.c_float)] * 6
+    v, e, d = c32(v), c32(e), c32(d)
+    nx, nz = v.shape
+    mig = np.zeros((nxs, nz), _f)
+    pcal = np.zeros((nxs, nt), _f)
+    rc = L.ref_rtm_mpi_shot(nx, nz, npd, nt, dx, dz, dt_ms, favg, pfac, fs_sxd, ds_sxd, zs_sxd, is_, nxs,
+                            _fp(v), _fp(e), _fp(d), _fp(acc), _fp(mig), _fp(pcal))
+    if rc:
+        raise ValueError("aperture window leaves the model")
+    return mig, pcal
+
+
+def ref_laplace2d_adj(img):
+    """laplac2_lop(adj=1) from the reference utility; `out` is pre-zeroed
+    here because the utility accumulates into it without clearing."""
+    L = C.CDLL(os.path.join(REF, "libreflap.so"))
+    L.laplac2_lop.argtypes = [C.c_int, C.c_int, C.c_int, C.POINTER(C.c_float), C.POINTER(C.c_float)]
+    img = c32(img)
+    out = np.zeros_like(img)
+    nx, nz = img.shape
+    L.laplac2_lop(1, nz, nx, _fp(img), _fp(out))
+    return out

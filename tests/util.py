@@ -1,0 +1,52 @@
+"""Shared helpers for the tests: seeded models and error measures."""
+import numpy as np
+
+
+def layered_model(nx, nz, seed=1, nlayers=5, vlo=2000.0, vhi=4000.0, emax=0.25, dmax=0.1):
+    """Flat layers with per-layer vp/eps/del drawn from a seeded generator,
+    sorted so velocity grows with depth."""
+    rng = np.random.default_rng(seed)
+    vp = np.sort(rng.uniform(vlo, vhi, nlayers))
+    ep = rng.uniform(0.0, emax, nlayers)
+    # delta <= eps per layer: the pseudo-acoustic VTI system is unstable
+    # where delta > eps, in the reference as much as here
+    de = np.minimum(rng.uniform(0.0, dmax, nlayers), ep)
+    bounds = np.linspace(0, nz, nlayers + 1).astype(int)
+    v = np.empty((nx, nz), np.float32)
+    e = np.empty((nx, nz), np.float32)
+    d = np.empty((nx, nz), np.float32)
+    for k in range(nlayers):
+        v[:, bounds[k]:bounds[k + 1]] = vp[k]
+        e[:, bounds[k]:bounds[k + 1]] = ep[k]
+        d[:, bounds[k]:bounds[k + 1]] = de[k]
+    return v, e, d
+
+
+def random_model_3d(nx, ny, nz, seed=2, vlo=1800.0, vhi=3200.0):
+    rng = np.random.default_rng(seed)
+    base = rng.uniform(0, 1, (ny, nx, nz)).astype(np.float32)
+    # a little smoothing so the field is not white noise
+    for ax in range(3):
+        base = (np.roll(base, 1, ax) + base + np.roll(base, -1, ax)) / 3
+    base = (base - base.min()) / (base.max() - base.min())
+    v = (vlo + (vhi - vlo) * base).astype(np.float32)
+    e = (0.2 * base).astype(np.float32)
+    d = (0.1 * base).astype(np.float32)
+    return v, e, d
+
+
+def rel_l2(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    n = np.linalg.norm(b)
+    return float(np.linalg.norm(a - b) / (n if n > 0 else 1.0))
+
+
+def to_np(x):
+    try:
+        import torch
+        if isinstance(x, torch.Tensor):
+            return x.detach().cpu().numpy()
+    except ImportError:
+        pass
+    return np.asarray(x)
