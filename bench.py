@@ -273,6 +273,26 @@ def run_ours(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def run_profile_case(args):
+    """Small case for ncu captures: 192^3 + 40 sponge (272^3 padded, each
+    field 80 MB, the working set well above L2), a 20-step shot."""
+    import torch
+
+    import geophysics_gb300 as geo
+    global NX, NY, NZ
+    NX = NY = NZ = 192
+    vp, eps, dl = make_model(device="cuda")
+    kw = plan_kwargs()
+    kw.update(nt=20, nrx=96, nry=96)
+    plan = geo.FD3DPlan(**kw)
+    plan.set_model(vp, eps, dl)
+    for _ in range(args.steps):
+        plan.run_shot(0, device="cuda")
+    torch.cuda.synchronize()
+    plan.close()
+    print(json.dumps({"case": "profile-small", "grid": 192, "nt": 20, "shots": args.steps}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -280,7 +300,12 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--case", default="full", choices=["full", "small"],
+                    help="small: the ncu profiling case (not a bench line)")
     args = ap.parse_args()
+    if args.case == "small":
+        run_profile_case(args)
+        return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if world > 1 and args.impl == "ours":
