@@ -67,6 +67,8 @@ def lib():
         "geo_last_error": (C.c_char_p, []),
         "geo_launch_count": (C.c_longlong, []),
         "geo_fd2d_shot": (_i, [C.POINTER(FD2DDesc), _vp, _vp, _vp, _vp, _vp, _i, _i, _vp]),
+        "geo_fd2d_shot_noalloc": (_i, [C.POINTER(FD2DDesc), _vp, _vp, _vp, _vp, _vp]),
+        "geo_fd2d_noalloc_limit": (C.c_size_t, []),
         "geo_fd3d_plan_create": (_i, [C.POINTER(_vp), C.POINTER(FD3DDesc)]),
         "geo_fd3d_plan_destroy": (_i, [_vp]),
         "geo_fd3d_set_model": (_i, [_vp, _vp, _vp, _vp, _i, _vp]),

@@ -19,6 +19,8 @@
 #ifndef GEOFD_H
 #define GEOFD_H
 
+#include <stddef.h>
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -109,6 +111,24 @@ typedef struct geo_fd2d_desc {
  * of (nx+2npd)*(nz+2npd)). */
 int geo_fd2d_shot(const geo_fd2d_desc *desc, const float *v, const float *e, const float *d,
                   float *shot, float *snap, int snap_every, int mem, void *stream);
+
+/* geo_fd2d_shot for callers that cannot allocate GPU memory (a program
+ * whose device memory is all reserved by its own pool, a framework that
+ * forbids allocation outside its allocator, a loop that must never block in
+ * the allocator).  No counterpart in the reference: it is an addition.
+ *   - v, e, d (nx*nz) and shot (nt*nx) are DEVICE pointers the caller owns;
+ *   - nothing is allocated: the wavefields live in one static device array
+ *     of geo_fd2d_noalloc_limit() bytes (32 MiB) that every GPU loading the
+ *     library keeps until exit; larger shots fail with GEO_ERR_ARG;
+ *   - CPU and GPU variants (SV taper and GPU-form mute included), no
+ *     snapshots;
+ *   - the first call on a device resolves the array's device address, so
+ *     make that first call before any stream capture on that device;
+ *   - all calls share the array: calls that overlap on the GPU (other
+ *     streams, other host threads) race and corrupt each other's results. */
+int geo_fd2d_shot_noalloc(const geo_fd2d_desc *desc, const float *v, const float *e, const float *d,
+                          float *shot, void *stream);
+size_t geo_fd2d_noalloc_limit(void);
 
 /* 3D forward modelling of one shot (GPU_vti3dfd semantics).
  * Replaces the per-shot body of GPU_vti3dfd_kernels.cu:113-160. */
