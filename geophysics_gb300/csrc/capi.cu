@@ -178,7 +178,7 @@ static int snap3d_cb(void *ctx, int it) {
     int nnx, nny, nnz;
     plan3d_dims(S->plan, &nnx, &nny, &nnz);
     S->full.resize((size_t)nnx * nny * nnz);
-    GEO_CUDA(cudaMemcpy(S->full.data(), plan3d_P(S->plan), S->full.size() * 4, cudaMemcpyDeviceToHost));
+    GEO_TRY(geo_fd3d_get_fields(S->plan, S->full.data(), nullptr, GEO_MEM_HOST, nullptr));
     S->win.resize((size_t)S->nx * S->ny * S->nz);
     for (int iy = 0; iy < S->ny; iy++)
         for (int ix = 0; ix < S->nx; ix++)

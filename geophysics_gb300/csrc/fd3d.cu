@@ -14,6 +14,9 @@
 // Layout: id = iz + nnz*(ix + nnx*iy), z fastest, as the reference.
 #include "geo_internal.h"
 #include "fd3d.cuh"
+#include "fd3d_fused.cuh"
+#include <algorithm>
+#include <cstdlib>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -22,90 +25,8 @@ using namespace geo;
 
 namespace geo {
 
-__constant__ float c3_fd[4] = {1.196289f, -0.0797526f, 0.009570313f, -0.0006975447f};
-
 // ---------------------------------------------------------------- kernels
-// Velocity update, one thread per point; the point source is applied on the
-// fly to the taps that read the source cell (P,Q += amp before the update,
-// GPU_vti3dfd_kernels.cu:135).
-__global__ void __launch_bounds__(256) k_vel3d(Grid3D g, StepArgs3D st) {
-    const int iz = blockIdx.x * 32 + threadIdx.x, ix = blockIdx.y * blockDim.y + threadIdx.y, iy = blockIdx.z;
-    if (iz < 4 || iz >= g.nnz - 4 || ix < 4 || ix >= g.nnx - 4 || iy < 4 || iy >= g.nny - 4) return;
-    const long sxy = g.sxy, id = iz + (long)g.ldz * ix + sxy * iy;
-    const float *P = g.P, *Q = g.Q;
-    float xx = 0.0f, yy = 0.0f, zz = 0.0f;
-    const bool near = st.src_on && ((iz == st.izs && ix == st.ixs && abs(iy - st.iys) <= 4) ||
-                                    (iz == st.izs && iy == st.iys && abs(ix - st.ixs) <= 4) ||
-                                    (ix == st.ixs && iy == st.iys && abs(iz - st.izs) <= 4));
-    if (!near) {
-#pragma unroll
-        for (int im = 0; im < 4; im++) {
-            yy += c3_fd[im] * (__ldg(P + id + (im + 1) * sxy) - __ldg(P + id - im * sxy));
-            xx += c3_fd[im] * (__ldg(P + id + (im + 1) * g.ldz) - __ldg(P + id - im * g.ldz));
-            zz += c3_fd[im] * (__ldg(Q + id + im + 1) - __ldg(Q + id - im));
-        }
-    } else {
-        auto ldp = [&](long k) { float v = P[k]; if (k == st.src) v = v + st.amp; return v; };
-        auto ldq = [&](long k) { float v = Q[k]; if (k == st.src) v = v + st.amp; return v; };
-#pragma unroll
-        for (int im = 0; im < 4; im++) {
-            yy += c3_fd[im] * (ldp(id + (im + 1) * sxy) - ldp(id - im * sxy));
-            xx += c3_fd[im] * (ldp(id + (im + 1) * g.ldz) - ldp(id - im * g.ldz));
-            zz += c3_fd[im] * (ldq(id + im + 1) - ldq(id - im));
-        }
-    }
-    g.u[id] = g.cx2[ix] * g.u[id] - g.cx1[ix] * g.dtx * xx;
-    g.v[id] = g.cy2[iy] * g.v[id] - g.cy1[iy] * g.dty * yy;
-    g.w[id] = g.cz2[iz] * g.w[id] - g.cz1[iz] * g.dtz * zz;
-}
-
-template <int MODE>
-__global__ void __launch_bounds__(256) k_stress3d(Grid3D g, StepArgs3D st) {
-    const int iz = blockIdx.x * 32 + threadIdx.x, ix = blockIdx.y * blockDim.y + threadIdx.y, iy = blockIdx.z;
-    if (iz < 4 || iz >= g.nnz - 4 || ix < 4 || ix >= g.nnx - 4 || iy < 4 || iy >= g.nny - 4) return;
-    const long sxy = g.sxy, id = iz + (long)g.ldz * ix + sxy * iy;
-    float xx = 0.0f, yy = 0.0f, zz = 0.0f;
-#pragma unroll
-    for (int im = 0; im < 4; im++) {
-        yy += c3_fd[im] * (__ldg(g.v + id + im * sxy) - __ldg(g.v + id - (im + 1) * sxy));
-        xx += c3_fd[im] * (__ldg(g.u + id + im * g.ldz) - __ldg(g.u + id - (im + 1) * g.ldz));
-        zz += c3_fd[im] * (__ldg(g.w + id + im) - __ldg(g.w + id - im - 1));
-    }
-    const float vp = __ldg(g.vp + id), e2 = __ldg(g.e2 + id), d2 = __ldg(g.d2 + id);
-    const bool inside = MODE == GEO_MODE_FAST && ix >= g.npd && ix < g.npd + g.nx && iy >= g.npd &&
-                        iy < g.npd + g.ny && iz >= g.npd && iz < g.npd + g.nz;
-    float P, Q;
-    if (inside) {
-        // all sponge factors are 1: acoff*vp == vp exactly, so each term is
-        // the reference's product chain; only the split sum is replaced
-        P = g.P[id] - vp * vp * e2 * g.dtx * xx - vp * vp * e2 * g.dty * yy - vp * vp * d2 * g.dtz * zz;
-        Q = g.Q[id] - vp * vp * d2 * g.dtx * xx - vp * vp * d2 * g.dty * yy - vp * vp * g.dtz * zz;
-    } else {
-        const float ax1 = g.ax1[ix], ax2 = g.ax2[ix], ay1 = g.ay1[iy], ay2 = g.ay2[iy], az1 = g.az1[iz], az2 = g.az2[iz];
-        const float px = ax2 * g.px[id] - ax1 * vp * vp * e2 * g.dtx * xx;
-        const float py = ay2 * g.py[id] - ay1 * vp * vp * e2 * g.dty * yy;
-        const float pz = az2 * g.pz[id] - az1 * vp * vp * d2 * g.dtz * zz;
-        const float qx = ax2 * g.qx[id] - ax1 * vp * vp * d2 * g.dtx * xx;
-        const float qy = ay2 * g.qy[id] - ay1 * vp * vp * d2 * g.dty * yy;
-        const float qz = az2 * g.qz[id] - az1 * vp * vp * g.dtz * zz;
-        g.px[id] = px; g.py[id] = py; g.pz[id] = pz;
-        g.qx[id] = qx; g.qy[id] = qy; g.qz[id] = qz;
-        P = px + py + pz;
-        Q = qx + qy + qz;
-    }
-    g.P[id] = P;
-    g.Q[id] = Q;
-    // receiver gather, time-major (shot_record3d, GPU_vti3dfd_kernels.cu:316-327)
-    if (st.rec && iz == st.rec_iz) {
-        const int rx = ix - g.npd - st.rx0, ry = iy - g.npd - st.ry0;
-        if (rx >= 0 && ry >= 0 && rx % st.drx == 0 && ry % st.dry == 0) {
-            const int irx = rx / st.drx, iry = ry / st.dry;
-            if (irx < st.nrx && iry < st.nry) st.rec[(long)st.it * st.nrx * st.nry + irx + (long)st.nrx * iry] = P;
-        }
-    }
-}
-
-// Write a B^3 box of (1+2eps, sqrtf(1+2del)) into the model, clipped.
+// Write a B^3 box of two model arrays (the SV taper), clipped to the grid.
 __global__ void k_box3d(Grid3D g, float *e2, float *d2, long x0, long y0, long z0, int B, const float *src) {
     const long n = (long)B * B * B;
     for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < n; k += (long)gridDim.x * blockDim.x) {
@@ -120,27 +41,35 @@ __global__ void k_box3d(Grid3D g, float *e2, float *d2, long x0, long y0, long z
 
 }  // namespace geo
 
+// Device state of one 3D grid.  Fields use the reference layout with the z
+// stride ldz rounded up to 4 floats (16 bytes, the TMA stride rule); points
+// iz >= nnz of a column are padding and never read or written.
 struct geo_fd3d_plan {
     geo_fd3d_desc d;
-    int nnx, nny, nnz;
-    size_t n;
+    int nnx, nny, nnz, ldz;
+    size_t n, nalloc;                  // padded points, allocated floats per field
     DevBuf vp, e2, d2, prof;
-    DevBuf u, v, w, P, Q, px, py, pz, qx, qy, qz;
-    DevBuf rec_tm, rec_tr, mute_hi, box;
+    DevBuf lev[2][5];                  // u v w P Q at two time levels
+    DevBuf px, py, pz, qx, qy, qz;
+    DevBuf rec_tm, rec_tr, mute_hi, box, err;
+    StepMaps maps[2];                  // reads of level 0 / level 1
+    int cur = 0;                       // level holding the current state
+    int chunk = 0, nitems = 0, ntz = 0, ntx = 0;
     std::vector<float> amp;
     std::vector<uint8_t> on;
-    std::vector<float> h_eps, h_del;   // padded raw eps/del, kept for the SV taper
+    std::vector<float> h_vp, h_eps, h_del;  // padded raw model, kept for the SV taper
     float vp1 = 0, eps1 = 0;           // padded model at linear index 1 (mute)
     bool model_set = false;
 };
 
 namespace geo {
 
+// Extents, profiles and current level of a plan.
 Grid3D make_grid(const geo_fd3d_plan *p) {
     Grid3D g;
     g.nnx = p->nnx; g.nny = p->nny; g.nnz = p->nnz;
-    g.ldz = p->nnz;
-    g.sxy = (long)p->nnz * p->nnx;
+    g.ldz = p->ldz;
+    g.sxy = (long)p->ldz * p->nnx;
     g.npd = p->d.npd;
     g.nx = p->d.nx; g.ny = p->d.ny; g.nz = p->d.nz;
     g.dtx = p->d.dt / p->d.dx;
@@ -152,31 +81,101 @@ Grid3D make_grid(const geo_fd3d_plan *p) {
     g.cy1 = pr + o; o += p->nny; g.cy2 = pr + o; o += p->nny; g.ay1 = pr + o; o += p->nny; g.ay2 = pr + o; o += p->nny;
     g.cz1 = pr + o; o += p->nnz; g.cz2 = pr + o; o += p->nnz; g.az1 = pr + o; o += p->nnz; g.az2 = pr + o;
     g.vp = p->vp.as<float>(); g.e2 = p->e2.as<float>(); g.d2 = p->d2.as<float>();
-    g.u = p->u.as<float>(); g.v = p->v.as<float>(); g.w = p->w.as<float>();
-    g.P = p->P.as<float>(); g.Q = p->Q.as<float>();
+    const int c = p->cur;
+    g.u = p->lev[c][0].as<float>(); g.v = p->lev[c][1].as<float>(); g.w = p->lev[c][2].as<float>();
+    g.P = p->lev[c][3].as<float>(); g.Q = p->lev[c][4].as<float>();
     g.px = p->px.as<float>(); g.py = p->py.as<float>(); g.pz = p->pz.as<float>();
     g.qx = p->qx.as<float>(); g.qy = p->qy.as<float>(); g.qz = p->qz.as<float>();
     return g;
 }
 
-static int step3d(const geo_fd3d_plan *p, const Grid3D &g, const StepArgs3D &st, cudaStream_t s) {
-    dim3 block(32, 8), grid((p->nnz + 31) / 32, (p->nnx + 7) / 8, p->nny);
-    k_vel3d<<<grid, block, 0, s>>>(g, st);
-    GEO_TRY(check_launch("vel3d"));
-    if (p->d.mode == GEO_MODE_FAST) k_stress3d<GEO_MODE_FAST><<<grid, block, 0, s>>>(g, st);
-    else k_stress3d<GEO_MODE_EXACT><<<grid, block, 0, s>>>(g, st);
-    return check_launch("stress3d");
+// Fused-kernel view: reads level cur (through the maps), writes level 1-cur.
+static Fused3D make_fused(const geo_fd3d_plan *p) {
+    const Grid3D g = make_grid(p);
+    Fused3D f;
+    f.nnx = g.nnx; f.nny = g.nny; f.nnz = g.nnz; f.ldz = g.ldz; f.sxy = g.sxy;
+    f.npd = g.npd; f.nx = g.nx; f.ny = g.ny; f.nz = g.nz;
+    f.dtx = g.dtx; f.dty = g.dty; f.dtz = g.dtz;
+    f.cx1 = g.cx1; f.cx2 = g.cx2; f.ax1 = g.ax1; f.ax2 = g.ax2;
+    f.cy1 = g.cy1; f.cy2 = g.cy2; f.ay1 = g.ay1; f.ay2 = g.ay2;
+    f.cz1 = g.cz1; f.cz2 = g.cz2; f.az1 = g.az1; f.az2 = g.az2;
+    f.m0 = g.vp; f.m1 = g.e2; f.m2 = g.d2;
+    f.P0 = g.P; f.Q0 = g.Q;
+    const int n = 1 - p->cur;
+    f.u1 = p->lev[n][0].as<float>(); f.v1 = p->lev[n][1].as<float>(); f.w1 = p->lev[n][2].as<float>();
+    f.P1 = p->lev[n][3].as<float>(); f.Q1 = p->lev[n][4].as<float>();
+    f.px = g.px; f.py = g.py; f.pz = g.pz; f.qx = g.qx; f.qy = g.qy; f.qz = g.qz;
+    f.ntz = p->ntz; f.ntx = p->ntx; f.ntiles = p->ntz * p->ntx; f.chunk = p->chunk; f.nitems = p->nitems;
+    f.err = p->err.as<int>();
+    return f;
+}
+
+static int build_maps(geo_fd3d_plan *p) {
+    for (int c = 0; c < 2; c++) {
+        StepMaps &M = p->maps[c];
+        const int nz = p->nnz, ld = p->ldz, nx = p->nnx, ny = p->nny;
+        GEO_TRY(encode_map(&M.m[0], p->lev[c][3].as<float>(), nz, ld, nx, ny, kTZ, kTXF + 14));  // P
+        GEO_TRY(encode_map(&M.m[1], p->lev[c][4].as<float>(), nz, ld, nx, ny, 48, kTXF));        // Q
+        GEO_TRY(encode_map(&M.m[2], p->lev[c][0].as<float>(), nz, ld, nx, ny, kTZ, kTXF + 8));   // u
+        GEO_TRY(encode_map(&M.m[3], p->lev[c][2].as<float>(), nz, ld, nx, ny, 48, kTXF));        // w
+        GEO_TRY(encode_map(&M.m[4], p->lev[c][1].as<float>(), nz, ld, nx, ny, kTZ, kTXF));       // v
+    }
+    return GEO_OK;
+}
+
+// y chunking: whole waves of resident blocks against the 7 warm-up planes
+// each chunk recomputes.
+static void choose_chunks(geo_fd3d_plan *p) {
+    int dev = 0, sms = 152;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int slots = sms * 2, planes = p->nny - 8, ntiles = p->ntz * p->ntx;
+    int best_c = 1;
+    double best = -1;
+    for (int c = 1; c <= 16; c++) {
+        const int len = (planes + c - 1) / c;
+        if (len < 8) break;
+        const double waves = (double)ntiles * c / slots;
+        const double fill = waves / std::ceil(waves);
+        const double score = fill / (1.0 + 7.0 / len);
+        if (score > best + 1e-9) { best = score; best_c = c; }
+    }
+    if (const char *e = getenv("GEO_FD3D_CHUNKS")) best_c = std::max(1, atoi(e));
+    p->chunk = (planes + best_c - 1) / best_c;
+    p->nitems = ntiles * ((planes + p->chunk - 1) / p->chunk);
+}
+
+// One time step: the fused kernel reads level cur and writes level 1-cur.
+static int step3d(geo_fd3d_plan *p, const StepArgs3D &st, cudaStream_t s) {
+    const Fused3D f = make_fused(p);
+    GEO_TRY(launch_fused3d(p->maps[p->cur], f, p->d.mode, st.it, st.src_on, st.amp, st.ixs, st.iys, st.izs, st.rec,
+                           st.rec_iz, st.rx0, st.drx, st.nrx, st.ry0, st.dry, st.nry, s));
+    p->cur ^= 1;
+    return GEO_OK;
 }
 
 static int zero_state(geo_fd3d_plan *p, cudaStream_t s) {
-    DevBuf *f[] = {&p->u, &p->v, &p->w, &p->P, &p->Q, &p->px, &p->py, &p->pz, &p->qx, &p->qy, &p->qz};
+    for (int c = 0; c < 2; c++)
+        for (int k = 0; k < 5; k++) GEO_TRY(p->lev[c][k].zero(s));
+    DevBuf *f[] = {&p->px, &p->py, &p->pz, &p->qx, &p->qy, &p->qz};
     for (DevBuf *b : f) GEO_TRY(b->zero(s));
+    GEO_TRY(p->err.zero(s));
+    p->cur = 0;
+    return GEO_OK;
+}
+
+static int check_err(geo_fd3d_plan *p, cudaStream_t s) {
+    int e = 0;
+    GEO_CUDA(cudaMemcpyAsync(&e, p->err.p, 4, cudaMemcpyDeviceToHost, s));
+    GEO_CUDA(cudaStreamSynchronize(s));
+    if (e) return fail(GEO_ERR_CUDA, "3D step: a TMA pipeline stage timed out");
     return GEO_OK;
 }
 
 // SV taper box for shot `is` (GPU_vti3dfd_kernels.cu:155-174: R=15, r=4,
 // centre fs+is*ds+npml-1): tapered=true writes the tapered coefficients,
-// false restores the untapered ones.
+// false restores the untapered ones.  Exact mode holds 1+2eps and
+// sqrtf(1+2del); fast mode A = vp^2(1+2eps) and B = vp^2 sqrtf(1+2del).
 static int taper_box_3d(geo_fd3d_plan *p, int is, bool tapered, cudaStream_t s) {
     const geo_fd3d_desc &D = p->d;
     const long cx = D.fsx + (long)is * D.dsx + D.npd - 1, cy = D.fsy + (long)is * D.dsy + D.npd - 1,
@@ -204,14 +203,23 @@ static int taper_box_3d(geo_fd3d_plan *p, int is, bool tapered, cudaStream_t s) 
                     }
                 }
                 const long k = bz + (long)B * (bx + (long)B * by);
-                h[k] = 1 + 2 * ee;
-                h[n + k] = sqrtf(1 + 2 * dd);
+                const float e2 = 1 + 2 * ee, d2 = sqrtf(1 + 2 * dd);
+                if (p->d.mode == GEO_MODE_FAST) {
+                    const float c2 = p->h_vp[id] * p->h_vp[id];
+                    h[k] = c2 * e2;
+                    h[n + k] = c2 * d2;
+                } else {
+                    h[k] = e2;
+                    h[n + k] = d2;
+                }
             }
     GEO_CUDA(cudaMemcpyAsync(p->box.p, h.data(), h.size() * 4, cudaMemcpyHostToDevice, s));
     Grid3D g = make_grid(p);
-    k_box3d<<<(int)((n + 255) / 256), 256, 0, s>>>(g, p->e2.as<float>(), p->d2.as<float>(), cx - 15, cy - 15, cz - 15, B,
-                                                 p->box.as<float>());
+    float *a0 = p->d.mode == GEO_MODE_FAST ? p->vp.as<float>() : p->e2.as<float>();
+    float *a1 = p->d.mode == GEO_MODE_FAST ? p->e2.as<float>() : p->d2.as<float>();
+    k_box3d<<<(int)((n + 255) / 256), 256, 0, s>>>(g, a0, a1, cx - 15, cy - 15, cz - 15, B, p->box.as<float>());
     GEO_TRY(check_launch("box3d"));
+    GEO_CUDA(cudaStreamSynchronize(s));  // h goes out of scope
     return GEO_OK;
 }
 
@@ -226,20 +234,20 @@ int run_shot_3d(geo_fd3d_plan *p, int is, cudaStream_t s, int (*on_step)(void *,
         return fail(GEO_ERR_ARG, "source outside the updated grid");
     GEO_TRY(zero_state(p, s));
     if (D.sv) GEO_TRY(taper_box_3d(p, is, true, s));
-    Grid3D g = make_grid(p);
     StepArgs3D st{};
     st.ixs = (int)ixs; st.iys = (int)iys; st.izs = (int)izs;
-    st.src = izs + (long)p->nnz * (ixs + (long)p->nnx * iys);
+    st.src = izs + (long)p->ldz * (ixs + (long)p->nnx * iys);
     st.rec = p->rec_tm.as<float>();
     st.rec_iz = D.rec_iz; st.rx0 = D.rx0; st.drx = D.drx; st.nrx = D.nrx; st.ry0 = D.ry0; st.dry = D.dry; st.nry = D.nry;
     for (int it = 0; it < D.nt; it++) {
         st.it = it;
         st.src_on = p->on[it];
         st.amp = p->amp[it];
-        GEO_TRY(step3d(p, g, st, s));
+        GEO_TRY(step3d(p, st, s));
         if (on_step) GEO_TRY(on_step(ctx, it));
     }
     if (D.sv) GEO_TRY(taper_box_3d(p, is, false, s));
+    GEO_TRY(check_err(p, s));
     const int ntr = D.nrx * D.nry;
     if (D.mute_tt > 0) {
         std::vector<int> hi;
@@ -248,13 +256,27 @@ int run_shot_3d(geo_fd3d_plan *p, int is, cudaStream_t s, int (*on_step)(void *,
                        p->vp1, p->eps1, D.mute_tt, hi);
         GEO_CUDA(cudaMemcpyAsync(p->mute_hi.p, hi.data(), hi.size() * 4, cudaMemcpyHostToDevice, s));
         GEO_TRY(launch_mute_records(p->rec_tm.as<float>(), ntr, D.nt, nullptr, p->mute_hi.as<int>(), s));
+        GEO_CUDA(cudaStreamSynchronize(s));
     }
     return GEO_OK;
 }
 
-const float *plan3d_P(const geo_fd3d_plan *p) { return p->P.as<float>(); }
 int plan3d_dims(const geo_fd3d_plan *p, int *nnx, int *nny, int *nnz) {
     *nnx = p->nnx; *nny = p->nny; *nnz = p->nnz;
+    return GEO_OK;
+}
+
+// Transpose the time-major record into the caller's trace-major buffer.
+int fetch_shot_3d(geo_fd3d_plan *p, float *shot, int mem, cudaStream_t s) {
+    const int ntr = p->d.nrx * p->d.nry;
+    const size_t bytes = (size_t)ntr * p->d.nt * 4;
+    if (mem == GEO_MEM_DEVICE) {
+        GEO_TRY(launch_transpose_records(p->rec_tm.as<float>(), shot, ntr, p->d.nt, s));
+    } else {
+        GEO_TRY(launch_transpose_records(p->rec_tm.as<float>(), p->rec_tr.as<float>(), ntr, p->d.nt, s));
+        GEO_CUDA(cudaMemcpyAsync(shot, p->rec_tr.p, bytes, cudaMemcpyDeviceToHost, s));
+    }
+    GEO_CUDA(cudaStreamSynchronize(s));
     return GEO_OK;
 }
 
@@ -277,22 +299,31 @@ extern "C" int geo_fd3d_plan_create(geo_fd3d_plan **out, const geo_fd3d_desc *de
     p->nnx = d.nx + 2 * d.npd;
     p->nny = d.ny + 2 * d.npd;
     p->nnz = d.nz + 2 * d.npd;
+    p->ldz = (p->nnz + 3) & ~3;
     p->n = (size_t)p->nnx * p->nny * p->nnz;
-    const size_t n = p->n, ntr = (size_t)d.nrx * d.nry;
+    p->nalloc = (size_t)p->nnx * p->nny * p->ldz;
+    p->ntz = (p->nnz + kTZ - 1) / kTZ;
+    p->ntx = (p->nnx + kTXF - 1) / kTXF;
+    const size_t n = p->nalloc, ntr = (size_t)d.nrx * d.nry;
     int st = GEO_OK;
-    DevBuf *fields[] = {&p->vp, &p->e2, &p->d2, &p->u, &p->v, &p->w, &p->P, &p->Q,
-                        &p->px, &p->py, &p->pz, &p->qx, &p->qy, &p->qz};
+    DevBuf *fields[] = {&p->vp, &p->e2, &p->d2, &p->px, &p->py, &p->pz, &p->qx, &p->qy, &p->qz};
     for (DevBuf *b : fields)
         if (st == GEO_OK) st = b->alloc(n * 4);
+    for (int c = 0; c < 2; c++)
+        for (int k = 0; k < 5; k++)
+            if (st == GEO_OK) st = p->lev[c][k].alloc(n * 4);
     if (st == GEO_OK) st = p->prof.alloc((size_t)4 * (p->nnx + p->nny + p->nnz) * 4);
     if (st == GEO_OK) st = p->rec_tm.alloc(ntr * d.nt * 4);
     if (st == GEO_OK) st = p->rec_tr.alloc(ntr * d.nt * 4);
     if (st == GEO_OK) st = p->mute_hi.alloc(ntr * 4);
     if (st == GEO_OK) st = p->box.alloc((size_t)2 * 31 * 31 * 31 * 4);
+    if (st == GEO_OK) st = p->err.alloc(16);
+    if (st == GEO_OK) st = build_maps(p);
     if (st != GEO_OK) {
         delete p;
         return st;
     }
+    choose_chunks(p);
     source_amplitudes(V_GPU, d.nt, d.dt, d.favg, d.pfac, d.wtype, p->amp, p->on);
     *out = p;
     return GEO_OK;
@@ -300,6 +331,13 @@ extern "C" int geo_fd3d_plan_create(geo_fd3d_plan **out, const geo_fd3d_desc *de
 
 extern "C" int geo_fd3d_plan_destroy(geo_fd3d_plan *p) {
     delete p;
+    return GEO_OK;
+}
+
+// Copy a padded nnz-contiguous host volume into an ldz-strided device field.
+static int upload_pitched(geo_fd3d_plan *p, DevBuf &dst, const float *src, cudaStream_t s) {
+    GEO_CUDA(cudaMemcpy2DAsync(dst.p, (size_t)p->ldz * 4, src, (size_t)p->nnz * 4, (size_t)p->nnz * 4,
+                               (size_t)p->nnx * p->nny, cudaMemcpyHostToDevice, s));
     return GEO_OK;
 }
 
@@ -339,38 +377,32 @@ extern "C" int geo_fd3d_set_model(geo_fd3d_plan *p, const float *v, const float 
     q += 4 * p->nny;
     sponge_profiles(V_GPU, D.nz, D.npd, D.dt, d0, q, q + p->nnz, q + 2 * p->nnz, q + 3 * p->nnz);
     if (D.sv) {
+        p->h_vp = pv;
         p->h_eps = pe;
         p->h_del = pd;
     }
-    // 1+2*eps and sqrtf(1+2*del) in float, as the stress kernel forms them
+    // exact: vp, 1+2eps, sqrtf(1+2del) in float, as the reference forms them;
+    // fast: A = vp^2(1+2eps), B = vp^2 sqrtf(1+2del), C = vp^2
     for (size_t k = 0; k < p->n; k++) {
-        pe[k] = 1 + 2 * pe[k];
-        pd[k] = sqrtf(1 + 2 * pd[k]);
+        const float e2 = 1 + 2 * pe[k], d2 = sqrtf(1 + 2 * pd[k]);
+        if (D.mode == GEO_MODE_FAST) {
+            const float c2 = pv[k] * pv[k];
+            pv[k] = c2 * e2;
+            pe[k] = c2 * d2;
+            pd[k] = c2;
+        } else {
+            pe[k] = e2;
+            pd[k] = d2;
+        }
     }
-    GEO_CUDA(cudaMemcpyAsync(p->vp.p, pv.data(), p->n * 4, cudaMemcpyHostToDevice, s));
-    GEO_CUDA(cudaMemcpyAsync(p->e2.p, pe.data(), p->n * 4, cudaMemcpyHostToDevice, s));
-    GEO_CUDA(cudaMemcpyAsync(p->d2.p, pd.data(), p->n * 4, cudaMemcpyHostToDevice, s));
+    GEO_TRY(upload_pitched(p, p->vp, pv.data(), s));
+    GEO_TRY(upload_pitched(p, p->e2, pe.data(), s));
+    GEO_TRY(upload_pitched(p, p->d2, pd.data(), s));
     GEO_CUDA(cudaMemcpyAsync(p->prof.p, prof.data(), prof.size() * 4, cudaMemcpyHostToDevice, s));
     GEO_CUDA(cudaStreamSynchronize(s));
     p->model_set = true;
     return GEO_OK;
 }
-
-namespace geo {
-// Transpose the time-major record into the caller's trace-major buffer.
-int fetch_shot_3d(geo_fd3d_plan *p, float *shot, int mem, cudaStream_t s) {
-    const int ntr = p->d.nrx * p->d.nry;
-    const size_t bytes = (size_t)ntr * p->d.nt * 4;
-    if (mem == GEO_MEM_DEVICE) {
-        GEO_TRY(launch_transpose_records(p->rec_tm.as<float>(), shot, ntr, p->d.nt, s));
-    } else {
-        GEO_TRY(launch_transpose_records(p->rec_tm.as<float>(), p->rec_tr.as<float>(), ntr, p->d.nt, s));
-        GEO_CUDA(cudaMemcpyAsync(shot, p->rec_tr.p, bytes, cudaMemcpyDeviceToHost, s));
-    }
-    GEO_CUDA(cudaStreamSynchronize(s));
-    return GEO_OK;
-}
-}  // namespace geo
 
 extern "C" int geo_fd3d_run_shot(geo_fd3d_plan *p, int is, float *shot, int mem, void *stream) {
     if (!p || !shot) return fail(GEO_ERR_ARG, "null argument");
@@ -383,14 +415,16 @@ extern "C" int geo_fd3d_run_shot(geo_fd3d_plan *p, int is, float *shot, int mem,
 extern "C" int geo_fd3d_time_steps(geo_fd3d_plan *p, int nsteps, float *ms, void *stream) {
     if (!p || nsteps < 1) return fail(GEO_ERR_ARG, "bad argument");
     cudaStream_t s = (cudaStream_t)stream;
-    Grid3D g = make_grid(p);
     StepArgs3D st{};
-    st.src = -1;
+    st.ixs = st.iys = st.izs = 0;
     cudaEvent_t a, b;
     GEO_CUDA(cudaEventCreate(&a));
     GEO_CUDA(cudaEventCreate(&b));
     GEO_CUDA(cudaEventRecord(a, s));
-    for (int k = 0; k < nsteps; k++) GEO_TRY(step3d(p, g, st, s));
+    for (int k = 0; k < nsteps; k++) {
+        st.it = k;
+        GEO_TRY(step3d(p, st, s));
+    }
     GEO_CUDA(cudaEventRecord(b, s));
     GEO_CUDA(cudaEventSynchronize(b));
     float t = 0;
@@ -398,15 +432,18 @@ extern "C" int geo_fd3d_time_steps(geo_fd3d_plan *p, int nsteps, float *ms, void
     cudaEventDestroy(a);
     cudaEventDestroy(b);
     if (ms) *ms = t;
-    return GEO_OK;
+    return check_err(p, s);
 }
 
 extern "C" int geo_fd3d_get_fields(geo_fd3d_plan *p, float *P, float *Q, int mem, void *stream) {
     if (!p) return fail(GEO_ERR_ARG, "null plan");
     cudaStream_t s = (cudaStream_t)stream;
     const cudaMemcpyKind k = mem == GEO_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
-    if (P) GEO_CUDA(cudaMemcpyAsync(P, p->P.p, p->n * 4, k, s));
-    if (Q) GEO_CUDA(cudaMemcpyAsync(Q, p->Q.p, p->n * 4, k, s));
+    float *dst[2] = {P, Q};
+    for (int f = 0; f < 2; f++)
+        if (dst[f])
+            GEO_CUDA(cudaMemcpy2DAsync(dst[f], (size_t)p->nnz * 4, p->lev[p->cur][3 + f].p, (size_t)p->ldz * 4,
+                                       (size_t)p->nnz * 4, (size_t)p->nnx * p->nny, k, s));
     GEO_CUDA(cudaStreamSynchronize(s));
     return GEO_OK;
 }

@@ -7,7 +7,7 @@ struct geo_fd3d_plan;
 namespace geo {
 
 struct Grid3D {
-    int nnx, nny, nnz, ldz;     // padded extents; ldz = z stride (== nnz)
+    int nnx, nny, nnz, ldz;     // padded extents; ldz = z stride (nnz rounded up to 4)
     long sxy;                   // y stride
     int npd, nx, ny, nz;        // sponge width and interior extents
     float dtx, dty, dtz;        // dt/dx etc. (float division, as the reference)
@@ -29,7 +29,6 @@ struct StepArgs3D {
 
 Grid3D make_grid(const geo_fd3d_plan *p);
 int run_shot_3d(geo_fd3d_plan *p, int is, cudaStream_t s, int (*on_step)(void *, int), void *ctx);
-const float *plan3d_P(const geo_fd3d_plan *p);
 int fetch_shot_3d(geo_fd3d_plan *p, float *shot, int mem, cudaStream_t s);
 int plan3d_dims(const geo_fd3d_plan *p, int *nnx, int *nny, int *nnz);
 

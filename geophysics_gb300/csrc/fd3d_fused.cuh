@@ -1,0 +1,50 @@
+// Fused 3D VTI time step: shared declarations between the plan (fd3d.cu)
+// and the y-marching TMA kernel (fd3d_fused.cu).
+#pragma once
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+namespace geo {
+
+// Tensor maps of one step's reads: 0 P (ring box), 1 Q (z-halo box),
+// 2 u (x-halo box), 3 w (z-halo box), 4 v (own box).
+constexpr int kNumMaps = 5;
+struct StepMaps {
+    CUtensorMap m[kNumMaps];
+};
+
+struct Fused3D {
+    int nnx, nny, nnz, ldz;
+    long sxy;
+    int npd, nx, ny, nz;
+    float dtx, dty, dtz;
+    const float *cx1, *cx2, *ax1, *ax2, *cy1, *cy2, *ay1, *ay2, *cz1, *cz2, *az1, *az2;
+    const float *m0, *m1, *m2;             // model: (vp, 1+2eps, sqrtf(1+2del)) exact,
+                                           //        (A, B, C) fast
+    const float *P0, *Q0;                  // current level (source cell)
+    float *u1, *v1, *w1, *P1, *Q1;         // next level
+    float *px, *py, *pz, *qx, *qy, *qz;    // split stresses (in place)
+    int ntz, ntx, ntiles, chunk, nitems;   // work decomposition
+    int *err;                              // device error word (wait timeouts)
+};
+
+// Tile and pipeline geometry.
+constexpr int kTZ = 32;                 // z points per tile (one warp's lanes)
+constexpr int kTXF = 16;                // x columns per tile (one warp each)
+constexpr int kStages = 4;              // TMA pipeline depth (planes)
+constexpr int kRing = 8 + kStages - 1;  // P planes resident
+constexpr int kPB = kTZ * (kTXF + 14);  // P box (z 32, x TX+14 from x0-7)
+constexpr int kQB = 48 * kTXF;          // Q / w box (z 48 from z0-8, x TX)
+constexpr int kUB = kTZ * (kTXF + 8);   // u box (z 32, x TX+8 from x0-4)
+constexpr int kOB = kTZ * kTXF;         // own box (z 32, x TX)
+constexpr int kStageFloats = kQB + kUB + kQB + kOB;   // Q, u, w, v
+constexpr int kUTile = (kTXF + 7) * kTZ;
+constexpr int kWTile = kTXF * 40;
+constexpr size_t kFusedSmem = (size_t)(kRing * kPB + kStages * kStageFloats + kUTile + kWTile) * 4 + 256;
+
+int launch_fused3d(const StepMaps &maps, const Fused3D &g, int mode, int it, int src_on, float amp, int ixs,
+                   int iys, int izs, float *rec, int rec_iz, int rx0, int drx, int nrx, int ry0, int dry, int nry,
+                   cudaStream_t s);
+int encode_map(CUtensorMap *map, const float *base, int nnz, int ldz, int nnx, int nny, int boxz, int boxx);
+
+}  // namespace geo

@@ -38,8 +38,10 @@
 
 #if defined(ORC_FP64)
 #define RSQRT(x) sqrt(x)
+#define RFMA(a, b, c) fma(a, b, c)
 #else
 #define RSQRT(x) sqrtf(x)
+#define RFMA(a, b, c) fmaf(a, b, c)
 #endif
 
 /* variant codes (which reference program's semantics) */
@@ -650,9 +652,11 @@ void orc_laplace3d_adj(int nz, int nx, int ny, const float *in, float *out)
 
 typedef struct {
     int nx, ny, nz, npd, nt, sv, wtype;
-    int mode;          /* 0: split sponge fields everywhere (the reference's
-                          arithmetic); 1: P,Q unsplit inside the physical box
-                          (the production fast path) */
+    int mode;          /* 0: split sponge fields everywhere, the reference's
+                          arithmetic; 1: the production fast path -- P,Q
+                          unsplit inside the physical box, fused multiply-adds
+                          at fixed places and the premultiplied model
+                          A=vp^2(1+2eps), B=vp^2 sqrtf(1+2del), C=vp^2 */
     float dx, dy, dz, dt, favg, pfac;
     int fsx, fsy, fsz, dsx, dsy, dsz, is;   /* is 0-based (GPU_vti3dfd_kernels.cu:113) */
     int rec_iz, rx0, drx, nrx, ry0, dry, nry;
@@ -713,11 +717,20 @@ int orc_fd3d(const orc_fd3d_desc *d, const float *v, const float *e, const float
     orc_sponge(ORC_V_GPU, d->nz, npd, d->dt, d0, cz1, cz2, az1, az2);
 
     REAL *vp = malloc(n * sizeof(REAL)), *e2 = malloc(n * sizeof(REAL)), *d2 = malloc(n * sizeof(REAL));
+    const int fast = d->mode == 1;
+    REAL *mA = fast ? malloc(n * sizeof(REAL)) : NULL, *mB = fast ? malloc(n * sizeof(REAL)) : NULL,
+         *mC = fast ? malloc(n * sizeof(REAL)) : NULL;
     long k;
     for (k = 0; k < n; k++) {
         vp[k] = vv[k];
         e2[k] = (REAL)1 + (REAL)2 * (REAL)ee[k];
         d2[k] = RSQRT((REAL)1 + (REAL)2 * (REAL)dd[k]);
+        if (fast) {
+            const REAL c2 = vp[k] * vp[k];
+            mA[k] = c2 * e2[k];
+            mB[k] = c2 * d2[k];
+            mC[k] = c2;
+        }
     }
     free(vv); free(ee); free(dd);
     REAL *u = calloc(n, sizeof(REAL)), *vv_ = calloc(n, sizeof(REAL)), *w = calloc(n, sizeof(REAL));
@@ -740,6 +753,20 @@ int orc_fd3d(const orc_fd3d_desc *d, const float *v, const float *e, const float
                 for (iz = 4; iz < nnz - 4; iz++) {
                     long id = iz + ix * nnz + iy * nxz; int im;
                     REAL xx = 0, yy = 0, zz = 0;
+                    if (fast) {
+                        yy = (REAL)C8[0] * (P[id + nxz] - P[id]);
+                        xx = (REAL)C8[0] * (P[id + nnz] - P[id]);
+                        zz = (REAL)C8[0] * (Q[id + 1] - Q[id]);
+                        for (im = 1; im < 4; im++) {
+                            yy = RFMA((REAL)C8[im], P[id + (im + 1) * nxz] - P[id - im * nxz], yy);
+                            xx = RFMA((REAL)C8[im], P[id + (im + 1) * nnz] - P[id - im * nnz], xx);
+                            zz = RFMA((REAL)C8[im], Q[id + im + 1] - Q[id - im], zz);
+                        }
+                        u[id] = RFMA(-(cx1[ix] * dtx), xx, cx2[ix] * u[id]);
+                        vv_[id] = RFMA(-(cy1[iy] * dty), yy, cy2[iy] * vv_[id]);
+                        w[id] = RFMA(-(cz1[iz] * dtz), zz, cz2[iz] * w[id]);
+                        continue;
+                    }
                     for (im = 0; im < 4; im++) {
                         yy += (REAL)C8[im] * (P[id + (im + 1) * nxz] - P[id - im * nxz]);
                         xx += (REAL)C8[im] * (P[id + (im + 1) * nnz] - P[id - im * nnz]);
@@ -755,6 +782,37 @@ int orc_fd3d(const orc_fd3d_desc *d, const float *v, const float *e, const float
                 for (iz = 4; iz < nnz - 4; iz++) {
                     long id = iz + ix * nnz + iy * nxz; int im;
                     REAL xx = 0, yy = 0, zz = 0, c = vp[id];
+                    if (fast) {
+                        /* premultiplied model: A = vp^2(1+2eps), B = vp^2 sqrtf(1+2del), C = vp^2 */
+                        const REAL A = mA[id], B = mB[id], Cc = mC[id];
+                        yy = (REAL)C8[0] * (vv_[id] - vv_[id - nxz]);
+                        xx = (REAL)C8[0] * (u[id] - u[id - nnz]);
+                        zz = (REAL)C8[0] * (w[id] - w[id - 1]);
+                        for (im = 1; im < 4; im++) {
+                            yy = RFMA((REAL)C8[im], vv_[id + im * nxz] - vv_[id - (im + 1) * nxz], yy);
+                            xx = RFMA((REAL)C8[im], u[id + im * nnz] - u[id - (im + 1) * nnz], xx);
+                            zz = RFMA((REAL)C8[im], w[id + im] - w[id - im - 1], zz);
+                        }
+                        const REAL Ax = A * dtx, Ay = A * dty, Bz = B * dtz, Bx = B * dtx, By = B * dty, Cz = Cc * dtz;
+                        int inside = ix >= npd && ix < npd + d->nx && iy >= npd && iy < npd + d->ny
+                                     && iz >= npd && iz < npd + d->nz;
+                        if (inside) {
+                            REAL p0 = (id == src) ? P_src0 : P[id], q0 = (id == src) ? Q_src0 : Q[id];
+                            p0 = RFMA(-Ax, xx, p0); p0 = RFMA(-Ay, yy, p0); p0 = RFMA(-Bz, zz, p0);
+                            q0 = RFMA(-Bx, xx, q0); q0 = RFMA(-By, yy, q0); q0 = RFMA(-Cz, zz, q0);
+                            P[id] = p0; Q[id] = q0;
+                        } else {
+                            px[id] = RFMA(-(ax1[ix] * Ax), xx, ax2[ix] * px[id]);
+                            py[id] = RFMA(-(ay1[iy] * Ay), yy, ay2[iy] * py[id]);
+                            pz[id] = RFMA(-(az1[iz] * Bz), zz, az2[iz] * pz[id]);
+                            qx[id] = RFMA(-(ax1[ix] * Bx), xx, ax2[ix] * qx[id]);
+                            qy[id] = RFMA(-(ay1[iy] * By), yy, ay2[iy] * qy[id]);
+                            qz[id] = RFMA(-(az1[iz] * Cz), zz, az2[iz] * qz[id]);
+                            P[id] = px[id] + py[id] + pz[id];
+                            Q[id] = qx[id] + qy[id] + qz[id];
+                        }
+                        continue;
+                    }
                     for (im = 0; im < 4; im++) {
                         yy += (REAL)C8[im] * (vv_[id + im * nxz] - vv_[id - (im + 1) * nxz]);
                         xx += (REAL)C8[im] * (u[id + im * nnz] - u[id - (im + 1) * nnz]);
@@ -792,6 +850,7 @@ int orc_fd3d(const orc_fd3d_desc *d, const float *v, const float *e, const float
     free(cz1); free(cz2); free(az1); free(az2);
     free(vp); free(e2); free(d2); free(u); free(vv_); free(w); free(P); free(Q);
     free(px); free(py); free(pz); free(qx); free(qy); free(qz); free(amp); free(act);
+    free(mA); free(mB); free(mC);
     return 0;
 }
 

@@ -56,3 +56,18 @@ def test_fd3d_dropin(geo, orc, tmp_path):
     orc.lib().orc_mute3d(16, 14, 120, np.float32(1e-3), 25.0, 10.0, 10.0, 10.0, 8, 7, 0, 0, 2, 0,
                          np.float32(v[0, 0, 0]), np.float32(e[0, 0, 0]), 100, ref.ctypes.data_as(C.POINTER(C.c_float)))
     assert np.array_equal(shot, ref)
+
+
+@pytest.mark.parametrize("chunks", ["1", "3"])
+@pytest.mark.parametrize("shape", [(21, 19, 27), (34, 17, 45)])
+def test_fd3d_chunks_and_ragged_extents(geo, orc, monkeypatch, chunks, shape):
+    """y split into chunks (warm-up planes recomputed per chunk) and z
+    extents whose padded length is not a multiple of 4 (padded z stride)."""
+    monkeypatch.setenv("GEO_FD3D_CHUNKS", chunks)
+    ny, nx, nz = shape
+    v, e, d = random_model_3d(nx, ny, nz, seed=11)
+    kw = dict(KW, npd=7, fsx=nx // 2, fsy=ny // 2, fsz=4)
+    for mode in (0, 1):
+        ref = orc.fd3d(v, e, d, mode=mode, **kw)
+        out = geo.fd3d_shot(v, e, d, mode=mode, **kw)
+        assert np.array_equal(out, ref), (mode, rel_l2(out, ref))
