@@ -114,11 +114,14 @@ static int build_maps(geo_fd3d_plan *p) {
     for (int c = 0; c < 2; c++) {
         StepMaps &M = p->maps[c];
         const int nz = p->nnz, ld = p->ldz, nx = p->nnx, ny = p->nny;
-        GEO_TRY(encode_map(&M.m[0], p->lev[c][3].as<float>(), nz, ld, nx, ny, kTZ, kTXF + 14));  // P
-        GEO_TRY(encode_map(&M.m[1], p->lev[c][4].as<float>(), nz, ld, nx, ny, 48, kTXF));        // Q
-        GEO_TRY(encode_map(&M.m[2], p->lev[c][0].as<float>(), nz, ld, nx, ny, kTZ, kTXF + 8));   // u
-        GEO_TRY(encode_map(&M.m[3], p->lev[c][2].as<float>(), nz, ld, nx, ny, 48, kTXF));        // w
-        GEO_TRY(encode_map(&M.m[4], p->lev[c][1].as<float>(), nz, ld, nx, ny, kTZ, kTXF));       // v
+        GEO_TRY(encode_map(&M.m[0], p->lev[c][3].as<float>(), nz, ld, nx, ny, kTZ, kTXF + 14));  // P halo
+        GEO_TRY(encode_map(&M.m[1], p->lev[c][3].as<float>(), nz, ld, nx, ny, kTZ, kTXF));       // P own
+        GEO_TRY(encode_map(&M.m[2], p->lev[c][4].as<float>(), nz, ld, nx, ny, 48, kTXF));        // Q
+        GEO_TRY(encode_map(&M.m[3], p->lev[c][0].as<float>(), nz, ld, nx, ny, kTZ, kTXF + 8));   // u
+        GEO_TRY(encode_map(&M.m[4], p->lev[c][2].as<float>(), nz, ld, nx, ny, 48, kTXF));        // w
+        GEO_TRY(encode_map(&M.m[5], p->lev[c][1].as<float>(), nz, ld, nx, ny, kTZ, kTXF));       // v
+        const DevBuf *own[9] = {&p->vp, &p->e2, &p->d2, &p->px, &p->py, &p->pz, &p->qx, &p->qy, &p->qz};
+        for (int r = 0; r < 9; r++) GEO_TRY(encode_map(&M.m[6 + r], own[r]->as<float>(), nz, ld, nx, ny, kTZ, kTXF));
     }
     return GEO_OK;
 }
@@ -129,7 +132,7 @@ static void choose_chunks(geo_fd3d_plan *p) {
     int dev = 0, sms = 152;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const int slots = sms * 2, planes = p->nny - 8, ntiles = p->ntz * p->ntx;
+    const int slots = sms * 2, planes = p->nny - 8, ntiles = p->ntz * p->ntx;  // 2 blocks per SM
     int best_c = 1;
     double best = -1;
     for (int c = 1; c <= 16; c++) {
@@ -137,7 +140,7 @@ static void choose_chunks(geo_fd3d_plan *p) {
         if (len < 8) break;
         const double waves = (double)ntiles * c / slots;
         const double fill = waves / std::ceil(waves);
-        const double score = fill / (1.0 + 7.0 / len);
+        const double score = fill / (1.0 + 14.0 / len);
         if (score > best + 1e-9) { best = score; best_c = c; }
     }
     if (const char *e = getenv("GEO_FD3D_CHUNKS")) best_c = std::max(1, atoi(e));
@@ -302,6 +305,10 @@ extern "C" int geo_fd3d_plan_create(geo_fd3d_plan **out, const geo_fd3d_desc *de
     p->ldz = (p->nnz + 3) & ~3;
     p->n = (size_t)p->nnx * p->nny * p->nnz;
     p->nalloc = (size_t)p->nnx * p->nny * p->ldz;
+    if (p->nalloc >= (size_t)1 << 31) {
+        delete p;
+        return fail(GEO_ERR_ARG, "grid of %zu points per field exceeds 2^31", (size_t)d.nx * d.ny * d.nz);
+    }
     p->ntz = (p->nnz + kTZ - 1) / kTZ;
     p->ntx = (p->nnx + kTXF - 1) / kTXF;
     const size_t n = p->nalloc, ntr = (size_t)d.nrx * d.nry;

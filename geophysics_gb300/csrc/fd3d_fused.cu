@@ -28,15 +28,20 @@ namespace geo {
 __constant__ float cf_fd[4] = {1.196289f, -0.0797526f, 0.009570313f, -0.0006975447f};
 
 // stage layout (floats)
-constexpr int OFF_Q = 0;
+constexpr int OFF_PO = 0;                 // P own box, plane y+7
+constexpr int OFF_V = OFF_PO + kOB;       // v own box, plane y+3
+constexpr int OFF_PH = OFF_V + kOB;       // P x-halo box, stress plane
+constexpr int OFF_Q = OFF_PH + kPB;
 constexpr int OFF_U = OFF_Q + kQB;
 constexpr int OFF_W = OFF_U + kUB;
-constexpr int OFF_V = OFF_W + kQB;
-static_assert(OFF_V + kOB == kStageFloats, "stage layout");
-static_assert((OFF_U * 4) % 128 == 0 && (OFF_W * 4) % 128 == 0 && (OFF_V * 4) % 128 == 0 &&
-                  (kStageFloats * 4) % 128 == 0 && (kPB * 4) % 128 == 0,
+constexpr int OFF_M = OFF_W + kQB;        // vp,e2,d2 or A,B,C
+constexpr int OFF_S = OFF_M + 3 * kOB;    // px py pz qx qy qz
+static_assert(OFF_S + 6 * kOB == kStageFloats, "stage layout");
+static_assert((OFF_V * 4) % 128 == 0 && (OFF_PH * 4) % 128 == 0 && (OFF_Q * 4) % 128 == 0 &&
+                  (OFF_U * 4) % 128 == 0 && (OFF_W * 4) % 128 == 0 && (OFF_M * 4) % 128 == 0 &&
+                  (OFF_S * 4) % 128 == 0 && (kStageFloats * 4) % 128 == 0,
               "TMA destinations must stay 128-byte aligned");
-static_assert(kRing >= 9, "the new plane must not land on a tap of the current plane");
+static_assert(kFusedSmem * 2 + 2048 <= 233472, "two blocks per SM must fit in shared memory");
 
 __device__ __forceinline__ uint32_t su32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -52,7 +57,7 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
     uint32_t ok;
     asm volatile(
         "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, 1000000;\n\t"
         "selp.u32 %0, 1, 0, p;\n\t}"
         : "=r"(ok)
         : "r"(su32(bar)), "r"(parity)
@@ -121,25 +126,29 @@ __device__ __forceinline__ float dline_bwd(const float *p, int s) {
 }
 
 template <int MODE>
-__global__ void __launch_bounds__(kTZ *kTXF, 2)
+__global__ void __launch_bounds__(kTZ *kWarps, 2)
     k_fused3d(const __grid_constant__ StepMaps tm, const Fused3D g, const StepArgs3D st) {
     extern __shared__ unsigned char smem_raw[];
     float *base = reinterpret_cast<float *>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
-    float *ring = base;
-    float *stages = ring + kRing * kPB;
+    float *stages = base;
     float *utile = stages + kStages * kStageFloats;
     float *wtile = utile + kUTile;
     uint64_t *bar = reinterpret_cast<uint64_t *>(wtile + kWTile);
     __shared__ int s_abort;
 
-    const int lane = threadIdx.x, wx = threadIdx.y, tid = wx * 32 + lane;
+    const int lane = threadIdx.x, wy = threadIdx.y, tid = wy * 32 + lane;
     const int tile = blockIdx.x % g.ntiles, chunk = blockIdx.x / g.ntiles;
     const int z0 = (tile % g.ntz) * kTZ, x0 = (tile / g.ntz) * kTXF;
     const int ylo = 4 + chunk * g.chunk;
     const int yhi = min(ylo + g.chunk, g.nny - 4);
-    const int NJ = (yhi - ylo) + 7;
-    const int ybase = ylo - 7;  // plane of iteration j is ybase + j
+    // iteration i brings P(ybase+i) into the queue, computes v(ybase+i-4)
+    // (i >= 7) and the stresses of plane ybase+i-7 (i >= 14)
+    const int ybase = ylo - 7;
+    const int NI = (yhi - ylo) + 14;
     const bool xz_inside = x0 >= g.npd && x0 + kTXF <= g.npd + g.nx && z0 >= g.npd && z0 + kTZ <= g.npd + g.nz;
+    auto needs_split = [&](int y) {
+        return MODE == GEO_MODE_EXACT || !xz_inside || y < g.npd || y >= g.npd + g.ny;
+    };
 
     if (tid == 0) {
         for (int s = 0; s < kStages; s++) mbar_init(&bar[s], 1);
@@ -148,71 +157,104 @@ __global__ void __launch_bounds__(kTZ *kTXF, 2)
     }
     __syncthreads();
 
-    // Loads of iteration j into stage j % kStages and ring slot (j+7) % kRing.
-    auto issue = [&](int j) {
-        const int s = j % kStages;
-        const int y = ybase + j;
+    // Loads of iteration i into stage i % kStages, spread over lane 0 of warps
+    // 0-3 (one per SM sub-partition).  The expected byte count may be posted
+    // after a copy completes: the phase cannot finish before warp 0 arrives.
+    auto issue = [&](int i) {
+        const int s = i % kStages;
+        const int y = ybase + i - 7;
         float *sp = stages + s * kStageFloats;
-        uint32_t bytes = (kPB + kOB) * 4;
-        if (j >= 7) bytes += (kQB + kUB + kQB) * 4;
-        if (j == 0) bytes += 7 * kPB * 4;
+        const bool sv = i >= 7, ss = i >= 14, split = ss && needs_split(y);
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        mbar_expect_tx(&bar[s], bytes);
-        if (j == 0)
-            for (int k = 0; k < 7; k++) tma3(ring + k * kPB, &tm.m[0], z0, x0 - 7, ybase + k, &bar[s]);
-        tma3(ring + ((j + 7) % kRing) * kPB, &tm.m[0], z0, x0 - 7, y + 7, &bar[s]);
-        tma3(sp + OFF_V, &tm.m[4], z0, x0, y + 3, &bar[s]);
-        if (j >= 7) {
-            tma3(sp + OFF_Q, &tm.m[1], z0 - 8, x0, y, &bar[s]);
-            tma3(sp + OFF_U, &tm.m[2], z0, x0 - 4, y, &bar[s]);
-            tma3(sp + OFF_W, &tm.m[3], z0 - 8, x0, y, &bar[s]);
+        if (wy == 0) {
+            uint32_t bytes = kOB * 4;
+            if (sv) bytes += kOB * 4;
+            if (ss) bytes += (kPB + kQB + kUB + kQB + 3 * kOB) * 4;
+            if (split) bytes += 6 * kOB * 4;
+            mbar_expect_tx(&bar[s], bytes);
+            tma3(sp + OFF_PO, &tm.m[1], z0, x0, ybase + i, &bar[s]);
+            if (sv) tma3(sp + OFF_V, &tm.m[5], z0, x0, y + 3, &bar[s]);
+        } else if (wy == 1) {
+            if (ss) {
+                tma3(sp + OFF_PH, &tm.m[0], z0, x0 - 7, y, &bar[s]);
+                tma3(sp + OFF_Q, &tm.m[2], z0 - 8, x0, y, &bar[s]);
+            }
+        } else if (wy == 2) {
+            if (ss) {
+                tma3(sp + OFF_U, &tm.m[3], z0, x0 - 4, y, &bar[s]);
+                tma3(sp + OFF_W, &tm.m[4], z0 - 8, x0, y, &bar[s]);
+                for (int r = 0; r < 3; r++) tma3(sp + OFF_M + r * kOB, &tm.m[6 + r], z0, x0, y, &bar[s]);
+            }
+        } else {
+            if (split)
+                for (int r = 0; r < 6; r++) tma3(sp + OFF_S + r * kOB, &tm.m[9 + r], z0, x0, y, &bar[s]);
         }
     };
-    if (tid == 0)
-        for (int j = 0; j < kStages && j < NJ; j++) issue(j);
+    if (lane == 0 && wy < 4)
+        for (int i = 0; i < kStages && i < NI; i++) issue(i);
 
-    // ---- per-thread constants
-    const int xo = x0 + wx, zo = z0 + lane;
-    const bool x_upd = xo >= 4 && xo < g.nnx - 4, z_upd = zo >= 4 && zo < g.nnz - 4;
-    const bool xz_upd = x_upd && z_upd;
-    const int xc = min(max(xo, 0), g.nnx - 1), zc = min(max(zo, 0), g.nnz - 1);
-    const float kx = g.cx1[xc] * g.dtx, cx2 = g.cx2[xc], ax1 = g.ax1[xc], ax2 = g.ax2[xc];
+    // ---- per-thread constants: columns ca = 2*wy and ca+1, depth zo
+    const int ca = 2 * wy, xa = x0 + ca, zo = z0 + lane;
+    const bool z_upd = zo >= 4 && zo < g.nnz - 4;
+    const bool upd_a = z_upd && xa >= 4 && xa < g.nnx - 4, upd_b = z_upd && xa + 1 >= 4 && xa + 1 < g.nnx - 4;
+    const bool z_in = zo >= g.npd && zo < g.npd + g.nz;
+    const bool in_a = z_in && xa >= g.npd && xa < g.npd + g.nx, in_b = z_in && xa + 1 >= g.npd && xa + 1 < g.npd + g.nx;
+    const int xca = min(max(xa, 0), g.nnx - 1), xcb = min(max(xa + 1, 0), g.nnx - 1), zc = min(max(zo, 0), g.nnz - 1);
+    const float kxa = g.cx1[xca] * g.dtx, cx2a = g.cx2[xca], ax1a = g.ax1[xca], ax2a = g.ax2[xca];
+    const float kxb = g.cx1[xcb] * g.dtx, cx2b = g.cx2[xcb], ax1b = g.ax1[xcb], ax2b = g.ax2[xcb];
     const float kz = g.cz1[zc] * g.dtz, cz2 = g.cz2[zc], az1 = g.az1[zc], az2 = g.az2[zc];
-    // halo velocities: warps 0-6 take u on the 7 halo columns (4 left, 3
-    // right of the tile), threads 224-335 take w on the 7 halo depths of each
-    // column (4 above, 3 below)
-    int h_col = 0, h_q = 0;
-    bool h_upd = false;
-    float hk = 0.0f, hc2 = 0.0f;
-    if (wx < 7) {
-        h_col = wx < 4 ? wx : kTXF + wx;  // utile / u-box column
-        const int x = x0 - 4 + h_col;
-        h_upd = x >= 4 && x < g.nnx - 4 && z_upd;
-        const int xcl = min(max(x, 0), g.nnx - 1);
-        hk = g.cx1[xcl] * g.dtx;
-        hc2 = g.cx2[xcl];
-    } else if (tid < 224 + 7 * kTXF) {
-        const int t = tid - 224;
-        h_col = t / 7;
-        const int h = t % 7;
-        h_q = h < 4 ? h : kTZ + h;  // wtile index (z0-4 origin)
-        const int z = z0 - 4 + h_q, x = x0 + h_col;
-        h_upd = z >= 4 && z < g.nnz - 4 && x >= 4 && x < g.nnx - 4;
-        const int zcl = min(max(z, 0), g.nnz - 1);
-        hk = g.cz1[zcl] * g.dtz;
-        hc2 = g.cz2[zcl];
+    // receiver traces along x (or -1)
+    int rec_a = -1, rec_b = -1;
+    if (st.rec && zo == st.rec_iz) {
+        const int ra = xa - g.npd - st.rx0, rb = ra + 1;
+        if (ra >= 0 && ra % st.drx == 0 && ra / st.drx < st.nrx) rec_a = ra / st.drx;
+        if (rb >= 0 && rb % st.drx == 0 && rb / st.drx < st.nrx) rec_b = rb / st.drx;
     }
-    const long ldz = g.ldz, sxy = g.sxy;
-    const long col_off = zo + ldz * xo;  // own column at y = 0
-    float q[8];
+    // halo velocities: items 0-223 are u on the 7 halo columns (4 left, 3
+    // right), items 224-335 w on the 7 halo depths of each column (4 above, 3
+    // below); thread t takes items t and t+256
+    int h1_idx = 0, h1_src = 0, h2_idx = 0, h2_src = 0;  // tile index, tap origin
+    bool h1_upd = false, h2_upd = false;
+    float h1k = 0, h1c2 = 0, h2k = 0, h2c2 = 0;
+    const bool h1_u = tid < 224, h2_on = tid + 256 < 224 + 7 * kTXF;
+    {
+        auto setup = [&](int h, int &idx, int &src, bool &upd, float &k, float &c2) {
+            if (h < 224) {
+                const int hc = h >> 5, hl = h & 31;
+                const int c = hc < 4 ? hc : kTXF + hc;  // u tile / u box column
+                const int x = x0 - 4 + c, z = z0 + hl;
+                upd = x >= 4 && x < g.nnx - 4 && z >= 4 && z < g.nnz - 4;
+                const int xcl = min(max(x, 0), g.nnx - 1);
+                k = g.cx1[xcl] * g.dtx;
+                c2 = g.cx2[xcl];
+                idx = c * 32 + hl;                 // u tile and u box
+                src = (c + 3) * 32 + hl;           // P halo box
+            } else {
+                const int t = h - 224, col = t / 7, hh = t % 7;
+                const int qz = hh < 4 ? hh : kTZ + hh;  // w tile index (z0-4 origin)
+                const int z = z0 - 4 + qz, x = x0 + col;
+                upd = z >= 4 && z < g.nnz - 4 && x >= 4 && x < g.nnx - 4;
+                const int zcl = min(max(z, 0), g.nnz - 1);
+                k = g.cz1[zcl] * g.dtz;
+                c2 = g.cz2[zcl];
+                idx = col * 40 + qz;               // w tile
+                src = col * 48 + qz + 4;           // Q / w box
+            }
+        };
+        setup(tid, h1_idx, h1_src, h1_upd, h1k, h1c2);
+        if (h2_on) setup(tid + 256, h2_idx, h2_src, h2_upd, h2k, h2c2);
+    }
+    // element offsets fit in 32 bits (checked on the host)
+    const int sxy = (int)g.sxy, ldz = g.ldz;
+    const int col_a = zo + ldz * xa;   // own columns at y = 0 (b = a + ldz)
+    const int oa = ca * 32 + lane;     // column a in an own box (b = +32)
+    float qa[8], qb[8], pa[8], pb[8];  // v(y-4 .. y+3), P(y .. y+7) per column
 #pragma unroll
-    for (int k = 0; k < 8; k++) q[k] = 0.0f;
+    for (int k = 0; k < 8; k++) qa[k] = qb[k] = pa[k] = pb[k] = 0.0f;
     uint32_t phase = 0;
-    int sj = 0;  // ring slot of plane ybase + j
 
-    for (int j = 0; j < NJ; j++) {
-        const int s = j % kStages;
-        const int y = ybase + j;
+    for (int i = 0; i < NI; i++) {
+        const int s = i % kStages;
         if (tid == 0 && !mbar_wait(&bar[s], (phase >> s) & 1u)) s_abort = 1;
         phase ^= 1u << s;
         __syncthreads();
@@ -228,140 +270,178 @@ __global__ void __launch_bounds__(kTZ *kTXF, 2)
             }
             return;
         }
-        // stage (j-1) % kStages and ring slot of plane ybase+j-1 are free now
-        if (tid == 0 && j >= 1 && j - 1 + kStages < NJ) issue(j - 1 + kStages);
+        // stage (i-1) % kStages is free now
+        if (lane == 0 && wy < 4 && i >= 1 && i - 1 + kStages < NI) issue(i - 1 + kStages);
         float *sp = stages + s * kStageFloats;
-        const long yoff = sxy * y;
-
-        // model and split stresses of this plane, consumed after the velocities
-        const bool stress_plane = j >= 7;
-        const bool need_split = MODE == GEO_MODE_EXACT || !xz_inside || y < g.npd || y >= g.npd + g.ny;
-        float m0 = 0, m1 = 0, m2 = 0, s0 = 0, s1 = 0, s2 = 0, s3 = 0, s4 = 0, s5 = 0;
-        if (stress_plane && xz_upd) {
-            const long id = col_off + yoff;
-            m0 = __ldg(g.m0 + id); m1 = __ldg(g.m1 + id); m2 = __ldg(g.m2 + id);
-            if (need_split) {
-                s0 = g.px[id]; s1 = g.py[id]; s2 = g.pz[id];
-                s3 = g.qx[id]; s4 = g.qy[id]; s5 = g.qz[id];
-            }
-        }
+        const int y = ybase + i - 7;           // stress plane
+        const bool stress_plane = i >= 14;
 
         // point source, P,Q += amp before the velocity update
-        // (GPU_vti3dfd_kernels.cu:135): patch the shared copies that hold the
+        // (GPU_vti3dfd_kernels.cu:135): patch the shared copies holding the
         // source cell; the own-point stress update reads P,Q from global.
         if (st.src_on) {
-            const int plo = (j == 0) ? ybase : y + 7;
-            const bool pP = st.iys >= plo && st.iys <= y + 7 && st.izs >= z0 && st.izs < z0 + kTZ &&
+            const bool pO = st.iys == ybase + i && st.izs >= z0 && st.izs < z0 + kTZ && st.ixs >= x0 &&
+                            st.ixs < x0 + kTXF;
+            const bool pH = stress_plane && st.iys == y && st.izs >= z0 && st.izs < z0 + kTZ &&
                             st.ixs >= x0 - 7 && st.ixs < x0 + kTXF + 7;
             const bool pQ = stress_plane && st.iys == y && st.ixs >= x0 && st.ixs < x0 + kTXF &&
                             st.izs >= z0 - 8 && st.izs < z0 + 40;
-            if (pP || pQ) {
+            if (pO || pH || pQ) {
                 if (tid == 0) {
-                    if (pP) ring[((st.iys - ybase) % kRing) * kPB + (st.ixs - (x0 - 7)) * 32 + (st.izs - z0)] += st.amp;
+                    if (pO) sp[OFF_PO + (st.ixs - x0) * 32 + (st.izs - z0)] += st.amp;
+                    if (pH) sp[OFF_PH + (st.ixs - (x0 - 7)) * 32 + (st.izs - z0)] += st.amp;
                     if (pQ) sp[OFF_Q + (st.ixs - x0) * 48 + (st.izs - (z0 - 8))] += st.amp;
+                    // these cells are later overwritten by the async proxy
+                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                 }
                 __syncthreads();
             }
         }
 
-        // slot of plane ybase + j + k
-        auto slot = [&](int k) { const int t = sj + k; return t >= kRing ? t - kRing : t; };
+        // own-column P queues
+#pragma unroll
+        for (int k = 0; k < 7; k++) {
+            pa[k] = pa[k + 1];
+            pb[k] = pb[k + 1];
+        }
+        pa[7] = sp[OFF_PO + oa];
+        pb[7] = sp[OFF_PO + oa + 32];
 
-        // v at plane y+3 from the ring (planes y .. y+7), into the queue
-        {
+        // v at plane yv = y+3 (taps P(yv-3 .. yv+4) = the queue), into the queues
+        if (i >= 7) {
             const int yv = y + 3;
-            const float vold = sp[OFF_V + wx * 32 + lane];
-            float vn = vold;
-            if (xz_upd && yv >= 4 && yv < g.nny - 4) {
-                const int col = (wx + 7) * 32 + lane;
-                const float yy = deriv<MODE>(ring[slot(4) * kPB + col], ring[slot(3) * kPB + col],
-                                             ring[slot(5) * kPB + col], ring[slot(2) * kPB + col],
-                                             ring[slot(6) * kPB + col], ring[slot(1) * kPB + col],
-                                             ring[slot(7) * kPB + col], ring[slot(0) * kPB + col]);
-                vn = vel_update<MODE>(g.cy2[yv], vold, g.cy1[yv] * g.dty, yy);
-                g.v1[col_off + sxy * yv] = vn;
+            const float va = sp[OFF_V + oa], vb = sp[OFF_V + oa + 32];
+            float vna = va, vnb = vb;
+            if (yv >= 4 && yv < g.nny - 4) {
+                const float ky = g.cy1[yv] * g.dty, cy2 = g.cy2[yv];
+                const int iv = col_a + sxy * yv;
+                if (upd_a) {
+                    vna = vel_update<MODE>(cy2, va, ky, deriv<MODE>(pa[4], pa[3], pa[5], pa[2], pa[6], pa[1], pa[7], pa[0]));
+                    g.v1[iv] = vna;
+                }
+                if (upd_b) {
+                    vnb = vel_update<MODE>(cy2, vb, ky, deriv<MODE>(pb[4], pb[3], pb[5], pb[2], pb[6], pb[1], pb[7], pb[0]));
+                    g.v1[iv + ldz] = vnb;
+                }
             }
 #pragma unroll
-            for (int k = 0; k < 7; k++) q[k] = q[k + 1];
-            q[7] = vn;
+            for (int k = 0; k < 7; k++) {
+                qa[k] = qa[k + 1];
+                qb[k] = qb[k + 1];
+            }
+            qa[7] = vna;
+            qb[7] = vnb;
         }
 
         if (stress_plane) {
-            const float *ry = ring + sj * kPB;
-            // own u (column wx+4 of the u tile) and own w (depth lane+4)
+            const float *ph = sp + OFF_PH;
+            const int yoff = sxy * y;
+            // own u at u-tile columns ca+4, ca+5 (P-halo columns ca+7, ca+8):
+            // taps on P-halo columns ca+4 .. ca+12, shared by the two
             {
-                const int c = wx + 4;
-                const float uo = sp[OFF_U + c * 32 + lane];
-                float un = uo;
-                if (xz_upd) {
-                    un = vel_update<MODE>(cx2, uo, kx, dline_fwd<MODE>(ry + (c + 3) * 32 + lane, 32));
-                    g.u1[col_off + yoff] = un;
+                float p[9];
+#pragma unroll
+                for (int k = 0; k < 9; k++) p[k] = ph[(ca + 4 + k) * 32 + lane];
+                const float uoa = sp[OFF_U + (ca + 4) * 32 + lane], uob = sp[OFF_U + (ca + 5) * 32 + lane];
+                float una = uoa, unb = uob;
+                const int iu = col_a + yoff;
+                if (upd_a) {
+                    una = vel_update<MODE>(cx2a, uoa, kxa, deriv<MODE>(p[4], p[3], p[5], p[2], p[6], p[1], p[7], p[0]));
+                    g.u1[iu] = una;
                 }
-                utile[c * 32 + lane] = un;
-                const float wo = sp[OFF_W + wx * 48 + lane + 8];
-                float wn = wo;
-                if (xz_upd) {
-                    wn = vel_update<MODE>(cz2, wo, kz, dline_fwd<MODE>(sp + OFF_Q + wx * 48 + lane + 8, 1));
-                    g.w1[col_off + yoff] = wn;
+                if (upd_b) {
+                    unb = vel_update<MODE>(cx2b, uob, kxb, deriv<MODE>(p[5], p[4], p[6], p[3], p[7], p[2], p[8], p[1]));
+                    g.u1[iu + ldz] = unb;
                 }
-                wtile[wx * 40 + lane + 4] = wn;
+                utile[(ca + 4) * 32 + lane] = una;
+                utile[(ca + 5) * 32 + lane] = unb;
+            }
+            // own w at depth lane+4 of columns ca, ca+1
+            {
+                const float *Qa = sp + OFF_Q + ca * 48 + lane + 8, *Qb = Qa + 48;
+                const float woa = sp[OFF_W + ca * 48 + lane + 8], wob = sp[OFF_W + ca * 48 + 48 + lane + 8];
+                float wna = woa, wnb = wob;
+                const int iw = col_a + yoff;
+                if (upd_a) {
+                    wna = vel_update<MODE>(cz2, woa, kz, dline_fwd<MODE>(Qa, 1));
+                    g.w1[iw] = wna;
+                }
+                if (upd_b) {
+                    wnb = vel_update<MODE>(cz2, wob, kz, dline_fwd<MODE>(Qb, 1));
+                    g.w1[iw + ldz] = wnb;
+                }
+                wtile[ca * 40 + lane + 4] = wna;
+                wtile[ca * 40 + 40 + lane + 4] = wnb;
             }
             // halo u and w
-            if (wx < 7) {
-                const float uo = sp[OFF_U + h_col * 32 + lane];
-                float un = uo;
-                if (h_upd) un = vel_update<MODE>(hc2, uo, hk, dline_fwd<MODE>(ry + (h_col + 3) * 32 + lane, 32));
-                utile[h_col * 32 + lane] = un;
-            } else if (tid < 224 + 7 * kTXF) {
-                const float wo = sp[OFF_W + h_col * 48 + h_q + 4];
-                float wn = wo;
-                if (h_upd) wn = vel_update<MODE>(hc2, wo, hk, dline_fwd<MODE>(sp + OFF_Q + h_col * 48 + h_q + 4, 1));
-                wtile[h_col * 40 + h_q] = wn;
+            {
+                if (h1_u) {
+                    const float uo = sp[OFF_U + h1_idx];
+                    utile[h1_idx] = h1_upd ? vel_update<MODE>(h1c2, uo, h1k, dline_fwd<MODE>(ph + h1_src, 32)) : uo;
+                } else {
+                    const float wo = sp[OFF_W + h1_src];
+                    wtile[h1_idx] = h1_upd ? vel_update<MODE>(h1c2, wo, h1k, dline_fwd<MODE>(sp + OFF_Q + h1_src, 1)) : wo;
+                }
+                if (h2_on) {
+                    const float wo = sp[OFF_W + h2_src];
+                    wtile[h2_idx] = h2_upd ? vel_update<MODE>(h2c2, wo, h2k, dline_fwd<MODE>(sp + OFF_Q + h2_src, 1)) : wo;
+                }
             }
             __syncthreads();
 
-            if (xz_upd) {
+            // stresses of columns a and b
+            float t[9];
+#pragma unroll
+            for (int k = 0; k < 9; k++) t[k] = utile[(ca + k) * 32 + lane];
+            const float ay1 = g.ay1[y], ay2 = g.ay2[y];
+            const bool y_in = y >= g.npd && y < g.npd + g.ny;
+#pragma unroll
+            for (int cb = 0; cb < 2; cb++) {
+                const bool upd = cb ? upd_b : upd_a;
+                if (!upd) continue;
+                const float *q = cb ? qb : qa;
+                const int o = oa + 32 * cb;
+                const float m0 = sp[OFF_M + o], m1 = sp[OFF_M + kOB + o], m2 = sp[OFF_M + 2 * kOB + o];
                 const float yy = deriv<MODE>(q[4], q[3], q[5], q[2], q[6], q[1], q[7], q[0]);
-                const float xx = dline_bwd<MODE>(utile + (wx + 4) * 32 + lane, 32);
-                const float zz = dline_bwd<MODE>(wtile + wx * 40 + lane + 4, 1);
-                const long id = col_off + yoff;
-                const bool inside = MODE == GEO_MODE_FAST && xo >= g.npd && xo < g.npd + g.nx && y >= g.npd &&
-                                    y < g.npd + g.ny && zo >= g.npd && zo < g.npd + g.nz;
+                const float xx = cb ? deriv<MODE>(t[5], t[4], t[6], t[3], t[7], t[2], t[8], t[1])
+                                    : deriv<MODE>(t[4], t[3], t[5], t[2], t[6], t[1], t[7], t[0]);
+                const float zz = dline_bwd<MODE>(wtile + (ca + cb) * 40 + lane + 4, 1);
+                const float ax1 = cb ? ax1b : ax1a, ax2 = cb ? ax2b : ax2a;
+                const int id = col_a + yoff + cb * ldz;
                 float P, Q;
-                if (MODE == GEO_MODE_FAST) {
-                    // m0,m1,m2 = A,B,C
+                if (MODE == GEO_MODE_FAST && (cb ? in_b : in_a) && y_in) {
+                    // m = A, B, C; all sponge factors are 1
                     const float Ax = m0 * g.dtx, Ay = m0 * g.dty, Bz = m1 * g.dtz;
                     const float Bx = m1 * g.dtx, By = m1 * g.dty, Cz = m2 * g.dtz;
-                    if (inside) {
-                        float p0 = ry[(wx + 7) * 32 + lane], q0 = sp[OFF_Q + wx * 48 + lane + 8];
-                        if (st.src_on && id == st.src) {
-                            p0 = g.P0[id];
-                            q0 = g.Q0[id];
-                        }
-                        P = __fmaf_rn(-Bz, zz, __fmaf_rn(-Ay, yy, __fmaf_rn(-Ax, xx, p0)));
-                        Q = __fmaf_rn(-Cz, zz, __fmaf_rn(-By, yy, __fmaf_rn(-Bx, xx, q0)));
-                    } else {
-                        const float ay1 = g.ay1[y], ay2 = g.ay2[y];
-                        const float px = __fmaf_rn(-(ax1 * Ax), xx, ax2 * s0);
-                        const float py = __fmaf_rn(-(ay1 * Ay), yy, ay2 * s1);
-                        const float pz = __fmaf_rn(-(az1 * Bz), zz, az2 * s2);
-                        const float qx = __fmaf_rn(-(ax1 * Bx), xx, ax2 * s3);
-                        const float qy = __fmaf_rn(-(ay1 * By), yy, ay2 * s4);
-                        const float qz = __fmaf_rn(-(az1 * Cz), zz, az2 * s5);
-                        g.px[id] = px; g.py[id] = py; g.pz[id] = pz;
-                        g.qx[id] = qx; g.qy[id] = qy; g.qz[id] = qz;
-                        P = px + py + pz;
-                        Q = qx + qy + qz;
+                    float p0 = cb ? pb[0] : pa[0], q0 = sp[OFF_Q + (ca + cb) * 48 + lane + 8];
+                    if (st.src_on && id == (int)st.src) {
+                        p0 = g.P0[id];
+                        q0 = g.Q0[id];
                     }
+                    P = __fmaf_rn(-Bz, zz, __fmaf_rn(-Ay, yy, __fmaf_rn(-Ax, xx, p0)));
+                    Q = __fmaf_rn(-Cz, zz, __fmaf_rn(-By, yy, __fmaf_rn(-Bx, xx, q0)));
                 } else {
-                    // m0,m1,m2 = vp, 1+2eps, sqrtf(1+2del); the reference's chain
-                    const float vp = m0, e2 = m1, d2 = m2, ay1 = g.ay1[y], ay2 = g.ay2[y];
-                    const float px = ax2 * s0 - ax1 * vp * vp * e2 * g.dtx * xx;
-                    const float py = ay2 * s1 - ay1 * vp * vp * e2 * g.dty * yy;
-                    const float pz = az2 * s2 - az1 * vp * vp * d2 * g.dtz * zz;
-                    const float qx = ax2 * s3 - ax1 * vp * vp * d2 * g.dtx * xx;
-                    const float qy = ay2 * s4 - ay1 * vp * vp * d2 * g.dty * yy;
-                    const float qz = az2 * s5 - az1 * vp * vp * g.dtz * zz;
+                    const float *S = sp + OFF_S + o;
+                    float px, py, pz, qx, qy, qz;
+                    if (MODE == GEO_MODE_FAST) {
+                        const float Ax = m0 * g.dtx, Ay = m0 * g.dty, Bz = m1 * g.dtz;
+                        const float Bx = m1 * g.dtx, By = m1 * g.dty, Cz = m2 * g.dtz;
+                        px = __fmaf_rn(-(ax1 * Ax), xx, ax2 * S[0]);
+                        py = __fmaf_rn(-(ay1 * Ay), yy, ay2 * S[kOB]);
+                        pz = __fmaf_rn(-(az1 * Bz), zz, az2 * S[2 * kOB]);
+                        qx = __fmaf_rn(-(ax1 * Bx), xx, ax2 * S[3 * kOB]);
+                        qy = __fmaf_rn(-(ay1 * By), yy, ay2 * S[4 * kOB]);
+                        qz = __fmaf_rn(-(az1 * Cz), zz, az2 * S[5 * kOB]);
+                    } else {
+                        // m = vp, 1+2eps, sqrtf(1+2del); the reference's chain
+                        const float vp = m0, e2 = m1, d2 = m2;
+                        px = ax2 * S[0] - ax1 * vp * vp * e2 * g.dtx * xx;
+                        py = ay2 * S[kOB] - ay1 * vp * vp * e2 * g.dty * yy;
+                        pz = az2 * S[2 * kOB] - az1 * vp * vp * d2 * g.dtz * zz;
+                        qx = ax2 * S[3 * kOB] - ax1 * vp * vp * d2 * g.dtx * xx;
+                        qy = ay2 * S[4 * kOB] - ay1 * vp * vp * d2 * g.dty * yy;
+                        qz = az2 * S[5 * kOB] - az1 * vp * vp * g.dtz * zz;
+                    }
                     g.px[id] = px; g.py[id] = py; g.pz[id] = pz;
                     g.qx[id] = qx; g.qy[id] = qy; g.qz[id] = qz;
                     P = px + py + pz;
@@ -369,17 +449,14 @@ __global__ void __launch_bounds__(kTZ *kTXF, 2)
                 }
                 g.P1[id] = P;
                 g.Q1[id] = Q;
-                if (st.rec && zo == st.rec_iz) {
-                    const int rx = xo - g.npd - st.rx0, rr = y - g.npd - st.ry0;
-                    if (rx >= 0 && rr >= 0 && rx % st.drx == 0 && rr % st.dry == 0) {
-                        const int irx = rx / st.drx, iry = rr / st.dry;
-                        if (irx < st.nrx && iry < st.nry)
-                            st.rec[(long)st.it * st.nrx * st.nry + irx + (long)st.nrx * iry] = P;
-                    }
+                const int rix = cb ? rec_b : rec_a;
+                if (rix >= 0) {
+                    const int rr = y - g.npd - st.ry0;
+                    if (rr >= 0 && rr % st.dry == 0 && rr / st.dry < st.nry)
+                        st.rec[(long)st.it * st.nrx * st.nry + rix + (long)st.nrx * (rr / st.dry)] = P;
                 }
             }
         }
-        sj = sj + 1 == kRing ? 0 : sj + 1;
     }
 }
 
@@ -416,7 +493,7 @@ int launch_fused3d(const StepMaps &maps, const Fused3D &g, int mode, int it, int
     st.ixs = ixs; st.iys = iys; st.izs = izs;
     st.src = izs + (long)g.ldz * (ixs + (long)g.nnx * iys);
     st.rec = rec; st.rec_iz = rec_iz; st.rx0 = rx0; st.drx = drx; st.nrx = nrx; st.ry0 = ry0; st.dry = dry; st.nry = nry;
-    dim3 block(kTZ, kTXF), grid(g.nitems);
+    dim3 block(kTZ, kWarps), grid(g.nitems);
     if (mode == GEO_MODE_FAST) {
         if (!attr_set[0]) {
             GEO_CUDA(cudaFuncSetAttribute(k_fused3d<GEO_MODE_FAST>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFusedSmem));

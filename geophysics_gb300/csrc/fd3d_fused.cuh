@@ -6,9 +6,10 @@
 
 namespace geo {
 
-// Tensor maps of one step's reads: 0 P (ring box), 1 Q (z-halo box),
-// 2 u (x-halo box), 3 w (z-halo box), 4 v (own box).
-constexpr int kNumMaps = 5;
+// Tensor maps of one step's reads.  Per time level: 0 P x-halo box, 1 P own
+// box, 2 Q z-halo box, 3 u x-halo box, 4 w z-halo box, 5 v own box; then
+// the level-independent own boxes 6-8 model, 9-14 split stresses.
+constexpr int kNumMaps = 15;
 struct StepMaps {
     CUtensorMap m[kNumMaps];
 };
@@ -30,17 +31,19 @@ struct Fused3D {
 
 // Tile and pipeline geometry.
 constexpr int kTZ = 32;                 // z points per tile (one warp's lanes)
-constexpr int kTXF = 16;                // x columns per tile (one warp each)
-constexpr int kStages = 4;              // TMA pipeline depth (planes)
-constexpr int kRing = 8 + kStages - 1;  // P planes resident
-constexpr int kPB = kTZ * (kTXF + 14);  // P box (z 32, x TX+14 from x0-7)
+constexpr int kTXF = 16;                // x columns per tile (two per thread)
+constexpr int kWarps = kTXF / 2;        // warps per block
+constexpr int kStages = 3;              // TMA pipeline depth (planes)
+constexpr int kPB = kTZ * (kTXF + 14);  // P x-halo box (z 32, x TX+14 from x0-7)
 constexpr int kQB = 48 * kTXF;          // Q / w box (z 48 from z0-8, x TX)
 constexpr int kUB = kTZ * (kTXF + 8);   // u box (z 32, x TX+8 from x0-4)
 constexpr int kOB = kTZ * kTXF;         // own box (z 32, x TX)
-constexpr int kStageFloats = kQB + kUB + kQB + kOB;   // Q, u, w, v
+// stage: P own (plane y+7), v (plane y+3), then the stress plane's P halo,
+// Q, u, w, model (3) and split stresses (6)
+constexpr int kStageFloats = kOB + kOB + kPB + kQB + kUB + kQB + 3 * kOB + 6 * kOB;
 constexpr int kUTile = (kTXF + 7) * kTZ;
 constexpr int kWTile = kTXF * 40;
-constexpr size_t kFusedSmem = (size_t)(kRing * kPB + kStages * kStageFloats + kUTile + kWTile) * 4 + 256;
+constexpr size_t kFusedSmem = (size_t)(kStages * kStageFloats + kUTile + kWTile) * 4 + 256;
 
 int launch_fused3d(const StepMaps &maps, const Fused3D &g, int mode, int it, int src_on, float amp, int ixs,
                    int iys, int izs, float *rec, int rec_iz, int rx0, int drx, int nrx, int ry0, int dry, int nry,
