@@ -229,9 +229,11 @@ def run_ours(args, rank, world):
     peak, peak_kind = measured_peak()
     achieved = algorithmic_bytes_per_step() / (step_ms / 1000) / 1e9
     traffic = None
-    tf = os.path.join(ROOT, "profiles", "fd3d_step_traffic.json")
+    tf = os.path.join(ROOT, "profiles", "fd3d_fused_400cube_traffic.md")
     if os.path.exists(tf):
-        traffic = json.load(open(tf)).get("bytes_per_step")
+        for line in open(tf):
+            if line.startswith("bytes_per_step:"):
+                traffic = int(line.split(":")[1])
 
     # end to end through the C ABI with host buffers
     hv, he, hd = (a.cpu().numpy() for a in (vp, eps, dl))
@@ -293,6 +295,21 @@ def run_profile_case(args):
     print(json.dumps({"case": "profile-small", "grid": 192, "nt": 20, "shots": args.steps}))
 
 
+def run_traffic_case(args):
+    """The full 400^3 grid with a handful of bare time steps, for a one-pass
+    ncu capture of the stencil's DRAM bytes per launch."""
+    import torch
+
+    import geophysics_gb300 as geo
+    vp, eps, dl = make_model(device="cuda")
+    plan = geo.FD3DPlan(**plan_kwargs())
+    plan.set_model(vp, eps, dl)
+    plan.time_steps(max(1, args.steps))
+    torch.cuda.synchronize()
+    plan.close()
+    print(json.dumps({"case": "traffic", "grid": NX, "steps": args.steps}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -300,11 +317,14 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--case", default="full", choices=["full", "small"],
-                    help="small: the ncu profiling case (not a bench line)")
+    ap.add_argument("--case", default="full", choices=["full", "small", "traffic"],
+                    help="small / traffic: ncu profiling cases (not a bench line)")
     args = ap.parse_args()
     if args.case == "small":
         run_profile_case(args)
+        return
+    if args.case == "traffic":
+        run_traffic_case(args)
         return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

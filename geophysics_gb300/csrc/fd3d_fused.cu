@@ -6,13 +6,19 @@
 // updates the stresses, so u,v,w never make a round trip through HBM between
 // the two half-steps of the reference (GPU_vti3dfd_kernels.cu:90-201).
 //
-// Data movement: the old level's P, Q, u, w, v arrive by TMA
-// (cp.async.bulk.tensor) into shared memory, paced by one mbarrier per
-// stage of a 4-deep plane pipeline; P planes stay resident in a ring (the 8
-// y taps of dv/dt plus the planes in flight).  The model and the split
-// sponge stresses, read only at their own point, come as coalesced loads
-// issued at the top of each plane.  Writes are plain coalesced stores to the
-// next level (u,v,w,P,Q ping-pong between steps; split stresses in place).
+// Each thread owns two adjacent x columns at one depth (lane = z), so the
+// x taps of the two columns share shared-memory loads and the per-plane
+// bookkeeping is paid once per two points.
+//
+// Data movement: every read goes through TMA (cp.async.bulk.tensor) into a
+// 3-stage shared-memory pipeline, one mbarrier per stage.  Iteration i
+// brings the own-column box of P at plane ybase+i (feeding an 8-deep
+// register queue for dP/dy), v at plane ybase+i-4, and for the stress plane
+// y = ybase+i-7 the x-halo box of P (an L2 hit: fetched 7 planes earlier),
+// Q and w with a z halo, u with an x halo, the model and, where the tile
+// touches the sponge, the split stresses.  Writes are plain coalesced
+// stores to the next level (u,v,w,P,Q ping-pong between steps; split
+// stresses in place).
 //
 // Arithmetic: GEO_MODE_EXACT keeps the reference's operation chain (no
 // contraction) and is bit-identical to it; GEO_MODE_FAST uses fused
@@ -252,8 +258,19 @@ __global__ void __launch_bounds__(kTZ *kWarps, 2)
 #pragma unroll
     for (int k = 0; k < 8; k++) qa[k] = qb[k] = pa[k] = pb[k] = 0.0f;
     uint32_t phase = 0;
+    // y-direction sponge factors (v plane y+3, stress plane y), loaded one
+    // iteration ahead so their latency hides behind a plane of work
+    auto ycoef = [&](int i, float &c1, float &c2, float &a1, float &a2) {
+        const int y = ybase + i - 7;
+        const int yv = min(max(y + 3, 0), g.nny - 1), ys = min(max(y, 0), g.nny - 1);
+        c1 = __ldg(g.cy1 + yv); c2 = __ldg(g.cy2 + yv); a1 = __ldg(g.ay1 + ys); a2 = __ldg(g.ay2 + ys);
+    };
+    float ncy1, ncy2, nay1, nay2;
+    ycoef(0, ncy1, ncy2, nay1, nay2);
 
     for (int i = 0; i < NI; i++) {
+        const float cy1 = ncy1, cy2 = ncy2, ay1 = nay1, ay2 = nay2;
+        if (i + 1 < NI) ycoef(i + 1, ncy1, ncy2, nay1, nay2);
         const int s = i % kStages;
         if (tid == 0 && !mbar_wait(&bar[s], (phase >> s) & 1u)) s_abort = 1;
         phase ^= 1u << s;
@@ -313,7 +330,7 @@ __global__ void __launch_bounds__(kTZ *kWarps, 2)
             const float va = sp[OFF_V + oa], vb = sp[OFF_V + oa + 32];
             float vna = va, vnb = vb;
             if (yv >= 4 && yv < g.nny - 4) {
-                const float ky = g.cy1[yv] * g.dty, cy2 = g.cy2[yv];
+                const float ky = cy1 * g.dty;
                 const int iv = col_a + sxy * yv;
                 if (upd_a) {
                     vna = vel_update<MODE>(cy2, va, ky, deriv<MODE>(pa[4], pa[3], pa[5], pa[2], pa[6], pa[1], pa[7], pa[0]));
@@ -393,7 +410,6 @@ __global__ void __launch_bounds__(kTZ *kWarps, 2)
             float t[9];
 #pragma unroll
             for (int k = 0; k < 9; k++) t[k] = utile[(ca + k) * 32 + lane];
-            const float ay1 = g.ay1[y], ay2 = g.ay2[y];
             const bool y_in = y >= g.npd && y < g.npd + g.ny;
 #pragma unroll
             for (int cb = 0; cb < 2; cb++) {
