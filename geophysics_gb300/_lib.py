@@ -40,6 +40,10 @@ class FD3DDesc(C.Structure):
                                        "rec_iz", "rx0", "drx", "nrx", "ry0", "dry", "nry", "mute_tt")]
 
 
+class RTM3DDesc(C.Structure):
+    _fields_ = [("fd", FD3DDesc), ("ns", C.c_int), ("mute_tt", C.c_int)]
+
+
 class RTM2DDesc(C.Structure):
     _fields_ = [(n, C.c_int) for n in ("nx", "nz", "npd", "nt")] + \
                [(n, C.c_float) for n in ("dx", "dz", "dt_ms", "favg", "pfac")] + \
@@ -77,6 +81,7 @@ def lib():
         "geo_fd3d_get_fields": (_i, [_vp, _vp, _vp, _i, _vp]),
         "geo_fd3d_shot": (_i, [C.POINTER(FD3DDesc), _i, _vp, _vp, _vp, _vp, _i, _vp]),
         "geo_rtm2d_batch": (_i, [C.POINTER(RTM2DDesc), _vp, _vp, _vp, _vp, _vp, _i, _vp]),
+        "geo_rtm3d": (_i, [C.POINTER(RTM3DDesc), _vp, _vp, _vp, _vp, _vp, _vp, _i, _vp]),
         "geo_laplace2d": (_i, [_i, _i, _vp, _vp, _i, _vp]),
         "geo_laplace3d": (_i, [_i, _i, _i, _vp, _vp, _i, _vp]),
         "geo_par_load": (_i, [C.c_char_p, C.POINTER(_vp)]),

@@ -10,7 +10,7 @@ import ctypes as C
 import numpy as np
 
 from ._lib import (FD2DDesc, FD3DDesc, GEO_MEM_DEVICE, GEO_MEM_HOST, GEO_MODE_EXACT, GEO_MODE_FAST,
-                   GEO_VARIANT_CPU, GEO_VARIANT_GPU, GEO_VARIANT_MPI, RTM2DDesc, check, lib)
+                   GEO_VARIANT_CPU, GEO_VARIANT_GPU, GEO_VARIANT_MPI, RTM2DDesc, RTM3DDesc, check, lib)
 
 _VARIANTS = {"cpu": GEO_VARIANT_CPU, "gpu": GEO_VARIANT_GPU, "mpi": GEO_VARIANT_MPI}
 _MODES = {"exact": GEO_MODE_EXACT, "fast": GEO_MODE_FAST}
@@ -171,6 +171,28 @@ def fd3d_shot(v, e, d, is_=0, **kw):
         return plan.run_shot(is_, device=v.device if _is_dev(v) else None)
     finally:
         plan.close()
+
+
+def rtm3d(v, e, d, *, npd, nt, dx, dy, dz, dt, favg, fsx, fsy, fsz, ns=1, dsx=0, dsy=0, dsz=0, mute_tt=70,
+          pfac=10.0, wtype=1, sv=0, mode="fast", laplace=True, illum=False):
+    """3D boundary-saving RTM over shots 0..ns-1 (the 3D GPU RTM program's
+    semantics); v,e,d shaped (ny, nx, nz).  Returns the illumination-divided
+    image, then the Laplacian-filtered image if `laplace`, then the
+    illumination if `illum`."""
+    b = _Bufs(v, e, d)
+    ny, nx, nz = v.shape
+    fd = FD3DDesc(nx=nx, ny=ny, nz=nz, npd=npd, nt=nt, dx=dx, dy=dy, dz=dz, dt=dt, favg=favg, pfac=pfac,
+                  wtype=wtype, sv=sv, mode=_MODES[mode] if isinstance(mode, str) else int(mode),
+                  fsx=fsx, fsy=fsy, fsz=fsz, dsx=dsx, dsy=dsy, dsz=dsz, rec_iz=npd, rx0=0, drx=1, nrx=nx,
+                  ry0=0, dry=1, nry=ny, mute_tt=0)
+    desc = RTM3DDesc(fd=fd, ns=ns, mute_tt=mute_tt)
+    pv, pe, pd = b.inp(v), b.inp(e), b.inp(d)
+    mig, pm = b.out((ny, nx, nz), v)
+    lap, pl = b.out((ny, nx, nz), v) if laplace else (None, None)
+    ill, pi = b.out((ny, nx, nz), v) if illum else (None, None)
+    check(lib().geo_rtm3d(C.byref(desc), pv, pe, pd, pm, pl, pi, b.mem, b.stream()), "geo_rtm3d")
+    out = [mig] + ([lap] if laplace else []) + ([ill] if illum else [])
+    return out[0] if len(out) == 1 else tuple(out)
 
 
 def rtm2d_batch(v, e, d, *, npd, nt, dx, dz, dt_ms, favg, pfac, zs, shot_x, shot_nxs, laplace=True,

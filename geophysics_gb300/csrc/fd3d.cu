@@ -20,6 +20,7 @@
 #include <cmath>
 #include <cstring>
 #include <vector>
+#include <memory>
 
 using namespace geo;
 
@@ -39,7 +40,58 @@ __global__ void k_box3d(Grid3D g, float *e2, float *d2, long x0, long y0, long z
     }
 }
 
+// One ring of P,Q just outside the physical box (faces z=npml-1, z=npml+nz,
+// x=npml-1, x=npml+nx, y=npml-1, y=npml+ny in the 3D RTM program's order,
+// wavefield_bndr :405-506): save after a forward step or restore before a
+// backward step.  Faces do not overlap.
+__global__ void k_ring3d(Grid3D g, float *P, float *Q, float *bp, float *bq, long L, int it, int save) {
+    const int nx = g.nx, ny = g.ny, nz = g.nz, npd = g.npd;
+    for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < L; k += (long)gridDim.x * blockDim.x) {
+        long r = k;
+        int iz, ix, iy;
+        const long fxy = (long)nx * ny, fzy = (long)nz * ny, fxz = (long)nx * nz;
+        if (r < fxy) { iz = npd - 1; ix = npd + (int)(r % nx); iy = npd + (int)(r / nx); }
+        else if ((r -= fxy) < fxy) { iz = npd + nz; ix = npd + (int)(r % nx); iy = npd + (int)(r / nx); }
+        else if ((r -= fxy) < fzy) { iz = npd + (int)(r % nz); ix = npd - 1; iy = npd + (int)(r / nz); }
+        else if ((r -= fzy) < fzy) { iz = npd + (int)(r % nz); ix = npd + nx; iy = npd + (int)(r / nz); }
+        else if ((r -= fzy) < fxz) { iz = npd + (int)(r % nz); ix = npd + (int)(r / nz); iy = npd - 1; }
+        else { r -= fxz; iz = npd + (int)(r % nz); ix = npd + (int)(r / nz); iy = npd + ny; }
+        const long id = iz + (long)g.ldz * ix + g.sxy * iy, b = (long)it * L + k;
+        if (save) { bp[b] = P[id]; bq[b] = Q[id]; }
+        else { P[id] = bp[b]; Q[id] = bq[b]; }
+    }
+}
+
+// Receiver injection before a backward step: the muted record into P and Q
+// of the receiver field at z = npml-1 (shot_record, flag false, :319-334).
+__global__ void k_inject3d(Grid3D g, float *P, float *Q, const float *rec_tm, int it) {
+    const int nx = g.nx, ny = g.ny, npd = g.npd;
+    const long n = (long)nx * ny;
+    for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < n; k += (long)gridDim.x * blockDim.x) {
+        const int ix = (int)(k % nx), iy = (int)(k / nx);
+        const long id = (npd - 1) + (long)g.ldz * (npd + ix) + g.sxy * (npd + iy);
+        const float r = rec_tm[(long)it * n + k];
+        P[id] = r;
+        Q[id] = r;
+    }
+}
+
+// migration_illum (:539-553): mig /= illum where illum != 0.
+__global__ void k_image_illum(float *mig, const float *ill, long n) {
+    for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < n; k += (long)gridDim.x * blockDim.x)
+        if (ill[k] != 0.0f) mig[k] = mig[k] / ill[k];
+}
+
 }  // namespace geo
+
+// One wavefield set: u,v,w,P,Q at two time levels (ping-pong), split stresses
+// in place, and the tensor maps of both levels.
+struct FieldSet3D {
+    DevBuf lev[2][5];
+    DevBuf px, py, pz, qx, qy, qz;
+    StepMaps maps[2];
+    int cur = 0;
+};
 
 // Device state of one 3D grid.  Fields use the reference layout with the z
 // stride ldz rounded up to 4 floats (16 bytes, the TMA stride rule); points
@@ -48,12 +100,10 @@ struct geo_fd3d_plan {
     geo_fd3d_desc d;
     int nnx, nny, nnz, ldz;
     size_t n, nalloc;                  // padded points, allocated floats per field
-    DevBuf vp, e2, d2, prof;
-    DevBuf lev[2][5];                  // u v w P Q at two time levels
-    DevBuf px, py, pz, qx, qy, qz;
-    DevBuf rec_tm, rec_tr, mute_hi, box, err;
-    StepMaps maps[2];                  // reads of level 0 / level 1
-    int cur = 0;                       // level holding the current state
+    DevBuf vp, e2, d2, prof;           // model (exact: vp,1+2eps,sqrtf(1+2del); fast: A,B,C)
+    FieldSet3D fs[2];                  // [0] forward / source side, [1] receiver side (RTM)
+    int nfs = 1;
+    DevBuf rec_tm, rec_tr, mute_lo, mute_hi, box, err;
     int chunk = 0, nitems = 0, ntz = 0, ntx = 0;
     std::vector<float> amp;
     std::vector<uint8_t> on;
@@ -64,8 +114,8 @@ struct geo_fd3d_plan {
 
 namespace geo {
 
-// Extents, profiles and current level of a plan.
-Grid3D make_grid(const geo_fd3d_plan *p) {
+// Extents, profiles and the current level of field set f.
+static Grid3D grid_of(const geo_fd3d_plan *p, int f) {
     Grid3D g;
     g.nnx = p->nnx; g.nny = p->nny; g.nnz = p->nnz;
     g.ldz = p->ldz;
@@ -81,53 +131,64 @@ Grid3D make_grid(const geo_fd3d_plan *p) {
     g.cy1 = pr + o; o += p->nny; g.cy2 = pr + o; o += p->nny; g.ay1 = pr + o; o += p->nny; g.ay2 = pr + o; o += p->nny;
     g.cz1 = pr + o; o += p->nnz; g.cz2 = pr + o; o += p->nnz; g.az1 = pr + o; o += p->nnz; g.az2 = pr + o;
     g.vp = p->vp.as<float>(); g.e2 = p->e2.as<float>(); g.d2 = p->d2.as<float>();
-    const int c = p->cur;
-    g.u = p->lev[c][0].as<float>(); g.v = p->lev[c][1].as<float>(); g.w = p->lev[c][2].as<float>();
-    g.P = p->lev[c][3].as<float>(); g.Q = p->lev[c][4].as<float>();
-    g.px = p->px.as<float>(); g.py = p->py.as<float>(); g.pz = p->pz.as<float>();
-    g.qx = p->qx.as<float>(); g.qy = p->qy.as<float>(); g.qz = p->qz.as<float>();
+    const FieldSet3D &F = p->fs[f];
+    const int c = F.cur;
+    g.u = F.lev[c][0].as<float>(); g.v = F.lev[c][1].as<float>(); g.w = F.lev[c][2].as<float>();
+    g.P = F.lev[c][3].as<float>(); g.Q = F.lev[c][4].as<float>();
+    g.px = F.px.as<float>(); g.py = F.py.as<float>(); g.pz = F.pz.as<float>();
+    g.qx = F.qx.as<float>(); g.qy = F.qy.as<float>(); g.qz = F.qz.as<float>();
     return g;
 }
 
-// Fused-kernel view: reads level cur (through the maps), writes level 1-cur.
-static Fused3D make_fused(const geo_fd3d_plan *p) {
-    const Grid3D g = make_grid(p);
-    Fused3D f;
-    f.nnx = g.nnx; f.nny = g.nny; f.nnz = g.nnz; f.ldz = g.ldz; f.sxy = g.sxy;
-    f.npd = g.npd; f.nx = g.nx; f.ny = g.ny; f.nz = g.nz;
-    f.dtx = g.dtx; f.dty = g.dty; f.dtz = g.dtz;
-    f.cx1 = g.cx1; f.cx2 = g.cx2; f.ax1 = g.ax1; f.ax2 = g.ax2;
-    f.cy1 = g.cy1; f.cy2 = g.cy2; f.ay1 = g.ay1; f.ay2 = g.ay2;
-    f.cz1 = g.cz1; f.cz2 = g.cz2; f.az1 = g.az1; f.az2 = g.az2;
-    f.m0 = g.vp; f.m1 = g.e2; f.m2 = g.d2;
-    f.P0 = g.P; f.Q0 = g.Q;
-    const int n = 1 - p->cur;
-    f.u1 = p->lev[n][0].as<float>(); f.v1 = p->lev[n][1].as<float>(); f.w1 = p->lev[n][2].as<float>();
-    f.P1 = p->lev[n][3].as<float>(); f.Q1 = p->lev[n][4].as<float>();
-    f.px = g.px; f.py = g.py; f.pz = g.pz; f.qx = g.qx; f.qy = g.qy; f.qz = g.qz;
-    f.ntz = p->ntz; f.ntx = p->ntx; f.ntiles = p->ntz * p->ntx; f.chunk = p->chunk; f.nitems = p->nitems;
-    f.err = p->err.as<int>();
-    return f;
+Grid3D make_grid(const geo_fd3d_plan *p) { return grid_of(p, 0); }
+
+// Fused-kernel view of field set f: reads level cur (through the maps),
+// writes level 1-cur.
+static Fused3D make_fused(const geo_fd3d_plan *p, int f) {
+    const Grid3D g = grid_of(p, f);
+    const FieldSet3D &F = p->fs[f];
+    Fused3D r;
+    r.nnx = g.nnx; r.nny = g.nny; r.nnz = g.nnz; r.ldz = g.ldz; r.sxy = g.sxy;
+    r.npd = g.npd; r.nx = g.nx; r.ny = g.ny; r.nz = g.nz;
+    r.dtx = g.dtx; r.dty = g.dty; r.dtz = g.dtz;
+    r.cx1 = g.cx1; r.cx2 = g.cx2; r.ax1 = g.ax1; r.ax2 = g.ax2;
+    r.cy1 = g.cy1; r.cy2 = g.cy2; r.ay1 = g.ay1; r.ay2 = g.ay2;
+    r.cz1 = g.cz1; r.cz2 = g.cz2; r.az1 = g.az1; r.az2 = g.az2;
+    r.m0 = g.vp; r.m1 = g.e2; r.m2 = g.d2;
+    r.P0 = g.P; r.Q0 = g.Q;
+    const int n = 1 - F.cur;
+    r.u1 = F.lev[n][0].as<float>(); r.v1 = F.lev[n][1].as<float>(); r.w1 = F.lev[n][2].as<float>();
+    r.P1 = F.lev[n][3].as<float>(); r.Q1 = F.lev[n][4].as<float>();
+    r.px = g.px; r.py = g.py; r.pz = g.pz; r.qx = g.qx; r.qy = g.qy; r.qz = g.qz;
+    r.ntz = p->ntz; r.ntx = p->ntx; r.ntiles = p->ntz * p->ntx; r.chunk = p->chunk; r.nitems = p->nitems;
+    r.err = p->err.as<int>();
+    return r;
 }
 
-static int build_maps(geo_fd3d_plan *p) {
+static int alloc_fields(geo_fd3d_plan *p, int f) {
+    FieldSet3D &F = p->fs[f];
+    const size_t n = p->nalloc;
+    for (int c = 0; c < 2; c++)
+        for (int k = 0; k < 5; k++) GEO_TRY(F.lev[c][k].alloc(n * 4));
+    DevBuf *sp[6] = {&F.px, &F.py, &F.pz, &F.qx, &F.qy, &F.qz};
+    for (DevBuf *b : sp) GEO_TRY(b->alloc(n * 4));
     for (int c = 0; c < 2; c++) {
-        StepMaps &M = p->maps[c];
+        StepMaps &M = F.maps[c];
         const int nz = p->nnz, ld = p->ldz, nx = p->nnx, ny = p->nny;
-        GEO_TRY(encode_map(&M.m[0], p->lev[c][3].as<float>(), nz, ld, nx, ny, kTZ, kTXF + 14));  // P halo
-        GEO_TRY(encode_map(&M.m[1], p->lev[c][3].as<float>(), nz, ld, nx, ny, kTZ, kTXF));       // P own
-        GEO_TRY(encode_map(&M.m[2], p->lev[c][4].as<float>(), nz, ld, nx, ny, 48, kTXF));        // Q
-        GEO_TRY(encode_map(&M.m[3], p->lev[c][0].as<float>(), nz, ld, nx, ny, kTZ, kTXF + 8));   // u
-        GEO_TRY(encode_map(&M.m[4], p->lev[c][2].as<float>(), nz, ld, nx, ny, 48, kTXF));        // w
-        GEO_TRY(encode_map(&M.m[5], p->lev[c][1].as<float>(), nz, ld, nx, ny, kTZ, kTXF));       // v
-        const DevBuf *own[9] = {&p->vp, &p->e2, &p->d2, &p->px, &p->py, &p->pz, &p->qx, &p->qy, &p->qz};
+        GEO_TRY(encode_map(&M.m[0], F.lev[c][3].as<float>(), nz, ld, nx, ny, kTZ, kTXF + 14));  // P halo
+        GEO_TRY(encode_map(&M.m[1], F.lev[c][3].as<float>(), nz, ld, nx, ny, kTZ, kTXF));       // P own
+        GEO_TRY(encode_map(&M.m[2], F.lev[c][4].as<float>(), nz, ld, nx, ny, 48, kTXF));        // Q
+        GEO_TRY(encode_map(&M.m[3], F.lev[c][0].as<float>(), nz, ld, nx, ny, kTZ, kTXF + 8));   // u
+        GEO_TRY(encode_map(&M.m[4], F.lev[c][2].as<float>(), nz, ld, nx, ny, 48, kTXF));        // w
+        GEO_TRY(encode_map(&M.m[5], F.lev[c][1].as<float>(), nz, ld, nx, ny, kTZ, kTXF));       // v
+        const DevBuf *own[9] = {&p->vp, &p->e2, &p->d2, &F.px, &F.py, &F.pz, &F.qx, &F.qy, &F.qz};
         for (int r = 0; r < 9; r++) GEO_TRY(encode_map(&M.m[6 + r], own[r]->as<float>(), nz, ld, nx, ny, kTZ, kTXF));
     }
     return GEO_OK;
 }
 
-// y chunking: whole waves of resident blocks against the 7 warm-up planes
-// each chunk recomputes.
+// y chunking: whole waves of resident blocks against the warm-up planes each
+// chunk recomputes.
 static void choose_chunks(geo_fd3d_plan *p) {
     int dev = 0, sms = 152;
     cudaGetDevice(&dev);
@@ -148,22 +209,22 @@ static void choose_chunks(geo_fd3d_plan *p) {
     p->nitems = ntiles * ((planes + p->chunk - 1) / p->chunk);
 }
 
-// One time step: the fused kernel reads level cur and writes level 1-cur.
-static int step3d(geo_fd3d_plan *p, const StepArgs3D &st, cudaStream_t s) {
-    const Fused3D f = make_fused(p);
-    GEO_TRY(launch_fused3d(p->maps[p->cur], f, p->d.mode, st.it, st.src_on, st.amp, st.ixs, st.iys, st.izs, st.rec,
-                           st.rec_iz, st.rx0, st.drx, st.nrx, st.ry0, st.dry, st.nry, s));
-    p->cur ^= 1;
+// One time step of field set f: the fused kernel reads level cur and writes
+// level 1-cur.
+static int step3d(geo_fd3d_plan *p, int f, const StepArgs3D &st, cudaStream_t s) {
+    const Fused3D r = make_fused(p, f);
+    GEO_TRY(launch_fused3d(p->fs[f].maps[p->fs[f].cur], r, p->d.mode, st, s));
+    p->fs[f].cur ^= 1;
     return GEO_OK;
 }
 
-static int zero_state(geo_fd3d_plan *p, cudaStream_t s) {
+static int zero_state(geo_fd3d_plan *p, int f, cudaStream_t s) {
+    FieldSet3D &F = p->fs[f];
     for (int c = 0; c < 2; c++)
-        for (int k = 0; k < 5; k++) GEO_TRY(p->lev[c][k].zero(s));
-    DevBuf *f[] = {&p->px, &p->py, &p->pz, &p->qx, &p->qy, &p->qz};
-    for (DevBuf *b : f) GEO_TRY(b->zero(s));
-    GEO_TRY(p->err.zero(s));
-    p->cur = 0;
+        for (int k = 0; k < 5; k++) GEO_TRY(F.lev[c][k].zero(s));
+    DevBuf *sp[6] = {&F.px, &F.py, &F.pz, &F.qx, &F.qy, &F.qz};
+    for (DevBuf *b : sp) GEO_TRY(b->zero(s));
+    F.cur = 0;
     return GEO_OK;
 }
 
@@ -226,27 +287,33 @@ static int taper_box_3d(geo_fd3d_plan *p, int is, bool tapered, cudaStream_t s) 
     return GEO_OK;
 }
 
-// Forward run of shot `is` into the plan's time-major record buffer;
-// `on_step(it)` (optional) runs after each step (snapshots).
-int run_shot_3d(geo_fd3d_plan *p, int is, cudaStream_t s, int (*on_step)(void *, int), void *ctx) {
-    if (!p->model_set) return fail(GEO_ERR_ARG, "model not set");
+static int source_cell(const geo_fd3d_plan *p, int is, StepArgs3D &st) {
     const geo_fd3d_desc &D = p->d;
     const long ixs = D.fsx + (long)is * D.dsx + D.npd - 1, iys = D.fsy + (long)is * D.dsy + D.npd - 1,
                izs = D.fsz + (long)is * D.dsz + D.npd - 1;
     if (ixs < 4 || ixs >= p->nnx - 4 || iys < 4 || iys >= p->nny - 4 || izs < 4 || izs >= p->nnz - 4)
         return fail(GEO_ERR_ARG, "source outside the updated grid");
-    GEO_TRY(zero_state(p, s));
-    if (D.sv) GEO_TRY(taper_box_3d(p, is, true, s));
-    StepArgs3D st{};
     st.ixs = (int)ixs; st.iys = (int)iys; st.izs = (int)izs;
-    st.src = izs + (long)p->ldz * (ixs + (long)p->nnx * iys);
+    return GEO_OK;
+}
+
+// Forward run of shot `is` into the plan's time-major record buffer;
+// `on_step(it)` (optional) runs after each step (snapshots).
+int run_shot_3d(geo_fd3d_plan *p, int is, cudaStream_t s, int (*on_step)(void *, int), void *ctx) {
+    if (!p->model_set) return fail(GEO_ERR_ARG, "model not set");
+    const geo_fd3d_desc &D = p->d;
+    StepArgs3D st{};
+    GEO_TRY(source_cell(p, is, st));
+    GEO_TRY(zero_state(p, 0, s));
+    GEO_TRY(p->err.zero(s));
+    if (D.sv) GEO_TRY(taper_box_3d(p, is, true, s));
     st.rec = p->rec_tm.as<float>();
     st.rec_iz = D.rec_iz; st.rx0 = D.rx0; st.drx = D.drx; st.nrx = D.nrx; st.ry0 = D.ry0; st.dry = D.dry; st.nry = D.nry;
     for (int it = 0; it < D.nt; it++) {
         st.it = it;
         st.src_on = p->on[it];
         st.amp = p->amp[it];
-        GEO_TRY(step3d(p, st, s));
+        GEO_TRY(step3d(p, 0, st, s));
         if (on_step) GEO_TRY(on_step(ctx, it));
     }
     if (D.sv) GEO_TRY(taper_box_3d(p, is, false, s));
@@ -283,11 +350,7 @@ int fetch_shot_3d(geo_fd3d_plan *p, float *shot, int mem, cudaStream_t s) {
     return GEO_OK;
 }
 
-}  // namespace geo
-
-extern "C" int geo_fd3d_plan_create(geo_fd3d_plan **out, const geo_fd3d_desc *desc) {
-    if (!out || !desc) return fail(GEO_ERR_ARG, "null argument");
-    const geo_fd3d_desc &d = *desc;
+static int check_desc(const geo_fd3d_desc &d) {
     if (d.nx < 2 || d.ny < 2 || d.nz < 2 || d.npd < 5 || d.nt < 1)
         return fail(GEO_ERR_ARG, "grid too small (npd must be >= 5)");
     if (!(d.dt > 0) || !(d.dx > 0) || !(d.dy > 0) || !(d.dz > 0)) return fail(GEO_ERR_ARG, "bad spacing");
@@ -297,8 +360,17 @@ extern "C" int geo_fd3d_plan_create(geo_fd3d_plan **out, const geo_fd3d_desc *de
     if (d.rec_iz < 4 || d.rec_iz >= d.nz + 2 * d.npd - 4) return fail(GEO_ERR_ARG, "receiver depth outside grid");
     if (d.mode != GEO_MODE_EXACT && d.mode != GEO_MODE_FAST) return fail(GEO_ERR_ARG, "bad mode");
     if (!(d.favg > 0)) return fail(GEO_ERR_ARG, "favg must be > 0");
+    return GEO_OK;
+}
+
+// Plan with nfs wavefield sets.
+int plan3d_create(geo_fd3d_plan **out, const geo_fd3d_desc *desc, int nfs) {
+    if (!out || !desc) return fail(GEO_ERR_ARG, "null argument");
+    const geo_fd3d_desc &d = *desc;
+    GEO_TRY(check_desc(d));
     geo_fd3d_plan *p = new geo_fd3d_plan();
     p->d = d;
+    p->nfs = nfs;
     p->nnx = d.nx + 2 * d.npd;
     p->nny = d.ny + 2 * d.npd;
     p->nnz = d.nz + 2 * d.npd;
@@ -313,19 +385,18 @@ extern "C" int geo_fd3d_plan_create(geo_fd3d_plan **out, const geo_fd3d_desc *de
     p->ntx = (p->nnx + kTXF - 1) / kTXF;
     const size_t n = p->nalloc, ntr = (size_t)d.nrx * d.nry;
     int st = GEO_OK;
-    DevBuf *fields[] = {&p->vp, &p->e2, &p->d2, &p->px, &p->py, &p->pz, &p->qx, &p->qy, &p->qz};
-    for (DevBuf *b : fields)
+    DevBuf *model[3] = {&p->vp, &p->e2, &p->d2};
+    for (DevBuf *b : model)
         if (st == GEO_OK) st = b->alloc(n * 4);
-    for (int c = 0; c < 2; c++)
-        for (int k = 0; k < 5; k++)
-            if (st == GEO_OK) st = p->lev[c][k].alloc(n * 4);
+    for (int f = 0; f < nfs && st == GEO_OK; f++) st = alloc_fields(p, f);
     if (st == GEO_OK) st = p->prof.alloc((size_t)4 * (p->nnx + p->nny + p->nnz) * 4);
     if (st == GEO_OK) st = p->rec_tm.alloc(ntr * d.nt * 4);
     if (st == GEO_OK) st = p->rec_tr.alloc(ntr * d.nt * 4);
+    if (st == GEO_OK) st = p->mute_lo.alloc(ntr * 4);
     if (st == GEO_OK) st = p->mute_hi.alloc(ntr * 4);
     if (st == GEO_OK) st = p->box.alloc((size_t)2 * 31 * 31 * 31 * 4);
     if (st == GEO_OK) st = p->err.alloc(16);
-    if (st == GEO_OK) st = build_maps(p);
+    if (st == GEO_OK) st = p->err.zero(nullptr);
     if (st != GEO_OK) {
         delete p;
         return st;
@@ -334,6 +405,12 @@ extern "C" int geo_fd3d_plan_create(geo_fd3d_plan **out, const geo_fd3d_desc *de
     source_amplitudes(V_GPU, d.nt, d.dt, d.favg, d.pfac, d.wtype, p->amp, p->on);
     *out = p;
     return GEO_OK;
+}
+
+}  // namespace geo
+
+extern "C" int geo_fd3d_plan_create(geo_fd3d_plan **out, const geo_fd3d_desc *desc) {
+    return plan3d_create(out, desc, 1);
 }
 
 extern "C" int geo_fd3d_plan_destroy(geo_fd3d_plan *p) {
@@ -348,8 +425,9 @@ static int upload_pitched(geo_fd3d_plan *p, DevBuf &dst, const float *src, cudaS
     return GEO_OK;
 }
 
-// Model upload: pad on the host, build vp, 1+2eps, sqrtf(1+2del) and the
-// sponge profiles (d0 from the padded centre velocity, GPU_vti3dfd_kernels.cu:203-206).
+// Model upload: pad on the host, build the model arrays of the chosen form
+// and the sponge profiles (d0 from the padded centre velocity,
+// GPU_vti3dfd_kernels.cu:203-206).
 extern "C" int geo_fd3d_set_model(geo_fd3d_plan *p, const float *v, const float *e, const float *d, int mem,
                                   void *stream) {
     if (!p || !v || !e || !d) return fail(GEO_ERR_ARG, "null argument");
@@ -423,14 +501,13 @@ extern "C" int geo_fd3d_time_steps(geo_fd3d_plan *p, int nsteps, float *ms, void
     if (!p || nsteps < 1) return fail(GEO_ERR_ARG, "bad argument");
     cudaStream_t s = (cudaStream_t)stream;
     StepArgs3D st{};
-    st.ixs = st.iys = st.izs = 0;
     cudaEvent_t a, b;
     GEO_CUDA(cudaEventCreate(&a));
     GEO_CUDA(cudaEventCreate(&b));
     GEO_CUDA(cudaEventRecord(a, s));
     for (int k = 0; k < nsteps; k++) {
         st.it = k;
-        GEO_TRY(step3d(p, st, s));
+        GEO_TRY(step3d(p, 0, st, s));
     }
     GEO_CUDA(cudaEventRecord(b, s));
     GEO_CUDA(cudaEventSynchronize(b));
@@ -447,9 +524,10 @@ extern "C" int geo_fd3d_get_fields(geo_fd3d_plan *p, float *P, float *Q, int mem
     cudaStream_t s = (cudaStream_t)stream;
     const cudaMemcpyKind k = mem == GEO_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
     float *dst[2] = {P, Q};
+    const FieldSet3D &F = p->fs[0];
     for (int f = 0; f < 2; f++)
         if (dst[f])
-            GEO_CUDA(cudaMemcpy2DAsync(dst[f], (size_t)p->nnz * 4, p->lev[p->cur][3 + f].p, (size_t)p->ldz * 4,
+            GEO_CUDA(cudaMemcpy2DAsync(dst[f], (size_t)p->nnz * 4, F.lev[F.cur][3 + f].p, (size_t)p->ldz * 4,
                                        (size_t)p->nnz * 4, (size_t)p->nnx * p->nny, k, s));
     GEO_CUDA(cudaStreamSynchronize(s));
     return GEO_OK;
@@ -463,4 +541,105 @@ extern "C" int geo_fd3d_shot(const geo_fd3d_desc *desc, int is, const float *v, 
     if (st == GEO_OK) st = geo_fd3d_run_shot(p, is, shot, mem, stream);
     geo_fd3d_plan_destroy(p);
     return st;
+}
+
+// ---------------------------------------------------------------- RTM 3D
+// Boundary-saving RTM with the 3D GPU RTM program's semantics
+// (3D-vti-fd+rtm-cuda/Toa_gpu_3dvti_rtm_adcigs_1orderfunction.cu:882-981).
+extern "C" int geo_rtm3d(const geo_rtm3d_desc *desc, const float *v, const float *e, const float *d, float *mig_out,
+                         float *lap_out, float *illum_out, int mem, void *stream) {
+    if (!desc || !v || !e || !d || !mig_out) return fail(GEO_ERR_ARG, "null argument");
+    if (mem != GEO_MEM_HOST && mem != GEO_MEM_DEVICE) return fail(GEO_ERR_ARG, "bad mem kind");
+    const geo_rtm3d_desc &R = *desc;
+    if (R.ns < 1) return fail(GEO_ERR_ARG, "ns must be >= 1");
+    geo_fd3d_desc D = R.fd;
+    // every surface node records P+Q at z = npml (shot_record :319-334)
+    D.rec_iz = D.npd; D.rx0 = 0; D.drx = 1; D.nrx = D.nx; D.ry0 = 0; D.dry = 1; D.nry = D.ny;
+    D.mute_tt = 0;
+    cudaStream_t s = (cudaStream_t)stream;
+    geo_fd3d_plan *p = nullptr;
+    GEO_TRY(plan3d_create(&p, &D, 2));
+    std::unique_ptr<geo_fd3d_plan, int (*)(geo_fd3d_plan *)> guard(p, geo_fd3d_plan_destroy);
+    GEO_TRY(geo_fd3d_set_model(p, v, e, d, mem, stream));
+    const long nimg = (long)D.nx * D.ny * D.nz;
+    const long L = 2L * D.nx * D.ny + 2L * D.nz * D.ny + 2L * D.nx * D.nz;
+    DevBuf ring, mig, ill, lap;
+    GEO_TRY(ring.alloc((size_t)2 * D.nt * L * 4));
+    GEO_TRY(mig.alloc(nimg * 4));
+    GEO_TRY(ill.alloc(nimg * 4));
+    GEO_TRY(mig.zero(s));
+    GEO_TRY(ill.zero(s));
+    float *bp = ring.as<float>(), *bq = bp + (size_t)D.nt * L;
+    const int ntr = D.nx * D.ny;
+    auto launch_ring = [&](int it, int save) -> int {
+        Grid3D g = grid_of(p, 0);
+        const int blocks = (int)std::min<long>((L + 255) / 256, 152L * 16);
+        k_ring3d<<<blocks, 256, 0, s>>>(g, g.P, g.Q, bp, bq, L, it, save);
+        return check_launch("ring3d");
+    };
+    for (int is = 0; is < R.ns; is++) {
+        StepArgs3D st{};
+        GEO_TRY(source_cell(p, is, st));
+        GEO_TRY(zero_state(p, 0, s));
+        GEO_TRY(zero_state(p, 1, s));
+        if (D.sv) GEO_TRY(taper_box_3d(p, is, true, s));
+        // forward: record P+Q, source illumination, save the ring
+        st.rec = p->rec_tm.as<float>();
+        st.rec_iz = D.rec_iz; st.rx0 = 0; st.drx = 1; st.nrx = D.nx; st.ry0 = 0; st.dry = 1; st.nry = D.ny;
+        st.rec_pq = 1;
+        st.ill = ill.as<float>();
+        for (int it = 0; it < D.nt; it++) {
+            st.it = it;
+            st.src_on = p->on[it];
+            st.amp = p->amp[it];
+            GEO_TRY(step3d(p, 0, st, s));
+            GEO_TRY(launch_ring(it, 1));
+        }
+        // direct-wave mute, window form (mute_directwave :352-390)
+        if (R.mute_tt > 0) {
+            std::vector<int> lo, hi;
+            mute_window_3d_band(D.nx, D.ny, D.nt, D.dt, D.favg, D.dx, D.dy, D.dz, D.fsx, D.fsy, D.dsx, D.dsy, D.fsz,
+                                is, p->vp1, p->eps1, R.mute_tt, lo, hi);
+            GEO_CUDA(cudaMemcpyAsync(p->mute_lo.p, lo.data(), lo.size() * 4, cudaMemcpyHostToDevice, s));
+            GEO_CUDA(cudaMemcpyAsync(p->mute_hi.p, hi.data(), hi.size() * 4, cudaMemcpyHostToDevice, s));
+            GEO_TRY(launch_mute_records(p->rec_tm.as<float>(), ntr, D.nt, p->mute_lo.as<int>(), p->mute_hi.as<int>(), s));
+            GEO_CUDA(cudaStreamSynchronize(s));
+        }
+        // backward: reconstruct the source side from the ring, propagate the
+        // record from the surface, image
+        StepArgs3D sb{}, gb{};
+        sb.ixs = gb.ixs = st.ixs; sb.iys = gb.iys = st.iys; sb.izs = gb.izs = st.izs;
+        gb.ill = ill.as<float>();
+        gb.mig = mig.as<float>();
+        for (int it = D.nt - 1; it >= 0; it--) {
+            sb.it = gb.it = it;
+            GEO_TRY(launch_ring(it, 0));
+            GEO_TRY(step3d(p, 0, sb, s));
+            {
+                Grid3D gg = grid_of(p, 1);
+                const int blocks = (int)std::min<long>((ntr + 255) / 256, 152L * 16);
+                k_inject3d<<<blocks, 256, 0, s>>>(gg, gg.P, gg.Q, p->rec_tm.as<float>(), it);
+                GEO_TRY(check_launch("inject3d"));
+            }
+            gb.other_P = grid_of(p, 0).P;  // the source side's new level
+            GEO_TRY(step3d(p, 1, gb, s));
+        }
+        if (D.sv) GEO_TRY(taper_box_3d(p, is, false, s));
+        GEO_TRY(check_err(p, s));
+    }
+    {
+        const int blocks = (int)std::min<long>((nimg + 255) / 256, 152L * 32);
+        k_image_illum<<<blocks, 256, 0, s>>>(mig.as<float>(), ill.as<float>(), nimg);
+        GEO_TRY(check_launch("image_illum"));
+    }
+    const cudaMemcpyKind k = mem == GEO_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+    GEO_CUDA(cudaMemcpyAsync(mig_out, mig.p, nimg * 4, k, s));
+    if (illum_out) GEO_CUDA(cudaMemcpyAsync(illum_out, ill.p, nimg * 4, k, s));
+    if (lap_out) {
+        GEO_TRY(lap.alloc(nimg * 4));
+        GEO_TRY(launch_laplace3d(D.nx, D.ny, D.nz, mig.as<float>(), lap.as<float>(), s));
+        GEO_CUDA(cudaMemcpyAsync(lap_out, lap.p, nimg * 4, k, s));
+    }
+    GEO_CUDA(cudaStreamSynchronize(s));
+    return GEO_OK;
 }

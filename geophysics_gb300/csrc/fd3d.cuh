@@ -25,6 +25,10 @@ struct StepArgs3D {
     long src;                   // linear source index (or -1)
     float *rec;                 // time-major record (nt x nrx*nry) or null
     int rec_iz, rx0, drx, nrx, ry0, dry, nry;
+    int rec_pq;                 // record P+Q instead of P (the 3D RTM program)
+    float *ill;                 // interior illumination += P^2+Q^2 (or null)
+    float *mig;                 // interior image += other_P * P (or null)
+    const float *other_P;       // the source-side field's P (same layout)
 };
 
 Grid3D make_grid(const geo_fd3d_plan *p);

@@ -469,7 +469,14 @@ __global__ void __launch_bounds__(kTZ *kWarps, 2)
                 if (rix >= 0) {
                     const int rr = y - g.npd - st.ry0;
                     if (rr >= 0 && rr % st.dry == 0 && rr / st.dry < st.nry)
-                        st.rec[(long)st.it * st.nrx * st.nry + rix + (long)st.nrx * (rr / st.dry)] = P;
+                        st.rec[(long)st.it * st.nrx * st.nry + rix + (long)st.nrx * (rr / st.dry)] = st.rec_pq ? P + Q : P;
+                }
+                // RTM imaging epilogue on the physical box
+                // (cal_illumination / cal_migration, 3D RTM program :508-537)
+                if ((st.ill || st.mig) && (cb ? in_b : in_a) && y_in) {
+                    const long o = (long)(zo - g.npd) + (long)g.nz * ((xa + cb - g.npd) + (long)g.nx * (y - g.npd));
+                    if (st.ill) st.ill[o] = st.ill[o] + (P * P + Q * Q);
+                    if (st.mig) st.mig[o] = st.mig[o] + st.other_P[id] * P;
                 }
             }
         }
@@ -500,15 +507,10 @@ int encode_map(CUtensorMap *map, const float *base, int nnz, int ldz, int nnx, i
     return GEO_OK;
 }
 
-int launch_fused3d(const StepMaps &maps, const Fused3D &g, int mode, int it, int src_on, float amp, int ixs, int iys,
-                   int izs, float *rec, int rec_iz, int rx0, int drx, int nrx, int ry0, int dry, int nry,
-                   cudaStream_t s) {
+int launch_fused3d(const StepMaps &maps, const Fused3D &g, int mode, const StepArgs3D &args, cudaStream_t s) {
     static bool attr_set[2] = {false, false};
-    StepArgs3D st{};
-    st.it = it; st.src_on = src_on; st.amp = amp;
-    st.ixs = ixs; st.iys = iys; st.izs = izs;
-    st.src = izs + (long)g.ldz * (ixs + (long)g.nnx * iys);
-    st.rec = rec; st.rec_iz = rec_iz; st.rx0 = rx0; st.drx = drx; st.nrx = nrx; st.ry0 = ry0; st.dry = dry; st.nry = nry;
+    StepArgs3D st = args;
+    st.src = st.izs + (long)g.ldz * (st.ixs + (long)g.nnx * st.iys);
     dim3 block(kTZ, kWarps), grid(g.nitems);
     if (mode == GEO_MODE_FAST) {
         if (!attr_set[0]) {

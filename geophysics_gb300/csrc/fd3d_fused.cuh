@@ -45,9 +45,8 @@ constexpr int kUTile = (kTXF + 7) * kTZ;
 constexpr int kWTile = kTXF * 40;
 constexpr size_t kFusedSmem = (size_t)(kStages * kStageFloats + kUTile + kWTile) * 4 + 256;
 
-int launch_fused3d(const StepMaps &maps, const Fused3D &g, int mode, int it, int src_on, float amp, int ixs,
-                   int iys, int izs, float *rec, int rec_iz, int rx0, int drx, int nrx, int ry0, int dry, int nry,
-                   cudaStream_t s);
+struct StepArgs3D;
+int launch_fused3d(const StepMaps &maps, const Fused3D &g, int mode, const StepArgs3D &st, cudaStream_t s);
 int encode_map(CUtensorMap *map, const float *base, int nnz, int ldz, int nnx, int nny, int boxz, int boxx);
 
 }  // namespace geo

@@ -82,6 +82,9 @@ void mute_window_mpi(int nx, int nt, float dt_ms, float favg, float dx, float dz
 void mute_window_3d(int nx, int ny, int nt, float dt, float favg, float dx, float dy, float dz,
                     int fsx, int fsy, int dsx, int dsy, int fsz, int is, float vp1, float eps1, int tt,
                     std::vector<int> &hi);
+void mute_window_3d_band(int nx, int ny, int nt, float dt, float favg, float dx, float dy, float dz,
+                         int fsx, int fsy, int dsx, int dsy, int fsz, int is, float vp1, float eps1, int tt,
+                         std::vector<int> &lo, std::vector<int> &hi);
 
 // Model sanity: finite, velocity > 0.
 int check_model(const float *v, const float *e, const float *d, size_t n);

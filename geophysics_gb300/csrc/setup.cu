@@ -263,6 +263,27 @@ void mute_window_3d(int nx, int ny, int nt, float dt, float favg, float dx, floa
         }
 }
 
+// mute_directwave (3D-vti-fd+rtm-cuda/Toa_gpu_3dvti_rtm_adcigs_1orderfunction.cu:352-390),
+// window form: zero mu_t0/dt - tt < it < mu_nt, as [lo, hi) per receiver.
+void mute_window_3d_band(int nx, int ny, int nt, float dt, float favg, float dx, float dy, float dz,
+                         int fsx, int fsy, int dsx, int dsy, int fsz, int is, float vp1, float eps1, int tt,
+                         std::vector<int> &lo, std::vector<int> &hi) {
+    lo.assign((size_t)nx * ny, 0);
+    hi.assign((size_t)nx * ny, 0);
+    for (int iy = 0; iy < ny; iy++)
+        for (int ix = 0; ix < nx; ix++) {
+            const float mu_x = dx * std::abs(ix - fsx - is * dsx), mu_y = dy * std::abs(iy - fsy - is * dsy);
+            const float mu_z = dz * fsz;
+            const float mu_t0 = sqrtf((float)(std::pow(mu_x, 2) + std::pow(mu_y, 2) + std::pow(mu_z, 2))) /
+                                (vp1 * sqrtf(1 + 2 * eps1));
+            const int mu_t = (int)(2.0 / (dt * favg));
+            const int mu_nt = (int)(mu_t0 / dt) + mu_t + tt;
+            const int a = (int)(mu_t0 / dt) - tt + 1;
+            lo[(size_t)iy * nx + ix] = a < 0 ? 0 : (a < nt ? a : nt);
+            hi[(size_t)iy * nx + ix] = mu_nt < 0 ? 0 : (mu_nt < nt ? mu_nt : nt);
+        }
+}
+
 int check_model(const float *v, const float *e, const float *d, size_t n) {
     for (size_t i = 0; i < n; i++) {
         if (!std::isfinite(v[i]) || !(v[i] > 0.0f)) return fail(GEO_ERR_MODEL, "velocity[%zu]=%g", i, v[i]);

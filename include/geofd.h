@@ -164,6 +164,28 @@ int geo_fd3d_get_fields(geo_fd3d_plan *plan, float *P, float *Q, int mem, void *
 int geo_fd3d_shot(const geo_fd3d_desc *desc, int is, const float *v, const float *e, const float *d,
                   float *shot, int mem, void *stream);
 
+/* 3D boundary-saving RTM with the 3D GPU RTM program's semantics
+ * (3D-vti-fd+rtm-cuda/Toa_gpu_3dvti_rtm_adcigs_1orderfunction.cu:882-981):
+ * per shot a forward run records P+Q at z = npml on every surface node and
+ * saves one ring of P,Q just outside the model box per step; the record is
+ * muted (window form, tt = mute_tt); the backward loop rebuilds the source
+ * field from the ring and back-propagates the record; illumination sums
+ * P^2+Q^2 of both fields, the image sums sP*gP.  Replaces that program's
+ * shot loop and its migration_illum / laplace_3d_filter tail (:970-981).
+ * fd.rec_* and fd.mute_tt are ignored (the receivers are the whole
+ * surface); shots are is = 0..ns-1 at fs + is*ds. */
+typedef struct geo_rtm3d_desc {
+    geo_fd3d_desc fd;
+    int   ns;                /* number of shots                              */
+    int   mute_tt;           /* window half-width of the direct-wave mute    */
+} geo_rtm3d_desc;
+
+/* v,e,d: nx*ny*nz.  mig: nx*ny*nz image divided by the illumination where
+ * it is non-zero.  mig_lap, illum (optional, may be NULL): the image after
+ * laplace_3d_filter, and the illumination. */
+int geo_rtm3d(const geo_rtm3d_desc *desc, const float *v, const float *e, const float *d,
+              float *mig, float *mig_lap, float *illum, int mem, void *stream);
+
 /* 2D RTM with the MPI CPU program's semantics on per-shot aperture windows
  * (2D-vti-fd+rtm-mpi/Toa_rtm_vti_adcig_cdp.c:295-392 with
  * model_vti_get_boundry :483 and RTM_corr_adcig :739).  All shots run

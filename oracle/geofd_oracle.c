@@ -662,21 +662,47 @@ typedef struct {
     int rec_iz, rx0, drx, nrx, ry0, dry, nry;
 } orc_fd3d_desc;
 
-/* 3D VTI forward modelling of one shot with the GUI GPU program's semantics
- * (GPU_vti3dfd_kernels.cu): point Ricker source added to P,Q before the
- * velocity update (:53-88), velocity (:90-129) and split-sponge stress
- * (:131-201) updates on [4, nn-4) in every axis, optional SV taper (R=15,
- * r=4, centre fs+is*ds+npml-1), sponge profiles of the GPU form, d0 from the
- * centre velocity (:203-206).  shot is (nt x nrx*nry) trace-major,
- * shot[it + nt*(irx + nrx*iry)] = P[rec_iz, npd+rx0+irx*drx, npd+ry0+iry*dry].
- * final_fields (optional) receives the padded P, Q at the end. */
-int orc_fd3d(const orc_fd3d_desc *d, const float *v, const float *e, const float *dl,
-             float *shot, float *final_P, float *final_Q)
+/* 3D working set: model, sponge profiles and one or more wavefield sets. */
+typedef struct {
+    long nnx, nny, nnz, nxz, n;
+    int npd, nx, ny, nz, fast;
+    REAL dtx, dty, dtz;
+    float *cx1, *cx2, *ax1, *ax2, *cy1, *cy2, *ay1, *ay2, *cz1, *cz2, *az1, *az2;
+    REAL *vp, *e2, *d2, *mA, *mB, *mC;
+    float *amp; unsigned char *act;
+    long src;
+} orc_g3d;
+
+typedef struct {
+    REAL *u, *v, *w, *P, *Q, *px, *py, *pz, *qx, *qy, *qz;
+} orc_f3d;
+
+static void f3d_alloc(orc_f3d *f, long n)
+{
+    f->u = calloc(n, sizeof(REAL)); f->v = calloc(n, sizeof(REAL)); f->w = calloc(n, sizeof(REAL));
+    f->P = calloc(n, sizeof(REAL)); f->Q = calloc(n, sizeof(REAL));
+    f->px = calloc(n, sizeof(REAL)); f->py = calloc(n, sizeof(REAL)); f->pz = calloc(n, sizeof(REAL));
+    f->qx = calloc(n, sizeof(REAL)); f->qy = calloc(n, sizeof(REAL)); f->qz = calloc(n, sizeof(REAL));
+}
+
+static void f3d_free(orc_f3d *f)
+{
+    free(f->u); free(f->v); free(f->w); free(f->P); free(f->Q);
+    free(f->px); free(f->py); free(f->pz); free(f->qx); free(f->qy); free(f->qz);
+}
+
+/* Model set-up with the GUI GPU program's semantics (GPU_vti3dfd_kernels.cu):
+ * edge padding, optional SV taper (R=15, r=4, centre fs+is*ds+npml-1),
+ * sponge profiles of the GPU form with d0 from the centre velocity. */
+static void g3d_init(orc_g3d *G, const orc_fd3d_desc *d, const float *v, const float *e, const float *dl)
 {
     const int npd = d->npd;
     const long nnx = d->nx + 2 * npd, nny = d->ny + 2 * npd, nnz = d->nz + 2 * npd, nxz = nnx * nnz;
     const long n = nxz * nny;
-    long ix, iy, iz;
+    long ix, iy, iz, k;
+    memset(G, 0, sizeof *G);
+    G->nnx = nnx; G->nny = nny; G->nnz = nnz; G->nxz = nxz; G->n = n;
+    G->npd = npd; G->nx = d->nx; G->ny = d->ny; G->nz = d->nz; G->fast = d->mode == 1;
     float *vv = calloc(n, 4), *ee = calloc(n, 4), *dd = calloc(n, 4);
     REAL *tmp = malloc(n * sizeof(REAL));
     for (iy = 0; iy < d->ny; iy++) for (ix = 0; ix < d->nx; ix++) for (iz = 0; iz < d->nz; iz++) {
@@ -684,7 +710,7 @@ int orc_fd3d(const orc_fd3d_desc *d, const float *v, const float *e, const float
         vv[g] = v[s]; ee[g] = e[s]; dd[g] = dl[s];
     }
     {
-        float *arrs[3] = {ee, dd, vv}; int a; long k;
+        float *arrs[3] = {ee, dd, vv}; int a;
         for (a = 0; a < 3; a++) {
             for (k = 0; k < n; k++) tmp[k] = arrs[a][k];
             orc_pad3d(d->nx, d->ny, d->nz, npd, tmp);
@@ -709,149 +735,269 @@ int orc_fd3d(const orc_fd3d_desc *d, const float *v, const float *e, const float
         }
     }
     float d0 = orc_d0(ORC_V_GPU, 3, 0.0f, vv[nny * nnx * nnz / 2], npd, d->dx, d->dy, d->dz);
-    float *cx1 = malloc(nnx * 4), *cx2 = malloc(nnx * 4), *ax1 = malloc(nnx * 4), *ax2 = malloc(nnx * 4);
-    float *cy1 = malloc(nny * 4), *cy2 = malloc(nny * 4), *ay1 = malloc(nny * 4), *ay2 = malloc(nny * 4);
-    float *cz1 = malloc(nnz * 4), *cz2 = malloc(nnz * 4), *az1 = malloc(nnz * 4), *az2 = malloc(nnz * 4);
-    orc_sponge(ORC_V_GPU, d->nx, npd, d->dt, d0, cx1, cx2, ax1, ax2);
-    orc_sponge(ORC_V_GPU, d->ny, npd, d->dt, d0, cy1, cy2, ay1, ay2);
-    orc_sponge(ORC_V_GPU, d->nz, npd, d->dt, d0, cz1, cz2, az1, az2);
-
-    REAL *vp = malloc(n * sizeof(REAL)), *e2 = malloc(n * sizeof(REAL)), *d2 = malloc(n * sizeof(REAL));
-    const int fast = d->mode == 1;
-    REAL *mA = fast ? malloc(n * sizeof(REAL)) : NULL, *mB = fast ? malloc(n * sizeof(REAL)) : NULL,
-         *mC = fast ? malloc(n * sizeof(REAL)) : NULL;
-    long k;
+    G->cx1 = malloc(nnx * 4); G->cx2 = malloc(nnx * 4); G->ax1 = malloc(nnx * 4); G->ax2 = malloc(nnx * 4);
+    G->cy1 = malloc(nny * 4); G->cy2 = malloc(nny * 4); G->ay1 = malloc(nny * 4); G->ay2 = malloc(nny * 4);
+    G->cz1 = malloc(nnz * 4); G->cz2 = malloc(nnz * 4); G->az1 = malloc(nnz * 4); G->az2 = malloc(nnz * 4);
+    orc_sponge(ORC_V_GPU, d->nx, npd, d->dt, d0, G->cx1, G->cx2, G->ax1, G->ax2);
+    orc_sponge(ORC_V_GPU, d->ny, npd, d->dt, d0, G->cy1, G->cy2, G->ay1, G->ay2);
+    orc_sponge(ORC_V_GPU, d->nz, npd, d->dt, d0, G->cz1, G->cz2, G->az1, G->az2);
+    G->vp = malloc(n * sizeof(REAL)); G->e2 = malloc(n * sizeof(REAL)); G->d2 = malloc(n * sizeof(REAL));
+    if (G->fast) { G->mA = malloc(n * sizeof(REAL)); G->mB = malloc(n * sizeof(REAL)); G->mC = malloc(n * sizeof(REAL)); }
     for (k = 0; k < n; k++) {
-        vp[k] = vv[k];
-        e2[k] = (REAL)1 + (REAL)2 * (REAL)ee[k];
-        d2[k] = RSQRT((REAL)1 + (REAL)2 * (REAL)dd[k]);
-        if (fast) {
-            const REAL c2 = vp[k] * vp[k];
-            mA[k] = c2 * e2[k];
-            mB[k] = c2 * d2[k];
-            mC[k] = c2;
+        G->vp[k] = vv[k];
+        G->e2[k] = (REAL)1 + (REAL)2 * (REAL)ee[k];
+        G->d2[k] = RSQRT((REAL)1 + (REAL)2 * (REAL)dd[k]);
+        if (G->fast) {
+            const REAL c2 = G->vp[k] * G->vp[k];
+            G->mA[k] = c2 * G->e2[k];
+            G->mB[k] = c2 * G->d2[k];
+            G->mC[k] = c2;
         }
     }
     free(vv); free(ee); free(dd);
-    REAL *u = calloc(n, sizeof(REAL)), *vv_ = calloc(n, sizeof(REAL)), *w = calloc(n, sizeof(REAL));
-    REAL *P = calloc(n, sizeof(REAL)), *Q = calloc(n, sizeof(REAL));
-    REAL *px = calloc(n, sizeof(REAL)), *py = calloc(n, sizeof(REAL)), *pz = calloc(n, sizeof(REAL));
-    REAL *qx = calloc(n, sizeof(REAL)), *qy = calloc(n, sizeof(REAL)), *qz = calloc(n, sizeof(REAL));
-    float *amp = malloc(d->nt * 4); unsigned char *act = malloc(d->nt);
-    orc_source_amp(ORC_V_GPU, d->nt, d->dt, d->favg, d->pfac, d->wtype, amp, act);
-    const long ixs = d->fsx + d->is * d->dsx + npd - 1, iys = d->fsy + d->is * d->dsy + npd - 1,
-               izs = d->fsz + d->is * d->dsz + npd - 1;
-    const long src = izs + ixs * nnz + iys * nxz;
-    const REAL dtx = (REAL)(d->dt / d->dx), dty = (REAL)(d->dt / d->dy), dtz = (REAL)(d->dt / d->dz);
-    int it;
-    for (it = 0; it < d->nt; it++) {
-        REAL P_src0 = P[src], Q_src0 = Q[src];
-        if (act[it]) { P[src] += (REAL)amp[it]; Q[src] += (REAL)amp[it]; }
+    G->amp = malloc(d->nt * 4); G->act = malloc(d->nt);
+    orc_source_amp(ORC_V_GPU, d->nt, d->dt, d->favg, d->pfac, d->wtype, G->amp, G->act);
+    {
+        const long ixs = d->fsx + d->is * d->dsx + npd - 1, iys = d->fsy + d->is * d->dsy + npd - 1,
+                   izs = d->fsz + d->is * d->dsz + npd - 1;
+        G->src = izs + ixs * nnz + iys * nxz;
+    }
+    G->dtx = (REAL)(d->dt / d->dx); G->dty = (REAL)(d->dt / d->dy); G->dtz = (REAL)(d->dt / d->dz);
+}
+
+static void g3d_free(orc_g3d *G)
+{
+    free(G->cx1); free(G->cx2); free(G->ax1); free(G->ax2); free(G->cy1); free(G->cy2); free(G->ay1); free(G->ay2);
+    free(G->cz1); free(G->cz2); free(G->az1); free(G->az2);
+    free(G->vp); free(G->e2); free(G->d2); free(G->mA); free(G->mB); free(G->mC); free(G->amp); free(G->act);
+}
+
+/* One 3D time step of field set F; the point source (amp, when src_on) is
+ * added to P,Q before the velocity update (GPU_vti3dfd_kernels.cu:135) and
+ * only affects the velocities (the stress update overwrites P,Q). */
+static void g3d_step(const orc_g3d *G, orc_f3d *F, int src_on, REAL amp)
+{
+    const long nnx = G->nnx, nny = G->nny, nnz = G->nnz, nxz = G->nxz, src = G->src;
+    const int npd = G->npd, fast = G->fast;
+    const REAL dtx = G->dtx, dty = G->dty, dtz = G->dtz;
+    REAL *u = F->u, *vv_ = F->v, *w = F->w, *P = F->P, *Q = F->Q;
+    REAL *px = F->px, *py = F->py, *pz = F->pz, *qx = F->qx, *qy = F->qy, *qz = F->qz;
+    const float *cx1 = G->cx1, *cx2 = G->cx2, *cy1 = G->cy1, *cy2 = G->cy2, *cz1 = G->cz1, *cz2 = G->cz2;
+    const float *ax1 = G->ax1, *ax2 = G->ax2, *ay1 = G->ay1, *ay2 = G->ay2, *az1 = G->az1, *az2 = G->az2;
+    const REAL *vp = G->vp, *e2 = G->e2, *d2 = G->d2, *mA = G->mA, *mB = G->mB, *mC = G->mC;
+    long ix, iy, iz;
+    REAL P_src0 = P[src], Q_src0 = Q[src];
+    if (src_on) { P[src] += amp; Q[src] += amp; }
 #pragma omp parallel for schedule(static) private(ix, iz)
-        for (iy = 4; iy < nny - 4; iy++)
-            for (ix = 4; ix < nnx - 4; ix++)
-                for (iz = 4; iz < nnz - 4; iz++) {
-                    long id = iz + ix * nnz + iy * nxz; int im;
-                    REAL xx = 0, yy = 0, zz = 0;
-                    if (fast) {
-                        yy = (REAL)C8[0] * (P[id + nxz] - P[id]);
-                        xx = (REAL)C8[0] * (P[id + nnz] - P[id]);
-                        zz = (REAL)C8[0] * (Q[id + 1] - Q[id]);
-                        for (im = 1; im < 4; im++) {
-                            yy = RFMA((REAL)C8[im], P[id + (im + 1) * nxz] - P[id - im * nxz], yy);
-                            xx = RFMA((REAL)C8[im], P[id + (im + 1) * nnz] - P[id - im * nnz], xx);
-                            zz = RFMA((REAL)C8[im], Q[id + im + 1] - Q[id - im], zz);
-                        }
-                        u[id] = RFMA(-(cx1[ix] * dtx), xx, cx2[ix] * u[id]);
-                        vv_[id] = RFMA(-(cy1[iy] * dty), yy, cy2[iy] * vv_[id]);
-                        w[id] = RFMA(-(cz1[iz] * dtz), zz, cz2[iz] * w[id]);
-                        continue;
+    for (iy = 4; iy < nny - 4; iy++)
+        for (ix = 4; ix < nnx - 4; ix++)
+            for (iz = 4; iz < nnz - 4; iz++) {
+                long id = iz + ix * nnz + iy * nxz; int im;
+                REAL xx = 0, yy = 0, zz = 0;
+                if (fast) {
+                    yy = (REAL)C8[0] * (P[id + nxz] - P[id]);
+                    xx = (REAL)C8[0] * (P[id + nnz] - P[id]);
+                    zz = (REAL)C8[0] * (Q[id + 1] - Q[id]);
+                    for (im = 1; im < 4; im++) {
+                        yy = RFMA((REAL)C8[im], P[id + (im + 1) * nxz] - P[id - im * nxz], yy);
+                        xx = RFMA((REAL)C8[im], P[id + (im + 1) * nnz] - P[id - im * nnz], xx);
+                        zz = RFMA((REAL)C8[im], Q[id + im + 1] - Q[id - im], zz);
                     }
-                    for (im = 0; im < 4; im++) {
-                        yy += (REAL)C8[im] * (P[id + (im + 1) * nxz] - P[id - im * nxz]);
-                        xx += (REAL)C8[im] * (P[id + (im + 1) * nnz] - P[id - im * nnz]);
-                        zz += (REAL)C8[im] * (Q[id + im + 1] - Q[id - im]);
-                    }
-                    u[id] = cx2[ix] * u[id] - cx1[ix] * dtx * xx;
-                    vv_[id] = cy2[iy] * vv_[id] - cy1[iy] * dty * yy;
-                    w[id] = cz2[iz] * w[id] - cz1[iz] * dtz * zz;
+                    u[id] = RFMA(-(cx1[ix] * dtx), xx, cx2[ix] * u[id]);
+                    vv_[id] = RFMA(-(cy1[iy] * dty), yy, cy2[iy] * vv_[id]);
+                    w[id] = RFMA(-(cz1[iz] * dtz), zz, cz2[iz] * w[id]);
+                    continue;
                 }
+                for (im = 0; im < 4; im++) {
+                    yy += (REAL)C8[im] * (P[id + (im + 1) * nxz] - P[id - im * nxz]);
+                    xx += (REAL)C8[im] * (P[id + (im + 1) * nnz] - P[id - im * nnz]);
+                    zz += (REAL)C8[im] * (Q[id + im + 1] - Q[id - im]);
+                }
+                u[id] = cx2[ix] * u[id] - cx1[ix] * dtx * xx;
+                vv_[id] = cy2[iy] * vv_[id] - cy1[iy] * dty * yy;
+                w[id] = cz2[iz] * w[id] - cz1[iz] * dtz * zz;
+            }
 #pragma omp parallel for schedule(static) private(ix, iz)
-        for (iy = 4; iy < nny - 4; iy++)
-            for (ix = 4; ix < nnx - 4; ix++)
-                for (iz = 4; iz < nnz - 4; iz++) {
-                    long id = iz + ix * nnz + iy * nxz; int im;
-                    REAL xx = 0, yy = 0, zz = 0, c = vp[id];
-                    if (fast) {
-                        /* premultiplied model: A = vp^2(1+2eps), B = vp^2 sqrtf(1+2del), C = vp^2 */
-                        const REAL A = mA[id], B = mB[id], Cc = mC[id];
-                        yy = (REAL)C8[0] * (vv_[id] - vv_[id - nxz]);
-                        xx = (REAL)C8[0] * (u[id] - u[id - nnz]);
-                        zz = (REAL)C8[0] * (w[id] - w[id - 1]);
-                        for (im = 1; im < 4; im++) {
-                            yy = RFMA((REAL)C8[im], vv_[id + im * nxz] - vv_[id - (im + 1) * nxz], yy);
-                            xx = RFMA((REAL)C8[im], u[id + im * nnz] - u[id - (im + 1) * nnz], xx);
-                            zz = RFMA((REAL)C8[im], w[id + im] - w[id - im - 1], zz);
-                        }
-                        const REAL Ax = A * dtx, Ay = A * dty, Bz = B * dtz, Bx = B * dtx, By = B * dty, Cz = Cc * dtz;
-                        int inside = ix >= npd && ix < npd + d->nx && iy >= npd && iy < npd + d->ny
-                                     && iz >= npd && iz < npd + d->nz;
-                        if (inside) {
-                            REAL p0 = (id == src) ? P_src0 : P[id], q0 = (id == src) ? Q_src0 : Q[id];
-                            p0 = RFMA(-Ax, xx, p0); p0 = RFMA(-Ay, yy, p0); p0 = RFMA(-Bz, zz, p0);
-                            q0 = RFMA(-Bx, xx, q0); q0 = RFMA(-By, yy, q0); q0 = RFMA(-Cz, zz, q0);
-                            P[id] = p0; Q[id] = q0;
-                        } else {
-                            px[id] = RFMA(-(ax1[ix] * Ax), xx, ax2[ix] * px[id]);
-                            py[id] = RFMA(-(ay1[iy] * Ay), yy, ay2[iy] * py[id]);
-                            pz[id] = RFMA(-(az1[iz] * Bz), zz, az2[iz] * pz[id]);
-                            qx[id] = RFMA(-(ax1[ix] * Bx), xx, ax2[ix] * qx[id]);
-                            qy[id] = RFMA(-(ay1[iy] * By), yy, ay2[iy] * qy[id]);
-                            qz[id] = RFMA(-(az1[iz] * Cz), zz, az2[iz] * qz[id]);
-                            P[id] = px[id] + py[id] + pz[id];
-                            Q[id] = qx[id] + qy[id] + qz[id];
-                        }
-                        continue;
+    for (iy = 4; iy < nny - 4; iy++)
+        for (ix = 4; ix < nnx - 4; ix++)
+            for (iz = 4; iz < nnz - 4; iz++) {
+                long id = iz + ix * nnz + iy * nxz; int im;
+                REAL xx = 0, yy = 0, zz = 0, c = vp[id];
+                if (fast) {
+                    const REAL A = mA[id], B = mB[id], Cc = mC[id];
+                    yy = (REAL)C8[0] * (vv_[id] - vv_[id - nxz]);
+                    xx = (REAL)C8[0] * (u[id] - u[id - nnz]);
+                    zz = (REAL)C8[0] * (w[id] - w[id - 1]);
+                    for (im = 1; im < 4; im++) {
+                        yy = RFMA((REAL)C8[im], vv_[id + im * nxz] - vv_[id - (im + 1) * nxz], yy);
+                        xx = RFMA((REAL)C8[im], u[id + im * nnz] - u[id - (im + 1) * nnz], xx);
+                        zz = RFMA((REAL)C8[im], w[id + im] - w[id - im - 1], zz);
                     }
-                    for (im = 0; im < 4; im++) {
-                        yy += (REAL)C8[im] * (vv_[id + im * nxz] - vv_[id - (im + 1) * nxz]);
-                        xx += (REAL)C8[im] * (u[id + im * nnz] - u[id - (im + 1) * nnz]);
-                        zz += (REAL)C8[im] * (w[id + im] - w[id - im - 1]);
-                    }
-                    int inside = d->mode == 1 && ix >= npd && ix < npd + d->nx && iy >= npd && iy < npd + d->ny
-                                 && iz >= npd && iz < npd + d->nz;
+                    const REAL Ax = A * dtx, Ay = A * dty, Bz = B * dtz, Bx = B * dtx, By = B * dty, Cz = Cc * dtz;
+                    int inside = ix >= npd && ix < npd + G->nx && iy >= npd && iy < npd + G->ny
+                                 && iz >= npd && iz < npd + G->nz;
                     if (inside) {
                         REAL p0 = (id == src) ? P_src0 : P[id], q0 = (id == src) ? Q_src0 : Q[id];
-                        P[id] = p0 - c * c * e2[id] * dtx * xx - c * c * e2[id] * dty * yy - c * c * d2[id] * dtz * zz;
-                        Q[id] = q0 - c * c * d2[id] * dtx * xx - c * c * d2[id] * dty * yy - c * c * dtz * zz;
+                        p0 = RFMA(-Ax, xx, p0); p0 = RFMA(-Ay, yy, p0); p0 = RFMA(-Bz, zz, p0);
+                        q0 = RFMA(-Bx, xx, q0); q0 = RFMA(-By, yy, q0); q0 = RFMA(-Cz, zz, q0);
+                        P[id] = p0; Q[id] = q0;
                     } else {
-                        px[id] = ax2[ix] * px[id] - ax1[ix] * c * c * e2[id] * dtx * xx;
-                        py[id] = ay2[iy] * py[id] - ay1[iy] * c * c * e2[id] * dty * yy;
-                        pz[id] = az2[iz] * pz[id] - az1[iz] * c * c * d2[id] * dtz * zz;
-                        qx[id] = ax2[ix] * qx[id] - ax1[ix] * c * c * d2[id] * dtx * xx;
-                        qy[id] = ay2[iy] * qy[id] - ay1[iy] * c * c * d2[id] * dty * yy;
-                        qz[id] = az2[iz] * qz[id] - az1[iz] * c * c * dtz * zz;
+                        px[id] = RFMA(-(ax1[ix] * Ax), xx, ax2[ix] * px[id]);
+                        py[id] = RFMA(-(ay1[iy] * Ay), yy, ay2[iy] * py[id]);
+                        pz[id] = RFMA(-(az1[iz] * Bz), zz, az2[iz] * pz[id]);
+                        qx[id] = RFMA(-(ax1[ix] * Bx), xx, ax2[ix] * qx[id]);
+                        qy[id] = RFMA(-(ay1[iy] * By), yy, ay2[iy] * qy[id]);
+                        qz[id] = RFMA(-(az1[iz] * Cz), zz, az2[iz] * qz[id]);
                         P[id] = px[id] + py[id] + pz[id];
                         Q[id] = qx[id] + qy[id] + qz[id];
                     }
+                    continue;
                 }
-        {
-            int irx, iry;
-            for (iry = 0; iry < d->nry; iry++)
-                for (irx = 0; irx < d->nrx; irx++) {
-                    long gx = npd + d->rx0 + (long)irx * d->drx, gy = npd + d->ry0 + (long)iry * d->dry;
-                    shot[it + (long)d->nt * (irx + (long)d->nrx * iry)] = (float)P[d->rec_iz + nnz * gx + nxz * gy];
+                for (im = 0; im < 4; im++) {
+                    yy += (REAL)C8[im] * (vv_[id + im * nxz] - vv_[id - (im + 1) * nxz]);
+                    xx += (REAL)C8[im] * (u[id + im * nnz] - u[id - (im + 1) * nnz]);
+                    zz += (REAL)C8[im] * (w[id + im] - w[id - im - 1]);
                 }
+                px[id] = ax2[ix] * px[id] - ax1[ix] * c * c * e2[id] * dtx * xx;
+                py[id] = ay2[iy] * py[id] - ay1[iy] * c * c * e2[id] * dty * yy;
+                pz[id] = az2[iz] * pz[id] - az1[iz] * c * c * d2[id] * dtz * zz;
+                qx[id] = ax2[ix] * qx[id] - ax1[ix] * c * c * d2[id] * dtx * xx;
+                qy[id] = ay2[iy] * qy[id] - ay1[iy] * c * c * d2[id] * dty * yy;
+                qz[id] = az2[iz] * qz[id] - az1[iz] * c * c * dtz * zz;
+                P[id] = px[id] + py[id] + pz[id];
+                Q[id] = qx[id] + qy[id] + qz[id];
+            }
+}
+
+/* 3D VTI forward modelling of one shot with the GUI GPU program's semantics
+ * (GPU_vti3dfd_kernels.cu): point Ricker source added to P,Q before the
+ * velocity update (:53-88), velocity (:90-129) and split-sponge stress
+ * (:131-201) updates on [4, nn-4) in every axis, optional SV taper (R=15,
+ * r=4, centre fs+is*ds+npml-1), sponge profiles of the GPU form, d0 from the
+ * centre velocity (:203-206).  shot is (nt x nrx*nry) trace-major,
+ * shot[it + nt*(irx + nrx*iry)] = P[rec_iz, npd+rx0+irx*drx, npd+ry0+iry*dry].
+ * final_P/final_Q (optional) receive the padded P, Q at the end. */
+int orc_fd3d(const orc_fd3d_desc *d, const float *v, const float *e, const float *dl,
+             float *shot, float *final_P, float *final_Q)
+{
+    orc_g3d G; orc_f3d F;
+    int it; long k;
+    g3d_init(&G, d, v, e, dl);
+    f3d_alloc(&F, G.n);
+    for (it = 0; it < d->nt; it++) {
+        g3d_step(&G, &F, G.act[it], (REAL)G.amp[it]);
+        int irx, iry;
+        for (iry = 0; iry < d->nry; iry++)
+            for (irx = 0; irx < d->nrx; irx++) {
+                long gx = d->npd + d->rx0 + (long)irx * d->drx, gy = d->npd + d->ry0 + (long)iry * d->dry;
+                shot[it + (long)d->nt * (irx + (long)d->nrx * iry)] = (float)F.P[d->rec_iz + G.nnz * gx + G.nxz * gy];
+            }
+    }
+    if (final_P) for (k = 0; k < G.n; k++) final_P[k] = (float)F.P[k];
+    if (final_Q) for (k = 0; k < G.n; k++) final_Q[k] = (float)F.Q[k];
+    f3d_free(&F); g3d_free(&G);
+    return 0;
+}
+
+/* 3D RTM of one shot with the 3D GPU RTM program's semantics
+ * (3D-vti-fd+rtm-cuda/Toa_gpu_3dvti_rtm_adcigs_1orderfunction.cu:882-968):
+ *   forward: source step (SV taper on), save one ring of P,Q just outside
+ *     the interior (faces z=npml-1, z=npml+nz, x=npml-1, x=npml+nx,
+ *     y=npml-1, y=npml+ny; wavefield_bndr :405-506), record P+Q at z=npml
+ *     for every surface node (:319-334), illum += P^2+Q^2 (:523-537);
+ *   mute the record (window form, tt; :352-390);
+ *   backward it=nt-1..0: restore the ring into the source field and step it
+ *     again (the program's boundary-driven reconstruction), write the record
+ *     into P,Q of the receiver field at z=npml-1 and step it, illum +=
+ *     gP^2+gQ^2, mig += sP*gP (:926-968).
+ * mig and illum (nx*ny*nz interior, iz + nz*(ix + nx*iy)) accumulate over
+ * calls; the caller divides (migration_illum :539-553) and filters.  The
+ * wavefields start from zero for every shot (the program zeroes them once
+ * before its shot loop). */
+int orc_rtm3d_shot(const orc_fd3d_desc *d, int mute_tt, const float *v, const float *e, const float *dl,
+                   float *mig, float *illum, float *rec_out)
+{
+    orc_g3d G; orc_f3d S, R;
+    const int nx = d->nx, ny = d->ny, nz = d->nz, npd = d->npd, nt = d->nt;
+    long it, ix, iy, iz;
+    g3d_init(&G, d, v, e, dl);
+    f3d_alloc(&S, G.n);
+    f3d_alloc(&R, G.n);
+    const long L = 2L * nx * ny + 2L * nz * ny + 2L * nx * nz;
+    float *bp = calloc((size_t)nt * L, 4), *bq = calloc((size_t)nt * L, 4);
+    float *rec = calloc((size_t)nt * nx * ny, 4);
+#define GID(z, x, y) ((long)(z) + G.nnz * (long)(x) + G.nxz * (long)(y))
+    /* ring position of entry k (the program's face order) */
+#define RING(k, gid) do { long k_ = (k); \
+        if (k_ < (long)nx * ny) { gid = GID(npd - 1, npd + k_ % nx, npd + k_ / nx); } \
+        else if (k_ < 2L * nx * ny) { k_ -= (long)nx * ny; gid = GID(npd + nz, npd + k_ % nx, npd + k_ / nx); } \
+        else if (k_ < 2L * nx * ny + (long)nz * ny) { k_ -= 2L * nx * ny; gid = GID(npd + k_ % nz, npd - 1, npd + k_ / nz); } \
+        else if (k_ < 2L * nx * ny + 2L * nz * ny) { k_ -= 2L * nx * ny + (long)nz * ny; gid = GID(npd + k_ % nz, npd + nx, npd + k_ / nz); } \
+        else if (k_ < 2L * nx * ny + 2L * nz * ny + (long)nx * nz) { k_ -= 2L * nx * ny + 2L * nz * ny; gid = GID(npd + k_ % nz, npd + k_ / nz, npd - 1); } \
+        else { k_ -= 2L * nx * ny + 2L * nz * ny + (long)nx * nz; gid = GID(npd + k_ % nz, npd + k_ / nz, npd + ny); } } while (0)
+    for (it = 0; it < nt; it++) {
+        long k;
+        g3d_step(&G, &S, G.act[it], (REAL)G.amp[it]);
+        for (k = 0; k < L; k++) {
+            long gid; RING(k, gid);
+            bp[it * L + k] = (float)S.P[gid]; bq[it * L + k] = (float)S.Q[gid];
+        }
+        for (iy = 0; iy < ny; iy++) for (ix = 0; ix < nx; ix++) {
+            long gid = GID(npd, npd + ix, npd + iy);
+            rec[it + (long)nt * ix + (long)nt * nx * iy] = (float)(S.P[gid] + S.Q[gid]);
+        }
+        for (iy = 0; iy < ny; iy++) for (ix = 0; ix < nx; ix++) for (iz = 0; iz < nz; iz++) {
+            long gid = GID(npd + iz, npd + ix, npd + iy), o = iz + (long)nz * ix + (long)nz * nx * iy;
+            REAL p = S.P[gid], q = S.Q[gid];
+            illum[o] = (float)(illum[o] + (p * p + q * q));
         }
     }
-    if (final_P) for (k = 0; k < n; k++) final_P[k] = (float)P[k];
-    if (final_Q) for (k = 0; k < n; k++) final_Q[k] = (float)Q[k];
-    free(cx1); free(cx2); free(ax1); free(ax2); free(cy1); free(cy2); free(ay1); free(ay2);
-    free(cz1); free(cz2); free(az1); free(az2);
-    free(vp); free(e2); free(d2); free(u); free(vv_); free(w); free(P); free(Q);
-    free(px); free(py); free(pz); free(qx); free(qy); free(qz); free(amp); free(act);
-    free(mA); free(mB); free(mC);
+    /* mute_directwave, window form (:352-390), source at (fsx+is*dsx, fsy+is*dsy) */
+    {
+        /* vp[1], eps[1] of the padded model = the model's first cell */
+        const float eps1 = e[0], vp1 = v[0];
+        for (iy = 0; iy < ny; iy++) for (ix = 0; ix < nx; ix++) {
+            float mu_x = d->dx * abs((int)ix - d->fsx - d->is * d->dsx), mu_y = d->dy * abs((int)iy - d->fsy - d->is * d->dsy);
+            float mu_z = d->dz * d->fsz;
+            float mu_t0 = sqrtf((float)(pow(mu_x, 2) + pow(mu_y, 2) + pow(mu_z, 2))) / (vp1 * sqrtf(1 + 2 * eps1));
+            int mu_t = (int)(2.0 / (d->dt * d->favg));
+            int mu_nt = (int)(mu_t0 / d->dt) + mu_t + mute_tt;
+            for (it = 0; it < nt; it++)
+                if ((it > (int)(mu_t0 / d->dt) - mute_tt) && (it < mu_nt)) rec[it + (long)nt * ix + (long)nt * nx * iy] = 0.0f;
+        }
+    }
+    if (rec_out) memcpy(rec_out, rec, (size_t)nt * nx * ny * 4);
+    for (it = nt - 1; it >= 0; it--) {
+        long k;
+        for (k = 0; k < L; k++) {
+            long gid; RING(k, gid);
+            S.P[gid] = (REAL)bp[it * L + k]; S.Q[gid] = (REAL)bq[it * L + k];
+        }
+        g3d_step(&G, &S, 0, 0);
+        for (iy = 0; iy < ny; iy++) for (ix = 0; ix < nx; ix++) {
+            long gid = GID(npd - 1, npd + ix, npd + iy);
+            R.P[gid] = R.Q[gid] = (REAL)rec[it + (long)nt * ix + (long)nt * nx * iy];
+        }
+        g3d_step(&G, &R, 0, 0);
+        for (iy = 0; iy < ny; iy++) for (ix = 0; ix < nx; ix++) for (iz = 0; iz < nz; iz++) {
+            long gid = GID(npd + iz, npd + ix, npd + iy), o = iz + (long)nz * ix + (long)nz * nx * iy;
+            REAL gp = R.P[gid], gq = R.Q[gid];
+            illum[o] = (float)(illum[o] + (gp * gp + gq * gq));
+            mig[o] = (float)(mig[o] + S.P[gid] * gp);
+        }
+    }
+#undef RING
+#undef GID
+    free(bp); free(bq); free(rec);
+    f3d_free(&S); f3d_free(&R); g3d_free(&G);
     return 0;
+}
+
+/* migration_illum (:539-553): mig /= illum where illum != 0. */
+void orc_image_illum(long n, float *mig, const float *illum)
+{
+    long k;
+    for (k = 0; k < n; k++) if (illum[k] != 0) mig[k] = mig[k] / illum[k];
 }
 
 /* Direct-wave mute of a 3D record (mute_directwave3d, GPU_vti3dfd_kernels.cu:342-369):

@@ -1,0 +1,40 @@
+"""3D boundary-saving RTM on the GPU against the oracle (bit-exact)."""
+import numpy as np
+import pytest
+
+from tests.util import random_model_3d, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+KW = dict(npd=8, nt=150, dx=10.0, dy=10.0, dz=10.0, dt=np.float32(1e-3), favg=25.0, pfac=10.0,
+          fsx=6, fsy=8, fsz=2, dsx=7, ns=2, mute_tt=20)
+
+
+@pytest.mark.parametrize("mode,sv", [(0, 0), (1, 0), (1, 1)])
+def test_rtm3d_bit_exact(geo, orc, mode, sv):
+    v, e, d = random_model_3d(20, 17, 23, seed=11)
+    mig_o, ill_o, _ = orc.rtm3d(v, e, d, mode=mode, sv=sv, **KW)
+    lap_o = orc.laplace3d_adj(mig_o)
+    mig, lap, ill = geo.rtm3d(v, e, d, mode=mode, sv=sv, laplace=True, illum=True, **KW)
+    assert np.abs(mig_o).max() > 0 and np.abs(ill_o).max() > 0
+    assert np.array_equal(ill, ill_o), rel_l2(ill, ill_o)
+    assert np.array_equal(mig, mig_o), rel_l2(mig, mig_o)
+    assert np.array_equal(lap, lap_o), rel_l2(lap, lap_o)
+
+
+def test_rtm3d_device_buffers(geo, orc):
+    import torch
+    v, e, d = random_model_3d(18, 16, 20, seed=12)
+    kw = dict(KW, ns=1)
+    mig_o, _, _ = orc.rtm3d(v, e, d, mode=1, **kw)
+    tv, te, td = (torch.from_numpy(a).cuda() for a in (v, e, d))
+    mig = geo.rtm3d(tv, te, td, mode="fast", laplace=False, **kw)
+    assert mig.is_cuda
+    assert np.array_equal(mig.cpu().numpy(), mig_o)
+
+
+def test_rtm3d_fast_close_to_exact(geo):
+    v, e, d = random_model_3d(20, 18, 22, seed=13)
+    a = geo.rtm3d(v, e, d, mode="exact", laplace=False, **KW)
+    b = geo.rtm3d(v, e, d, mode="fast", laplace=False, **KW)
+    assert rel_l2(b, a) < 1e-4
