@@ -13,6 +13,7 @@ GEO_OK = 0
 GEO_MEM_HOST, GEO_MEM_DEVICE = 0, 1
 GEO_VARIANT_CPU, GEO_VARIANT_GPU, GEO_VARIANT_MPI = 0, 1, 2
 GEO_MODE_EXACT, GEO_MODE_FAST = 0, 1
+GEO_RTM_BOUNDARY, GEO_RTM_SNAPSHOT, GEO_RTM_LEARNED = 0, 1, 2
 
 STATUS = {0: "GEO_OK", 1: "GEO_ERR_ARG", 2: "GEO_ERR_CUDA", 3: "GEO_ERR_IO", 4: "GEO_ERR_MODEL",
           5: "GEO_ERR_CFL", 6: "GEO_ERR_WINDOW", 7: "GEO_ERR_NOMEM", 8: "GEO_ERR_NAN"}
@@ -41,7 +42,8 @@ class FD3DDesc(C.Structure):
 
 
 class RTM3DDesc(C.Structure):
-    _fields_ = [("fd", FD3DDesc), ("ns", C.c_int), ("mute_tt", C.c_int)]
+    _fields_ = [("fd", FD3DDesc), ("ns", C.c_int), ("mute_tt", C.c_int), ("method", C.c_int),
+                ("snap_every", C.c_int), ("ae", C.c_void_p)]
 
 
 class RTM2DDesc(C.Structure):
@@ -82,6 +84,19 @@ def lib():
         "geo_fd3d_shot": (_i, [C.POINTER(FD3DDesc), _i, _vp, _vp, _vp, _vp, _i, _vp]),
         "geo_rtm2d_batch": (_i, [C.POINTER(RTM2DDesc), _vp, _vp, _vp, _vp, _vp, _i, _vp]),
         "geo_rtm3d": (_i, [C.POINTER(RTM3DDesc), _vp, _vp, _vp, _vp, _vp, _vp, _i, _vp]),
+        "geo_ae_create": (_i, [C.POINTER(_vp), C.c_ulonglong]),
+        "geo_ae_destroy": (_i, [_vp]),
+        "geo_ae_num_params": (C.c_size_t, []),
+        "geo_ae_get_params": (_i, [_vp, _vp]),
+        "geo_ae_set_params": (_i, [_vp, _vp]),
+        "geo_ae_reserve": (_i, [_vp, C.c_longlong]),
+        "geo_ae_num_blocks": (C.c_longlong, [_vp]),
+        "geo_ae_add_blocks": (_i, [_vp, _vp, C.c_longlong, _i]),
+        "geo_ae_add_shot": (_i, [_vp, _vp, _i, _i, _i, _f, _vp]),
+        "geo_ae_train": (_i, [_vp, _i, _i, _f, _vp, _vp]),
+        "geo_ae_eval": (_i, [_vp, _vp, _i, _vp, C.POINTER(C.c_double), _vp, _i, _vp]),
+        "geo_ae_roundtrip": (_i, [_vp, _i, _i, _i, _vp, _vp, _vp]),
+        "geo_tc_gemm_bf16": (_i, [_i, _i, _i, _vp, _vp, _vp, _i, _vp, _i, _vp]),
         "geo_laplace2d": (_i, [_i, _i, _vp, _vp, _i, _vp]),
         "geo_laplace3d": (_i, [_i, _i, _i, _vp, _vp, _i, _vp]),
         "geo_par_load": (_i, [C.c_char_p, C.POINTER(_vp)]),

@@ -10,7 +10,8 @@ import ctypes as C
 import numpy as np
 
 from ._lib import (FD2DDesc, FD3DDesc, GEO_MEM_DEVICE, GEO_MEM_HOST, GEO_MODE_EXACT, GEO_MODE_FAST,
-                   GEO_VARIANT_CPU, GEO_VARIANT_GPU, GEO_VARIANT_MPI, RTM2DDesc, RTM3DDesc, check, lib)
+                   GEO_RTM_BOUNDARY, GEO_RTM_LEARNED, GEO_RTM_SNAPSHOT, GEO_VARIANT_CPU, GEO_VARIANT_GPU,
+                   GEO_VARIANT_MPI, RTM2DDesc, RTM3DDesc, check, lib)
 
 _VARIANTS = {"cpu": GEO_VARIANT_CPU, "gpu": GEO_VARIANT_GPU, "mpi": GEO_VARIANT_MPI}
 _MODES = {"exact": GEO_MODE_EXACT, "fast": GEO_MODE_FAST}
@@ -173,19 +174,27 @@ def fd3d_shot(v, e, d, is_=0, **kw):
         plan.close()
 
 
+_RTM = {"boundary": GEO_RTM_BOUNDARY, "snapshot": GEO_RTM_SNAPSHOT, "learned": GEO_RTM_LEARNED}
+
+
 def rtm3d(v, e, d, *, npd, nt, dx, dy, dz, dt, favg, fsx, fsy, fsz, ns=1, dsx=0, dsy=0, dsz=0, mute_tt=70,
-          pfac=10.0, wtype=1, sv=0, mode="fast", laplace=True, illum=False):
-    """3D boundary-saving RTM over shots 0..ns-1 (the 3D GPU RTM program's
-    semantics); v,e,d shaped (ny, nx, nz).  Returns the illumination-divided
-    image, then the Laplacian-filtered image if `laplace`, then the
-    illumination if `illum`."""
+          pfac=10.0, wtype=1, sv=0, mode="fast", laplace=True, illum=False, method="boundary", snap_every=4,
+          codec=None):
+    """3D RTM over shots 0..ns-1; v,e,d shaped (ny, nx, nz).
+
+    method "boundary": the 3D GPU RTM program's boundary-saving recompute;
+    "snapshot": source P kept every snap_every steps (fp32);
+    "learned": the same snapshots through `codec` (a trained Codec).
+    Returns the illumination-divided image, then the Laplacian-filtered image
+    if `laplace`, then the illumination if `illum`."""
     b = _Bufs(v, e, d)
     ny, nx, nz = v.shape
     fd = FD3DDesc(nx=nx, ny=ny, nz=nz, npd=npd, nt=nt, dx=dx, dy=dy, dz=dz, dt=dt, favg=favg, pfac=pfac,
                   wtype=wtype, sv=sv, mode=_MODES[mode] if isinstance(mode, str) else int(mode),
                   fsx=fsx, fsy=fsy, fsz=fsz, dsx=dsx, dsy=dsy, dsz=dsz, rec_iz=npd, rx0=0, drx=1, nrx=nx,
                   ry0=0, dry=1, nry=ny, mute_tt=0)
-    desc = RTM3DDesc(fd=fd, ns=ns, mute_tt=mute_tt)
+    desc = RTM3DDesc(fd=fd, ns=ns, mute_tt=mute_tt, method=_RTM[method] if isinstance(method, str) else int(method),
+                     snap_every=snap_every, ae=codec._p if codec is not None else None)
     pv, pe, pd = b.inp(v), b.inp(e), b.inp(d)
     mig, pm = b.out((ny, nx, nz), v)
     lap, pl = b.out((ny, nx, nz), v) if laplace else (None, None)
@@ -193,6 +202,104 @@ def rtm3d(v, e, d, *, npd, nt, dx, dy, dz, dt, favg, fsx, fsy, fsz, ns=1, dsx=0,
     check(lib().geo_rtm3d(C.byref(desc), pv, pe, pd, pm, pl, pi, b.mem, b.stream()), "geo_rtm3d")
     out = [mig] + ([lap] if laplace else []) + ([ill] if illum else [])
     return out[0] if len(out) == 1 else tuple(out)
+
+
+def morton_order():
+    """perm[m] = natural index (z + 16*x + 256*y) of Morton index m of a
+    16^3 block (bit 3l = z bit l, 3l+1 = x bit l, 3l+2 = y bit l)."""
+    m = np.arange(4096)
+    z = sum(((m >> (3 * l)) & 1) << l for l in range(4))
+    x = sum(((m >> (3 * l + 1)) & 1) << l for l in range(4))
+    y = sum(((m >> (3 * l + 2)) & 1) << l for l in range(4))
+    return z + 16 * x + 256 * y
+
+
+class Codec:
+    """The learned snapshot codec (geo_ae_*): a 4-level convolutional
+    autoencoder over 16^3 blocks trained on the GPU."""
+
+    def __init__(self, seed=1):
+        self._p = C.c_void_p()
+        check(lib().geo_ae_create(C.byref(self._p), C.c_ulonglong(seed)), "geo_ae_create")
+
+    @staticmethod
+    def num_params():
+        return int(lib().geo_ae_num_params())
+
+    def params(self):
+        out = np.empty(self.num_params(), np.float32)
+        check(lib().geo_ae_get_params(self._p, C.c_void_p(out.ctypes.data)), "geo_ae_get_params")
+        return out
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, np.float32)
+        check(lib().geo_ae_set_params(self._p, C.c_void_p(p.ctypes.data)), "geo_ae_set_params")
+
+    def reserve(self, max_blocks):
+        check(lib().geo_ae_reserve(self._p, int(max_blocks)), "geo_ae_reserve")
+
+    def num_blocks(self):
+        return int(lib().geo_ae_num_blocks(self._p))
+
+    def add_blocks(self, blocks):
+        b = _Bufs(blocks)
+        n = blocks.shape[0]
+        check(lib().geo_ae_add_blocks(self._p, b.inp(blocks), n, b.mem), "geo_ae_add_blocks")
+
+    def add_shot(self, plan, is_=0, snap_every=10, t_first=0, rel=1e-3):
+        check(lib().geo_ae_add_shot(self._p, plan._p, is_, snap_every, t_first, C.c_float(rel), None),
+              "geo_ae_add_shot")
+
+    def train(self, iters, batch=256, lr=1e-3):
+        loss = np.zeros(iters, np.float32)
+        check(lib().geo_ae_train(self._p, iters, batch, C.c_float(lr), C.c_void_p(loss.ctypes.data), None),
+              "geo_ae_train")
+        return loss
+
+    def eval(self, blocks, grad=True):
+        """(recon, loss, grad) on nb (multiple of 128) blocks (nb, 4096)."""
+        b = _Bufs(blocks)
+        nb = blocks.shape[0]
+        rec, pr = b.out((nb, 4096), blocks)
+        g, pg = b.out((self.num_params(),), blocks) if grad else (None, None)
+        loss = C.c_double()
+        check(lib().geo_ae_eval(self._p, b.inp(blocks), nb, pr, C.byref(loss), pg, b.mem, b.stream()), "geo_ae_eval")
+        return rec, loss.value, g
+
+    def roundtrip(self, vol):
+        """Encode + decode a (ny, nx, nz) CUDA tensor; returns the reconstruction."""
+        t = _torch()
+        vol = vol.to(t.float32).contiguous()
+        ny, nx, nz = vol.shape
+        out = t.empty_like(vol)
+        check(lib().geo_ae_roundtrip(self._p, nx, ny, nz, C.c_void_p(vol.data_ptr()), C.c_void_p(out.data_ptr()),
+                                     C.c_void_p(t.cuda.current_stream().cuda_stream)), "geo_ae_roundtrip")
+        return out
+
+    def close(self):
+        if self._p:
+            lib().geo_ae_destroy(self._p)
+            self._p = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def tc_gemm_bf16(A, B, bias=None, act=False, out_f32=True):
+    """out = A @ B^T (+bias) (leaky ReLU) with the codec's tcgen05 GEMM;
+    A (M, K), B (N, K) bf16 CUDA tensors."""
+    t = _torch()
+    M, K = A.shape
+    N = B.shape[0]
+    out = t.empty((M, N), dtype=t.float32 if out_f32 else t.bfloat16, device=A.device)
+    bp = C.c_void_p(bias.data_ptr()) if bias is not None else None
+    check(lib().geo_tc_gemm_bf16(M, N, K, C.c_void_p(A.data_ptr()), C.c_void_p(B.data_ptr()), bp, 1 if act else 0,
+                                 C.c_void_p(out.data_ptr()), 1 if out_f32 else 0,
+                                 C.c_void_p(t.cuda.current_stream().cuda_stream)), "geo_tc_gemm_bf16")
+    return out
 
 
 def rtm2d_batch(v, e, d, *, npd, nt, dx, dz, dt_ms, favg, pfac, zs, shot_x, shot_nxs, laplace=True,

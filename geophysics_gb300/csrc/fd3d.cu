@@ -15,6 +15,7 @@
 #include "geo_internal.h"
 #include "fd3d.cuh"
 #include "fd3d_fused.cuh"
+#include "ae.cuh"
 #include <algorithm>
 #include <cstdlib>
 #include <cmath>
@@ -544,14 +545,46 @@ extern "C" int geo_fd3d_shot(const geo_fd3d_desc *desc, int is, const float *v, 
 }
 
 // ---------------------------------------------------------------- RTM 3D
-// Boundary-saving RTM with the 3D GPU RTM program's semantics
-// (3D-vti-fd+rtm-cuda/Toa_gpu_3dvti_rtm_adcigs_1orderfunction.cu:882-981).
+namespace geo {
+
+// Source P of the interior box into a dense snapshot (iz + nz*(ix + nx*iy)).
+__global__ void k_snap_store(Grid3D g, const float *P, float *snap) {
+    const long n = (long)g.nx * g.ny * g.nz;
+    for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < n; k += (long)gridDim.x * blockDim.x) {
+        const int iz = (int)(k % g.nz), ix = (int)((k / g.nz) % g.nx), iy = (int)(k / ((long)g.nz * g.nx));
+        snap[k] = P[(g.npd + iz) + (long)g.ldz * (g.npd + ix) + g.sxy * (g.npd + iy)];
+    }
+}
+
+// mig += w * snap * gP on the interior box (the codec's imaging, same order).
+__global__ void k_snap_image(Grid3D g, const float *snap, const float *gP, float *mig, float w) {
+    const long n = (long)g.nx * g.ny * g.nz;
+    for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < n; k += (long)gridDim.x * blockDim.x) {
+        const int iz = (int)(k % g.nz), ix = (int)((k / g.nz) % g.nx), iy = (int)(k / ((long)g.nz * g.nx));
+        mig[k] = mig[k] + w * snap[k] * gP[(g.npd + iz) + (long)g.ldz * (g.npd + ix) + g.sxy * (g.npd + iy)];
+    }
+}
+
+static int grid_blocks(long n) { return (int)std::min<long>((n + 255) / 256, 152L * 16); }
+
+}  // namespace geo
+
+// 3D RTM.  Method GEO_RTM_BOUNDARY follows the 3D GPU RTM program
+// (3D-vti-fd+rtm-cuda/Toa_gpu_3dvti_rtm_adcigs_1orderfunction.cu:882-981):
+// ring save in the forward pass, source re-propagation driven by the ring in
+// the backward pass.  GEO_RTM_SNAPSHOT and GEO_RTM_LEARNED keep snapshots of
+// the source P instead and propagate only the receiver field backwards.
 extern "C" int geo_rtm3d(const geo_rtm3d_desc *desc, const float *v, const float *e, const float *d, float *mig_out,
                          float *lap_out, float *illum_out, int mem, void *stream) {
     if (!desc || !v || !e || !d || !mig_out) return fail(GEO_ERR_ARG, "null argument");
     if (mem != GEO_MEM_HOST && mem != GEO_MEM_DEVICE) return fail(GEO_ERR_ARG, "bad mem kind");
     const geo_rtm3d_desc &R = *desc;
     if (R.ns < 1) return fail(GEO_ERR_ARG, "ns must be >= 1");
+    const int method = R.method;
+    if (method != GEO_RTM_BOUNDARY && method != GEO_RTM_SNAPSHOT && method != GEO_RTM_LEARNED)
+        return fail(GEO_ERR_ARG, "unknown RTM method %d", method);
+    if (method != GEO_RTM_BOUNDARY && R.snap_every < 1) return fail(GEO_ERR_ARG, "snap_every must be >= 1");
+    if (method == GEO_RTM_LEARNED && !R.ae) return fail(GEO_ERR_ARG, "the learned method needs a codec");
     geo_fd3d_desc D = R.fd;
     // every surface node records P+Q at z = npml (shot_record :319-334)
     D.rec_iz = D.npd; D.rx0 = 0; D.drx = 1; D.nrx = D.nx; D.ry0 = 0; D.dry = 1; D.nry = D.ny;
@@ -563,8 +596,20 @@ extern "C" int geo_rtm3d(const geo_rtm3d_desc *desc, const float *v, const float
     GEO_TRY(geo_fd3d_set_model(p, v, e, d, mem, stream));
     const long nimg = (long)D.nx * D.ny * D.nz;
     const long L = 2L * D.nx * D.ny + 2L * D.nz * D.ny + 2L * D.nx * D.nz;
-    DevBuf ring, mig, ill, lap;
-    GEO_TRY(ring.alloc((size_t)2 * D.nt * L * 4));
+    const int k = method == GEO_RTM_BOUNDARY ? 1 : R.snap_every;
+    const int nsnap = method == GEO_RTM_BOUNDARY ? 0 : D.nt / k;
+    DevBuf ring, mig, ill, lap, snaps, codes, scales;
+    const Grid3D g0 = grid_of(p, 0);
+    const AeVolume box = ae_volume(nullptr, g0.ldz, g0.sxy, D.npd, D.npd, D.npd, D.nz, D.nx, D.ny);
+    const int crow = ae_code_rows(box);
+    if (method == GEO_RTM_BOUNDARY) {
+        GEO_TRY(ring.alloc((size_t)2 * D.nt * L * 4));
+    } else if (method == GEO_RTM_SNAPSHOT) {
+        GEO_TRY(snaps.alloc((size_t)std::max(nsnap, 1) * nimg * 4));
+    } else {
+        GEO_TRY(codes.alloc((size_t)std::max(nsnap, 1) * crow * kAeLat * 2));
+        GEO_TRY(scales.alloc((size_t)std::max(nsnap, 1) * crow * 4));
+    }
     GEO_TRY(mig.alloc(nimg * 4));
     GEO_TRY(ill.alloc(nimg * 4));
     GEO_TRY(mig.zero(s));
@@ -573,17 +618,17 @@ extern "C" int geo_rtm3d(const geo_rtm3d_desc *desc, const float *v, const float
     const int ntr = D.nx * D.ny;
     auto launch_ring = [&](int it, int save) -> int {
         Grid3D g = grid_of(p, 0);
-        const int blocks = (int)std::min<long>((L + 255) / 256, 152L * 16);
-        k_ring3d<<<blocks, 256, 0, s>>>(g, g.P, g.Q, bp, bq, L, it, save);
+        k_ring3d<<<grid_blocks(L), 256, 0, s>>>(g, g.P, g.Q, bp, bq, L, it, save);
         return check_launch("ring3d");
     };
+    auto is_snap = [&](int it) { return method != GEO_RTM_BOUNDARY && it % k == k - 1 && it / k < nsnap; };
     for (int is = 0; is < R.ns; is++) {
         StepArgs3D st{};
         GEO_TRY(source_cell(p, is, st));
         GEO_TRY(zero_state(p, 0, s));
         GEO_TRY(zero_state(p, 1, s));
         if (D.sv) GEO_TRY(taper_box_3d(p, is, true, s));
-        // forward: record P+Q, source illumination, save the ring
+        // forward: record P+Q, source illumination, keep the ring or the snapshots
         st.rec = p->rec_tm.as<float>();
         st.rec_iz = D.rec_iz; st.rx0 = 0; st.drx = 1; st.nrx = D.nx; st.ry0 = 0; st.dry = 1; st.nry = D.ny;
         st.rec_pq = 1;
@@ -593,7 +638,21 @@ extern "C" int geo_rtm3d(const geo_rtm3d_desc *desc, const float *v, const float
             st.src_on = p->on[it];
             st.amp = p->amp[it];
             GEO_TRY(step3d(p, 0, st, s));
-            GEO_TRY(launch_ring(it, 1));
+            if (method == GEO_RTM_BOUNDARY) {
+                GEO_TRY(launch_ring(it, 1));
+            } else if (is_snap(it)) {
+                const Grid3D g = grid_of(p, 0);
+                const int j = it / k;
+                if (method == GEO_RTM_SNAPSHOT) {
+                    k_snap_store<<<grid_blocks(nimg), 256, 0, s>>>(g, g.P, snaps.as<float>() + (size_t)j * nimg);
+                    GEO_TRY(check_launch("snap_store"));
+                } else {
+                    AeVolume vb = box;
+                    vb.src = g.P;
+                    GEO_TRY(ae_encode_volume(R.ae, vb, codes.as<__nv_bfloat16>() + (size_t)j * crow * kAeLat,
+                                             scales.as<float>() + (size_t)j * crow, s));
+                }
+            }
         }
         // direct-wave mute, window form (mute_directwave :352-390)
         if (R.mute_tt > 0) {
@@ -605,40 +664,51 @@ extern "C" int geo_rtm3d(const geo_rtm3d_desc *desc, const float *v, const float
             GEO_TRY(launch_mute_records(p->rec_tm.as<float>(), ntr, D.nt, p->mute_lo.as<int>(), p->mute_hi.as<int>(), s));
             GEO_CUDA(cudaStreamSynchronize(s));
         }
-        // backward: reconstruct the source side from the ring, propagate the
-        // record from the surface, image
+        // backward: propagate the record from the surface, image
         StepArgs3D sb{}, gb{};
         sb.ixs = gb.ixs = st.ixs; sb.iys = gb.iys = st.iys; sb.izs = gb.izs = st.izs;
         gb.ill = ill.as<float>();
-        gb.mig = mig.as<float>();
+        if (method == GEO_RTM_BOUNDARY) gb.mig = mig.as<float>();
         for (int it = D.nt - 1; it >= 0; it--) {
             sb.it = gb.it = it;
-            GEO_TRY(launch_ring(it, 0));
-            GEO_TRY(step3d(p, 0, sb, s));
+            if (method == GEO_RTM_BOUNDARY) {
+                GEO_TRY(launch_ring(it, 0));
+                GEO_TRY(step3d(p, 0, sb, s));
+            }
             {
                 Grid3D gg = grid_of(p, 1);
-                const int blocks = (int)std::min<long>((ntr + 255) / 256, 152L * 16);
-                k_inject3d<<<blocks, 256, 0, s>>>(gg, gg.P, gg.Q, p->rec_tm.as<float>(), it);
+                k_inject3d<<<grid_blocks(ntr), 256, 0, s>>>(gg, gg.P, gg.Q, p->rec_tm.as<float>(), it);
                 GEO_TRY(check_launch("inject3d"));
             }
-            gb.other_P = grid_of(p, 0).P;  // the source side's new level
+            if (method == GEO_RTM_BOUNDARY) gb.other_P = grid_of(p, 0).P;  // the source side's new level
             GEO_TRY(step3d(p, 1, gb, s));
+            if (is_snap(it)) {
+                const Grid3D g = grid_of(p, 1);
+                const int j = it / k;
+                if (method == GEO_RTM_SNAPSHOT) {
+                    k_snap_image<<<grid_blocks(nimg), 256, 0, s>>>(g, snaps.as<float>() + (size_t)j * nimg, g.P,
+                                                                    mig.as<float>(), (float)k);
+                    GEO_TRY(check_launch("snap_image"));
+                } else {
+                    GEO_TRY(ae_decode_volume(R.ae, box, codes.as<__nv_bfloat16>() + (size_t)j * crow * kAeLat,
+                                             scales.as<float>() + (size_t)j * crow, 1, nullptr, g.P, mig.as<float>(),
+                                             (float)k, s));
+                }
+            }
         }
         if (D.sv) GEO_TRY(taper_box_3d(p, is, false, s));
         GEO_TRY(check_err(p, s));
+        if (method == GEO_RTM_LEARNED) GEO_TRY(ae_check_err(R.ae, s));
     }
-    {
-        const int blocks = (int)std::min<long>((nimg + 255) / 256, 152L * 32);
-        k_image_illum<<<blocks, 256, 0, s>>>(mig.as<float>(), ill.as<float>(), nimg);
-        GEO_TRY(check_launch("image_illum"));
-    }
-    const cudaMemcpyKind k = mem == GEO_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
-    GEO_CUDA(cudaMemcpyAsync(mig_out, mig.p, nimg * 4, k, s));
-    if (illum_out) GEO_CUDA(cudaMemcpyAsync(illum_out, ill.p, nimg * 4, k, s));
+    k_image_illum<<<grid_blocks(nimg), 256, 0, s>>>(mig.as<float>(), ill.as<float>(), nimg);
+    GEO_TRY(check_launch("image_illum"));
+    const cudaMemcpyKind kind = mem == GEO_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+    GEO_CUDA(cudaMemcpyAsync(mig_out, mig.p, nimg * 4, kind, s));
+    if (illum_out) GEO_CUDA(cudaMemcpyAsync(illum_out, ill.p, nimg * 4, kind, s));
     if (lap_out) {
         GEO_TRY(lap.alloc(nimg * 4));
         GEO_TRY(launch_laplace3d(D.nx, D.ny, D.nz, mig.as<float>(), lap.as<float>(), s));
-        GEO_CUDA(cudaMemcpyAsync(lap_out, lap.p, nimg * 4, k, s));
+        GEO_CUDA(cudaMemcpyAsync(lap_out, lap.p, nimg * 4, kind, s));
     }
     GEO_CUDA(cudaStreamSynchronize(s));
     return GEO_OK;

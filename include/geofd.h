@@ -174,15 +174,32 @@ int geo_fd3d_shot(const geo_fd3d_desc *desc, int is, const float *v, const float
  * shot loop and its migration_illum / laplace_3d_filter tail (:970-981).
  * fd.rec_* and fd.mute_tt are ignored (the receivers are the whole
  * surface); shots are is = 0..ns-1 at fs + is*ds. */
+typedef struct geo_ae geo_ae;
+
+enum {
+    GEO_RTM_BOUNDARY = 0,    /* the program's boundary-saving recompute      */
+    GEO_RTM_SNAPSHOT = 1,    /* source P stored every snap_every steps       */
+    GEO_RTM_LEARNED  = 2     /* same snapshots through the learned codec     */
+};
+
 typedef struct geo_rtm3d_desc {
     geo_fd3d_desc fd;
     int   ns;                /* number of shots                              */
     int   mute_tt;           /* window half-width of the direct-wave mute    */
+    int   method;            /* GEO_RTM_*                                    */
+    int   snap_every;        /* snapshot interval (methods 1, 2)             */
+    geo_ae *ae;              /* trained codec (method 2)                     */
 } geo_rtm3d_desc;
 
 /* v,e,d: nx*ny*nz.  mig: nx*ny*nz image divided by the illumination where
  * it is non-zero.  mig_lap, illum (optional, may be NULL): the image after
- * laplace_3d_filter, and the illumination. */
+ * laplace_3d_filter, and the illumination.
+ * Methods 1 and 2 are additions without a reference counterpart: the
+ * forward pass keeps the source P of every snap_every-th step (it %
+ * snap_every == snap_every-1) -- as fp32 (SNAPSHOT) or as the codec's
+ * 16x-smaller code (LEARNED) -- so the backward pass propagates only the
+ * receiver field and images mig += snap_every * sP * gP at those steps.
+ * Illumination is the same as method 0 (every step, both fields). */
 int geo_rtm3d(const geo_rtm3d_desc *desc, const float *v, const float *e, const float *d,
               float *mig, float *mig_lap, float *illum, int mem, void *stream);
 
@@ -217,6 +234,44 @@ int geo_laplace2d(int nx, int nz, const float *in, float *out, int mem, void *st
 /* 3D form (laplace_3d_filter, 3D-vti-fd+rtm-cuda/
  * Toa_gpu_3dvti_rtm_adcigs_1orderfunction.cu:555-616). */
 int geo_laplace3d(int nx, int ny, int nz, const float *in, float *out, int mem, void *stream);
+
+/* ---- learned snapshot codec (no reference counterpart) -----------------
+ * A 4-level convolutional autoencoder over 16^3 blocks (kernel = stride = 2
+ * per level, leaky ReLU, bf16 weights and activations, fp32 accumulation on
+ * the tensor cores): 4096 fp32 points -> 512 bf16 + one fp32 scale.  It is
+ * trained on the GPU on snapshots the solver generates. */
+int geo_ae_create(geo_ae **ae, unsigned long long seed);
+int geo_ae_destroy(geo_ae *ae);
+size_t geo_ae_num_params(void);
+/* Flat fp32 parameters: per level E1 E2 E3 E4 D4 D3 D2 D1, W [N x K] then b [N]. */
+int geo_ae_get_params(geo_ae *ae, float *host);
+int geo_ae_set_params(geo_ae *ae, const float *host);
+/* Training store: room for max_blocks blocks (16 KiB each, device). */
+int geo_ae_reserve(geo_ae *ae, long long max_blocks);
+long long geo_ae_num_blocks(geo_ae *ae);
+/* Append n blocks (Morton order within the block, raw amplitudes). */
+int geo_ae_add_blocks(geo_ae *ae, const float *blocks, long long n, int mem);
+/* Run shot `is` on a 3D plan and append, every snap_every steps from
+ * t_first, the full interior blocks of P whose max |P| exceeds rel times
+ * the snapshot's. */
+int geo_ae_add_shot(geo_ae *ae, geo_fd3d_plan *plan, int is, int snap_every, int t_first, float rel,
+                    void *stream);
+/* iters Adam steps on batches of `batch` (multiple of 128) blocks drawn from
+ * the store; loss (host, optional) receives each step's mean squared error
+ * in block-normalized units. */
+int geo_ae_train(geo_ae *ae, int iters, int batch, float lr, float *loss, void *stream);
+/* Forward (and backward when grad != NULL) on nb (multiple of 128) given
+ * blocks: recon = normalized reconstruction, loss = mean squared error,
+ * grad = d loss / d params. */
+int geo_ae_eval(geo_ae *ae, const float *blocks, int nb, float *recon, double *loss, float *grad, int mem,
+                void *stream);
+/* Encode + decode a dense nx*ny*nz volume (iz + nz*(ix + nx*iy), device). */
+int geo_ae_roundtrip(geo_ae *ae, int nx, int ny, int nz, const float *vol, float *out, void *stream);
+/* The codec's tensor-core GEMM (device pointers, bf16 row-major A [M x K],
+ * B [N x K]): out[M x N] = A * B^T (+bias) (leaky ReLU if act), fp32 or bf16
+ * out.  M % 128, N % 64, K % 64 must be 0. */
+int geo_tc_gemm_bf16(int M, int N, int K, const void *A, const void *B, const float *bias, int act, void *out,
+                     int out_f32, void *stream);
 
 /* ---- par file -------------------------------------------------------- */
 /* `key= value` lines (the reference's .par format, e.g.

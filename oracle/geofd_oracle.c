@@ -993,6 +993,73 @@ int orc_rtm3d_shot(const orc_fd3d_desc *d, int mute_tt, const float *v, const fl
     return 0;
 }
 
+/* 3D RTM of one shot with stored source snapshots (the library's
+ * GEO_RTM_SNAPSHOT method; no reference counterpart): the forward pass of
+ * orc_rtm3d_shot (record, source illumination, window mute) keeping the
+ * interior P of every step it with it % k == k-1; the backward pass
+ * propagates only the receiver field (same injection and illumination) and
+ * at those steps adds mig += (k * snap) * gP. */
+int orc_rtm3d_snap_shot(const orc_fd3d_desc *d, int mute_tt, int k, const float *v, const float *e, const float *dl,
+                        float *mig, float *illum)
+{
+    orc_g3d G; orc_f3d S, R;
+    const int nx = d->nx, ny = d->ny, nz = d->nz, npd = d->npd, nt = d->nt;
+    const long nimg = (long)nx * ny * nz;
+    const int nsnap = nt / k;
+    long it, ix, iy, iz;
+    g3d_init(&G, d, v, e, dl);
+    f3d_alloc(&S, G.n);
+    f3d_alloc(&R, G.n);
+    float *snap = calloc((size_t)(nsnap > 0 ? nsnap : 1) * nimg, 4);
+    float *rec = calloc((size_t)nt * nx * ny, 4);
+#define GID(z, x, y) ((long)(z) + G.nnz * (long)(x) + G.nxz * (long)(y))
+    for (it = 0; it < nt; it++) {
+        g3d_step(&G, &S, G.act[it], (REAL)G.amp[it]);
+        for (iy = 0; iy < ny; iy++) for (ix = 0; ix < nx; ix++) {
+            long gid = GID(npd, npd + ix, npd + iy);
+            rec[it + (long)nt * ix + (long)nt * nx * iy] = (float)(S.P[gid] + S.Q[gid]);
+        }
+        for (iy = 0; iy < ny; iy++) for (ix = 0; ix < nx; ix++) for (iz = 0; iz < nz; iz++) {
+            long gid = GID(npd + iz, npd + ix, npd + iy), o = iz + (long)nz * ix + (long)nz * nx * iy;
+            REAL p = S.P[gid], q = S.Q[gid];
+            illum[o] = (float)(illum[o] + (p * p + q * q));
+            if (it % k == k - 1 && it / k < nsnap) snap[(it / k) * nimg + o] = (float)p;
+        }
+    }
+    {
+        const float eps1 = e[0], vp1 = v[0];
+        for (iy = 0; iy < ny; iy++) for (ix = 0; ix < nx; ix++) {
+            float mu_x = d->dx * abs((int)ix - d->fsx - d->is * d->dsx), mu_y = d->dy * abs((int)iy - d->fsy - d->is * d->dsy);
+            float mu_z = d->dz * d->fsz;
+            float mu_t0 = sqrtf((float)(pow(mu_x, 2) + pow(mu_y, 2) + pow(mu_z, 2))) / (vp1 * sqrtf(1 + 2 * eps1));
+            int mu_t = (int)(2.0 / (d->dt * d->favg));
+            int mu_nt = (int)(mu_t0 / d->dt) + mu_t + mute_tt;
+            for (it = 0; it < nt; it++)
+                if ((it > (int)(mu_t0 / d->dt) - mute_tt) && (it < mu_nt)) rec[it + (long)nt * ix + (long)nt * nx * iy] = 0.0f;
+        }
+    }
+    for (it = nt - 1; it >= 0; it--) {
+        for (iy = 0; iy < ny; iy++) for (ix = 0; ix < nx; ix++) {
+            long gid = GID(npd - 1, npd + ix, npd + iy);
+            R.P[gid] = R.Q[gid] = (REAL)rec[it + (long)nt * ix + (long)nt * nx * iy];
+        }
+        g3d_step(&G, &R, 0, 0);
+        for (iy = 0; iy < ny; iy++) for (ix = 0; ix < nx; ix++) for (iz = 0; iz < nz; iz++) {
+            long gid = GID(npd + iz, npd + ix, npd + iy), o = iz + (long)nz * ix + (long)nz * nx * iy;
+            REAL gp = R.P[gid], gq = R.Q[gid];
+            illum[o] = (float)(illum[o] + (gp * gp + gq * gq));
+            if (it % k == k - 1 && it / k < nsnap) {
+                float w = (float)k * snap[(it / k) * nimg + o];
+                mig[o] = (float)(mig[o] + w * gp);
+            }
+        }
+    }
+#undef GID
+    free(snap); free(rec);
+    f3d_free(&S); f3d_free(&R); g3d_free(&G);
+    return 0;
+}
+
 /* migration_illum (:539-553): mig /= illum where illum != 0. */
 void orc_image_illum(long n, float *mig, const float *illum)
 {

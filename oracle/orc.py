@@ -64,6 +64,7 @@ def lib(prec=32):
         L.orc_mute3d.argtypes = [C.c_int] * 3 + [C.c_float] * 5 + [C.c_int] * 6 + [C.c_float] * 2 + \
             [C.c_int, C.POINTER(C.c_float)]
         L.orc_rtm3d_shot.argtypes = [C.POINTER(FD3DDesc), C.c_int] + [C.POINTER(C.c_float)] * 6
+        L.orc_rtm3d_snap_shot.argtypes = [C.POINTER(FD3DDesc), C.c_int, C.c_int] + [C.POINTER(C.c_float)] * 5
         L.orc_image_illum.argtypes = [C.c_long, C.POINTER(C.c_float), C.POINTER(C.c_float)]
         _libs[key] = L
     return _libs[key]
@@ -113,10 +114,11 @@ def fd3d(v, e, d, *, npd, nt, dx, dy, dz, dt, favg, pfac, fsx, fsy, fsz, dsx=0, 
 
 
 def rtm3d(v, e, d, *, npd, nt, dx, dy, dz, dt, favg, pfac, fsx, fsy, fsz, dsx=0, dsy=0, dsz=0,
-          ns=1, sv=0, wtype=1, mode=0, mute_tt=70, prec=32):
+          ns=1, sv=0, wtype=1, mode=0, mute_tt=70, snap_every=0, prec=32):
     """3D boundary-saving RTM over shots 0..ns-1 (3D GPU RTM program
-    semantics); v,e,d shaped (ny, nx, nz).  Returns (mig divided by the
-    illumination, illum, last shot's muted record (ny, nx, nt))."""
+    semantics; with snap_every > 0 the stored-snapshot method instead);
+    v,e,d shaped (ny, nx, nz).  Returns (mig divided by the illumination,
+    illum, last shot's muted record (ny, nx, nt); zeros for snap_every > 0)."""
     v, e, d = c32(v), c32(e), c32(d)
     ny, nx, nz = v.shape
     mig = np.zeros((ny, nx, nz), _f)
@@ -127,7 +129,11 @@ def rtm3d(v, e, d, *, npd, nt, dx, dy, dz, dt, favg, pfac, fsx, fsy, fsz, dsx=0,
                         dx=dx, dy=dy, dz=dz, dt=dt, favg=favg, pfac=pfac, fsx=fsx, fsy=fsy, fsz=fsz,
                         dsx=dsx, dsy=dsy, dsz=dsz, is_=is_, rec_iz=npd,
                         rx0=0, drx=1, nrx=nx, ry0=0, dry=1, nry=ny)
-        lib(prec).orc_rtm3d_shot(C.byref(desc), mute_tt, _fp(v), _fp(e), _fp(d), _fp(mig), _fp(ill), _fp(rec))
+        if snap_every:
+            lib(prec).orc_rtm3d_snap_shot(C.byref(desc), mute_tt, snap_every, _fp(v), _fp(e), _fp(d), _fp(mig),
+                                          _fp(ill))
+        else:
+            lib(prec).orc_rtm3d_shot(C.byref(desc), mute_tt, _fp(v), _fp(e), _fp(d), _fp(mig), _fp(ill), _fp(rec))
     lib(prec).orc_image_illum(mig.size, _fp(mig), _fp(ill))
     return mig, ill, rec
 

@@ -50,3 +50,22 @@ def to_np(x):
     except ImportError:
         pass
     return np.asarray(x)
+
+
+def wave_blocks(nb, seed):
+    """Band-limited random 16^3 blocks in Morton order (sums of plane waves
+    under a Gaussian envelope, amplitudes over two decades)."""
+    from oracle import ae_oracle as A
+    rng = np.random.default_rng(seed)
+    z, x, y = np.meshgrid(np.arange(16), np.arange(16), np.arange(16), indexing="ij")
+    out = np.zeros((nb, 4096), np.float32)
+    perm = A.morton_order()
+    zz, xx, yy = perm % 16, (perm // 16) % 16, perm // 256
+    for b in range(nb):
+        f = np.zeros((16, 16, 16))
+        for _ in range(3):
+            k = rng.normal(0, 0.6, 3)
+            f += rng.normal() * np.cos(k[0] * z + k[1] * x + k[2] * y + rng.uniform(0, 6.28))
+        f *= np.exp(-((z - 8) ** 2 + (x - 8) ** 2 + (y - 8) ** 2) / rng.uniform(20, 80))
+        out[b] = (rng.uniform(0.1, 10) * f)[zz, xx, yy]
+    return out
