@@ -95,7 +95,9 @@ def lib():
         "geo_ae_add_shot": (_i, [_vp, _vp, _i, _i, _i, _f, _vp]),
         "geo_ae_train": (_i, [_vp, _i, _i, _f, _vp, _vp]),
         "geo_ae_eval": (_i, [_vp, _vp, _i, _vp, C.POINTER(C.c_double), _vp, _i, _vp]),
-        "geo_ae_roundtrip": (_i, [_vp, _i, _i, _i, _vp, _vp, _vp]),
+        "geo_ae_roundtrip": (_i, [_vp, _i, _i, _i, _vp, _vp, _i, C.POINTER(_i), _vp]),
+        "geo_ae_set_escape": (_i, [_vp, _f, _f]),
+        "geo_ae_stats": (_i, [_vp, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]),
         "geo_tc_gemm_bf16": (_i, [_i, _i, _i, _vp, _vp, _vp, _i, _vp, _i, _vp]),
         "geo_laplace2d": (_i, [_i, _i, _vp, _vp, _i, _vp]),
         "geo_laplace3d": (_i, [_i, _i, _i, _vp, _vp, _i, _vp]),

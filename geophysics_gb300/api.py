@@ -266,15 +266,29 @@ class Codec:
         check(lib().geo_ae_eval(self._p, b.inp(blocks), nb, pr, C.byref(loss), pg, b.mem, b.stream()), "geo_ae_eval")
         return rec, loss.value, g
 
-    def roundtrip(self, vol):
-        """Encode + decode a (ny, nx, nz) CUDA tensor; returns the reconstruction."""
+    def roundtrip(self, vol, escape=False):
+        """Encode + decode a (ny, nx, nz) CUDA tensor; returns the
+        reconstruction (and the number of escaped blocks if `escape`)."""
         t = _torch()
         vol = vol.to(t.float32).contiguous()
         ny, nx, nz = vol.shape
         out = t.empty_like(vol)
+        ne = C.c_int(0)
         check(lib().geo_ae_roundtrip(self._p, nx, ny, nz, C.c_void_p(vol.data_ptr()), C.c_void_p(out.data_ptr()),
+                                     1 if escape else 0, C.byref(ne),
                                      C.c_void_p(t.cuda.current_stream().cuda_stream)), "geo_ae_roundtrip")
-        return out
+        return (out, ne.value) if escape else out
+
+    def set_escape(self, tau=0.05, frac=0.03):
+        """Per snapshot, keep bf16 residuals of the (at most frac of the)
+        blocks with the largest decoding error above tau times their norm."""
+        check(lib().geo_ae_set_escape(self._p, C.c_float(tau), C.c_float(frac)), "geo_ae_set_escape")
+
+    def stats(self):
+        """(blocks coded, blocks escaped) over the learned RTM shots so far."""
+        b, e = C.c_longlong(), C.c_longlong()
+        check(lib().geo_ae_stats(self._p, C.byref(b), C.byref(e)), "geo_ae_stats")
+        return b.value, e.value
 
     def close(self):
         if self._p:

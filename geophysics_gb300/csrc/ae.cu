@@ -194,6 +194,8 @@ struct D1Args {
     int step0;
     const float *wrow;            // mode 2: block weights (null: all 1)
     const float *wsum;            // mode 2: batch weight sum slot base (null: block count)
+    const int *esc;               // modes 0/1: escaped-block slot per row (-1: none), or null
+    const __nv_bfloat16 *res;     // modes 0/1: residual pool (4096 per slot, Morton)
 };
 
 __global__ void __launch_bounds__(256) k_ae_d1(const D1Args a) {
@@ -265,6 +267,14 @@ __global__ void __launch_bounds__(256) k_ae_d1(const D1Args a) {
         dst[0] = o4[0];
         dst[1] = o4[1];
     }
+    if (a.mode != 2 && a.esc) {
+        const int slot = a.esc[b];
+        if (slot >= 0) {
+            __syncthreads();
+            const __nv_bfloat16 *r = a.res + (long)slot * kAePts;
+            for (int m = t; m < kAePts; m += 256) ys[m] += __bfloat162float(r[m]);
+        }
+    }
     if (a.mode == 2) {
 #pragma unroll
         for (int o = 16; o; o >>= 1) lsum += __shfl_xor_sync(0xffffffffu, lsum, o);
@@ -296,6 +306,121 @@ __global__ void __launch_bounds__(256) k_ae_d1(const D1Args a) {
             a.mig[o] = a.mig[o] + a.wimg * val * a.gP[id];
         }
     }
+}
+
+// Escape pass 1 after encoding: decode each block (D1 from g1), keep its
+// residual x - decoded (bf16, all rows) and its squared error and norm.
+struct CheckArgs {
+    AeVolume vol;
+    int nb;
+    const __nv_bfloat16 *g1;
+    const float *v1, *c1, *scale;
+    __nv_bfloat16 *resall;        // [rows x 4096]
+    float *err2, *norm2;          // [rows]
+};
+
+__global__ void __launch_bounds__(256) k_ae_check(const CheckArgs a) {
+    __shared__ float ys[kAePts];
+    __shared__ float red[2][8];
+    const int b = blockIdx.x, t = threadIdx.x;
+    if (b >= a.nb) return;
+    const float s = a.scale[b];
+#pragma unroll 1
+    for (int r = 0; r < 2; r++) {
+        const int p = t + 256 * r;
+        const uint4 *src = reinterpret_cast<const uint4 *>(a.g1 + ((long)b * 512 + p) * 16);
+        uint4 q[2] = {src[0], src[1]};
+        const __nv_bfloat16 *qb = reinterpret_cast<const __nv_bfloat16 *>(q);
+#pragma unroll
+        for (int c = 0; c < 8; c++) {
+            float acc = 0.0f;
+#pragma unroll
+            for (int j = 0; j < 16; j++) acc += a.v1[c * 16 + j] * __bfloat162float(qb[j]);
+            ys[p * 8 + c] = (acc + a.c1[c]) * s;
+        }
+    }
+    __syncthreads();
+    const AeVolume &v = a.vol;
+    const int bz = b % v.nbz, bx = (b / v.nbz) % v.nbx, by = b / (v.nbz * v.nbx);
+    float e2 = 0.0f, x2 = 0.0f;
+    __nv_bfloat16 *rb = a.resall + (long)b * kAePts;
+    for (int p = 0; p < 16; p++) {
+        const int idx = p * 256 + t, z = idx & 15, x = (idx >> 4) & 15, y = idx >> 8;
+        const int iz = bz * 16 + z, ix = bx * 16 + x, iy = by * 16 + y;
+        const int m = morton_of(z, x, y);
+        float val = 0.0f;
+        if (iz < v.nz && ix < v.nx && iy < v.ny)
+            val = v.src[(long)(v.oz + iz) + v.ldz * (v.ox + ix) + v.sxy * (v.oy + iy)];
+        const float d = val - ys[m];
+        rb[m] = __float2bfloat16_rn(d);
+        e2 += d * d;
+        x2 += val * val;
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+        e2 += __shfl_xor_sync(0xffffffffu, e2, o);
+        x2 += __shfl_xor_sync(0xffffffffu, x2, o);
+    }
+    if ((t & 31) == 0) {
+        red[0][t >> 5] = e2;
+        red[1][t >> 5] = x2;
+    }
+    __syncthreads();
+    if (t == 0) {
+        float E = 0.0f, X = 0.0f;
+        for (int w = 0; w < 8; w++) {
+            E += red[0][w];
+            X += red[1][w];
+        }
+        a.err2[b] = E;
+        a.norm2[b] = X;
+    }
+}
+
+// Escape pass 2 (one block of 1024 threads): the cap blocks with the
+// largest squared error, among those with err2 > tau2 * norm2, get residual
+// slots: a binary search on the float bits of err2 finds the threshold.
+__global__ void __launch_bounds__(1024) k_ae_select(const float *err2, const float *norm2, int nb, float tau2, int cap,
+                                                    int *esc, int *count) {
+    __shared__ int cnt;
+    __shared__ int next;
+    auto eligible = [&](int b) { return err2[b] > 0.0f && err2[b] > tau2 * norm2[b]; };
+    // smallest threshold bits T with #{eligible, bits(err2) > T} <= cap
+    unsigned lo = 0u, hi = 0x7f800000u;   // error bits of non-negative floats
+    while (lo < hi) {
+        const unsigned mid = lo + (hi - lo) / 2;
+        if (threadIdx.x == 0) cnt = 0;
+        __syncthreads();
+        int c = 0;
+        for (int b = threadIdx.x; b < nb; b += blockDim.x) c += eligible(b) && __float_as_uint(err2[b]) > mid;
+        atomicAdd(&cnt, c);
+        __syncthreads();
+        const int total = cnt;
+        __syncthreads();
+        if (total <= cap) hi = mid;
+        else lo = mid + 1;
+    }
+    if (threadIdx.x == 0) next = 0;
+    __syncthreads();
+    for (int b = threadIdx.x; b < nb; b += blockDim.x) {
+        int sl = -1;
+        if (eligible(b) && __float_as_uint(err2[b]) > lo) sl = atomicAdd(&next, 1);
+        esc[b] = sl < cap ? sl : -1;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) *count = min(next, cap);
+}
+
+// Escape pass 3: copy the selected residuals into their slots.
+__global__ void __launch_bounds__(256) k_ae_escape_copy(const int *esc, const __nv_bfloat16 *resall,
+                                                        __nv_bfloat16 *res, int nb) {
+    const int b = blockIdx.x;
+    if (b >= nb) return;
+    const int sl = esc[b];
+    if (sl < 0) return;
+    const uint4 *src = reinterpret_cast<const uint4 *>(resall + (long)b * kAePts);
+    uint4 *dst = reinterpret_cast<uint4 *>(res + (long)sl * kAePts);
+    for (int i = threadIdx.x; i < kAePts / 8; i += 256) dst[i] = src[i];
 }
 
 // E1 weight and bias gradients from the normalized input and the gated
@@ -484,6 +609,11 @@ struct geo_ae {
     // training scratch
     int trows = 0;
     DevBuf xn, dg1, dg2, dg3, dz, dh3, dh2, dh1, wrow;
+    // escape settings
+    float tau = 0.05f, frac = 0.03f;
+    DevBuf resall, err2, norm2;
+    int erows = 0;
+    long long st_blocks = 0, st_escaped = 0;   // totals over RTM shots
 };
 
 namespace geo {
@@ -660,8 +790,16 @@ AeVolume ae_volume(const float *src, long ldz, long sxy, int oz, int ox, int oy,
 
 int ae_code_rows(const AeVolume &v) { return pad128(blocks_of(v)); }
 
-// Encode the interior box v into code[rows x 512] (bf16) and scale[rows].
-int ae_encode_volume(geo_ae *ae, const AeVolume &v, void *code, float *scale, cudaStream_t s) {
+int ae_escape_cap(geo_ae *ae, const AeVolume &v) {
+    const int nb = blocks_of(v);
+    return std::min(nb, (int)std::ceil(ae->frac * nb));
+}
+
+// Encode the interior box v into code[rows x 512] (bf16) and scale[rows];
+// with esc != null also decode, and keep the residuals of the blocks the
+// code misses (esc[rows], res[cap x 4096] bf16, *count escaped blocks).
+int ae_encode_volume(geo_ae *ae, const AeVolume &v, void *code, float *scale, int *esc, void *res, int *count,
+                     cudaStream_t s) {
     const int nb = blocks_of(v), rows = pad128(nb);
     GEO_TRY(ensure_rows(ae, rows));
     E1Args a = e1_args(ae, nb);
@@ -669,13 +807,39 @@ int ae_encode_volume(geo_ae *ae, const AeVolume &v, void *code, float *scale, cu
     a.scale = scale;
     k_ae_e1<<<rows, 256, 0, s>>>(a);
     GEO_TRY(check_launch("ae_e1"));
-    return encode_rows(ae, rows, static_cast<__nv_bfloat16 *>(code), s);
+    GEO_TRY(encode_rows(ae, rows, static_cast<__nv_bfloat16 *>(code), s));
+    if (!esc) return GEO_OK;
+    if (rows > ae->erows) {
+        GEO_TRY(ae->resall.alloc((size_t)rows * kAePts * 2));
+        GEO_TRY(ae->err2.alloc((size_t)rows * 4));
+        GEO_TRY(ae->norm2.alloc((size_t)rows * 4));
+        ae->erows = rows;
+    }
+    GEO_TRY(decode_rows(ae, rows, static_cast<const __nv_bfloat16 *>(code), s));
+    CheckArgs c{};
+    c.vol = v;
+    c.nb = nb;
+    c.g1 = bf(ae->g1);
+    c.v1 = ae->small.as<float>() + 128;
+    c.c1 = ae->params.as<float>() + ae->off.b[7];
+    c.scale = scale;
+    c.resall = bf(ae->resall);
+    c.err2 = ae->err2.as<float>();
+    c.norm2 = ae->norm2.as<float>();
+    k_ae_check<<<nb, 256, 0, s>>>(c);
+    GEO_TRY(check_launch("ae_check"));
+    k_ae_select<<<1, 1024, 0, s>>>(ae->err2.as<float>(), ae->norm2.as<float>(), nb, ae->tau * ae->tau,
+                                   ae_escape_cap(ae, v), esc, count);
+    GEO_TRY(check_launch("ae_select"));
+    k_ae_escape_copy<<<nb, 256, 0, s>>>(esc, bf(ae->resall), static_cast<__nv_bfloat16 *>(res), nb);
+    return check_launch("ae_escape_copy");
 }
 
-// Decode code/scale of box geometry v: mode 0 writes the snapshot into dst
-// (v's strides), mode 1 adds w * snapshot * gP to mig.
-int ae_decode_volume(geo_ae *ae, const AeVolume &v, const void *code, const float *scale, int mode, float *dst,
-                     const float *gP, float *mig, float w, cudaStream_t s) {
+// Decode code/scale (and escaped residuals) of box geometry v: mode 0
+// writes the snapshot into dst (v's strides), mode 1 adds w * snapshot * gP
+// to mig.
+int ae_decode_volume(geo_ae *ae, const AeVolume &v, const void *code, const float *scale, const int *esc,
+                     const void *res, int mode, float *dst, const float *gP, float *mig, float w, cudaStream_t s) {
     const int nb = blocks_of(v), rows = pad128(nb);
     GEO_TRY(ensure_rows(ae, rows));
     GEO_TRY(decode_rows(ae, rows, static_cast<const __nv_bfloat16 *>(code), s));
@@ -686,6 +850,8 @@ int ae_decode_volume(geo_ae *ae, const AeVolume &v, const void *code, const floa
     a.gP = gP;
     a.mig = mig;
     a.wimg = w;
+    a.esc = esc;
+    a.res = static_cast<const __nv_bfloat16 *>(res);
     k_ae_d1<<<rows, 256, 0, s>>>(a);
     return check_launch("ae_d1");
 }
@@ -986,18 +1152,54 @@ extern "C" int geo_ae_train(geo_ae *ae, int iters, int batch, float lr, float *l
     return GEO_OK;
 }
 
+void geo::ae_note_run(geo_ae *ae, long long blocks, long long escaped) {
+    ae->st_blocks += blocks;
+    ae->st_escaped += escaped;
+}
+
+// Coded and escaped blocks over the RTM shots run with this codec.
+extern "C" int geo_ae_stats(geo_ae *ae, long long *blocks, long long *escaped) {
+    if (!ae) return fail(GEO_ERR_ARG, "null codec");
+    if (blocks) *blocks = ae->st_blocks;
+    if (escaped) *escaped = ae->st_escaped;
+    return GEO_OK;
+}
+
+// Escape settings: per snapshot, the (at most frac of all) blocks with the
+// largest squared decoding error, among those whose error exceeds tau times
+// their norm, keep their residual.
+extern "C" int geo_ae_set_escape(geo_ae *ae, float tau, float frac) {
+    if (!ae || !(tau >= 0) || !(frac >= 0) || frac > 1) return fail(GEO_ERR_ARG, "bad argument");
+    ae->tau = tau;
+    ae->frac = frac;
+    return GEO_OK;
+}
+
 // Encode + decode a dense nz-fastest volume (nx*ny*nz, layout
-// iz + nz*(ix + nx*iy), device pointers): out = the codec's reconstruction.
-extern "C" int geo_ae_roundtrip(geo_ae *ae, int nx, int ny, int nz, const float *vol, float *out, void *stream) {
+// iz + nz*(ix + nx*iy), device pointers): out = the codec's reconstruction
+// (with escapes when `escape`); *nesc (optional) = escaped blocks.
+extern "C" int geo_ae_roundtrip(geo_ae *ae, int nx, int ny, int nz, const float *vol, float *out, int escape,
+                                int *nesc, void *stream) {
     if (!ae || !vol || !out || nx < 1 || ny < 1 || nz < 1) return fail(GEO_ERR_ARG, "bad argument");
     cudaStream_t s = (cudaStream_t)stream;
     const AeVolume v = ae_volume(vol, nz, (long)nz * nx, 0, 0, 0, nz, nx, ny);
-    const int rows = ae_code_rows(v);
-    DevBuf code, scale;
+    const int rows = ae_code_rows(v), cap = ae_escape_cap(ae, v);
+    DevBuf code, scale, esc, res, cnt;
     GEO_TRY(code.alloc((size_t)rows * kAeLat * 2));
     GEO_TRY(scale.alloc((size_t)rows * 4));
+    if (escape) {
+        GEO_TRY(esc.alloc((size_t)rows * 4));
+        GEO_TRY(res.alloc((size_t)std::max(cap, 1) * kAePts * 2));
+        GEO_TRY(cnt.alloc(16));
+        GEO_TRY(cnt.zero(s));
+    }
     GEO_CUDA(cudaMemsetAsync(ae->err.p, 0, 4, s));
-    GEO_TRY(ae_encode_volume(ae, v, code.p, scale.as<float>(), s));
-    GEO_TRY(ae_decode_volume(ae, v, code.p, scale.as<float>(), 0, out, nullptr, nullptr, 0.0f, s));
+    GEO_TRY(ae_encode_volume(ae, v, code.p, scale.as<float>(), esc.as<int>(), res.p, cnt.as<int>(), s));
+    GEO_TRY(ae_decode_volume(ae, v, code.p, scale.as<float>(), esc.as<int>(), res.p, 0, out, nullptr, nullptr, 0.0f,
+                             s));
+    if (nesc) {
+        *nesc = 0;
+        if (escape) GEO_CUDA(cudaMemcpyAsync(nesc, cnt.p, 4, cudaMemcpyDeviceToHost, s));
+    }
     return ae_check_err(ae, s);
 }

@@ -52,11 +52,17 @@ struct AeVolume {
 AeVolume ae_volume(const float *src, long ldz, long sxy, int oz, int ox, int oy, int nz, int nx, int ny);
 // Padded block count of a box (codes and scales are allocated per row).
 int ae_code_rows(const AeVolume &v);
-int ae_encode_volume(geo_ae *ae, const AeVolume &v, void *code, float *scale, cudaStream_t s);
+// Residual slots per snapshot for escaped blocks.
+int ae_escape_cap(geo_ae *ae, const AeVolume &v);
+// esc/res/count may be null (no escapes).
+int ae_encode_volume(geo_ae *ae, const AeVolume &v, void *code, float *scale, int *esc, void *res, int *count,
+                     cudaStream_t s);
 // mode 0: write the decoded snapshot to dst (v's strides); mode 1: add
 // w * snapshot * gP (v's strides) to the image mig (iz + nz*(ix + nx*iy)).
-int ae_decode_volume(geo_ae *ae, const AeVolume &v, const void *code, const float *scale, int mode, float *dst,
-                     const float *gP, float *mig, float w, cudaStream_t s);
+int ae_decode_volume(geo_ae *ae, const AeVolume &v, const void *code, const float *scale, const int *esc,
+                     const void *res, int mode, float *dst, const float *gP, float *mig, float w, cudaStream_t s);
 int ae_check_err(geo_ae *ae, cudaStream_t s);
+// Record coded and escaped block counts of an RTM shot (geo_ae_stats).
+void ae_note_run(geo_ae *ae, long long blocks, long long escaped);
 
 }  // namespace geo

@@ -598,17 +598,22 @@ extern "C" int geo_rtm3d(const geo_rtm3d_desc *desc, const float *v, const float
     const long L = 2L * D.nx * D.ny + 2L * D.nz * D.ny + 2L * D.nx * D.nz;
     const int k = method == GEO_RTM_BOUNDARY ? 1 : R.snap_every;
     const int nsnap = method == GEO_RTM_BOUNDARY ? 0 : D.nt / k;
-    DevBuf ring, mig, ill, lap, snaps, codes, scales;
+    DevBuf ring, mig, ill, lap, snaps, codes, scales, escs, resid, nesc;
     const Grid3D g0 = grid_of(p, 0);
     const AeVolume box = ae_volume(nullptr, g0.ldz, g0.sxy, D.npd, D.npd, D.npd, D.nz, D.nx, D.ny);
     const int crow = ae_code_rows(box);
+    const int ecap = method == GEO_RTM_LEARNED ? ae_escape_cap(R.ae, box) : 0;
     if (method == GEO_RTM_BOUNDARY) {
         GEO_TRY(ring.alloc((size_t)2 * D.nt * L * 4));
     } else if (method == GEO_RTM_SNAPSHOT) {
         GEO_TRY(snaps.alloc((size_t)std::max(nsnap, 1) * nimg * 4));
     } else {
-        GEO_TRY(codes.alloc((size_t)std::max(nsnap, 1) * crow * kAeLat * 2));
-        GEO_TRY(scales.alloc((size_t)std::max(nsnap, 1) * crow * 4));
+        const size_t ns1 = (size_t)std::max(nsnap, 1);
+        GEO_TRY(codes.alloc(ns1 * crow * kAeLat * 2));
+        GEO_TRY(scales.alloc(ns1 * crow * 4));
+        GEO_TRY(escs.alloc(ns1 * crow * 4));
+        GEO_TRY(resid.alloc(ns1 * std::max(ecap, 1) * kAePts * 2));
+        GEO_TRY(nesc.alloc(ns1 * 4));
     }
     GEO_TRY(mig.alloc(nimg * 4));
     GEO_TRY(ill.alloc(nimg * 4));
@@ -628,6 +633,7 @@ extern "C" int geo_rtm3d(const geo_rtm3d_desc *desc, const float *v, const float
         GEO_TRY(zero_state(p, 0, s));
         GEO_TRY(zero_state(p, 1, s));
         if (D.sv) GEO_TRY(taper_box_3d(p, is, true, s));
+        if (method == GEO_RTM_LEARNED) GEO_TRY(nesc.zero(s));
         // forward: record P+Q, source illumination, keep the ring or the snapshots
         st.rec = p->rec_tm.as<float>();
         st.rec_iz = D.rec_iz; st.rx0 = 0; st.drx = 1; st.nrx = D.nx; st.ry0 = 0; st.dry = 1; st.nry = D.ny;
@@ -650,7 +656,9 @@ extern "C" int geo_rtm3d(const geo_rtm3d_desc *desc, const float *v, const float
                     AeVolume vb = box;
                     vb.src = g.P;
                     GEO_TRY(ae_encode_volume(R.ae, vb, codes.as<__nv_bfloat16>() + (size_t)j * crow * kAeLat,
-                                             scales.as<float>() + (size_t)j * crow, s));
+                                             scales.as<float>() + (size_t)j * crow, escs.as<int>() + (size_t)j * crow,
+                                             resid.as<__nv_bfloat16>() + (size_t)j * ecap * kAePts,
+                                             nesc.as<int>() + j, s));
                 }
             }
         }
@@ -691,14 +699,23 @@ extern "C" int geo_rtm3d(const geo_rtm3d_desc *desc, const float *v, const float
                     GEO_TRY(check_launch("snap_image"));
                 } else {
                     GEO_TRY(ae_decode_volume(R.ae, box, codes.as<__nv_bfloat16>() + (size_t)j * crow * kAeLat,
-                                             scales.as<float>() + (size_t)j * crow, 1, nullptr, g.P, mig.as<float>(),
-                                             (float)k, s));
+                                             scales.as<float>() + (size_t)j * crow, escs.as<int>() + (size_t)j * crow,
+                                             resid.as<__nv_bfloat16>() + (size_t)j * ecap * kAePts, 1, nullptr, g.P,
+                                             mig.as<float>(), (float)k, s));
                 }
             }
         }
         if (D.sv) GEO_TRY(taper_box_3d(p, is, false, s));
         GEO_TRY(check_err(p, s));
-        if (method == GEO_RTM_LEARNED) GEO_TRY(ae_check_err(R.ae, s));
+        if (method == GEO_RTM_LEARNED) {
+            GEO_TRY(ae_check_err(R.ae, s));
+            std::vector<int> ne(std::max(nsnap, 1));
+            GEO_CUDA(cudaMemcpy(ne.data(), nesc.p, ne.size() * 4, cudaMemcpyDeviceToHost));
+            long long tot = 0;
+            for (int j = 0; j < nsnap; j++) tot += std::min(ne[j], ecap);
+            ae_note_run(R.ae, (long long)nsnap * (D.nx / 16 + (D.nx % 16 != 0)) * (D.ny / 16 + (D.ny % 16 != 0)) *
+                                  (D.nz / 16 + (D.nz % 16 != 0)), tot);
+        }
     }
     k_image_illum<<<grid_blocks(nimg), 256, 0, s>>>(mig.as<float>(), ill.as<float>(), nimg);
     GEO_TRY(check_launch("image_illum"));

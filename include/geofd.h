@@ -265,8 +265,17 @@ int geo_ae_train(geo_ae *ae, int iters, int batch, float lr, float *loss, void *
  * grad = d loss / d params. */
 int geo_ae_eval(geo_ae *ae, const float *blocks, int nb, float *recon, double *loss, float *grad, int mem,
                 void *stream);
-/* Encode + decode a dense nx*ny*nz volume (iz + nz*(ix + nx*iy), device). */
-int geo_ae_roundtrip(geo_ae *ae, int nx, int ny, int nz, const float *vol, float *out, void *stream);
+/* Encode + decode a dense nx*ny*nz volume (iz + nz*(ix + nx*iy), device);
+ * with `escape`, blocks the code misses keep a bf16 residual (*nesc of them). */
+int geo_ae_roundtrip(geo_ae *ae, int nx, int ny, int nz, const float *vol, float *out, int escape, int *nesc,
+                     void *stream);
+/* Escaped blocks: per snapshot, the blocks with the largest squared
+ * decoding error (at most frac of the snapshot's blocks, and only blocks
+ * whose error exceeds tau times their norm) keep their residual x - x' in
+ * bf16 (8 KiB each).  Defaults tau 0.05, frac 0.03. */
+int geo_ae_set_escape(geo_ae *ae, float tau, float frac);
+/* Blocks coded and blocks escaped over the learned RTM shots run so far. */
+int geo_ae_stats(geo_ae *ae, long long *blocks, long long *escaped);
 /* The codec's tensor-core GEMM (device pointers, bf16 row-major A [M x K],
  * B [N x K]): out[M x N] = A * B^T (+bias) (leaky ReLU if act), fp32 or bf16
  * out.  M % 128, N % 64, K % 64 must be 0. */

@@ -103,3 +103,34 @@ def test_learned_rtm_gains_over_untrained(geo, trained):
     assert np.isfinite(got).all()
     e_trained, e_untrained = rel_l2(got, ref), rel_l2(raw, ref)
     assert e_trained < 0.25 * e_untrained, (e_trained, e_untrained)
+
+
+def test_learned_rtm_with_every_block_escaped_matches_snapshots(geo, trained):
+    """With every block keeping its bf16 residual the coded snapshots equal
+    the stored ones up to bf16 rounding of the residual."""
+    from geophysics_gb300 import media
+    codec, _ = trained
+    v, e, d = media.random_vti(N3, N3, N3, seed=8, corr=15.0)
+    kw = dict(FD, nt=240, fsx=30, fsy=30, mute_tt=40, laplace=False)
+    ref = geo.rtm3d(v, e, d, method="snapshot", snap_every=4, **kw)
+    codec.set_escape(0.0, 1.0)
+    b0, e0 = codec.stats()
+    got = geo.rtm3d(v, e, d, method="learned", snap_every=4, codec=codec, **kw)
+    b1, e1 = codec.stats()
+    codec.set_escape()
+    assert e1 - e0 > 0.5 * (b1 - b0)
+    assert rel_l2(got, ref) < 2e-3
+
+
+def test_codec_roundtrip_escape_budget(geo, trained):
+    import torch
+    codec, _ = trained
+    rng = np.random.default_rng(2)
+    vol = torch.from_numpy(rng.normal(size=(32, 48, 40)).astype(np.float32)).cuda()   # ragged z blocks
+    codec.set_escape(0.0, 0.25)
+    out, ne = codec.roundtrip(vol, escape=True)
+    codec.set_escape()
+    nb = 2 * 3 * 3
+    assert ne == int(np.ceil(0.25 * nb))
+    base = codec.roundtrip(vol)
+    assert rel_l2(out.cpu().numpy(), vol.cpu().numpy()) < rel_l2(base.cpu().numpy(), vol.cpu().numpy())
