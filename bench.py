@@ -52,24 +52,26 @@ def algorithmic_bytes_per_step():
     return interior * 52 + sponge * 84
 
 
-def make_model(seed=2, device="cuda"):
+def make_model(seed=2, device="cuda", shape=None, corr=40.0):
+    """Seeded Gaussian random field (correlation `corr` cells) plus 3 dipping
+    interfaces; (ny, nx, nz) tensors vp, eps, del."""
     import torch
+    ny, nx, nz = shape or (NY, NX, NZ)
     g = torch.Generator(device="cpu").manual_seed(seed)
-    noise = torch.randn((NY, NX, NZ), generator=g, dtype=torch.float32).to(device)
-    L = 40.0
-    sig = L / 2.0
-    fy = torch.fft.fftfreq(NY, device=device)[:, None, None]
-    fx = torch.fft.fftfreq(NX, device=device)[None, :, None]
-    fz = torch.fft.rfftfreq(NZ, device=device)[None, None, :]
+    noise = torch.randn((ny, nx, nz), generator=g, dtype=torch.float32).to(device)
+    sig = corr / 2.0
+    fy = torch.fft.fftfreq(ny, device=device)[:, None, None]
+    fx = torch.fft.fftfreq(nx, device=device)[None, :, None]
+    fz = torch.fft.rfftfreq(nz, device=device)[None, None, :]
     filt = torch.exp(-2.0 * (torch.pi ** 2) * sig ** 2 * (fx ** 2 + fy ** 2 + fz ** 2))
-    G = torch.fft.irfftn(torch.fft.rfftn(noise) * filt, s=(NY, NX, NZ))
+    G = torch.fft.irfftn(torch.fft.rfftn(noise) * filt, s=(ny, nx, nz))
     G = (G - G.min()) / (G.max() - G.min())
     vp = 1500.0 + 2100.0 * G
-    iy = torch.arange(NY, device=device, dtype=torch.float32)[:, None, None]
-    ix = torch.arange(NX, device=device, dtype=torch.float32)[None, :, None]
-    iz = torch.arange(NZ, device=device, dtype=torch.float32)[None, None, :]
-    for z0, ax, ay in ((110.0, 0.10, 0.05), (210.0, -0.08, 0.12), (300.0, 0.05, -0.10)):
-        vp = vp + 300.0 * (iz > z0 + ax * (ix - NX / 2) + ay * (iy - NY / 2)).float()
+    iy = torch.arange(ny, device=device, dtype=torch.float32)[:, None, None]
+    ix = torch.arange(nx, device=device, dtype=torch.float32)[None, :, None]
+    iz = torch.arange(nz, device=device, dtype=torch.float32)[None, None, :]
+    for fz0, ax, ay in ((0.275, 0.10, 0.05), (0.525, -0.08, 0.12), (0.75, 0.05, -0.10)):
+        vp = vp + 300.0 * (iz > fz0 * nz + ax * (ix - nx / 2) + ay * (iy - ny / 2)).float()
     eps = 0.3 * (vp - 1500.0) / 3000.0
     dl = 0.15 * (vp - 1500.0) / 3000.0
     return vp.float().contiguous(), eps.float().contiguous(), dl.float().contiguous()
@@ -310,6 +312,125 @@ def run_traffic_case(args):
     print(json.dumps({"case": "traffic", "grid": NX, "steps": args.steps}))
 
 
+def train_codec(geo, iters, models=32, n=96, seed=1):
+    """The codec trained on snapshots the solver generates: `models` seeded
+    random-field media of n^3 (correlation 8-40 cells, random surface
+    source), P every 12 steps of a 560-step shot (SV taper on)."""
+    import numpy as np
+    import torch
+    codec = geo.Codec(seed=seed)
+    codec.reserve(150000)
+    rng = np.random.default_rng(seed)
+    kw = dict(npd=16, nt=560, dx=DX, dy=DX, dz=DX, dt=DT, favg=FAVG, fsz=1, mode="fast", sv=1)
+    t0 = time.perf_counter()
+    for s in range(models):
+        v, e, d = make_model(seed=100 + s, device="cuda", shape=(n, n, n), corr=float(rng.uniform(8, 40)))
+        plan = geo.FD3DPlan(nx=n, ny=n, nz=n, fsx=int(rng.integers(16, n - 16)), fsy=int(rng.integers(16, n - 16)),
+                            **kw)
+        plan.set_model(v, e, d)
+        codec.add_shot(plan, 0, snap_every=12, t_first=8)
+        plan.close()
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    loss = codec.train(iters, batch=256, lr=1e-3)
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    return codec, {"models": models, "grid": n, "blocks": codec.num_blocks(), "iters": iters,
+                   "collect_s": round(t1 - t0, 2), "train_s": round(t2 - t1, 2), "final_loss": float(loss[-50:].mean())}
+
+
+def run_rtm_learned_case(args):
+    """3D VTI RTM, one shot, 512x512x384 at 10 m (+40 sponge), dt 0.8 ms,
+    15 Hz: plain boundary-saving recompute against snapshots every 4 steps
+    through the learned codec (shots/hour), and the codec's image error
+    against stored fp32 snapshots (on the first err_nt steps: all 3000
+    steps of fp32 snapshots would need 302 GB)."""
+    import numpy as np
+    import torch
+
+    import geophysics_gb300 as geo
+    from geophysics_gb300 import build as B
+    B.build()
+    nx, ny, nz = 512, 512, 384
+    vp, eps, dl = make_model(seed=4, device="cuda", shape=(ny, nx, nz))
+    rk = dict(npd=NPD, dx=DX, dy=DX, dz=DX, dt=DT, favg=FAVG, fsx=nx // 2, fsy=ny // 2, fsz=1, mute_tt=70,
+              laplace=True, mode="fast", sv=1)
+    codec, tinfo = train_codec(geo, args.train_iters)
+
+    def timed(**kw):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        out = geo.rtm3d(vp, eps, dl, **rk, **kw)
+        torch.cuda.synchronize()
+        return out, time.perf_counter() - t0
+
+    res = {}
+    _, res["boundary"] = timed(nt=args.nt, method="boundary")
+    codec.set_escape(0.02, 0.0)
+    _, res["learned16"] = timed(nt=args.nt, method="learned", snap_every=4, codec=codec)
+    codec.set_escape(0.02, args.escape)
+    b0, e0 = codec.stats()
+    _, res["learned_esc"] = timed(nt=args.nt, method="learned", snap_every=4, codec=codec)
+    b1, e1 = codec.stats()
+    # image error on err_nt steps
+    ref, _ = timed(nt=args.err_nt, method="snapshot", snap_every=4)
+    codec.set_escape(0.02, 0.0)
+    l16, _ = timed(nt=args.err_nt, method="learned", snap_every=4, codec=codec)
+    codec.set_escape(0.02, args.escape)
+    les, _ = timed(nt=args.err_nt, method="learned", snap_every=4, codec=codec)
+    bnd, _ = timed(nt=args.err_nt, method="boundary")
+
+    def rel(a, b):
+        a, b = a[0].double(), b[0].double()
+        return float((a - b).norm() / b.norm())
+
+    esc_frac = (e1 - e0) / max(1, b1 - b0)
+
+    def per_block(f):   # bytes per 16^3 block: code, scale, escape slot map, residuals
+        return 1024 + 4 + 4 + f * 8192
+    line = {"case": "rtm-learned", "metric": "3D RTM shots/hr, learned snapshot codec vs boundary-saving recompute",
+            "grid": [nx, ny, nz], "sponge": NPD, "nt": args.nt, "snap_every": 4,
+            "shots_per_hr": {k: 3600.0 / v for k, v in res.items()}, "seconds": res,
+            "speedup_vs_boundary": {"learned16": res["boundary"] / res["learned16"],
+                                    "learned_esc": res["boundary"] / res["learned_esc"]},
+            "image_rel_l2_vs_fp32_snapshots": {"learned16": rel(l16, ref), "learned_esc": rel(les, ref),
+                                               "boundary": rel(bnd, ref), "err_nt": args.err_nt,
+                                               "image": "Laplacian-filtered, illumination-divided"},
+            "compression": {"learned16": 16384 / per_block(0.0),
+                            "learned_esc": 16384 / per_block(esc_frac), "escaped_block_frac": esc_frac,
+                            "escape_budget": args.escape},
+            "training": tinfo, "dtype": "f32 propagation, bf16 codec", "data": "synthetic"}
+    print(json.dumps(line), flush=True)
+
+
+def run_rtm_methods_case(args):
+    """Launch-list case: each RTM method of `--methods` for `--nt` steps on
+    the 512x512x384 grid (untrained codec: the timing does not depend on the
+    weights), then 45 bare steps of the same grid."""
+    import torch
+
+    import geophysics_gb300 as geo
+    nx, ny, nz = 512, 512, 384
+    vp, eps, dl = make_model(seed=4, device="cuda", shape=(ny, nx, nz))
+    rk = dict(npd=NPD, dx=DX, dy=DX, dz=DX, dt=DT, favg=FAVG, fsx=nx // 2, fsy=ny // 2, fsz=1, mute_tt=70,
+              laplace=False, mode="fast", sv=1, nt=args.nt)
+    codec = geo.Codec(seed=1)
+    out = {}
+    for m in args.methods.split(","):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        geo.rtm3d(vp, eps, dl, method=m, snap_every=4, codec=codec, **rk)
+        torch.cuda.synchronize()
+        out[m] = time.perf_counter() - t0
+    plan = geo.FD3DPlan(nx=nx, ny=ny, nz=nz, npd=NPD, nt=10, dx=DX, dy=DX, dz=DX, dt=DT, favg=FAVG, fsx=nx // 2,
+                        fsy=ny // 2, fsz=1, mode="fast")
+    plan.set_model(vp, eps, dl)
+    plan.time_steps(5)
+    out["bare_step_ms"] = plan.time_steps(40) / 40
+    plan.close()
+    print(json.dumps({"case": "rtm-methods", "grid": [nx, ny, nz], "nt": args.nt, "seconds": out}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -317,9 +438,20 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--case", default="full", choices=["full", "small", "traffic"],
-                    help="small / traffic: ncu profiling cases (not a bench line)")
+    ap.add_argument("--case", default="full", choices=["full", "small", "traffic", "rtm-learned", "rtm-methods"],
+                    help="small / traffic: ncu profiling cases; rtm-learned: the learned-codec RTM comparison")
+    ap.add_argument("--nt", type=int, default=3000, help="rtm-learned: time steps")
+    ap.add_argument("--err-nt", type=int, default=1200, help="rtm-learned: steps of the image-error comparison")
+    ap.add_argument("--train-iters", type=int, default=16000, help="rtm-learned: codec training steps")
+    ap.add_argument("--escape", type=float, default=0.03, help="rtm-learned: escaped-block budget")
+    ap.add_argument("--methods", default="boundary,learned", help="rtm-methods: methods to run")
     args = ap.parse_args()
+    if args.case == "rtm-methods":
+        run_rtm_methods_case(args)
+        return
+    if args.case == "rtm-learned":
+        run_rtm_learned_case(args)
+        return
     if args.case == "small":
         run_profile_case(args)
         return
