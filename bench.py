@@ -431,6 +431,108 @@ def run_rtm_methods_case(args):
     print(json.dumps({"case": "rtm-methods", "grid": [nx, ny, nz], "nt": args.nt, "seconds": out}), flush=True)
 
 
+def run_fd2d_case(args):
+    """2D VTI FD, one shot, with the CPU program's arithmetic (CPU_vti2dfd):
+    401x401 at 10 m, dt 1 ms, 2000 steps, 50-cell sponge, 20 Hz Ricker at
+    (200, 5), every surface node recorded at z = 5; 5 flat seeded layers.
+    The working set (~15 fields of 1 MB) stays in L2: the figure is grid-point
+    updates per second, not an HBM fraction.  cpu: the oracle's restatement
+    of the same shot on one host core (sample: 200 steps)."""
+    import numpy as np
+    import torch
+
+    import geophysics_gb300 as geo
+    from geophysics_gb300 import media
+    from geophysics_gb300 import build as B
+    B.build()
+    nx = nz = 401
+    npd, nt = 50, 2000
+    v, e, d = media.layered_vti(nx, nz, seed=1)
+    kw = dict(npd=npd, nt=nt, dx=10.0, dz=10.0, dt=1e-3, favg=20.0, fs=200, zs=5, variant="cpu", rec_iz=npd + 4)
+    tv, te, td = (torch.from_numpy(a).cuda() for a in (v, e, d))
+    for _ in range(args.warmup):
+        geo.fd2d_shot(tv, te, td, **kw)
+    torch.cuda.synchronize()
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        geo.fd2d_shot(tv, te, td, **kw)
+        torch.cuda.synchronize()
+        times.append(time.perf_counter() - t0)
+    t_host = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        geo.fd2d_shot(v, e, d, **kw)
+        t_host.append(time.perf_counter() - t0)
+    upd = (nx + 2 * npd - 8) * (nz + 2 * npd - 8) * nt
+    cpu = None
+    if not args.no_cpu:
+        from oracle import orc
+        orc.build(with_ref=False)
+        ns = 200
+        t0 = time.perf_counter()
+        orc.fd2d(v, e, d, npd=npd, nt=ns, dx=10.0, dz=10.0, dt=np.float32(1e-3), favg=20.0, pfac=10.0, fs=200, zs=5,
+                 rec_iz=npd + 4)
+        dt = time.perf_counter() - t0
+        cpu = {"value": (nx + 2 * npd - 8) * (nz + 2 * npd - 8) * ns / dt / 1e9, "unit": "Gpt/s", "cores": 1,
+               "kind": "port", "sample": "200 of the 2000 steps, CPU program arithmetic, one core"}
+    med = statistics.median(times)
+    print(json.dumps({"case": "fd2d", "metric": "grid-pt updates/s", "value": upd / med / 1e9, "unit": "Gpt/s",
+                      "ms_per_shot": 1000 * med, "e2e_ms_per_shot": 1000 * statistics.median(t_host),
+                      "config": {"workload": "2D VTI FD 401x401, 2000 steps, dt 1 ms, 50 sponge, CPU_vti2dfd "
+                                             "arithmetic"}, "cpu_baseline": cpu, "dtype": "f32"}), flush=True)
+
+
+def run_rtm2d_case(args):
+    """Batched 2D RTM: 128 shots on a 2401x601 layered + random-field model
+    (10 m), aperture widths odd in 401..1199 (seeded), sources evenly over
+    x = 601..1801, 3000 steps at dt 1 ms, 20 Hz, every node of the window
+    recorded; per-shot image, stacked, adjoint Laplacian.  One persistent
+    launch per half-step over all shots' tiles, the time loop in CUDA graphs,
+    tiles from the autotuner.  cpu: the oracle's MPI-program restatement of
+    one shot on one core (sample: 300 steps of the widest window)."""
+    import numpy as np
+    import torch
+
+    import geophysics_gb300 as geo
+    from geophysics_gb300 import media
+    from geophysics_gb300 import build as B
+    B.build()
+    nx, nz, npd, nt, ns = 2401, 601, 50, 3000, 128
+    v, e, d = media.layered_random_vti(nx, nz, seed=3)
+    rng = np.random.default_rng(3)
+    widths = (rng.integers(200, 600, ns) * 2 + 1).astype(int)
+    xs = np.round(np.linspace(601, 1801, ns)).astype(int)
+    kw = dict(npd=npd, nt=nt, dx=10.0, dz=10.0, dt_ms=1.0, favg=20.0, pfac=10.0, zs=5, shot_x=xs, shot_nxs=widths)
+    tv, te, td = (torch.from_numpy(a).cuda() for a in (v, e, d))
+    geo.rtm2d_batch(tv, te, td, **dict(kw, nt=100))  # warm-up: autotune + graphs on a short run
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    img = geo.rtm2d_batch(tv, te, td, **kw)
+    torch.cuda.synchronize()
+    sec = time.perf_counter() - t0
+    upd = sum((int(w) + 2 * npd - 8) * (nz + 2 * npd - 8) for w in widths) * nt * 3
+    cpu = None
+    if not args.no_cpu:
+        from oracle import orc
+        orc.build(with_ref=False)
+        k = int(np.argmax(widths))
+        s_nt = 300
+        t1 = time.perf_counter()
+        orc.rtm2d_mpi_shot(v, e, d, npd=npd, nt=s_nt, dx=10.0, dz=10.0, dt_ms=1.0, favg=20.0, pfac=10.0,
+                           fs_sxd=int(xs[k]), ds_sxd=0, zs_sxd=5, is_=1, nxs=int(widths[k]))
+        dt = time.perf_counter() - t1
+        cu = (int(widths[k]) + 2 * npd - 8) * (nz + 2 * npd - 8) * s_nt * 3
+        cpu = {"value": cu / dt / 1e9, "unit": "Gpt/s", "cores": 1, "kind": "port",
+               "sample": "one shot (the widest window), 300 of 3000 steps, MPI-program arithmetic, one core",
+               "shots_per_hr_extrapolated": 3600.0 / (dt * nt / s_nt * upd / ns / 3 / cu * 3)}
+    print(json.dumps({"case": "rtm2d", "metric": "shots/hr", "value": ns * 3600.0 / sec, "unit": "shots/hr",
+                      "seconds": sec, "grid_pt_updates_per_s": upd / sec / 1e9,
+                      "image_finite": bool(torch.isfinite(torch.as_tensor(img)).all()),
+                      "config": {"workload": "128-shot batched 2D VTI RTM, 2401x601, widths 401-1199, 3000 steps"},
+                      "cpu_baseline": cpu, "dtype": "f32"}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -438,7 +540,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--case", default="full", choices=["full", "small", "traffic", "rtm-learned", "rtm-methods"],
+    ap.add_argument("--case", default="full", choices=["full", "small", "traffic", "rtm-learned", "rtm-methods", "fd2d", "rtm2d"],
                     help="small / traffic: ncu profiling cases; rtm-learned: the learned-codec RTM comparison")
     ap.add_argument("--nt", type=int, default=3000, help="rtm-learned: time steps")
     ap.add_argument("--err-nt", type=int, default=1200, help="rtm-learned: steps of the image-error comparison")
@@ -446,6 +548,12 @@ def main():
     ap.add_argument("--escape", type=float, default=0.03, help="rtm-learned: escaped-block budget")
     ap.add_argument("--methods", default="boundary,learned", help="rtm-methods: methods to run")
     args = ap.parse_args()
+    if args.case == "fd2d":
+        run_fd2d_case(args)
+        return
+    if args.case == "rtm2d":
+        run_rtm2d_case(args)
+        return
     if args.case == "rtm-methods":
         run_rtm_methods_case(args)
         return
