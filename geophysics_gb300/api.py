@@ -102,6 +102,26 @@ def fd2d_shot(v, e, d, *, npd, nt, dx, dz, dt, favg, fs, zs, pfac=10.0, ds=0.0, 
     return (shot, snaps) if snap_every else shot
 
 
+def tti2d_shot(v, e, d, theta, *, npd, nt, dx, dz, dt, favg, fs, zs, pfac=10.0, ds=0.0, is_=1, sv=0, wtype=1,
+               rec_iz=None, snap_every=0):
+    """One 2D TTI shot (the GPU TTI program's semantics); theta in degrees,
+    all arrays (nx, nz).  Returns the record (nx, nt) [and padded P
+    snapshots at it = snap_every, 2*snap_every, ...]."""
+    b = _Bufs(v, e, d, theta)
+    nx, nz = v.shape
+    desc = FD2DDesc(nx=nx, nz=nz, npd=npd, nt=nt, dx=dx, dz=dz, dt=dt, favg=favg, pfac=pfac, wtype=wtype,
+                    fs=fs, ds=ds, zs=zs, is_=is_, variant=GEO_VARIANT_GPU, sv=sv,
+                    rec_iz=npd if rec_iz is None else rec_iz, rec_scale=1.0, mute_tt=0)
+    pv, pe, pd, pt = b.inp(v), b.inp(e), b.inp(d), b.inp(theta)
+    shot, ps = b.out((nx, nt), v)
+    snaps, psn = (None, None)
+    if snap_every:
+        snaps, psn = b.out(((nt - 1) // snap_every, nx + 2 * npd, nz + 2 * npd), v)
+    check(lib().geo_tti2d_shot(C.byref(desc), pv, pe, pd, pt, ps, psn, snap_every, b.mem, b.stream()),
+          "geo_tti2d_shot")
+    return (shot, snaps) if snap_every else shot
+
+
 class FD3DPlan:
     """Device state for repeated 3D shots on one grid (geo_fd3d_plan_*)."""
 

@@ -1,0 +1,203 @@
+// 2D TTI (tilted VTI) staggered-grid FD with the semantics of the GPU TTI
+// program (2D-tti-fd+rtm-cuda/Toa_gpu_2dtti_fd_1orderfunction.cu):
+//   update_vel (:81-112)     u <- cx2 cz2 u - cx1 cz1 (cos t dtx dP/dx - sin t dtz dP/dz)
+//                            w <- cx2 cz2 w - cx1 cz1 (sin t dtx dQ/dx + cos t dtz dQ/dz)
+//   update_stress (:114-183) px,pz,qx,qz with the same rotated derivatives of
+//                            u and w, P = px + pz, Q = qx + qz
+// with the sponge applied as products of the x and z profiles, the point
+// source added to P and Q before the velocity update (add_source :47-79),
+// the record taken from P at the surface row after each step
+// (shot_record :273-283) and padded-P snapshots every snap_every steps from
+// snap_every on (:451-456).  The program swaps its old/new pointers without
+// keeping two buffers (u0 = u1 after the first step), so every field is
+// updated in place; this file does that directly.
+// cos and sin of the tilt are formed once on the host (cosf/sinf of the
+// angle in radians, theta * pi/180 as the program converts it).
+#include "geo_internal.h"
+#include <cmath>
+#include <vector>
+
+namespace geo {
+
+__constant__ float c_tti[4] = {1.196289f, -0.0797526f, 0.009570313f, -0.0006975447f};
+
+struct Tti2D {
+    int nnx, nnz;
+    float dtx, dtz;
+    const float *cx1, *cx2, *cz1, *cz2, *ax1, *ax2, *az1, *az2;
+    const float *vp, *e2, *d2, *ct, *st;
+    float *u, *w, *px, *pz, *qx, *qz, *P, *Q;
+};
+
+__global__ void k_tti_src(Tti2D g, long id, float amp) {
+    g.P[id] += amp;
+    g.Q[id] += amp;
+}
+
+__global__ void k_tti_vel(Tti2D g) {
+    const long n = (long)g.nnx * g.nnz;
+    for (long id = blockIdx.x * (long)blockDim.x + threadIdx.x; id < n; id += (long)gridDim.x * blockDim.x) {
+        const int ix = (int)(id / g.nnz), iz = (int)(id % g.nnz);
+        if (ix < 4 || ix >= g.nnx - 4 || iz < 4 || iz >= g.nnz - 4) continue;
+        const long s = g.nnz;
+        float Px = 0.0f, Pz = 0.0f, Qz = 0.0f, Qx = 0.0f;
+#pragma unroll
+        for (int im = 0; im < 4; im++) {
+            Px += c_tti[im] * (g.P[id + (im + 1) * s] - g.P[id - im * s]);
+            Pz += c_tti[im] * (g.P[id + im + 1] - g.P[id - im]);
+            Qz += c_tti[im] * (g.Q[id + im + 1] - g.Q[id - im]);
+            Qx += c_tti[im] * (g.Q[id + (im + 1) * s] - g.Q[id - im * s]);
+        }
+        const float ct = g.ct[id], st = g.st[id];
+        const float k2 = g.cx2[ix] * g.cz2[iz], k1 = g.cx1[ix] * g.cz1[iz];
+        g.u[id] = k2 * g.u[id] - k1 * (ct * g.dtx * Px - st * g.dtz * Pz);
+        g.w[id] = k2 * g.w[id] - k1 * (st * g.dtx * Qx + ct * g.dtz * Qz);
+    }
+}
+
+__global__ void k_tti_stress(Tti2D g) {
+    const long n = (long)g.nnx * g.nnz;
+    for (long id = blockIdx.x * (long)blockDim.x + threadIdx.x; id < n; id += (long)gridDim.x * blockDim.x) {
+        const int ix = (int)(id / g.nnz), iz = (int)(id % g.nnz);
+        if (ix < 4 || ix >= g.nnx - 4 || iz < 4 || iz >= g.nnz - 4) continue;
+        const long s = g.nnz;
+        float ux = 0.0f, uz = 0.0f, wz = 0.0f, wx = 0.0f;
+#pragma unroll
+        for (int im = 0; im < 4; im++) {
+            ux += c_tti[im] * (g.u[id + im * s] - g.u[id - (im + 1) * s]);
+            uz += c_tti[im] * (g.u[id + im] - g.u[id - im - 1]);
+            wz += c_tti[im] * (g.w[id + im] - g.w[id - im - 1]);
+            wx += c_tti[im] * (g.w[id + im * s] - g.w[id - (im + 1) * s]);
+        }
+        const float ct = g.ct[id], st = g.st[id], vp = g.vp[id];
+        const float A = ct * g.dtx * ux - st * g.dtz * uz, B = st * g.dtx * wx + ct * g.dtz * wz;
+        const float k2 = g.ax2[ix] * g.az2[iz], k1 = g.ax1[ix] * g.az1[iz];
+        const float px = k2 * g.px[id] - k1 * vp * vp * g.e2[id] * A;
+        const float pz = k2 * g.pz[id] - k1 * vp * vp * g.d2[id] * B;
+        const float qx = k2 * g.qx[id] - k1 * vp * vp * g.d2[id] * A;
+        const float qz = k2 * g.qz[id] - k1 * vp * vp * B;
+        g.px[id] = px; g.pz[id] = pz; g.qx[id] = qx; g.qz[id] = qz;
+        g.P[id] = px + pz;
+        g.Q[id] = qx + qz;
+    }
+}
+
+__global__ void k_tti_rec(const float *P, float *shot, int nnz, int nx, int npd, int rec_iz, int it, int nt) {
+    const int ix = blockIdx.x * blockDim.x + threadIdx.x;
+    if (ix < nx) shot[it + (long)nt * ix] = P[rec_iz + (long)nnz * (ix + npd)];
+}
+
+}  // namespace geo
+
+using namespace geo;
+
+extern "C" int geo_tti2d_shot(const geo_fd2d_desc *desc, const float *v, const float *e, const float *d,
+                              const float *theta, float *shot, float *snap, int snap_every, int mem, void *stream) {
+    if (!desc || !v || !e || !d || !theta || !shot) return fail(GEO_ERR_ARG, "null argument");
+    const geo_fd2d_desc &D = *desc;
+    if (D.nx < 2 || D.nz < 2 || D.npd < 5 || D.nt < 1) return fail(GEO_ERR_ARG, "grid too small (npd must be >= 5)");
+    if (!(D.dt > 0) || !(D.dx > 0) || !(D.dz > 0) || !(D.favg > 0)) return fail(GEO_ERR_ARG, "bad spacing");
+    if (mem != GEO_MEM_HOST && mem != GEO_MEM_DEVICE) return fail(GEO_ERR_ARG, "bad mem kind");
+    if (snap && snap_every < 1) return fail(GEO_ERR_ARG, "snap_every must be >= 1");
+    const int nx = D.nx, nz = D.nz, npd = D.npd, nt = D.nt;
+    const int nnx = nx + 2 * npd, nnz = nz + 2 * npd;
+    const size_t n0 = (size_t)nx * nz, n = (size_t)nnx * nnz;
+    if (D.rec_iz < 0 || D.rec_iz >= nnz) return fail(GEO_ERR_ARG, "receiver row outside the grid");
+    cudaStream_t s = (cudaStream_t)stream;
+    std::vector<float> hv(n0), he(n0), hd(n0), ht(n0);
+    const float *src[4] = {v, e, d, theta};
+    float *dst[4] = {hv.data(), he.data(), hd.data(), ht.data()};
+    for (int k = 0; k < 4; k++) {
+        if (mem == GEO_MEM_DEVICE) GEO_CUDA(cudaMemcpyAsync(dst[k], src[k], n0 * 4, cudaMemcpyDeviceToHost, s));
+        else std::copy(src[k], src[k] + n0, dst[k]);
+    }
+    GEO_CUDA(cudaStreamSynchronize(s));
+    GEO_TRY(check_model(hv.data(), he.data(), hd.data(), n0));
+    for (size_t k = 0; k < n0; k++)
+        if (!std::isfinite(ht[k])) return fail(GEO_ERR_MODEL, "theta[%zu] not finite", k);
+    std::vector<float> pv(n), pe(n), pd(n), pt(n);
+    pad_model_2d(nx, nz, npd, hv.data(), pv.data());
+    pad_model_2d(nx, nz, npd, he.data(), pe.data());
+    pad_model_2d(nx, nz, npd, hd.data(), pd.data());
+    pad_model_2d(nx, nz, npd, ht.data(), pt.data());
+    // source cell (add_source :71-72), shot is 1-based
+    const float fsx = D.fs + (D.is - 1) * D.ds;
+    const int ixs = (int)(fsx + 0.5f) + npd - 1, izs = (int)(D.zs + 0.5f) + npd - 1;
+    if (ixs < 4 || ixs >= nnx - 4 || izs < 4 || izs >= nnz - 4) return fail(GEO_ERR_ARG, "source outside the grid");
+    if (D.sv) {
+        // centre (fs+(is-1)ds+npml, zs+npml) (:131-132): one cell right/down of the source cell
+        Taper2D tp;
+        sv_taper_2d(V_GPU, nnx, nnz, npd, ixs + 1, izs + 1, pe.data(), pd.data(), tp);
+        for (int bx = 0; bx < tp.n; bx++)
+            for (int bz = 0; bz < tp.n; bz++) {
+                const int ix = tp.x0 + bx, iz = tp.z0 + bz;
+                if (ix < 0 || ix >= nnx || iz < 0 || iz >= nnz) continue;
+                pe[(size_t)ix * nnz + iz] = tp.e[bx * tp.n + bz];
+                pd[(size_t)ix * nnz + iz] = tp.d[bx * tp.n + bz];
+            }
+    }
+    // model arrays: vp, 1+2eps, sqrtf(1+2del), cos and sin of the tilt
+    std::vector<float> model(5 * n);
+    for (size_t k = 0; k < n; k++) {
+        const float th = (float)((double)pt[k] * (kPiGui / 180.0));   // read_file :235
+        model[k] = pv[k];
+        model[n + k] = 1 + 2 * pe[k];
+        model[2 * n + k] = sqrtf(1 + 2 * pd[k]);
+        model[3 * n + k] = std::cos(th);
+        model[4 * n + k] = std::sin(th);
+    }
+    // sponge (get_d0 :186-189 from the padded centre velocity; initial_coffe :227-271)
+    const float d0 = sponge_d0(V_GPU, 2, 0.0f, pv[n / 2], npd, D.dx, D.dx, D.dz);
+    std::vector<float> prof(4 * (size_t)(nnx + nnz));
+    float *q = prof.data();
+    sponge_profiles(V_GPU, nx, npd, D.dt, d0, q, q + nnx, q + 2 * nnx, q + 3 * nnx);
+    q += 4 * nnx;
+    sponge_profiles(V_GPU, nz, npd, D.dt, d0, q, q + nnz, q + 2 * nnz, q + 3 * nnz);
+    std::vector<float> amp;
+    std::vector<uint8_t> on;
+    source_amplitudes(V_GPU, nt, D.dt, D.favg, D.pfac, D.wtype, amp, on);
+
+    DevBuf dm, dprof, df, drec;
+    GEO_TRY(dm.alloc(5 * n * 4));
+    GEO_TRY(dprof.alloc(prof.size() * 4));
+    GEO_TRY(df.alloc(8 * n * 4));
+    GEO_TRY(drec.alloc((size_t)nx * nt * 4));
+    GEO_CUDA(cudaMemcpyAsync(dm.p, model.data(), 5 * n * 4, cudaMemcpyHostToDevice, s));
+    GEO_CUDA(cudaMemcpyAsync(dprof.p, prof.data(), prof.size() * 4, cudaMemcpyHostToDevice, s));
+    GEO_TRY(df.zero(s));
+    GEO_TRY(drec.zero(s));
+    Tti2D g{};
+    g.nnx = nnx;
+    g.nnz = nnz;
+    g.dtx = D.dt / D.dx;
+    g.dtz = D.dt / D.dz;
+    const float *pp = dprof.as<float>();
+    g.cx1 = pp; g.cx2 = pp + nnx; g.ax1 = pp + 2 * nnx; g.ax2 = pp + 3 * nnx;
+    pp += 4 * nnx;
+    g.cz1 = pp; g.cz2 = pp + nnz; g.az1 = pp + 2 * nnz; g.az2 = pp + 3 * nnz;
+    const float *m = dm.as<float>();
+    g.vp = m; g.e2 = m + n; g.d2 = m + 2 * n; g.ct = m + 3 * n; g.st = m + 4 * n;
+    float *f = df.as<float>();
+    g.u = f; g.w = f + n; g.px = f + 2 * n; g.pz = f + 3 * n; g.qx = f + 4 * n; g.qz = f + 5 * n;
+    g.P = f + 6 * n; g.Q = f + 7 * n;
+    const int blocks = (int)std::min<size_t>((n + 255) / 256, 152 * 16);
+    const long src_id = (long)ixs * nnz + izs;
+    const cudaMemcpyKind kout = mem == GEO_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+    for (int it = 0; it < nt; it++) {
+        if (on[it]) {
+            k_tti_src<<<1, 1, 0, s>>>(g, src_id, amp[it]);
+            GEO_TRY(check_launch("tti_src"));
+        }
+        k_tti_vel<<<blocks, 256, 0, s>>>(g);
+        GEO_TRY(check_launch("tti_vel"));
+        k_tti_stress<<<blocks, 256, 0, s>>>(g);
+        GEO_TRY(check_launch("tti_stress"));
+        k_tti_rec<<<(nx + 255) / 256, 256, 0, s>>>(g.P, drec.as<float>(), nnz, nx, npd, D.rec_iz, it, nt);
+        GEO_TRY(check_launch("tti_rec"));
+        if (snap && it % snap_every == 0 && it != 0)
+            GEO_CUDA(cudaMemcpyAsync(snap + (size_t)(it / snap_every - 1) * n, g.P, n * 4, kout, s));
+    }
+    GEO_CUDA(cudaMemcpyAsync(shot, drec.p, (size_t)nx * nt * 4, kout, s));
+    GEO_CUDA(cudaStreamSynchronize(s));
+    return GEO_OK;
+}

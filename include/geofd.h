@@ -130,6 +130,15 @@ int geo_fd2d_shot_noalloc(const geo_fd2d_desc *desc, const float *v, const float
                           float *shot, void *stream);
 size_t geo_fd2d_noalloc_limit(void);
 
+/* 2D TTI forward modelling of one shot with the GPU TTI program's
+ * semantics (2D-tti-fd+rtm-cuda/Toa_gpu_2dtti_fd_1orderfunction.cu:81-183,
+ * replacing its main() shot loop :421-461).  desc as for geo_fd2d_shot
+ * (variant ignored, mute_tt and rec_scale unused); theta: nx*nz tilt in
+ * degrees.  shot: nx*nt (shot[it + nt*ix]); snap (optional): padded P at
+ * it = snap_every, 2*snap_every, ... ((nt-1)/snap_every frames). */
+int geo_tti2d_shot(const geo_fd2d_desc *desc, const float *v, const float *e, const float *d, const float *theta,
+                   float *shot, float *snap, int snap_every, int mem, void *stream);
+
 /* 3D forward modelling of one shot (GPU_vti3dfd semantics).
  * Replaces the per-shot body of GPU_vti3dfd_kernels.cu:113-160. */
 typedef struct geo_fd3d_desc {

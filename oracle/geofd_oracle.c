@@ -456,6 +456,119 @@ int orc_fd2d(const orc_fd2d_desc *d, const float *v, const float *e, const float
     return 0;
 }
 
+/* 2D TTI forward modelling with the GPU TTI program's semantics
+ * (2D-tti-fd+rtm-cuda/Toa_gpu_2dtti_fd_1orderfunction.cu):
+ *   theta (degrees) -> theta * (pi/180.0) in double, stored float (:235);
+ *   d0 from the padded centre velocity (get_d0 :186-189), GPU-form sponge
+ *   profiles (initial_coffe :227-271) applied as x*z products;
+ *   point source P,Q += pfac*w(t) before the velocity update (:47-79),
+ *   t from dt by float accumulation;
+ *   update_vel (:81-112) and update_stress (:114-183) in place (the program's
+ *   u0 = u1 pointer assignment leaves one buffer per field);
+ *   record P at row rec_iz after each step; padded-P snapshots at it =
+ *   snap_every, 2 snap_every, ... (:451-456);
+ *   optional SV taper of the GPU form (R=15, r=4, centre one cell
+ *   right/down of the source cell).
+ * cos/sin of the tilt: cosf/sinf of the float angle. */
+int orc_tti2d(const orc_fd2d_desc *d, const float *v, const float *e, const float *dl, const float *theta,
+              float *shot, float *snaps, int snap_every)
+{
+    const int nx = d->nx, nz = d->nz, npd = d->npd, nt = d->nt;
+    const int nnx = nx + 2 * npd, nnz = nz + 2 * npd;
+    const long n = (long)nnx * nnz;
+    long id, ix, iz;
+    int it, im;
+    REAL *vp = calloc(n, sizeof(REAL)), *ee = calloc(n, sizeof(REAL)), *dd = calloc(n, sizeof(REAL));
+    REAL *th = calloc(n, sizeof(REAL));
+    float *ct = malloc(n * 4), *st = malloc(n * 4), *e2 = malloc(n * 4), *d2 = malloc(n * 4);
+    REAL *u = calloc(n, sizeof(REAL)), *w = calloc(n, sizeof(REAL)), *P = calloc(n, sizeof(REAL)), *Q = calloc(n, sizeof(REAL));
+    REAL *px = calloc(n, sizeof(REAL)), *pz = calloc(n, sizeof(REAL)), *qx = calloc(n, sizeof(REAL)), *qz = calloc(n, sizeof(REAL));
+    float *cx1 = malloc(nnx * 4), *cx2 = malloc(nnx * 4), *ax1 = malloc(nnx * 4), *ax2 = malloc(nnx * 4);
+    float *cz1 = malloc(nnz * 4), *cz2 = malloc(nnz * 4), *az1 = malloc(nnz * 4), *az2 = malloc(nnz * 4);
+    float *amp = malloc(nt * 4);
+    unsigned char *act = malloc(nt);
+    for (ix = 0; ix < nx; ix++)
+        for (iz = 0; iz < nz; iz++) {
+            id = (ix + npd) * nnz + iz + npd;
+            vp[id] = v[ix * nz + iz]; ee[id] = e[ix * nz + iz]; dd[id] = dl[ix * nz + iz];
+            th[id] = (float)((double)theta[ix * nz + iz] * (PI_GUI / 180.0));
+        }
+    orc_pad2d(nx, nz, npd, vp); orc_pad2d(nx, nz, npd, ee); orc_pad2d(nx, nz, npd, dd); orc_pad2d(nx, nz, npd, th);
+    {
+        const float fsx = d->fs + (d->is - 1) * d->ds;
+        const int ixs = (int)(fsx + 0.5f) + npd - 1, izs = (int)(d->zs + 0.5f) + npd - 1;
+        const float d0 = (float)(10.0 * (float)vp[n / 2] * log(100000.0) / (2.0 * npd * ((d->dx + d->dz) / 2.0)));
+        float *te = malloc(n * 4), *td = malloc(n * 4), *te2 = malloc(n * 4), *td2 = malloc(n * 4);
+        for (id = 0; id < n; id++) { te[id] = (float)ee[id]; td[id] = (float)dd[id]; }
+        if (d->sv) {
+            orc_sv_taper2d(ORC_V_GPU, nnx, nnz, npd, d->fs, d->ds, d->zs, d->is, te, td, te2, td2);
+            memcpy(te, te2, n * 4); memcpy(td, td2, n * 4);
+        }
+        for (id = 0; id < n; id++) {
+            float thf = (float)th[id];
+            e2[id] = 1 + 2 * te[id];
+            d2[id] = sqrtf(1 + 2 * td[id]);
+            ct[id] = cosf(thf);
+            st[id] = sinf(thf);
+        }
+        free(te); free(td); free(te2); free(td2);
+        orc_sponge(ORC_V_GPU, nx, npd, d->dt, d0, cx1, cx2, ax1, ax2);
+        orc_sponge(ORC_V_GPU, nz, npd, d->dt, d0, cz1, cz2, az1, az2);
+        orc_source_amp(ORC_V_GPU, nt, d->dt, d->favg, d->pfac, d->wtype, amp, act);
+        {
+            const float dtx = d->dt / d->dx, dtz = d->dt / d->dz;
+            const long s = nnz;
+            for (it = 0; it < nt; it++) {
+                if (act[it]) { P[(long)ixs * nnz + izs] += amp[it]; Q[(long)ixs * nnz + izs] += amp[it]; }
+                for (ix = 4; ix < nnx - 4; ix++)
+                    for (iz = 4; iz < nnz - 4; iz++) {
+                        REAL Px = 0, Pz = 0, Qz = 0, Qx = 0, k1, k2;
+                        id = ix * nnz + iz;
+                        for (im = 0; im < 4; im++) {
+                            Px += C8[im] * (P[id + (im + 1) * s] - P[id - im * s]);
+                            Pz += C8[im] * (P[id + im + 1] - P[id - im]);
+                            Qz += C8[im] * (Q[id + im + 1] - Q[id - im]);
+                            Qx += C8[im] * (Q[id + (im + 1) * s] - Q[id - im * s]);
+                        }
+                        k2 = (REAL)cx2[ix] * cz2[iz];
+                        k1 = (REAL)cx1[ix] * cz1[iz];
+                        u[id] = k2 * u[id] - k1 * ((REAL)ct[id] * dtx * Px - (REAL)st[id] * dtz * Pz);
+                        w[id] = k2 * w[id] - k1 * ((REAL)st[id] * dtx * Qx + (REAL)ct[id] * dtz * Qz);
+                    }
+                for (ix = 4; ix < nnx - 4; ix++)
+                    for (iz = 4; iz < nnz - 4; iz++) {
+                        REAL ux = 0, uz = 0, wz = 0, wx = 0, A, B, k1, k2, a, b, c_, e_;
+                        id = ix * nnz + iz;
+                        for (im = 0; im < 4; im++) {
+                            ux += C8[im] * (u[id + im * s] - u[id - (im + 1) * s]);
+                            uz += C8[im] * (u[id + im] - u[id - im - 1]);
+                            wz += C8[im] * (w[id + im] - w[id - im - 1]);
+                            wx += C8[im] * (w[id + im * s] - w[id - (im + 1) * s]);
+                        }
+                        A = (REAL)ct[id] * dtx * ux - (REAL)st[id] * dtz * uz;
+                        B = (REAL)st[id] * dtx * wx + (REAL)ct[id] * dtz * wz;
+                        k2 = (REAL)ax2[ix] * az2[iz];
+                        k1 = (REAL)ax1[ix] * az1[iz];
+                        a = k2 * px[id] - k1 * vp[id] * vp[id] * e2[id] * A;
+                        b = k2 * pz[id] - k1 * vp[id] * vp[id] * d2[id] * B;
+                        c_ = k2 * qx[id] - k1 * vp[id] * vp[id] * d2[id] * A;
+                        e_ = k2 * qz[id] - k1 * vp[id] * vp[id] * B;
+                        px[id] = a; pz[id] = b; qx[id] = c_; qz[id] = e_;
+                        P[id] = a + b;
+                        Q[id] = c_ + e_;
+                    }
+                for (ix = 0; ix < nx; ix++) shot[it + (long)nt * ix] = (float)P[d->rec_iz + (long)nnz * (ix + npd)];
+                if (snaps && snap_every > 0 && it % snap_every == 0 && it != 0)
+                    for (id = 0; id < n; id++) snaps[(long)(it / snap_every - 1) * n + id] = (float)P[id];
+            }
+        }
+    }
+    free(vp); free(ee); free(dd); free(th); free(ct); free(st); free(e2); free(d2);
+    free(u); free(w); free(P); free(Q); free(px); free(pz); free(qx); free(qz);
+    free(cx1); free(cx2); free(ax1); free(ax2); free(cz1); free(cz2); free(az1); free(az2); free(amp); free(act);
+    return 0;
+}
+
 /* Direct-wave mute of a (nx traces x nt) record.
  *  GPU form (GPU_vti2dfd_kernels.cu:151-174): zero (t0/dt - tt, t0/dt+2/(dt f)+tt)
  *    with t0 = offset/(vp[1]*sqrt(1+2 eps[1])) from the padded model;

@@ -53,6 +53,7 @@ def lib(prec=32):
             build(with_ref=False)
         L = C.CDLL(path)
         L.orc_fd2d.argtypes = [C.POINTER(FD2DDesc)] + [C.POINTER(C.c_float)] * 5 + [C.c_int]
+        L.orc_tti2d.argtypes = [C.POINTER(FD2DDesc)] + [C.POINTER(C.c_float)] * 6 + [C.c_int]
         L.orc_fd3d.argtypes = [C.POINTER(FD3DDesc)] + [C.POINTER(C.c_float)] * 6
         L.orc_rtm2d_mpi_shot.argtypes = [C.c_int] * 4 + [C.c_float] * 5 + [C.c_int] * 5 + \
             [C.POINTER(C.c_float)] * 4 + [C.POINTER(C.c_int), C.POINTER(C.c_float)]
@@ -89,6 +90,19 @@ def fd2d(v, e, d, *, npd, nt, dx, dz, dt, favg, pfac, fs, zs, ds=0.0, is_=1, var
         nn = (nx + 2 * npd) * (nz + 2 * npd)
         snaps = np.zeros(((nt - 1) // snap_every + 1, nx + 2 * npd, nz + 2 * npd), _f)
     lib(prec).orc_fd2d(C.byref(desc), _fp(v), _fp(e), _fp(d), _fp(shot), _fp(snaps), snap_every)
+    return (shot, snaps) if snap_every else shot
+
+
+def tti2d(v, e, d, theta, *, npd, nt, dx, dz, dt, favg, pfac, fs, zs, ds=0.0, is_=1, sv=0, wtype=1, rec_iz=None,
+          snap_every=0, prec=32):
+    """2D TTI forward modelling (GPU TTI program semantics); theta in degrees."""
+    v, e, d, theta = c32(v), c32(e), c32(d), c32(theta)
+    nx, nz = v.shape
+    desc = FD2DDesc(nx=nx, nz=nz, npd=npd, nt=nt, variant=V_GPU, sv=sv, wtype=wtype, dx=dx, dz=dz, dt=dt, favg=favg,
+                    pfac=pfac, fs=fs, ds=ds, zs=zs, is_=is_, rec_iz=npd if rec_iz is None else rec_iz, rec_scale=1.0)
+    shot = np.zeros((nx, nt), _f)
+    snaps = np.zeros(((nt - 1) // snap_every, nx + 2 * npd, nz + 2 * npd), _f) if snap_every else None
+    lib(prec).orc_tti2d(C.byref(desc), _fp(v), _fp(e), _fp(d), _fp(theta), _fp(shot), _fp(snaps), snap_every)
     return (shot, snaps) if snap_every else shot
 
 
