@@ -177,7 +177,8 @@ __global__ void __launch_bounds__(256) k_ae_e1(const E1Args a) {
 
 struct D1Args {
     AeVolume vol;                 // geometry of the output / receiver field
-    int nb, mode;                 // 0 store the snapshot in vol (as dst), 1 image, 2 train
+    int nb, mode;                 // 0 store the snapshot in vol (as dst), 1 image, 2 train,
+                                  // 3 escape check against the field vol.src
     const __nv_bfloat16 *g1;      // [nbp*512 x 16]
     const float *v1, *c1;         // D1: W [8 x 16] (bf16 values), b [8]
     const float *scale;           // [nbp]
@@ -195,7 +196,9 @@ struct D1Args {
     const float *wrow;            // mode 2: block weights (null: all 1)
     const float *wsum;            // mode 2: batch weight sum slot base (null: block count)
     const int *esc;               // modes 0/1: escaped-block slot per row (-1: none), or null
-    const __nv_bfloat16 *res;     // modes 0/1: residual pool (4096 per slot, Morton)
+    const __nv_bfloat16 *res;     // modes 0/1: residual pool (4096 per slot, natural order)
+    __nv_bfloat16 *resall;        // mode 3: residual of every row (natural order)
+    float *err2, *norm2;          // mode 3: per-row squared error and squared norm
 };
 
 __global__ void __launch_bounds__(256) k_ae_d1(const D1Args a) {
@@ -267,14 +270,6 @@ __global__ void __launch_bounds__(256) k_ae_d1(const D1Args a) {
         dst[0] = o4[0];
         dst[1] = o4[1];
     }
-    if (a.mode != 2 && a.esc) {
-        const int slot = a.esc[b];
-        if (slot >= 0) {
-            __syncthreads();
-            const __nv_bfloat16 *r = a.res + (long)slot * kAePts;
-            for (int m = t; m < kAePts; m += 256) ys[m] += __bfloat162float(r[m]);
-        }
-    }
     if (a.mode == 2) {
 #pragma unroll
         for (int o = 16; o; o >>= 1) lsum += __shfl_xor_sync(0xffffffffu, lsum, o);
@@ -292,12 +287,52 @@ __global__ void __launch_bounds__(256) k_ae_d1(const D1Args a) {
     __syncthreads();
     const AeVolume &v = a.vol;
     const int bz = b % v.nbz, bx = (b / v.nbz) % v.nbx, by = b / (v.nbz * v.nbx);
+    if (a.mode == 3) {
+        float e2 = 0.0f, x2 = 0.0f;
+        __nv_bfloat16 *rb = a.resall + (long)b * kAePts;
+#pragma unroll 4
+        for (int p = 0; p < 16; p++) {
+            const int idx = p * 256 + t, z = idx & 15, x = (idx >> 4) & 15, y = idx >> 8;
+            const int iz = bz * 16 + z, ix = bx * 16 + x, iy = by * 16 + y;
+            float val = 0.0f;
+            if (iz < v.nz && ix < v.nx && iy < v.ny)
+                val = v.src[(long)(v.oz + iz) + v.ldz * (v.ox + ix) + v.sxy * (v.oy + iy)];
+            const float d = val - ys[morton_of(z, x, y)];
+            rb[idx] = __float2bfloat16_rn(d);
+            e2 += d * d;
+            x2 += val * val;
+        }
+#pragma unroll
+        for (int o = 16; o; o >>= 1) {
+            e2 += __shfl_xor_sync(0xffffffffu, e2, o);
+            x2 += __shfl_xor_sync(0xffffffffu, x2, o);
+        }
+        __shared__ float red2[2][8];
+        if ((t & 31) == 0) {
+            red2[0][t >> 5] = e2;
+            red2[1][t >> 5] = x2;
+        }
+        __syncthreads();
+        if (t == 0) {
+            float E = 0.0f, X = 0.0f;
+            for (int w = 0; w < 8; w++) {
+                E += red2[0][w];
+                X += red2[1][w];
+            }
+            a.err2[b] = E;
+            a.norm2[b] = X;
+        }
+        return;
+    }
+    const int slot = a.esc ? a.esc[b] : -1;
+    const __nv_bfloat16 *res = slot >= 0 ? a.res + (long)slot * kAePts : nullptr;
 #pragma unroll 4
     for (int p = 0; p < 16; p++) {
         const int idx = p * 256 + t, z = idx & 15, x = (idx >> 4) & 15, y = idx >> 8;
         const int iz = bz * 16 + z, ix = bx * 16 + x, iy = by * 16 + y;
         if (iz >= v.nz || ix >= v.nx || iy >= v.ny) continue;
-        const float val = ys[morton_of(z, x, y)];
+        float val = ys[morton_of(z, x, y)];
+        if (res) val += __bfloat162float(res[idx]);   // escaped block: decoded + residual
         const long id = (long)(v.oz + iz) + v.ldz * (v.ox + ix) + v.sxy * (v.oy + iy);
         if (a.mode == 0) {
             a.dst[id] = val;
@@ -308,74 +343,8 @@ __global__ void __launch_bounds__(256) k_ae_d1(const D1Args a) {
     }
 }
 
-// Escape pass 1 after encoding: decode each block (D1 from g1), keep its
-// residual x - decoded (bf16, all rows) and its squared error and norm.
-struct CheckArgs {
-    AeVolume vol;
-    int nb;
-    const __nv_bfloat16 *g1;
-    const float *v1, *c1, *scale;
-    __nv_bfloat16 *resall;        // [rows x 4096]
-    float *err2, *norm2;          // [rows]
-};
-
-__global__ void __launch_bounds__(256) k_ae_check(const CheckArgs a) {
-    __shared__ float ys[kAePts];
-    __shared__ float red[2][8];
-    const int b = blockIdx.x, t = threadIdx.x;
-    if (b >= a.nb) return;
-    const float s = a.scale[b];
-#pragma unroll 1
-    for (int r = 0; r < 2; r++) {
-        const int p = t + 256 * r;
-        const uint4 *src = reinterpret_cast<const uint4 *>(a.g1 + ((long)b * 512 + p) * 16);
-        uint4 q[2] = {src[0], src[1]};
-        const __nv_bfloat16 *qb = reinterpret_cast<const __nv_bfloat16 *>(q);
-#pragma unroll
-        for (int c = 0; c < 8; c++) {
-            float acc = 0.0f;
-#pragma unroll
-            for (int j = 0; j < 16; j++) acc += a.v1[c * 16 + j] * __bfloat162float(qb[j]);
-            ys[p * 8 + c] = (acc + a.c1[c]) * s;
-        }
-    }
-    __syncthreads();
-    const AeVolume &v = a.vol;
-    const int bz = b % v.nbz, bx = (b / v.nbz) % v.nbx, by = b / (v.nbz * v.nbx);
-    float e2 = 0.0f, x2 = 0.0f;
-    __nv_bfloat16 *rb = a.resall + (long)b * kAePts;
-    for (int p = 0; p < 16; p++) {
-        const int idx = p * 256 + t, z = idx & 15, x = (idx >> 4) & 15, y = idx >> 8;
-        const int iz = bz * 16 + z, ix = bx * 16 + x, iy = by * 16 + y;
-        const int m = morton_of(z, x, y);
-        float val = 0.0f;
-        if (iz < v.nz && ix < v.nx && iy < v.ny)
-            val = v.src[(long)(v.oz + iz) + v.ldz * (v.ox + ix) + v.sxy * (v.oy + iy)];
-        const float d = val - ys[m];
-        rb[m] = __float2bfloat16_rn(d);
-        e2 += d * d;
-        x2 += val * val;
-    }
-#pragma unroll
-    for (int o = 16; o; o >>= 1) {
-        e2 += __shfl_xor_sync(0xffffffffu, e2, o);
-        x2 += __shfl_xor_sync(0xffffffffu, x2, o);
-    }
-    if ((t & 31) == 0) {
-        red[0][t >> 5] = e2;
-        red[1][t >> 5] = x2;
-    }
-    __syncthreads();
-    if (t == 0) {
-        float E = 0.0f, X = 0.0f;
-        for (int w = 0; w < 8; w++) {
-            E += red[0][w];
-            X += red[1][w];
-        }
-        a.err2[b] = E;
-        a.norm2[b] = X;
-    }
-}
+// Escape pass 1 is k_ae_d1 in mode 3: decode, compare with the field, keep
+// every block's residual (bf16, natural order) and its squared error and norm.
 
 // Escape pass 2 (one block of 1024 threads): the cap blocks with the
 // largest squared error, among those with err2 > tau2 * norm2, get residual
@@ -816,17 +785,13 @@ int ae_encode_volume(geo_ae *ae, const AeVolume &v, void *code, float *scale, in
         ae->erows = rows;
     }
     GEO_TRY(decode_rows(ae, rows, static_cast<const __nv_bfloat16 *>(code), s));
-    CheckArgs c{};
+    D1Args c = d1_args(ae, nb, 3);
     c.vol = v;
-    c.nb = nb;
-    c.g1 = bf(ae->g1);
-    c.v1 = ae->small.as<float>() + 128;
-    c.c1 = ae->params.as<float>() + ae->off.b[7];
     c.scale = scale;
     c.resall = bf(ae->resall);
     c.err2 = ae->err2.as<float>();
     c.norm2 = ae->norm2.as<float>();
-    k_ae_check<<<nb, 256, 0, s>>>(c);
+    k_ae_d1<<<rows, 256, 0, s>>>(c);
     GEO_TRY(check_launch("ae_check"));
     k_ae_select<<<1, 1024, 0, s>>>(ae->err2.as<float>(), ae->norm2.as<float>(), nb, ae->tau * ae->tau,
                                    ae_escape_cap(ae, v), esc, count);

@@ -111,6 +111,7 @@ struct geo_fd3d_plan {
     std::vector<float> h_vp, h_eps, h_del;  // padded raw model, kept for the SV taper
     float vp1 = 0, eps1 = 0;           // padded model at linear index 1 (mute)
     bool model_set = false;
+    bool tuned = false;
 };
 
 namespace geo {
@@ -188,26 +189,25 @@ static int alloc_fields(geo_fd3d_plan *p, int f) {
     return GEO_OK;
 }
 
-// y chunking: whole waves of resident blocks against the warm-up planes each
-// chunk recomputes.
-static void choose_chunks(geo_fd3d_plan *p) {
-    int dev = 0, sms = 152;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const int slots = sms * 2, planes = p->nny - 8, ntiles = p->ntz * p->ntx;  // 2 blocks per SM
-    int best_c = 1;
-    double best = -1;
-    for (int c = 1; c <= 16; c++) {
-        const int len = (planes + c - 1) / c;
-        if (len < 8) break;
-        const double waves = (double)ntiles * c / slots;
-        const double fill = waves / std::ceil(waves);
-        const double score = fill / (1.0 + 14.0 / len);
-        if (score > best + 1e-9) { best = score; best_c = c; }
-    }
-    if (const char *e = getenv("GEO_FD3D_CHUNKS")) best_c = std::max(1, atoi(e));
-    p->chunk = (planes + best_c - 1) / best_c;
+// y chunking: a block marches over one chunk of y planes and recomputes 14
+// warm-up planes of its queues, so more chunks mean more blocks in flight at
+// different depths (better DRAM and L2 spread, shorter tails) at the price of
+// the warm-up.  The best count varies with the grid (measured on GB300: 4
+// for 480^3, 6 for 592x592x464, 8 for 272^3), so set_model times the
+// candidates (autotune_chunks); this is the starting guess.
+static void set_chunks(geo_fd3d_plan *p, int c) {
+    const int planes = p->nny - 8, ntiles = p->ntz * p->ntx;
+    c = std::max(1, std::min(c, planes / 8));
+    p->chunk = (planes + c - 1) / c;
     p->nitems = ntiles * ((planes + p->chunk - 1) / p->chunk);
+}
+
+static bool g_chunks_fixed() { return getenv("GEO_FD3D_CHUNKS") != nullptr; }
+
+static void choose_chunks(geo_fd3d_plan *p) {
+    int c = 4;
+    if (const char *e = getenv("GEO_FD3D_CHUNKS")) c = std::max(1, atoi(e));
+    set_chunks(p, c);
 }
 
 // One time step of field set f: the fused kernel reads level cur and writes
@@ -235,6 +235,46 @@ static int check_err(geo_fd3d_plan *p, cudaStream_t s) {
     GEO_CUDA(cudaStreamSynchronize(s));
     if (e) return fail(GEO_ERR_CUDA, "3D step: a TMA pipeline stage timed out");
     return GEO_OK;
+}
+
+// Autotuner for the y chunking: bare steps of the zeroed field set 0 (which
+// stays zero) timed with events for each candidate chunk count.
+static int autotune_chunks(geo_fd3d_plan *p, cudaStream_t s) {
+    if (g_chunks_fixed()) return GEO_OK;
+    GEO_TRY(zero_state(p, 0, s));
+    GEO_TRY(p->err.zero(s));
+    cudaEvent_t a, b;
+    GEO_CUDA(cudaEventCreate(&a));
+    GEO_CUDA(cudaEventCreate(&b));
+    StepArgs3D st{};
+    float best = 1e30f;
+    int best_c = 4;
+    const int planes = p->nny - 8;
+    for (int c : {2, 3, 4, 5, 6, 8, 10}) {
+        if (planes / c < 16) break;
+        set_chunks(p, c);
+        int rc = step3d(p, 0, st, s);
+        if (rc == GEO_OK && cudaEventRecord(a, s) != cudaSuccess) rc = fail(GEO_ERR_CUDA, "event record");
+        for (int k = 0; k < 3 && rc == GEO_OK; k++) rc = step3d(p, 0, st, s);
+        float ms = 0;
+        if (rc == GEO_OK && (cudaEventRecord(b, s) != cudaSuccess || cudaEventSynchronize(b) != cudaSuccess ||
+                             cudaEventElapsedTime(&ms, a, b) != cudaSuccess))
+            rc = fail(GEO_ERR_CUDA, "chunk autotune timing");
+        if (rc != GEO_OK) {
+            cudaEventDestroy(a);
+            cudaEventDestroy(b);
+            return rc;
+        }
+        if (ms < best) {
+            best = ms;
+            best_c = c;
+        }
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    set_chunks(p, best_c);
+    p->fs[0].cur = 0;
+    return check_err(p, s);
 }
 
 // SV taper box for shot `is` (GPU_vti3dfd_kernels.cu:155-174: R=15, r=4,
@@ -486,6 +526,10 @@ extern "C" int geo_fd3d_set_model(geo_fd3d_plan *p, const float *v, const float 
     GEO_TRY(upload_pitched(p, p->d2, pd.data(), s));
     GEO_CUDA(cudaMemcpyAsync(p->prof.p, prof.data(), prof.size() * 4, cudaMemcpyHostToDevice, s));
     GEO_CUDA(cudaStreamSynchronize(s));
+    if (!p->tuned) {
+        GEO_TRY(autotune_chunks(p, s));
+        p->tuned = true;
+    }
     p->model_set = true;
     return GEO_OK;
 }

@@ -3,7 +3,7 @@
 // One CTA computes a 128 x BN tile of C = A * B^T.  Four warps:
 //   warp 0 lane 0  TMA producer: per 64-wide K slice, one 128x64 tile of A
 //                  and one BNx64 tile of B (128-byte swizzle) into a
-//                  4-stage ring, one "full" mbarrier per stage;
+//                  2- to 4-stage ring, one "full" mbarrier per stage;
 //   warp 1 lane 0  MMA issuer: four tcgen05.mma (K = 16 each) per slice
 //                  into a 128 x BN fp32 accumulator in TMEM; tcgen05.commit
 //                  to the stage's "empty" mbarrier releases it to the
@@ -21,27 +21,32 @@
 namespace geo {
 using namespace tc;
 
-constexpr int kGM = 128, kGK = 64, kGStages = 4;
+constexpr int kGM = 128, kGK = 64;
 
+// Stage ring sized so two CTAs fit on an SM (one's epilogue overlaps the
+// other's main loop): 2 stages for BN 256, 3 for 128, 4 for 64.
 template <int BN>
 struct GemmShape {
     static constexpr int kA = kGM * kGK * 2;
     static constexpr int kB = BN * kGK * 2;
     static constexpr int kStage = kA + kB;
-    static constexpr size_t kSmem = (size_t)kGStages * kStage + 1024 + 256;
+    static constexpr int kStages = BN >= 256 ? 2 : (BN >= 128 ? 3 : 4);
+    static constexpr size_t kSmem = (size_t)kStages * kStage + 1024 + 256;
     static constexpr uint32_t kCols = BN < 32 ? 32 : BN;
     static_assert(kA % 1024 == 0 && kB % 1024 == 0, "swizzle atoms stay 1024-byte aligned");
     static_assert(BN % 16 == 0 && BN >= 16 && BN <= 256, "UMMA N for M = 128");
+    static_assert(2 * kSmem <= 232448, "two CTAs per SM");
 };
 
 __device__ __forceinline__ float leaky(float v) { return v > 0.0f ? v : kLeak * v; }
 
 template <int BN>
-__global__ void __launch_bounds__(128, 1)
+__global__ void __launch_bounds__(128, 2)
     k_tc_gemm(const __grid_constant__ CUtensorMap ta, const __grid_constant__ CUtensorMap tb, const TcGemm g) {
     using S = GemmShape<BN>;
     extern __shared__ unsigned char smem_raw[];
     uint8_t *sm = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    constexpr int kGStages = S::kStages;
     uint64_t *full = reinterpret_cast<uint64_t *>(sm + kGStages * S::kStage);
     uint64_t *empty = full + kGStages;
     uint64_t *done = empty + kGStages;
