@@ -778,6 +778,11 @@ int ae_encode_volume(geo_ae *ae, const AeVolume &v, void *code, float *scale, in
     GEO_TRY(check_launch("ae_e1"));
     GEO_TRY(encode_rows(ae, rows, static_cast<__nv_bfloat16 *>(code), s));
     if (!esc) return GEO_OK;
+    if (ae_escape_cap(ae, v) == 0) {   // no escape budget: no re-decode
+        GEO_CUDA(cudaMemsetAsync(esc, 0xff, (size_t)rows * 4, s));
+        if (count) GEO_CUDA(cudaMemsetAsync(count, 0, 4, s));
+        return GEO_OK;
+    }
     if (rows > ae->erows) {
         GEO_TRY(ae->resall.alloc((size_t)rows * kAePts * 2));
         GEO_TRY(ae->err2.alloc((size_t)rows * 4));
