@@ -83,6 +83,7 @@ def lib():
         "geo_fd3d_get_fields": (_i, [_vp, _vp, _vp, _i, _vp]),
         "geo_fd3d_shot": (_i, [C.POINTER(FD3DDesc), _i, _vp, _vp, _vp, _vp, _i, _vp]),
         "geo_rtm2d_batch": (_i, [C.POINTER(RTM2DDesc), _vp, _vp, _vp, _vp, _vp, _i, _vp]),
+        "geo_rtm2d_batch_adcig": (_i, [C.POINTER(RTM2DDesc), _vp, _vp, _vp, _vp, _vp, _vp, _i, _vp]),
         "geo_rtm3d": (_i, [C.POINTER(RTM3DDesc), _vp, _vp, _vp, _vp, _vp, _vp, _i, _vp]),
         "geo_tti2d_shot": (_i, [C.POINTER(FD2DDesc), _vp, _vp, _vp, _vp, _vp, _vp, _i, _i, _vp]),
         "geo_ae_create": (_i, [C.POINTER(_vp), C.c_ulonglong]),

@@ -337,9 +337,10 @@ def tc_gemm_bf16(A, B, bias=None, act=False, out_f32=True):
 
 
 def rtm2d_batch(v, e, d, *, npd, nt, dx, dz, dt_ms, favg, pfac, zs, shot_x, shot_nxs, laplace=True,
-                per_shot=False, tile_x=0):
+                per_shot=False, tile_x=0, adcig=False):
     """Batched 2D RTM with the MPI program's semantics; returns the stacked
-    (Laplacian-filtered) image (nx, nz) [and the per-shot images]."""
+    (Laplacian-filtered) image (nx, nz) [and the per-shot images] [and the
+    Poynting angle gathers (90, nx, nz) when `adcig`]."""
     b = _Bufs(v, e, d)
     nx, nz = v.shape
     ns = len(shot_x)
@@ -352,14 +353,21 @@ def rtm2d_batch(v, e, d, *, npd, nt, dx, dz, dt_ms, favg, pfac, zs, shot_x, shot
     shots = pshots = None
     if per_shot:
         shots, pshots = b.out((int(sum(int(w) for w in shot_nxs)) * nz,), v)
-    check(lib().geo_rtm2d_batch(C.byref(desc), pv, pe, pd, pi, pshots, b.mem, b.stream()), "geo_rtm2d_batch")
+    gathers = pg = None
+    if adcig:
+        gathers, pg = b.out((90, nx, nz), v)
+    check(lib().geo_rtm2d_batch_adcig(C.byref(desc), pv, pe, pd, pi, pshots, pg, b.mem, b.stream()),
+          "geo_rtm2d_batch")
+    res = [img]
     if per_shot:
         out, o = [], 0
         for w in shot_nxs:
             out.append(shots[o:o + int(w) * nz].reshape(int(w), nz))
             o += int(w) * nz
-        return img, out
-    return img
+        res.append(out)
+    if adcig:
+        res.append(gathers)
+    return res[0] if len(res) == 1 else tuple(res)
 
 
 def laplace2d(img):

@@ -36,7 +36,7 @@ struct ShotHost {
     std::vector<double> tpw;
     int ixs, izs;
     float mu_v;
-    DevBuf d_model, d_pw, d_prof, d_taper, d_tpw, d_fields, d_rec, d_edge, d_img;
+    DevBuf d_model, d_pw, d_prof, d_taper, d_tpw, d_fields, d_rec, d_edge, d_img, d_adcig;
 };
 
 // Build the propagation coefficients of one (padded) window from its
@@ -415,6 +415,11 @@ extern "C" int geo_fd2d_shot(const geo_fd2d_desc *desc, const float *v, const fl
 // ---------------------------------------------------------------- RTM 2D
 extern "C" int geo_rtm2d_batch(const geo_rtm2d_desc *desc, const float *v, const float *e, const float *d,
                                float *image, float *per_shot, int mem, void *stream) {
+    return geo_rtm2d_batch_adcig(desc, v, e, d, image, per_shot, nullptr, mem, stream);
+}
+
+extern "C" int geo_rtm2d_batch_adcig(const geo_rtm2d_desc *desc, const float *v, const float *e, const float *d,
+                                     float *image, float *per_shot, float *adcig, int mem, void *stream) {
     if (!desc || !v || !e || !d || !image || !desc->shot_x || !desc->shot_nxs) return fail(GEO_ERR_ARG, "null argument");
     const geo_rtm2d_desc &D = *desc;
     if (D.nx < 2 || D.nz < 2 || D.npd < 5 || D.nt < 1 || D.ns < 1) return fail(GEO_ERR_ARG, "bad sizes");
@@ -454,6 +459,10 @@ extern "C" int geo_rtm2d_batch(const geo_rtm2d_desc *desc, const float *v, const
         build_shot_host(*H[k], V_MPI, nxs, nz, npd, D.dx, D.dz, dt, wv.data(), we.data(), wd.data(),
                         (float)(nxs / 2 + 1), (float)D.zs, true);
         GEO_TRY(upload_shot(*H[k], B.S[k], 2, nt, true, true, true, dt / D.dx, dt / D.dz, ss.cs));
+        if (adcig) {
+            GEO_TRY(H[k]->d_adcig.alloc((size_t)kAdcigAngles * nxs * nz * 4));
+            B.S[k].adcig = H[k]->d_adcig.as<float>();
+        }
         maxline = std::max(maxline, 2 * nxs + 2 * nz);
     }
     // tile shape: caller's choice or the autotuner's
@@ -464,7 +473,9 @@ extern "C" int geo_rtm2d_batch(const geo_rtm2d_desc *desc, const float *v, const
     for (int k = 0; k < D.ns; k++) {
         GEO_TRY(H[k]->d_fields.zero(ss.cs));
         GEO_TRY(H[k]->d_img.zero(ss.cs));
+        if (adcig) GEO_TRY(H[k]->d_adcig.zero(ss.cs));
     }
+    if (adcig) GEO_TRY(load_adcig_tables(ss.cs));
 
     std::vector<float> amp;
     std::vector<uint8_t> on;
@@ -540,6 +551,26 @@ extern "C" int geo_rtm2d_batch(const geo_rtm2d_desc *desc, const float *v, const
     }
     const cudaMemcpyKind k = mem == GEO_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
     GEO_CUDA(cudaMemcpyAsync(image, result, nimg * 4, k, ss.cs));
+    DevBuf gathers, d_aptr;
+    if (adcig) {
+        // per shot: divide by the source illumination (Toa_rtm_vti_adcig_cdp.c:1083-1090), then stack
+        // every angle plane in shot order into [90][nx][nz] (adcig_ns0)
+        std::vector<const float *> ap((size_t)kAdcigAngles * D.ns);
+        for (int q = 0; q < D.ns; q++) {
+            const size_t m = (size_t)D.shot_nxs[q] * nz;
+            GEO_TRY(launch_normalize_planes(B.S[q].adcig, B.S[q].ill, m, kAdcigAngles, ss.cs));
+            for (int ia = 0; ia < kAdcigAngles; ia++) ap[(size_t)ia * D.ns + q] = B.S[q].adcig + ia * m;
+        }
+        GEO_TRY(d_aptr.alloc(ap.size() * sizeof(float *)));
+        GEO_CUDA(cudaMemcpyAsync(d_aptr.p, ap.data(), ap.size() * sizeof(float *), cudaMemcpyHostToDevice, ss.cs));
+        GEO_TRY(gathers.alloc((size_t)kAdcigAngles * nimg * 4));
+        GEO_TRY(gathers.zero(ss.cs));
+        for (int ia = 0; ia < kAdcigAngles; ia++)
+            GEO_TRY(launch_stack_image(gathers.as<float>() + ia * nimg, nz,
+                                       d_aptr.as<const float *const>() + (size_t)ia * D.ns, d_offs.as<int>(),
+                                       d_wid.as<int>(), D.ns, D.nx, ss.cs));
+        GEO_CUDA(cudaMemcpyAsync(adcig, gathers.p, (size_t)kAdcigAngles * nimg * 4, k, ss.cs));
+    }
     if (per_shot) {
         size_t o = 0;
         for (int q = 0; q < D.ns; q++) {

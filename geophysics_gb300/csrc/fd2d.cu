@@ -13,6 +13,8 @@
 //             MPI program Toa_rtm_vti_adcig_cdp.c:1227-1327 (rho*vp^2 form,
 //             pz/qx chains in double after pow(1+2del, 0.5))
 #include "geo_internal.h"
+#include <cmath>
+#include <cstring>
 
 namespace geo {
 
@@ -56,6 +58,27 @@ __device__ __forceinline__ float tap(const float *a, long idx, long src, float a
     float v = a[idx];
     if (PT_SRC && idx == src) v = v + amp;
     return v;
+}
+
+// Poynting-vector angle gathers (RTM_corr_adcig, Toa_rtm_vti_adcig_cdp.c:1004-1068):
+// per image point the angle bin ia of the opening angle between the source
+// and receiver Poynting vectors, and adcig[ia] += gP*sP*cos(ia)^3.  The
+// program bins with (int)(float)(0.5*acosf(a1)*180/pi); that bin is a
+// non-increasing function of the float a1, so the host finds, with the same
+// libm, the largest a1 of every bin count (c_adthr[k-1]: largest a1 whose
+// bin is >= k) and the kernel counts thresholds instead of calling acosf.
+__constant__ float c_adthr[kAdcigAngles];
+__constant__ double c_adw[kAdcigAngles];
+
+__device__ __forceinline__ int adcig_bin(float a1) {
+    if (!(a1 >= -1.0f && a1 <= 1.0f)) return 0;
+    int lo = 0, hi = kAdcigAngles;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (a1 <= c_adthr[mid - 1]) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo == kAdcigAngles ? kAdcigAngles - 1 : lo;   // ia == 90 -> 89
 }
 
 template <int VARIANT>
@@ -185,6 +208,16 @@ __global__ void __launch_bounds__(256) k_stress2d(const Shot2D *__restrict__ sho
             if (ill == 0.0f) ill = 1.0f;
             sh.ill[o] = ill;
             sh.mig[o] = sh.mig[o] + Pn[1] * sv;
+            if (sh.adcig) {
+                // Poynting vectors from the new P,Q and u,w of both fields
+                const float sx = -Pn[0] * sh.u[0][id], sz = -Qn[0] * sh.w[0][id];
+                const float gx = Pn[1] * sh.u[1][id], gz = Qn[1] * sh.w[1][id];
+                const float b1 = sx * sx + sz * sz, b2 = gx * gx + gz * gz, a = sx * gx + sz * gz;
+                const float a1 = (float)((double)a / ((double)sqrtf(b1 * b2) + 0.0000000000001));
+                const int ia = adcig_bin(a1);
+                float *ag = sh.adcig + (long)ia * sh.nx * sh.nz + o;
+                *ag = (float)((double)*ag + (double)(Pn[1] * sv) * c_adw[ia]);
+            }
         }
     }
 }
@@ -262,6 +295,52 @@ int launch_inject2d(const Shot2D *d_shots, int nshots, int maxline, int it, cuda
     dim3 g((maxline + 255) / 256, nshots);
     k_inject2d<<<g, 256, 0, s>>>(d_shots, maxline, it);
     return check_launch("inject2d");
+}
+
+// The MPI program's bin of one cosine a1 (before its 90 -> 89 clamp).
+static int ref_adcig_bin(float a1) {
+    const float a2 = (float)(0.5 * std::acos(a1) * 180 / kPiMpi);
+    return (int)(a2 / 1.0);
+}
+
+static uint32_t order_key(float f) {
+    uint32_t b;
+    memcpy(&b, &f, 4);
+    return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+
+static float key_float(uint32_t k) {
+    const uint32_t b = (k & 0x80000000u) ? (k & 0x7fffffffu) : ~k;
+    float f;
+    memcpy(&f, &b, 4);
+    return f;
+}
+
+int load_adcig_tables(cudaStream_t s) {
+    static float thr[kAdcigAngles];
+    static double w[kAdcigAngles];
+    static bool built = false;
+    if (!built) {
+        const uint32_t lo = order_key(-1.0f), hi = order_key(1.0f);
+        for (int k = 1; k <= kAdcigAngles; k++) {
+            if (ref_adcig_bin(-1.0f) < k) {
+                thr[k - 1] = -2.0f;   // no cosine reaches this bin
+                continue;
+            }
+            uint32_t a = lo, b = hi;  // ref_adcig_bin(key_float(a)) >= k
+            while (a < b) {
+                const uint32_t m = a + (b - a + 1) / 2;
+                if (ref_adcig_bin(key_float(m)) >= k) a = m;
+                else b = m - 1;
+            }
+            thr[k - 1] = key_float(a);
+        }
+        for (int ia = 0; ia < kAdcigAngles; ia++) w[ia] = std::pow(std::cos(ia * kPiMpi / 180.0), 3);
+        built = true;
+    }
+    GEO_CUDA(cudaMemcpyToSymbolAsync(c_adthr, thr, sizeof thr, 0, cudaMemcpyHostToDevice, s));
+    GEO_CUDA(cudaMemcpyToSymbolAsync(c_adw, w, sizeof w, 0, cudaMemcpyHostToDevice, s));
+    return GEO_OK;
 }
 
 }  // namespace geo

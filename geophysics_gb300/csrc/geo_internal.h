@@ -109,6 +109,7 @@ struct Shot2D {
     float *rec_p, *rec_q;           // time-major records nt x nx
     float *edge_p, *edge_q;         // time-major edge lines nt x (2nx+2nz)
     float *mig, *ill;               // image and source illumination nx*nz
+    float *adcig;                   // Poynting angle gathers [90][nx][nz], or null
     int tile_base, ntz;             // first work item, tiles along z
 };
 
@@ -130,6 +131,11 @@ int launch_inject2d(const Shot2D *d_shots, int nshots, int maxline, int it, cuda
 int launch_mute_records(float *rec, int nx, int nt, const int *lo, const int *hi, cudaStream_t s);
 int launch_transpose_records(const float *tm, float *out, int ntr, int nt, cudaStream_t s);
 int launch_normalize_image(float *mig, const float *ill, size_t n, cudaStream_t s);
+// a[p*n + k] /= ill[k] for p < planes.
+int launch_normalize_planes(float *a, const float *ill, size_t n, int planes, cudaStream_t s);
+// Angle-bin thresholds and cos^3 weights of the Poynting ADCIG into constant memory.
+int load_adcig_tables(cudaStream_t s);
+constexpr int kAdcigAngles = 90;
 int launch_stack_image(float *full, int nz, const float *const *imgs, const int *offsets,
                        const int *widths, int nshots, int nx, cudaStream_t s);
 int launch_laplace2d(int nx, int nz, const float *in, float *out, cudaStream_t s);

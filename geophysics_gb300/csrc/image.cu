@@ -56,6 +56,20 @@ int launch_normalize_image(float *mig, const float *ill, size_t n, cudaStream_t 
     return check_launch("normalize");
 }
 
+__global__ void k_normalize_planes(float *a, const float *ill, long n, int planes) {
+    const long tot = n * planes;
+    for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < tot; k += (long)gridDim.x * blockDim.x)
+        a[k] = a[k] / ill[k % n];
+}
+
+int launch_normalize_planes(float *a, const float *ill, size_t n, int planes, cudaStream_t s) {
+    const long tot = (long)n * planes;
+    int g = (int)((tot + 255) / 256);
+    if (g > 152 * 32) g = 152 * 32;
+    k_normalize_planes<<<g, 256, 0, s>>>(a, ill, (long)n, planes);
+    return check_launch("normalize_planes");
+}
+
 // Stack per-shot images into the full image.  Each output point sums the
 // shots covering it in shot order, so the float sum equals the reference's
 // sequential shot loop (Toa_rtm_vti_adcig_cdp.c:1102-1104: window column c

@@ -235,6 +235,12 @@ typedef struct geo_rtm2d_desc {
  * per_shot (optional): ns images concatenated, shot s of size nxs_s*nz. */
 int geo_rtm2d_batch(const geo_rtm2d_desc *desc, const float *v, const float *e, const float *d,
                     float *image, float *per_shot, int mem, void *stream);
+/* The same run with the Poynting-vector angle gathers of the MPI program
+ * (flag_adcig = 1, RTM_corr_adcig Toa_rtm_vti_adcig_cdp.c:1004-1068, stacked
+ * as adcig_ns0 :1083-1096): adcig receives 90*nx*nz floats in the program's
+ * array order adcig_ns[ia][ix][iz] (its output file stores ix, ia, iz). */
+int geo_rtm2d_batch_adcig(const geo_rtm2d_desc *desc, const float *v, const float *e, const float *d,
+                          float *image, float *per_shot, float *adcig, int mem, void *stream);
 
 /* Adjoint first-difference Laplacian (laplac2_lop adj=1,
  * utils-Laplacian-filter/laplace.c:9-53; the in-program copy

@@ -616,7 +616,7 @@ void orc_mute2d(int form, int nx, int nt, float dt, float favg, float dx, float 
 int orc_rtm2d_mpi_shot(int nx, int nz, int npd, int nt, float dx, float dz, float dt_ms,
                        float favg, float pfac, int fs_sxd, int ds_sxd, int zs_sxd, int is, int nxs,
                        const float *v, const float *e, const float *dl,
-                       float *mig_is, int *stack_offset, float *p_cal_x_out)
+                       float *mig_is, int *stack_offset, float *p_cal_x_out, float *adcig_is)
 {
     int nnzs = nz + 2 * npd, nnxs = nxs + 2 * npd, k = fs_sxd + (is - 1) * ds_sxd;
     int c, iz, it, i, j;
@@ -677,6 +677,7 @@ int orc_rtm2d_mpi_shot(int nx, int nz, int npd, int nt, float dx, float dz, floa
     prop2d_init(&rc, &d, vs, es, ds_, 0);
     float *srcx = calloc((size_t)nxs * nz, 4);
     memset(mig_is, 0, (size_t)nxs * nz * 4);
+    if (adcig_is) memset(adcig_is, 0, (size_t)90 * nxs * nz * 4);
     for (it = nt - 1; it >= 0; it--) {
         for (i = 0; i < nxs; i++) {
             sr.P[(size_t)(npd + i) * nnzs + npd] = (REAL)tx[(size_t)i * nt + it];
@@ -702,12 +703,30 @@ int orc_rtm2d_mpi_shot(int nx, int nz, int npd, int nt, float dx, float dz, floa
             for (j = npd; j < nz + npd; j++) {
                 size_t id = (size_t)i * nnzs + j, o = (size_t)(i - npd) * nz + (j - npd);
                 REAL sv = sr.P[id];
+                if (adcig_is) {
+                    /* Poynting ADCIG (flag_adcig = 1, :1004-1068): opening
+                     * angle of -sP*u_s, -sQ*w_s and gP*u_g, gQ*w_g */
+                    float sx = -(float)sr.P[id] * (float)sr.u[id], sz = -(float)sr.Q[id] * (float)sr.w[id];
+                    float gx = (float)rc.P[id] * (float)rc.u[id], gz = (float)rc.Q[id] * (float)rc.w[id];
+                    float b1 = sx * sx + sz * sz, b2 = gx * gx + gz * gz, a = sx * gx + sz * gz;
+                    float a1 = (float)(a / (sqrtf(b1 * b2) + 0.0000000000001)), a2;
+                    int ia = 0;
+                    if (a1 >= -1 && a1 <= 1) {
+                        a2 = (float)(0.5 * acosf(a1) * 180 / PI_MPI);
+                        ia = (int)(a2 / 1.0);
+                        if (ia == 90) ia -= 1;
+                    }
+                    float *ag = adcig_is + (size_t)ia * nxs * nz + o;
+                    *ag = (float)(*ag + (double)((float)rc.P[id] * (float)sv) * pow(cos(ia * PI_MPI / 180.0), 3));
+                }
                 srcx[o] = (float)((double)srcx[o] + pow((double)sv, 2));
                 if (srcx[o] == 0) srcx[o] = 1.0f;
                 mig_is[o] = (float)(mig_is[o] + (REAL)rc.P[id] * sv);
             }
     }
     for (size_t o = 0; o < (size_t)nxs * nz; o++) mig_is[o] = mig_is[o] / srcx[o];
+    if (adcig_is)
+        for (size_t q = 0; q < (size_t)90 * nxs * nz; q++) adcig_is[q] = adcig_is[q] / srcx[q % ((size_t)nxs * nz)];
     *stack_offset = k - nxs / 2 - 1;
     prop2d_free(&sr); prop2d_free(&rc);
     free(srcx); free(pcx); free(pcz); free(tx); free(bx); free(tz); free(bz); free(lx); free(rx); free(lz); free(rz);

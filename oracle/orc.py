@@ -56,7 +56,7 @@ def lib(prec=32):
         L.orc_tti2d.argtypes = [C.POINTER(FD2DDesc)] + [C.POINTER(C.c_float)] * 6 + [C.c_int]
         L.orc_fd3d.argtypes = [C.POINTER(FD3DDesc)] + [C.POINTER(C.c_float)] * 6
         L.orc_rtm2d_mpi_shot.argtypes = [C.c_int] * 4 + [C.c_float] * 5 + [C.c_int] * 5 + \
-            [C.POINTER(C.c_float)] * 4 + [C.POINTER(C.c_int), C.POINTER(C.c_float)]
+            [C.POINTER(C.c_float)] * 4 + [C.POINTER(C.c_int), C.POINTER(C.c_float), C.POINTER(C.c_float)]
         L.orc_laplace2d_adj.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_float), C.POINTER(C.c_float)]
         L.orc_laplace3d_adj.argtypes = [C.c_int] * 3 + [C.POINTER(C.c_float)] * 2
         L.orc_stack2d.argtypes = [C.c_int, C.c_int, C.c_int, C.POINTER(C.c_float), C.POINTER(C.c_float)]
@@ -153,16 +153,18 @@ def rtm3d(v, e, d, *, npd, nt, dx, dy, dz, dt, favg, pfac, fsx, fsy, fsz, dsx=0,
 
 
 def rtm2d_mpi_shot(v, e, d, *, npd, nt, dx, dz, dt_ms, favg, pfac, fs_sxd, ds_sxd, zs_sxd, is_, nxs,
-                   prec=32):
-    """One MPI-semantics RTM shot; returns (mig_is (nxs,nz), offset, p_cal_x (nxs,nt))."""
+                   prec=32, adcig=False):
+    """One MPI-semantics RTM shot; returns (mig_is (nxs,nz), offset, p_cal_x
+    (nxs,nt)) [+ the shot's angle gathers adcig_is (90,nxs,nz)]."""
     v, e, d = c32(v), c32(e), c32(d)
     nx, nz = v.shape
     mig = np.zeros((nxs, nz), _f)
     pcal = np.zeros((nxs, nt), _f)
+    ag = np.zeros((90, nxs, nz), _f) if adcig else None
     off = C.c_int(0)
     lib(prec).orc_rtm2d_mpi_shot(nx, nz, npd, nt, dx, dz, dt_ms, favg, pfac, fs_sxd, ds_sxd, zs_sxd,
-                                 is_, nxs, _fp(v), _fp(e), _fp(d), _fp(mig), C.byref(off), _fp(pcal))
-    return mig, off.value, pcal
+                                 is_, nxs, _fp(v), _fp(e), _fp(d), _fp(mig), C.byref(off), _fp(pcal), _fp(ag))
+    return (mig, off.value, pcal, ag) if adcig else (mig, off.value, pcal)
 
 
 def stack2d(full, mig_is, offset):
@@ -217,16 +219,18 @@ def ref_cpu_vti2dfd(v, e, d, *, npd, nt, dx, dz, dt_us, favg, fs, zs, ns=1, ds=0
     return shots, snaps
 
 
-def ref_rtm_mpi_shot(v, e, d, acc, *, npd, nt, dx, dz, dt_ms, favg, pfac, fs_sxd, ds_sxd, zs_sxd, is_, nxs):
-    """The reference MPI RTM for one shot; stacks into `acc` (nx,nz) in place."""
+def ref_rtm_mpi_shot(v, e, d, acc, *, npd, nt, dx, dz, dt_ms, favg, pfac, fs_sxd, ds_sxd, zs_sxd, is_, nxs,
+                     adcig_acc=None):
+    """The reference MPI RTM for one shot; stacks into `acc` (nx,nz) in place
+    (and its angle gathers into `adcig_acc` (90,nx,nz) when given)."""
     L = C.CDLL(os.path.join(REF, "librefrtm.so"))
-    L.ref_rtm_mpi_shot.argtypes = [C.c_int] * 4 + [C.c_float] * 5 + [C.c_int] * 5 + [C.POINTER(C.c_float)] * 6
+    L.ref_rtm_mpi_shot.argtypes = [C.c_int] * 4 + [C.c_float] * 5 + [C.c_int] * 5 + [C.POINTER(C.c_float)] * 7
     v, e, d = c32(v), c32(e), c32(d)
     nx, nz = v.shape
     mig = np.zeros((nxs, nz), _f)
     pcal = np.zeros((nxs, nt), _f)
     rc = L.ref_rtm_mpi_shot(nx, nz, npd, nt, dx, dz, dt_ms, favg, pfac, fs_sxd, ds_sxd, zs_sxd, is_, nxs,
-                            _fp(v), _fp(e), _fp(d), _fp(acc), _fp(mig), _fp(pcal))
+                            _fp(v), _fp(e), _fp(d), _fp(acc), _fp(mig), _fp(pcal), _fp(adcig_acc))
     if rc:
         raise ValueError("aperture window leaves the model")
     return mig, pcal

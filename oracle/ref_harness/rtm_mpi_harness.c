@@ -39,12 +39,14 @@ void RTM_corr_adcig(int nx, int nz, int vnx, int vnz, int nt, int npd, float dx,
                     int flag_snap, int seismic, int flag_adcig);
 
 /* v,e,d: unpadded nx*nz (x-major).  mig_ns0: nx*nz accumulator (stacked
- * image before the Laplacian), mig_is: nxs*nz, p_cal_x: nxs*nt muted record.
+ * image before the Laplacian), mig_is: nxs*nz, p_cal_x: nxs*nt muted record,
+ * adcig_ns0_acc (optional): 90*nx*nz accumulator of the angle gathers
+ * (adcig_ns0[ia][ix][iz]).
  * Returns 0, or 1 when the window leaves the model (the reference exits). */
 int ref_rtm_mpi_shot(int nx, int nz, int npd, int nt, float dx, float dz, float dt_ms,
                      float favg, float pfac, int fs_sxd, int ds_sxd, int zs_sxd, int is, int nxs,
                      const float *v, const float *e, const float *d,
-                     float *mig_ns0_acc, float *mig_is_out, float *p_cal_x_out)
+                     float *mig_ns0_acc, float *mig_is_out, float *p_cal_x_out, float *adcig_ns0_acc)
 {
     int i, j, k, nnz = nz + 2 * npd, nnx = nx + 2 * npd, nnxs = nxs + 2 * npd;
     float mu_v, tmax = nt * dt_ms / 1000.0f;
@@ -92,12 +94,20 @@ int ref_rtm_mpi_shot(int nx, int nz, int npd, int nt, float dx, float dz, float 
     float ***adcig_is = alloc3float(nz, nxs, 90), ***adcig_ns0 = alloc3float(nz, nx, 90);
     zero2float(mig_is, nz, nxs); zero3float(adcig_is, nz, nxs, 90); zero3float(adcig_ns0, nz, nx, 90);
     for (i = 0; i < nx; i++) memcpy(mig_ns0[i], mig_ns0_acc + (size_t)i * nz, (size_t)nz * 4);
+    if (adcig_ns0_acc)
+        for (k = 0; k < 90; k++)
+            for (i = 0; i < nx; i++)
+                memcpy(adcig_ns0[k][i], adcig_ns0_acc + ((size_t)k * nx + i) * nz, (size_t)nz * 4);
     char fn5[16] = "unused";
     RTM_corr_adcig(nxs, nz, nxs, nz, nt, npd, dx, dz, dx, dz, favg, tmax, dt_ms, dt_ms, pfac,
                    vps, epss, dels, rhos, fn5, 1, ds, fs, ds_sxd, fs_sxd, zs_sxd, is, 1,
                    tx, bx, lx, rx, tz, bz, lz, rz, pcx, pcz, 4, 1, 1, 1, mig_is, mig_ns0,
                    adcig_is, adcig_ns0, NULL, NULL, nxs / 2 + 1, 0, 1, 1);
     for (i = 0; i < nx; i++) memcpy(mig_ns0_acc + (size_t)i * nz, mig_ns0[i], (size_t)nz * 4);
+    if (adcig_ns0_acc)
+        for (k = 0; k < 90; k++)
+            for (i = 0; i < nx; i++)
+                memcpy(adcig_ns0_acc + ((size_t)k * nx + i) * nz, adcig_ns0[k][i], (size_t)nz * 4);
     if (mig_is_out) for (i = 0; i < nxs; i++) memcpy(mig_is_out + (size_t)i * nz, mig_is[i], (size_t)nz * 4);
     free2float(vp); free2float(rho); free2float(eps); free2float(del);
     free2float(vps); free2float(rhos); free2float(epss); free2float(dels);

@@ -47,15 +47,22 @@ def test_rtm2d_mpi_bit_exact_vs_reference(orc):
     v += rng.uniform(0, 40, v.shape).astype(np.float32)
     accr = np.zeros((nx, nz), np.float32)
     acco = np.zeros((nx, nz), np.float32)
+    agr = np.zeros((90, nx, nz), np.float32)
+    ago = np.zeros((90, nx, nz), np.float32)
     for is_, nxs in ((1, 41), (2, 53)):
         kw = dict(npd=15, nt=650, dx=10.0, dz=10.0, dt_ms=1.0, favg=20.0, pfac=1000.0, fs_sxd=35, ds_sxd=20,
                   zs_sxd=1, is_=is_, nxs=nxs)
-        mr, pr = orc.ref_rtm_mpi_shot(v, e, d, accr, **kw)
-        mo, off, po = orc.rtm2d_mpi_shot(v, e, d, **kw)
+        mr, pr = orc.ref_rtm_mpi_shot(v, e, d, accr, adcig_acc=agr, **kw)
+        mo, off, po, ag = orc.rtm2d_mpi_shot(v, e, d, adcig=True, **kw)
         orc.stack2d(acco, mo, off)
+        for ia in range(90):
+            orc.stack2d(ago[ia], ag[ia], off)
         assert np.array_equal(pr, po)
         assert np.array_equal(mr, mo)
     assert np.array_equal(accr, acco)
+    # Poynting angle gathers (flag_adcig = 1): every angle plane bit-exact
+    assert np.abs(agr).max() > 0 and (np.abs(agr).reshape(90, -1).max(axis=1) > 0).sum() > 10
+    assert np.array_equal(agr, ago)
     assert np.array_equal(orc.ref_laplace2d_adj(accr), orc.laplace2d_adj(acco))
 
 
