@@ -85,6 +85,9 @@ def lib():
         "geo_rtm2d_batch": (_i, [C.POINTER(RTM2DDesc), _vp, _vp, _vp, _vp, _vp, _i, _vp]),
         "geo_rtm2d_batch_adcig": (_i, [C.POINTER(RTM2DDesc), _vp, _vp, _vp, _vp, _vp, _vp, _i, _vp]),
         "geo_rtm3d": (_i, [C.POINTER(RTM3DDesc), _vp, _vp, _vp, _vp, _vp, _vp, _i, _vp]),
+        "geo_su_read": (_i, [C.c_char_p, _i, _i, _i, _vp, _vp]),
+        "geo_su_write": (_i, [C.c_char_p, _i, _i, _f, _i, _vp, _vp]),
+        "geo_su_replace_data": (_i, [C.c_char_p, C.c_char_p, C.c_char_p, _i, _i]),
         "geo_tti2d_shot": (_i, [C.POINTER(FD2DDesc), _vp, _vp, _vp, _vp, _vp, _vp, _i, _i, _vp]),
         "geo_ae_create": (_i, [C.POINTER(_vp), C.c_ulonglong]),
         "geo_ae_destroy": (_i, [_vp]),

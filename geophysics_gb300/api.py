@@ -413,6 +413,30 @@ def GPU_vti3dfd(nx, ny, nz, dx, dy, dz, npml, SV, FNv, FNe, FNd, favg, ns, fsx, 
                       fsz, dsz, _s(FNshot), _s(FNsnap), nt, dt, run_count)
 
 
+def su_read(path, ntr, ns, big_endian=True, headers=False):
+    """ntr traces of ns samples -> (ntr, ns) float32 [and (ntr, 240) uint8 headers]."""
+    data = np.empty((ntr, ns), np.float32)
+    hdr = np.empty((ntr, 240), np.uint8) if headers else None
+    check(lib().geo_su_read(_s(path), ntr, ns, 1 if big_endian else 0, C.c_void_p(data.ctypes.data),
+                            C.c_void_p(hdr.ctypes.data) if headers else None), "geo_su_read")
+    return (data, hdr) if headers else data
+
+
+def su_write(path, data, dt_us=1000.0, big_endian=True, headers=None):
+    """Write (ntr, ns) traces with generated (or given (ntr, 240)) headers."""
+    data = np.ascontiguousarray(data, np.float32)
+    ntr, ns = data.shape
+    h = None if headers is None else np.ascontiguousarray(headers, np.uint8)
+    check(lib().geo_su_write(_s(path), ntr, ns, C.c_float(dt_us), 1 if big_endian else 0,
+                             C.c_void_p(data.ctypes.data), C.c_void_p(h.ctypes.data) if h is not None else None),
+          "geo_su_write")
+
+
+def su_replace_data(template, raw, out, ntr, ns):
+    """The binary2segy utility: template headers + byte-swapped raw samples."""
+    check(lib().geo_su_replace_data(_s(template), _s(raw), _s(out), ntr, ns), "geo_su_replace_data")
+
+
 class Par:
     """A `key= value` par file read by geo_par_load."""
 

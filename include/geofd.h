@@ -250,6 +250,23 @@ int geo_laplace2d(int nx, int nz, const float *in, float *out, int mem, void *st
  * Toa_gpu_3dvti_rtm_adcigs_1orderfunction.cu:555-616). */
 int geo_laplace3d(int nx, int ny, int nz, const float *in, float *out, int mem, void *stream);
 
+/* ---- SU / SEG-Y traces ------------------------------------------------
+ * A trace = 240-byte header (the segy struct of hc/cjbsegy.h) + ns floats.
+ * geo_su_read: ntr traces into data[ntr*ns] (samples byte-swapped when
+ *   big_endian; the MPI RTM program's seismic==2 model reader,
+ *   2D-vti-fd+rtm-mpi/Toa_rtm_vti_adcig_cdp.c:1415-1453); headers (optional)
+ *   receives the raw 240-byte headers.
+ * geo_su_write: headers copied from `headers` when given, else generated
+ *   (tracl = tracr = trace number, trid = 1, ns, dt in microseconds), header
+ *   and samples big-endian when big_endian (SEG-Y trace order).
+ * geo_su_replace_data: the binary2segy utility (utils-binary2segy/
+ *   binary2segy.c:47-85): headers of the template file, samples from a raw
+ *   native float file, byte-swapped. */
+int geo_su_read(const char *path, int ntr, int ns, int big_endian, float *data, void *headers);
+int geo_su_write(const char *path, int ntr, int ns, float dt_us, int big_endian, const float *data,
+                 const void *headers);
+int geo_su_replace_data(const char *template_path, const char *raw_path, const char *out_path, int ntr, int ns);
+
 /* ---- learned snapshot codec (no reference counterpart) -----------------
  * A 4-level convolutional autoencoder over 16^3 blocks (kernel = stride = 2
  * per level, leaky ReLU, bf16 weights and activations, fp32 accumulation on
