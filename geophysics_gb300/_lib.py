@@ -46,6 +46,12 @@ class RTM3DDesc(C.Structure):
                 ("snap_every", C.c_int), ("ae", C.c_void_p)]
 
 
+class RTM2DGpuDesc(C.Structure):
+    _fields_ = [(n, C.c_int) for n in ("nx", "nz", "npml", "nt")] + \
+               [(n, C.c_float) for n in ("dx", "dz", "dt", "favg", "pfac")] + \
+               [(n, C.c_int) for n in ("wtype", "ns", "fs", "ds", "zs", "mute_tt", "nangle", "dangle")]
+
+
 class RTM2DDesc(C.Structure):
     _fields_ = [(n, C.c_int) for n in ("nx", "nz", "npd", "nt")] + \
                [(n, C.c_float) for n in ("dx", "dz", "dt_ms", "favg", "pfac")] + \
@@ -88,6 +94,7 @@ def lib():
         "geo_su_read": (_i, [C.c_char_p, _i, _i, _i, _vp, _vp]),
         "geo_su_write": (_i, [C.c_char_p, _i, _i, _f, _i, _vp, _vp]),
         "geo_su_replace_data": (_i, [C.c_char_p, C.c_char_p, C.c_char_p, _i, _i]),
+        "geo_rtm2d_gpu": (_i, [C.POINTER(RTM2DGpuDesc)] + [_vp] * 9 + [_i, _vp]),
         "geo_tti2d_shot": (_i, [C.POINTER(FD2DDesc), _vp, _vp, _vp, _vp, _vp, _vp, _i, _i, _vp]),
         "geo_ae_create": (_i, [C.POINTER(_vp), C.c_ulonglong]),
         "geo_ae_destroy": (_i, [_vp]),

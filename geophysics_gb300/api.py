@@ -11,7 +11,7 @@ import numpy as np
 
 from ._lib import (FD2DDesc, FD3DDesc, GEO_MEM_DEVICE, GEO_MEM_HOST, GEO_MODE_EXACT, GEO_MODE_FAST,
                    GEO_RTM_BOUNDARY, GEO_RTM_LEARNED, GEO_RTM_SNAPSHOT, GEO_VARIANT_CPU, GEO_VARIANT_GPU,
-                   GEO_VARIANT_MPI, RTM2DDesc, RTM3DDesc, check, lib)
+                   GEO_VARIANT_MPI, RTM2DDesc, RTM2DGpuDesc, RTM3DDesc, check, lib)
 
 _VARIANTS = {"cpu": GEO_VARIANT_CPU, "gpu": GEO_VARIANT_GPU, "mpi": GEO_VARIANT_MPI}
 _MODES = {"exact": GEO_MODE_EXACT, "fast": GEO_MODE_FAST}
@@ -222,6 +222,26 @@ def rtm3d(v, e, d, *, npd, nt, dx, dy, dz, dt, favg, fsx, fsy, fsz, ns=1, dsx=0,
     check(lib().geo_rtm3d(C.byref(desc), pv, pe, pd, pm, pl, pi, b.mem, b.stream()), "geo_rtm3d")
     out = [mig] + ([lap] if laplace else []) + ([ill] if illum else [])
     return out[0] if len(out) == 1 else tuple(out)
+
+
+def rtm2d_gpu(v, e, d, *, npml, nt, dx, dz, dt, favg, ns=1, fs=1, ds=0, zs=1, pfac=10.0, wtype=1, mute_tt=20,
+              nangle=70, dangle=1, obs=None):
+    """2D RTM with the 2D GPU RTM program's semantics (full-model shots,
+    ring saving, Poynting angle gathers).  Returns a dict: "mig_lap" (nx,nz),
+    "illum", "adcigs" (nx,nangle,nz), "stk_lap", "shots" (ns,nx,nt)."""
+    b = _Bufs(v, e, d, obs)
+    nx, nz = v.shape
+    desc = RTM2DGpuDesc(nx=nx, nz=nz, npml=npml, nt=nt, dx=dx, dz=dz, dt=dt, favg=favg, pfac=pfac, wtype=wtype,
+                        ns=ns, fs=fs, ds=ds, zs=zs, mute_tt=mute_tt, nangle=nangle, dangle=dangle)
+    pv, pe, pd, po = b.inp(v), b.inp(e), b.inp(d), b.inp(obs)
+    out = {}
+    ptrs = []
+    for name, shape in (("mig_lap", (nx, nz)), ("illum", (nx, nz)), ("adcigs", (nx, nangle, nz)),
+                        ("stk_lap", (nx, nz)), ("shots", (ns, nx, nt))):
+        out[name], p = b.out(shape, v)
+        ptrs.append(p)
+    check(lib().geo_rtm2d_gpu(C.byref(desc), pv, pe, pd, po, *ptrs, b.mem, b.stream()), "geo_rtm2d_gpu")
+    return out
 
 
 def morton_order():

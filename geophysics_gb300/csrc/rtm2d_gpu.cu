@@ -1,0 +1,452 @@
+// 2D RTM with the semantics of the 2D GPU RTM program
+// (2D-vti-fd+rtm-cuda/Toa_gpu2DvtiFdRtmAdcigsLaplace.cu, RTM() :1184-1566).
+// Per shot:
+//   forward, SV taper on (R=18, r=7, update_stress :303-404): point source
+//     before the velocity update (add_source :204), record P at row npml
+//     (shot_record :498), save the ring of P,Q (wavefield_bndr :532: rows
+//     npml-1 and npml+nz+1, columns npml-1 and npml+nx+1), source
+//     illumination ill += P*P + Q*Q, then <= 0 -> 1 (cal_illumination :654);
+//   direct-wave mute of the record (mute_directwave :614, tt = 20 in the
+//     program) -- the program launches one thread per sample rounded up to
+//     512 without a bound on the sample index, so the surplus threads zero
+//     samples of later traces; those samples are zeroed too;
+//   backward, SV taper off: restore the ring into the source field and step
+//     it forward, write the record into P and Q of the receiver field at row
+//     npml (shot_record with record = false) and step it, image mig += sP*gP
+//     (cal_migration :679) and the Poynting angle gathers (Poynting_Adcigs
+//     :718-766).
+// After the shots: mig /= ill, gathers /= ill (migration_illum :700,
+// adcigs_illum :768), the adjoint Laplacian of the image and of the angle
+// stack (stk_adcigs :799).  The image kernels of the program run over
+// nnx*nnz threads on nx*nz arrays (an overrun); here they cover nx*nz.
+// Fields are single buffers updated in place (the program's u0 = u1
+// pointer assignment).
+#include "geo_internal.h"
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+namespace geo {
+
+__constant__ float c_grtm[4] = {1.196289f, -0.0797526f, 0.009570313f, -0.0006975447f};
+__constant__ float c_gthr[128];   // angle-bin thresholds (largest cosine of bins >= k)
+__constant__ float c_gcos[128];   // cosf(ia*pi/180) per bin
+
+struct GRtm {
+    int nnx, nnz, nx, nz, npml, nangle;
+    float dtx, dtz;
+    const float *cx1, *cx2, *cz1, *cz2, *ax1, *ax2, *az1, *az2;
+    const float *vp;
+};
+
+struct GField {
+    float *u, *w, *P, *Q, *px, *pz, *qx, *qz;
+};
+
+__global__ void k_g_src(GField f, long id, float amp) {
+    f.P[id] += amp;
+    f.Q[id] += amp;
+}
+
+__global__ void k_g_vel(GRtm g, GField f) {
+    const long n = (long)g.nnx * g.nnz;
+    for (long id = blockIdx.x * (long)blockDim.x + threadIdx.x; id < n; id += (long)gridDim.x * blockDim.x) {
+        const int ix = (int)(id / g.nnz), iz = (int)(id % g.nnz);
+        if (ix < 4 || ix >= g.nnx - 4 || iz < 4 || iz >= g.nnz - 4) continue;
+        float xx = 0.0f, zz = 0.0f;
+#pragma unroll
+        for (int im = 0; im < 4; im++) {
+            xx += c_grtm[im] * (f.P[id + (im + 1) * (long)g.nnz] - f.P[id - im * (long)g.nnz]);
+            zz += c_grtm[im] * (f.Q[id + im + 1] - f.Q[id - im]);
+        }
+        f.u[id] = g.cx2[ix] * f.u[id] - g.cx1[ix] * g.dtx * xx;
+        f.w[id] = g.cz2[iz] * f.w[id] - g.cz1[iz] * g.dtz * zz;
+    }
+}
+
+__global__ void k_g_stress(GRtm g, GField f, const float *e2, const float *d2) {
+    const long n = (long)g.nnx * g.nnz;
+    for (long id = blockIdx.x * (long)blockDim.x + threadIdx.x; id < n; id += (long)gridDim.x * blockDim.x) {
+        const int ix = (int)(id / g.nnz), iz = (int)(id % g.nnz);
+        if (ix < 4 || ix >= g.nnx - 4 || iz < 4 || iz >= g.nnz - 4) continue;
+        float xx = 0.0f, zz = 0.0f;
+#pragma unroll
+        for (int im = 0; im < 4; im++) {
+            xx += c_grtm[im] * (f.u[id + im * (long)g.nnz] - f.u[id - (im + 1) * (long)g.nnz]);
+            zz += c_grtm[im] * (f.w[id + im] - f.w[id - im - 1]);
+        }
+        const float vp = g.vp[id];
+        const float px = g.ax2[ix] * f.px[id] - g.ax1[ix] * vp * vp * e2[id] * g.dtx * xx;
+        const float pz = g.az2[iz] * f.pz[id] - g.az1[iz] * vp * vp * d2[id] * g.dtz * zz;
+        const float qx = g.ax2[ix] * f.qx[id] - g.ax1[ix] * vp * vp * d2[id] * g.dtx * xx;
+        const float qz = g.az2[iz] * f.qz[id] - g.az1[iz] * vp * vp * g.dtz * zz;
+        f.px[id] = px; f.pz[id] = pz; f.qx[id] = qx; f.qz[id] = qz;
+        f.P[id] = px + pz;
+        f.Q[id] = qx + qz;
+    }
+}
+
+// record P at row npml (time-major), or with inject write it into P and Q
+__global__ void k_g_surface(GRtm g, GField f, float *rec, int it, int inject) {
+    const int ix = blockIdx.x * blockDim.x + threadIdx.x;
+    if (ix >= g.nx) return;
+    const long id = g.npml + (long)g.nnz * (ix + g.npml), r = (long)it * g.nx + ix;
+    if (inject) {
+        f.P[id] = rec[r];
+        f.Q[id] = rec[r];
+    } else {
+        rec[r] = f.P[id];
+    }
+}
+
+// ring of wavefield_bndr: up, bottom (row npml+nz+1), left, right (column npml+nx+1)
+__global__ void k_g_ring(GRtm g, GField f, float *bp, float *bq, int it, int save) {
+    const int L = 2 * g.nx + 2 * g.nz;
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= L) return;
+    long id;
+    if (k < g.nx) id = g.npml - 1 + (long)g.nnz * (k + g.npml);
+    else if (k < 2 * g.nx) id = g.npml + g.nz + 1 + (long)g.nnz * (k - g.nx + g.npml);
+    else if (k < 2 * g.nx + g.nz) id = k - 2 * g.nx + g.npml + (long)g.nnz * (g.npml - 1);
+    else id = k - 2 * g.nx - g.nz + g.npml + (long)g.nnz * (g.npml + g.nx + 1);
+    const long b = (long)it * L + k;
+    if (save) {
+        bp[b] = f.P[id];
+        bq[b] = f.Q[id];
+    } else {
+        f.P[id] = bp[b];
+        f.Q[id] = bq[b];
+    }
+}
+
+__global__ void k_g_illum(GRtm g, GField f, float *ill) {
+    const long n = (long)g.nx * g.nz;
+    for (long o = blockIdx.x * (long)blockDim.x + threadIdx.x; o < n; o += (long)gridDim.x * blockDim.x) {
+        const int ix = (int)(o / g.nz), iz = (int)(o % g.nz);
+        const long id = iz + g.npml + (long)g.nnz * (ix + g.npml);
+        float v = ill[o] + (f.P[id] * f.P[id] + f.Q[id] * f.Q[id]);
+        if (v <= 0.0f) v = 1.0f;
+        ill[o] = v;
+    }
+}
+
+__global__ void k_g_image(GRtm g, GField s, GField r, float *mig, float *adcig) {
+    const long n = (long)g.nx * g.nz;
+    for (long o = blockIdx.x * (long)blockDim.x + threadIdx.x; o < n; o += (long)gridDim.x * blockDim.x) {
+        const int ix = (int)(o / g.nz), iz = (int)(o % g.nz);
+        const long id = iz + g.npml + (long)g.nnz * (ix + g.npml);
+        const float sP = s.P[id], gP = r.P[id];
+        mig[o] = mig[o] + sP * gP;
+        if (!adcig) continue;
+        const float Ssx = -sP * s.u[id], Ssz = -s.Q[id] * s.w[id];
+        const float Sgx = gP * r.u[id], Sgz = r.Q[id] * r.w[id];
+        const float b1 = Ssx * Ssx + Ssz * Ssz, b2 = Sgx * Sgx + Sgz * Sgz;
+        const float a = (float)((double)(Ssx * Sgx + Ssz * Sgz) / ((double)sqrtf(b1 * b2) * (1 - 0.1)));
+        if (!(a >= -1.0f && a <= 1.0f)) continue;
+        int lo = 0, hi = g.nangle;          // bin = #thresholds at or above a
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (a <= c_gthr[mid - 1]) lo = mid;
+            else hi = mid - 1;
+        }
+        if (lo >= g.nangle) continue;
+        const float c = c_gcos[lo];
+        float *ag = adcig + iz + (long)g.nz * lo + (long)g.nz * g.nangle * ix;
+        *ag = *ag + sP * gP * c * c * c;
+    }
+}
+
+__global__ void k_g_mask(float *rec, const uint8_t *keep, long n) {
+    for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < n; k += (long)gridDim.x * blockDim.x)
+        if (!keep[k]) rec[k] = 0.0f;
+}
+
+// gathers [ix][ia][iz] /= ill[ix][iz]
+__global__ void k_g_adcig_norm(float *adcig, const float *ill, int nx, int nz, int nangle) {
+    const long n = (long)nx * nz * nangle;
+    for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < n; k += (long)gridDim.x * blockDim.x) {
+        const int ix = (int)(k / ((long)nz * nangle)), iz = (int)(k % nz);
+        adcig[k] = adcig[k] / ill[iz + (long)nz * ix];
+    }
+}
+
+// angle stack (stk_adcigs :799-818): stk = 0, += over the angles in order
+__global__ void k_g_stack_angles(const float *adcig, float *stk, int nx, int nz, int nangle) {
+    const long n = (long)nx * nz;
+    for (long o = blockIdx.x * (long)blockDim.x + threadIdx.x; o < n; o += (long)gridDim.x * blockDim.x) {
+        const int ix = (int)(o / nz), iz = (int)(o % nz);
+        float s = 0.0f;
+        for (int ia = 0; ia < nangle; ia++) s += adcig[(long)ix * nangle * nz + (long)ia * nz + iz];
+        stk[o] = s;
+    }
+}
+
+// The program's bin of a cosine a: (int)((float)(0.5*acosf(a)*180.0/pi) / (dangle*1.0)).
+static int ref_gpu_bin(float a, int dangle) {
+    const float deg = (float)(0.5 * std::acos(a) * 180.0 / kPiGui);
+    return (int)(deg / (dangle * 1.0));
+}
+
+static uint32_t okey(float f) {
+    uint32_t b;
+    memcpy(&b, &f, 4);
+    return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+
+static float kfloat(uint32_t k) {
+    const uint32_t b = (k & 0x80000000u) ? (k & 0x7fffffffu) : ~k;
+    float f;
+    memcpy(&f, &b, 4);
+    return f;
+}
+
+static int gpu_adcig_tables(int nangle, int dangle, cudaStream_t s) {
+    std::vector<float> thr(128, -2.0f), cs(128, 0.0f);
+    const uint32_t lo = okey(-1.0f), hi = okey(1.0f);
+    for (int k = 1; k <= nangle; k++) {
+        if (ref_gpu_bin(-1.0f, dangle) < k) continue;
+        uint32_t a = lo, b = hi;
+        while (a < b) {
+            const uint32_t m = a + (b - a + 1) / 2;
+            if (ref_gpu_bin(kfloat(m), dangle) >= k) a = m;
+            else b = m - 1;
+        }
+        thr[k - 1] = kfloat(a);
+    }
+    for (int ia = 0; ia < nangle; ia++) cs[ia] = std::cos((float)(ia * kPiGui / 180.0));
+    GEO_CUDA(cudaMemcpyToSymbolAsync(c_gthr, thr.data(), 128 * 4, 0, cudaMemcpyHostToDevice, s));
+    GEO_CUDA(cudaMemcpyToSymbolAsync(c_gcos, cs.data(), 128 * 4, 0, cudaMemcpyHostToDevice, s));
+    return GEO_OK;
+}
+
+// readFile's checks (:930-965): grid spacing for the frequency, dt, dispersion, stability.
+static int gpu_rtm_checks(const geo_rtm2d_gpu_desc &D, const std::vector<float> &v) {
+    float vmin = 999999.9f, vmax = -999999.9f;
+    for (float x : v) {
+        vmin = std::min(vmin, x);
+        vmax = std::max(vmax, x);
+    }
+    const float H_min = D.dx < D.dz ? D.dx : D.dz;
+    const float dt_max = (float)(0.5 * H_min / vmin), dxz_max = (float)(vmax / D.favg * 0.2);
+    if (dxz_max < D.dz || dxz_max < D.dx) return fail(GEO_ERR_CFL, "grid spacing too coarse for favg (redefine dx, dz)");
+    if (dt_max < D.dt) return fail(GEO_ERR_CFL, "dt too large (redefine dt)");
+    if (D.favg >= vmin / (5.0 * (D.dx > D.dz ? D.dx : D.dz))) return fail(GEO_ERR_CFL, "non-dispersion relation not satisfied");
+    const float tmp = (float)(D.dt * vmax * sqrtf((float)(1.0 / (D.dx * D.dx) + 1.0 / (D.dz * D.dz))));
+    if (tmp >= 0.777f) return fail(GEO_ERR_CFL, "stability condition not satisfied (%g >= 0.777)", tmp);
+    return GEO_OK;
+}
+
+static int grid_of_n(long n) { return (int)std::min<long>((n + 255) / 256, 152L * 16); }
+
+}  // namespace geo
+
+using namespace geo;
+
+extern "C" int geo_rtm2d_gpu(const geo_rtm2d_gpu_desc *desc, const float *v, const float *e, const float *d,
+                             const float *obs, float *mig_lap, float *illum, float *adcigs, float *stk_lap,
+                             float *shots, int mem, void *stream) {
+    if (!desc || !v || !e || !d || !mig_lap) return fail(GEO_ERR_ARG, "null argument");
+    const geo_rtm2d_gpu_desc &D = *desc;
+    if (D.nx < 2 || D.nz < 2 || D.npml < 5 || D.nt < 1 || D.ns < 1) return fail(GEO_ERR_ARG, "bad sizes");
+    if (!(D.dt > 0) || !(D.dx > 0) || !(D.dz > 0) || !(D.favg > 0)) return fail(GEO_ERR_ARG, "bad spacing");
+    if (D.nangle < 1 || D.nangle > 128 || D.dangle < 1) return fail(GEO_ERR_ARG, "nangle must be 1..128, dangle >= 1");
+    if (mem != GEO_MEM_HOST && mem != GEO_MEM_DEVICE) return fail(GEO_ERR_ARG, "bad mem kind");
+    const int nx = D.nx, nz = D.nz, npml = D.npml, nt = D.nt, nnx = nx + 2 * npml, nnz = nz + 2 * npml;
+    const size_t n0 = (size_t)nx * nz, n = (size_t)nnx * nnz;
+    cudaStream_t s = (cudaStream_t)stream;
+    std::vector<float> hv(n0), he(n0), hd(n0);
+    const float *src[3] = {v, e, d};
+    float *dst[3] = {hv.data(), he.data(), hd.data()};
+    for (int k = 0; k < 3; k++) {
+        if (mem == GEO_MEM_DEVICE) GEO_CUDA(cudaMemcpyAsync(dst[k], src[k], n0 * 4, cudaMemcpyDeviceToHost, s));
+        else memcpy(dst[k], src[k], n0 * 4);
+    }
+    GEO_CUDA(cudaStreamSynchronize(s));
+    GEO_TRY(check_model(hv.data(), he.data(), hd.data(), n0));
+    GEO_TRY(gpu_rtm_checks(D, hv));
+    for (int is = 1; is <= D.ns; is++) {
+        const int ixs = D.fs + (is - 1) * D.ds + npml - 1, izs = D.zs + npml - 1;
+        if (ixs < 4 || ixs >= nnx - 4 || izs < 4 || izs >= nnz - 4) return fail(GEO_ERR_ARG, "shot %d outside the grid", is);
+    }
+    std::vector<float> pv(n), pe(n), pd(n);
+    pad_model_2d(nx, nz, npml, hv.data(), pv.data());
+    pad_model_2d(nx, nz, npml, he.data(), pe.data());
+    pad_model_2d(nx, nz, npml, hd.data(), pd.data());
+    const float d0 = sponge_d0(V_GPU, 2, 0.0f, pv[n / 2], npml, D.dx, D.dx, D.dz);   // get_d0 :110-118
+    std::vector<float> prof(4 * (size_t)(nnx + nnz));
+    float *q = prof.data();
+    sponge_profiles(V_GPU, nx, npml, D.dt, d0, q, q + nnx, q + 2 * nnx, q + 3 * nnx);
+    q += 4 * nnx;
+    sponge_profiles(V_GPU, nz, npml, D.dt, d0, q, q + nnz, q + 2 * nnz, q + 3 * nnz);
+    std::vector<float> amp;
+    std::vector<uint8_t> on;
+    source_amplitudes(V_GPU, nt, D.dt, D.favg, D.pfac, D.wtype, amp, on);
+    // untapered 1+2eps, sqrtf(1+2del)
+    std::vector<float> e2(n), d2(n);
+    for (size_t k = 0; k < n; k++) {
+        e2[k] = 1 + 2 * pe[k];
+        d2[k] = sqrtf(1 + 2 * pd[k]);
+    }
+    const float mu_v = pv[1] * sqrtf(1 + 2 * pe[1]);
+    const int L = 2 * nx + 2 * nz;
+
+    DevBuf dvp, dprof, de2, dd2, dte2, dtd2, fs_, fr_, ring, rec, mig, ill, ag, lap, stk, mkeep, trs;
+    GEO_TRY(dvp.alloc(n * 4));
+    GEO_TRY(dprof.alloc(prof.size() * 4));
+    GEO_TRY(de2.alloc(n * 4));
+    GEO_TRY(dd2.alloc(n * 4));
+    GEO_TRY(dte2.alloc(n * 4));
+    GEO_TRY(dtd2.alloc(n * 4));
+    GEO_TRY(fs_.alloc(8 * n * 4));
+    GEO_TRY(fr_.alloc(8 * n * 4));
+    GEO_TRY(ring.alloc((size_t)2 * nt * L * 4));
+    GEO_TRY(rec.alloc((size_t)nt * nx * 4));
+    GEO_TRY(mig.alloc(n0 * 4));
+    GEO_TRY(ill.alloc(n0 * 4));
+    GEO_TRY(mkeep.alloc((size_t)nt * nx));
+    if (adcigs || stk_lap) {
+        GEO_TRY(ag.alloc((size_t)D.nangle * n0 * 4));
+        GEO_TRY(ag.zero(s));
+        GEO_TRY(gpu_adcig_tables(D.nangle, D.dangle, s));
+    }
+    GEO_CUDA(cudaMemcpyAsync(dvp.p, pv.data(), n * 4, cudaMemcpyHostToDevice, s));
+    GEO_CUDA(cudaMemcpyAsync(dprof.p, prof.data(), prof.size() * 4, cudaMemcpyHostToDevice, s));
+    GEO_CUDA(cudaMemcpyAsync(de2.p, e2.data(), n * 4, cudaMemcpyHostToDevice, s));
+    GEO_CUDA(cudaMemcpyAsync(dd2.p, d2.data(), n * 4, cudaMemcpyHostToDevice, s));
+    GEO_TRY(mig.zero(s));
+    GEO_TRY(ill.zero(s));
+    GRtm g{};
+    g.nnx = nnx; g.nnz = nnz; g.nx = nx; g.nz = nz; g.npml = npml; g.nangle = D.nangle;
+    g.dtx = D.dt / D.dx;
+    g.dtz = D.dt / D.dz;
+    const float *pp = dprof.as<float>();
+    g.cx1 = pp; g.cx2 = pp + nnx; g.ax1 = pp + 2 * nnx; g.ax2 = pp + 3 * nnx;
+    pp += 4 * nnx;
+    g.cz1 = pp; g.cz2 = pp + nnz; g.az1 = pp + 2 * nnz; g.az2 = pp + 3 * nnz;
+    g.vp = dvp.as<float>();
+    auto fields = [&](DevBuf &b) {
+        GField f;
+        float *p = b.as<float>();
+        f.u = p; f.w = p + n; f.P = p + 2 * n; f.Q = p + 3 * n;
+        f.px = p + 4 * n; f.pz = p + 5 * n; f.qx = p + 6 * n; f.qz = p + 7 * n;
+        return f;
+    };
+    const GField S = fields(fs_), R = fields(fr_);
+    float *bp = ring.as<float>(), *bq = bp + (size_t)nt * L;
+    const int gb = grid_of_n((long)n), gi = grid_of_n((long)n0);
+    const cudaMemcpyKind kout = mem == GEO_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+    const cudaMemcpyKind kin = mem == GEO_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    if (shots || obs) GEO_TRY(trs.alloc((size_t)nt * nx * 4));
+    for (int is = 1; is <= D.ns; is++) {
+        // SV taper box of this shot (R=18, r=7; centre fs+(is-1)ds+npml, zs+npml)
+        std::vector<float> te2(e2), td2(d2);
+        {
+            const int cx = D.fs + (is - 1) * D.ds + npml, cz = D.zs + npml, R2 = 18 * 18, r2 = 7 * 7;
+            for (int ix = std::max(0, cx - 18); ix <= std::min(nnx - 1, cx + 18); ix++)
+                for (int iz = std::max(0, cz - 18); iz <= std::min(nnz - 1, cz + 18); iz++) {
+                    const int rx = ix - cx, rz = iz - cz, q2 = rx * rx + rz * rz;
+                    if (q2 > R2) continue;
+                    const size_t id = (size_t)ix * nnz + iz;
+                    float ee = 0.0f, dd = 0.0f;
+                    if (q2 > r2) {
+                        const double gq = 0.5 * (1 - std::cos(kPiGui * ((sqrtf((float)q2) - 7) * 4.0 / (18 * 3.0 - 1))));
+                        ee = (float)(gq * pe[id]);
+                        dd = (float)(gq * pd[id]);
+                    }
+                    te2[id] = 1 + 2 * ee;
+                    td2[id] = sqrtf(1 + 2 * dd);
+                }
+        }
+        GEO_CUDA(cudaMemcpyAsync(dte2.p, te2.data(), n * 4, cudaMemcpyHostToDevice, s));
+        GEO_CUDA(cudaMemcpyAsync(dtd2.p, td2.data(), n * 4, cudaMemcpyHostToDevice, s));
+        GEO_TRY(fs_.zero(s));
+        GEO_TRY(fr_.zero(s));
+        GEO_TRY(rec.zero(s));
+        GEO_TRY(ring.zero(s));
+        const long src = (long)(D.fs + (is - 1) * D.ds + npml - 1) * nnz + (D.zs + npml - 1);
+        for (int it = 0; it < nt; it++) {
+            if (on[it]) {
+                k_g_src<<<1, 1, 0, s>>>(S, src, amp[it]);
+                GEO_TRY(check_launch("grtm_src"));
+            }
+            k_g_vel<<<gb, 256, 0, s>>>(g, S);
+            GEO_TRY(check_launch("grtm_vel"));
+            k_g_stress<<<gb, 256, 0, s>>>(g, S, dte2.as<float>(), dtd2.as<float>());
+            GEO_TRY(check_launch("grtm_stress"));
+            k_g_surface<<<(nx + 255) / 256, 256, 0, s>>>(g, S, rec.as<float>(), it, 0);
+            GEO_TRY(check_launch("grtm_record"));
+            k_g_ring<<<(L + 255) / 256, 256, 0, s>>>(g, S, bp, bq, it, 1);
+            GEO_TRY(check_launch("grtm_ring"));
+            k_g_illum<<<gi, 256, 0, s>>>(g, S, ill.as<float>());
+            GEO_TRY(check_launch("grtm_illum"));
+        }
+        // direct-wave mute (GPU form, tt), exactly as the program's kernel
+        // writes it: thread it < nt rounded up to 512 zeroes flat sample
+        // ix*nt + it of the trace-major record for every trace ix whose
+        // window holds it -- past nt that lands on later traces
+        {
+            std::vector<uint8_t> keep((size_t)nt * nx, 1);   // time-major
+            const int nt512 = (nt + 511) / 512 * 512;
+            for (int ix = 0; ix < nx; ix++) {
+                const float mu_x = D.dx * std::abs(ix - D.fs - (is - 1) * D.ds), mu_z = D.dz * D.zs;
+                const float mu_t0 = sqrtf((float)(std::pow(mu_x, 2) + std::pow(mu_z, 2))) / mu_v;
+                const int mu_t = (int)(2.0 / (D.dt * D.favg));
+                const int mu_nt = (int)(mu_t0 / D.dt) + mu_t + D.mute_tt;
+                const int first = std::max(0, (int)(mu_t0 / D.dt) - D.mute_tt + 1);
+                for (int it = first; it < std::min(mu_nt, nt512); it++) {
+                    const long j = (long)ix * nt + it;          // trace-major flat index
+                    if (j >= (long)nx * nt) break;
+                    keep[(size_t)(j % nt) * nx + (size_t)(j / nt)] = 0;
+                }
+            }
+            GEO_CUDA(cudaMemcpyAsync(mkeep.p, keep.data(), keep.size(), cudaMemcpyHostToDevice, s));
+            k_g_mask<<<grid_of_n((long)nt * nx), 256, 0, s>>>(rec.as<float>(), mkeep.as<uint8_t>(), (long)nt * nx);
+            GEO_TRY(check_launch("grtm_mute"));
+            GEO_CUDA(cudaStreamSynchronize(s));
+        }
+        if (shots) {
+            GEO_TRY(launch_transpose_records(rec.as<float>(), trs.as<float>(), nx, nt, s));
+            GEO_CUDA(cudaMemcpyAsync(shots + (size_t)(is - 1) * nx * nt, trs.p, (size_t)nx * nt * 4, kout, s));
+        }
+        if (obs) {
+            // observed shot (trace-major nx*nt) replaces the modelled record
+            GEO_CUDA(cudaMemcpyAsync(trs.p, obs + (size_t)(is - 1) * nx * nt, (size_t)nx * nt * 4, kin, s));
+            GEO_TRY(launch_transpose_records(trs.as<float>(), rec.as<float>(), nt, nx, s));
+        }
+        for (int it = nt - 1; it >= 0; it--) {
+            k_g_ring<<<(L + 255) / 256, 256, 0, s>>>(g, S, bp, bq, it, 0);
+            GEO_TRY(check_launch("grtm_ring"));
+            k_g_vel<<<gb, 256, 0, s>>>(g, S);
+            GEO_TRY(check_launch("grtm_vel"));
+            k_g_stress<<<gb, 256, 0, s>>>(g, S, de2.as<float>(), dd2.as<float>());
+            GEO_TRY(check_launch("grtm_stress"));
+            k_g_surface<<<(nx + 255) / 256, 256, 0, s>>>(g, R, rec.as<float>(), it, 1);
+            GEO_TRY(check_launch("grtm_inject"));
+            k_g_vel<<<gb, 256, 0, s>>>(g, R);
+            GEO_TRY(check_launch("grtm_vel"));
+            k_g_stress<<<gb, 256, 0, s>>>(g, R, de2.as<float>(), dd2.as<float>());
+            GEO_TRY(check_launch("grtm_stress"));
+            k_g_image<<<gi, 256, 0, s>>>(g, S, R, mig.as<float>(), ag.p ? ag.as<float>() : nullptr);
+            GEO_TRY(check_launch("grtm_image"));
+        }
+    }
+    GEO_TRY(launch_normalize_image(mig.as<float>(), ill.as<float>(), n0, s));
+    GEO_TRY(lap.alloc(n0 * 4));
+    GEO_TRY(launch_laplace2d(nx, nz, mig.as<float>(), lap.as<float>(), s));
+    GEO_CUDA(cudaMemcpyAsync(mig_lap, lap.p, n0 * 4, kout, s));
+    if (illum) GEO_CUDA(cudaMemcpyAsync(illum, ill.p, n0 * 4, kout, s));
+    if (ag.p) {
+        k_g_adcig_norm<<<grid_of_n((long)n0 * D.nangle), 256, 0, s>>>(ag.as<float>(), ill.as<float>(), nx, nz, D.nangle);
+        GEO_TRY(check_launch("grtm_adcig_norm"));
+        if (adcigs) GEO_CUDA(cudaMemcpyAsync(adcigs, ag.p, (size_t)D.nangle * n0 * 4, kout, s));
+        if (stk_lap) {
+            GEO_TRY(stk.alloc(n0 * 4));
+            k_g_stack_angles<<<gi, 256, 0, s>>>(ag.as<float>(), stk.as<float>(), nx, nz, D.nangle);
+            GEO_TRY(check_launch("grtm_stack_angles"));
+            GEO_TRY(launch_laplace2d(nx, nz, stk.as<float>(), lap.as<float>(), s));
+            GEO_CUDA(cudaMemcpyAsync(stk_lap, lap.p, n0 * 4, kout, s));
+        }
+    }
+    GEO_CUDA(cudaStreamSynchronize(s));
+    return GEO_OK;
+}

@@ -242,6 +242,31 @@ int geo_rtm2d_batch(const geo_rtm2d_desc *desc, const float *v, const float *e, 
 int geo_rtm2d_batch_adcig(const geo_rtm2d_desc *desc, const float *v, const float *e, const float *d,
                           float *image, float *per_shot, float *adcig, int mem, void *stream);
 
+/* 2D RTM with the 2D GPU RTM program's semantics
+ * (2D-vti-fd+rtm-cuda/Toa_gpu2DvtiFdRtmAdcigsLaplace.cu, RTM() :1184-1566):
+ * full-model shots is = 1..ns at fs + (is-1)*ds, ring saving of P,Q,
+ * forward-stepped reconstruction, receiver re-injection, image, forward
+ * source illumination and Poynting angle gathers, summed over the shots and
+ * divided by the illumination at the end.  obs (optional): observed shots
+ * ns*nx*nt (trace-major, readShot) replacing the modelled records.
+ * mig_lap: Laplacian of the image (the program's migration file); illum,
+ * adcigs (nx*nangle*nz, [ix][ia][iz]), stk_lap (Laplacian of the angle
+ * stack), shots (the muted modelled records ns*nx*nt): optional.  The
+ * readFile checks (:930-965) return GEO_ERR_CFL. */
+typedef struct geo_rtm2d_gpu_desc {
+    int   nx, nz, npml, nt;
+    float dx, dz, dt;        /* m, m, s                                      */
+    float favg, pfac;
+    int   wtype;
+    int   ns, fs, ds, zs;    /* shots; source x (1-based), step, depth       */
+    int   mute_tt;           /* 20 in the program                            */
+    int   nangle, dangle;    /* 70 and 1 in the program                      */
+} geo_rtm2d_gpu_desc;
+
+int geo_rtm2d_gpu(const geo_rtm2d_gpu_desc *desc, const float *v, const float *e, const float *d,
+                  const float *obs, float *mig_lap, float *illum, float *adcigs, float *stk_lap, float *shots,
+                  int mem, void *stream);
+
 /* Adjoint first-difference Laplacian (laplac2_lop adj=1,
  * utils-Laplacian-filter/laplace.c:9-53; the in-program copy
  * Toa_gpu2DvtiFdRtmAdcigsLaplace.cu:150-202 clears `out` first, as this does). */

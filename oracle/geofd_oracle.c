@@ -734,6 +734,136 @@ int orc_rtm2d_mpi_shot(int nx, int nz, int npd, int nt, float dx, float dz, floa
     return 0;
 }
 
+/* 2D RTM with the 2D GPU RTM program's semantics
+ * (2D-vti-fd+rtm-cuda/Toa_gpu2DvtiFdRtmAdcigsLaplace.cu, RTM() :1184-1566):
+ * per shot (is = 1..ns) forward with the GPU source and the R=18, r=7 SV
+ * taper, record P at row npml, ring of P,Q (rows npml-1, npml+nz+1,
+ * columns npml-1, npml+nx+1; wavefield_bndr :532-612), illumination
+ * ill += P*P + Q*Q then <= 0 -> 1 (:654-677); mute (:614-652, tt, with the
+ * surplus threads of its launch zeroing flat samples past nt); obs (optional)
+ * replaces the record; backward: ring restore + untapered step of the source
+ * field, record into P,Q of the receiver field at row npml + step, image
+ * += sP*gP (:679-698) and Poynting gathers (:718-766, acosf, cosf^3).
+ * After all shots mig /= ill and gathers /= ill; the caller filters.
+ * mig, ill: nx*nz; adcigs (optional): nx*nangle*nz [ix][ia][iz];
+ * shots (optional): the muted modelled records ns*nx*nt. */
+int orc_rtm2d_gpu(int nx, int nz, int npml, int nt, float dx, float dz, float dt, float favg, float pfac,
+                  int wtype, int ns, int fs, int ds, int zs, int mute_tt, int nangle, int dangle,
+                  const float *v, const float *e, const float *dl, const float *obs,
+                  float *mig, float *ill, float *adcigs, float *shots)
+{
+    const int nnx = nx + 2 * npml, nnz = nz + 2 * npml, L = 2 * nx + 2 * nz;
+    const size_t n = (size_t)nnx * nnz, n0 = (size_t)nx * nz;
+    int is, it, ix, iz, k;
+    float *rec = calloc((size_t)nt * nx, 4), *bp = calloc((size_t)nt * L, 4), *bq = calloc((size_t)nt * L, 4);
+    memset(mig, 0, n0 * 4);
+    memset(ill, 0, n0 * 4);
+    if (adcigs) memset(adcigs, 0, n0 * nangle * 4);
+    for (is = 1; is <= ns; is++) {
+        orc_fd2d_desc d;
+        orc_prop2d fw, sb, rc;
+        memset(&d, 0, sizeof d);
+        d.nx = nx; d.nz = nz; d.npd = npml; d.nt = nt; d.variant = ORC_V_GPURTM; d.sv = 1; d.wtype = wtype;
+        d.dx = dx; d.dz = dz; d.dt = dt; d.favg = favg; d.pfac = pfac;
+        d.fs = (float)fs; d.ds = (float)ds; d.zs = (float)zs; d.is = is;
+        prop2d_init(&fw, &d, v, e, dl, 1);
+        for (it = 0; it < nt; it++) {
+            prop2d_step(&fw, it);
+            for (ix = 0; ix < nx; ix++) rec[(size_t)ix * nt + it] = (float)fw.P[npml + (size_t)nnz * (ix + npml)];
+            for (k = 0; k < L; k++) {
+                size_t id;
+                if (k < nx) id = npml - 1 + (size_t)nnz * (k + npml);
+                else if (k < 2 * nx) id = npml + nz + 1 + (size_t)nnz * (k - nx + npml);
+                else if (k < 2 * nx + nz) id = k - 2 * nx + npml + (size_t)nnz * (npml - 1);
+                else id = k - 2 * nx - nz + npml + (size_t)nnz * (npml + nx + 1);
+                bp[(size_t)it * L + k] = (float)fw.P[id];
+                bq[(size_t)it * L + k] = (float)fw.Q[id];
+            }
+            for (ix = 0; ix < nx; ix++)
+                for (iz = 0; iz < nz; iz++) {
+                    size_t id = iz + npml + (size_t)nnz * (ix + npml), o = (size_t)ix * nz + iz;
+                    float pp = (float)fw.P[id], qq = (float)fw.Q[id];
+                    ill[o] += pp * pp + qq * qq;
+                    if (ill[o] <= 0.0f) ill[o] = 1.0f;
+                }
+        }
+        {
+            /* mute_directwave: one thread per sample it < roundup(nt, 512), all traces */
+            const float mu_v = (float)fw.vp[1] * sqrtf((float)(1 + 2 * e[0]));
+            const int nt512 = (nt + 511) / 512 * 512;
+            for (ix = 0; ix < nx; ix++) {
+                float mu_x = dx * abs(ix - fs - (is - 1) * ds), mu_z = dz * zs;
+                float mu_t0 = sqrtf((float)(pow(mu_x, 2) + pow(mu_z, 2))) / mu_v;
+                int mu_t = (int)(2.0 / (dt * favg));
+                int mu_nt = (int)(mu_t0 / dt) + mu_t + mute_tt;
+                for (it = 0; it < nt512; it++)
+                    if ((it > (int)(mu_t0 / dt) - mute_tt) && (it < mu_nt)) {
+                        long j = (long)ix * nt + it;
+                        if (j < (long)nx * nt) rec[j] = 0.0f;
+                    }
+            }
+        }
+        if (shots) memcpy(shots + (size_t)(is - 1) * nx * nt, rec, (size_t)nx * nt * 4);
+        if (obs) memcpy(rec, obs + (size_t)(is - 1) * nx * nt, (size_t)nx * nt * 4);
+        prop2d_init(&sb, &d, v, e, dl, 0);
+        prop2d_init(&rc, &d, v, e, dl, 0);
+        memcpy(sb.u, fw.u, n * sizeof(REAL)); memcpy(sb.w, fw.w, n * sizeof(REAL));
+        memcpy(sb.P, fw.P, n * sizeof(REAL)); memcpy(sb.Q, fw.Q, n * sizeof(REAL));
+        memcpy(sb.px, fw.px, n * sizeof(REAL)); memcpy(sb.pz, fw.pz, n * sizeof(REAL));
+        memcpy(sb.qx, fw.qx, n * sizeof(REAL)); memcpy(sb.qz, fw.qz, n * sizeof(REAL));
+        prop2d_free(&fw);
+        for (it = nt - 1; it >= 0; it--) {
+            for (k = 0; k < L; k++) {
+                size_t id;
+                if (k < nx) id = npml - 1 + (size_t)nnz * (k + npml);
+                else if (k < 2 * nx) id = npml + nz + 1 + (size_t)nnz * (k - nx + npml);
+                else if (k < 2 * nx + nz) id = k - 2 * nx + npml + (size_t)nnz * (npml - 1);
+                else id = k - 2 * nx - nz + npml + (size_t)nnz * (npml + nx + 1);
+                sb.P[id] = (REAL)bp[(size_t)it * L + k];
+                sb.Q[id] = (REAL)bq[(size_t)it * L + k];
+            }
+            vel2d(&sb.st, sb.u, sb.w, sb.P, sb.Q);
+            stress2d(&sb.st, sb.u, sb.w, sb.P, sb.Q, sb.px, sb.pz, sb.qx, sb.qz, NULL);
+            for (ix = 0; ix < nx; ix++) {
+                size_t id = npml + (size_t)nnz * (ix + npml);
+                rc.P[id] = rc.Q[id] = (REAL)rec[(size_t)ix * nt + it];
+            }
+            vel2d(&rc.st, rc.u, rc.w, rc.P, rc.Q);
+            stress2d(&rc.st, rc.u, rc.w, rc.P, rc.Q, rc.px, rc.pz, rc.qx, rc.qz, NULL);
+            for (ix = 0; ix < nx; ix++)
+                for (iz = 0; iz < nz; iz++) {
+                    size_t id = iz + npml + (size_t)nnz * (ix + npml), o = (size_t)ix * nz + iz;
+                    float sP = (float)sb.P[id], gP = (float)rc.P[id];
+                    mig[o] += sP * gP;
+                    if (adcigs) {
+                        float Ssx = -sP * (float)sb.u[id], Ssz = -(float)sb.Q[id] * (float)sb.w[id];
+                        float Sgx = gP * (float)rc.u[id], Sgz = (float)rc.Q[id] * (float)rc.w[id];
+                        float b1 = Ssx * Ssx + Ssz * Ssz, b2 = Sgx * Sgx + Sgz * Sgz;
+                        float a = (Ssx * Sgx + Ssz * Sgz) / (sqrtf(b1 * b2) * (1 - 0.1));
+                        if (a >= -1 && a <= 1) {
+                            int ia;
+                            a = 0.5 * acosf(a) * 180.0 / PI_GUI;
+                            ia = (int)(a / (dangle * 1.0));
+                            if (ia < nangle) {
+                                float c = cosf(ia * PI_GUI / 180.0);
+                                adcigs[iz + (size_t)nz * ia + (size_t)nz * nangle * ix] += sP * gP * c * c * c;
+                            }
+                        }
+                    }
+                }
+        }
+        prop2d_free(&sb); prop2d_free(&rc);
+    }
+    for (size_t o = 0; o < n0; o++) mig[o] /= ill[o];
+    if (adcigs)
+        for (size_t q = 0; q < n0 * nangle; q++) {
+            size_t ixq = q / ((size_t)nz * nangle), izq = q % nz;
+            adcigs[q] /= ill[izq + (size_t)nz * ixq];
+        }
+    free(rec); free(bp); free(bq);
+    return 0;
+}
+
 /* Stack per-shot images into the full image in shot order
  * (Toa_rtm_vti_adcig_cdp.c:1102-1104; single-rank MPI_Reduce is a copy). */
 void orc_stack2d(int nz, int nxs, int offset, const float *mig_is, float *mig_full)

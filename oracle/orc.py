@@ -66,6 +66,7 @@ def lib(prec=32):
             [C.c_int, C.POINTER(C.c_float)]
         L.orc_rtm3d_shot.argtypes = [C.POINTER(FD3DDesc), C.c_int] + [C.POINTER(C.c_float)] * 6
         L.orc_rtm3d_snap_shot.argtypes = [C.POINTER(FD3DDesc), C.c_int, C.c_int] + [C.POINTER(C.c_float)] * 5
+        L.orc_rtm2d_gpu.argtypes = [C.c_int] * 4 + [C.c_float] * 5 + [C.c_int] * 8 + [C.POINTER(C.c_float)] * 8
         L.orc_image_illum.argtypes = [C.c_long, C.POINTER(C.c_float), C.POINTER(C.c_float)]
         _libs[key] = L
     return _libs[key]
@@ -165,6 +166,22 @@ def rtm2d_mpi_shot(v, e, d, *, npd, nt, dx, dz, dt_ms, favg, pfac, fs_sxd, ds_sx
     lib(prec).orc_rtm2d_mpi_shot(nx, nz, npd, nt, dx, dz, dt_ms, favg, pfac, fs_sxd, ds_sxd, zs_sxd,
                                  is_, nxs, _fp(v), _fp(e), _fp(d), _fp(mig), C.byref(off), _fp(pcal), _fp(ag))
     return (mig, off.value, pcal, ag) if adcig else (mig, off.value, pcal)
+
+
+def rtm2d_gpu(v, e, d, *, npml, nt, dx, dz, dt, favg, pfac, wtype=1, ns=1, fs=1, ds=0, zs=1, mute_tt=20,
+              nangle=70, dangle=1, obs=None, prec=32):
+    """The 2D GPU RTM program; returns (mig/ill (nx,nz), ill, adcigs (nx,nangle,nz),
+    muted modelled shots (ns,nx,nt))."""
+    v, e, d = c32(v), c32(e), c32(d)
+    nx, nz = v.shape
+    mig = np.zeros((nx, nz), _f)
+    ill = np.zeros((nx, nz), _f)
+    ag = np.zeros((nx, nangle, nz), _f)
+    shots = np.zeros((ns, nx, nt), _f)
+    ob = c32(obs) if obs is not None else None
+    lib(prec).orc_rtm2d_gpu(nx, nz, npml, nt, dx, dz, dt, favg, pfac, wtype, ns, fs, ds, zs, mute_tt, nangle,
+                            dangle, _fp(v), _fp(e), _fp(d), _fp(ob), _fp(mig), _fp(ill), _fp(ag), _fp(shots))
+    return mig, ill, ag, shots
 
 
 def stack2d(full, mig_is, offset):

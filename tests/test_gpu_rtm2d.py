@@ -78,3 +78,42 @@ def test_rtm2d_adcig_bit_exact(geo, orc):
     assert gathers.shape == (90,) + v.shape
     assert (np.abs(ago).reshape(90, -1).max(axis=1) > 0).sum() > 10
     assert np.array_equal(gathers, ago)
+
+
+GKW = dict(npml=20, nt=700, dx=10.0, dz=10.0, dt=np.float32(1e-3), favg=20.0, pfac=10.0, ns=2, fs=30, ds=35, zs=2,
+           mute_tt=20, nangle=70, dangle=1)
+
+
+def test_rtm2d_gpu_program_bit_exact(geo, orc):
+    """The 2D GPU RTM program (ring saving, forward-stepped reconstruction,
+    Poynting gathers): image, illumination, gathers, angle stack and
+    records equal the oracle's."""
+    v, e, d = model(nx=96, nz=60)
+    mig, ill, ag, shots = orc.rtm2d_gpu(v, e, d, **GKW)
+    out = geo.rtm2d_gpu(v, e, d, **GKW)
+    assert np.abs(ill).max() > 0 and np.abs(ag).max() > 0
+    assert np.array_equal(out["shots"], shots)
+    assert np.array_equal(out["illum"], ill)
+    assert np.array_equal(out["mig_lap"], orc.laplace2d_adj(mig))
+    assert np.array_equal(out["adcigs"], ag)
+    stk = np.zeros(v.shape, np.float32)
+    for ia in range(GKW["nangle"]):
+        stk = (stk + ag[:, ia, :]).astype(np.float32)
+    assert np.array_equal(out["stk_lap"], orc.laplace2d_adj(stk))
+
+
+def test_rtm2d_gpu_program_observed_shots(geo, orc):
+    v, e, d = model(nx=96, nz=60)
+    kw = dict(GKW, ns=1, nt=520)          # nt < 512 rounding: the mute's surplus threads span traces
+    obs = np.random.default_rng(5).standard_normal((1, 96, 520)).astype(np.float32) * 1e-3
+    mig, ill, ag, _ = orc.rtm2d_gpu(v, e, d, obs=obs, **kw)
+    out = geo.rtm2d_gpu(v, e, d, obs=obs, **kw)
+    assert np.array_equal(out["mig_lap"], orc.laplace2d_adj(mig))
+    assert np.array_equal(out["adcigs"], ag)
+
+
+def test_rtm2d_gpu_program_stability_check(geo):
+    v, e, d = model(nx=96, nz=60)
+    with pytest.raises(geo.GeoError) as ei:
+        geo.rtm2d_gpu(v, e, d, **dict(GKW, dt=np.float32(5e-3)))
+    assert ei.value.status == 5
