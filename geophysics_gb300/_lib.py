@@ -43,7 +43,7 @@ class FD3DDesc(C.Structure):
 
 class RTM3DDesc(C.Structure):
     _fields_ = [("fd", FD3DDesc), ("ns", C.c_int), ("mute_tt", C.c_int), ("method", C.c_int),
-                ("snap_every", C.c_int), ("ae", C.c_void_p)]
+                ("snap_every", C.c_int), ("ae", C.c_void_p), ("na", C.c_int), ("da", C.c_int), ("dcdp", C.c_int)]
 
 
 class RTM2DGpuDesc(C.Structure):
@@ -91,6 +91,7 @@ def lib():
         "geo_rtm2d_batch": (_i, [C.POINTER(RTM2DDesc), _vp, _vp, _vp, _vp, _vp, _i, _vp]),
         "geo_rtm2d_batch_adcig": (_i, [C.POINTER(RTM2DDesc), _vp, _vp, _vp, _vp, _vp, _vp, _i, _vp]),
         "geo_rtm3d": (_i, [C.POINTER(RTM3DDesc), _vp, _vp, _vp, _vp, _vp, _vp, _i, _vp]),
+        "geo_rtm3d_adcig": (_i, [C.POINTER(RTM3DDesc), _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i, _vp]),
         "geo_su_read": (_i, [C.c_char_p, _i, _i, _i, _vp, _vp]),
         "geo_su_write": (_i, [C.c_char_p, _i, _i, _f, _i, _vp, _vp]),
         "geo_su_replace_data": (_i, [C.c_char_p, C.c_char_p, C.c_char_p, _i, _i]),

@@ -199,28 +199,32 @@ _RTM = {"boundary": GEO_RTM_BOUNDARY, "snapshot": GEO_RTM_SNAPSHOT, "learned": G
 
 def rtm3d(v, e, d, *, npd, nt, dx, dy, dz, dt, favg, fsx, fsy, fsz, ns=1, dsx=0, dsy=0, dsz=0, mute_tt=70,
           pfac=10.0, wtype=1, sv=0, mode="fast", laplace=True, illum=False, method="boundary", snap_every=4,
-          codec=None):
+          codec=None, adcig=None):
     """3D RTM over shots 0..ns-1; v,e,d shaped (ny, nx, nz).
 
     method "boundary": the 3D GPU RTM program's boundary-saving recompute;
     "snapshot": source P kept every snap_every steps (fp32);
     "learned": the same snapshots through `codec` (a trained Codec).
+    adcig = (na, da, dcdp) (boundary method): also the Poynting angle
+    gathers, shaped (ny//dcdp, nx//dcdp, na, nz), illumination-divided.
     Returns the illumination-divided image, then the Laplacian-filtered image
-    if `laplace`, then the illumination if `illum`."""
+    if `laplace`, then the illumination if `illum`, then the gathers."""
     b = _Bufs(v, e, d)
     ny, nx, nz = v.shape
     fd = FD3DDesc(nx=nx, ny=ny, nz=nz, npd=npd, nt=nt, dx=dx, dy=dy, dz=dz, dt=dt, favg=favg, pfac=pfac,
                   wtype=wtype, sv=sv, mode=_MODES[mode] if isinstance(mode, str) else int(mode),
                   fsx=fsx, fsy=fsy, fsz=fsz, dsx=dsx, dsy=dsy, dsz=dsz, rec_iz=npd, rx0=0, drx=1, nrx=nx,
                   ry0=0, dry=1, nry=ny, mute_tt=0)
+    na, da, dcdp = adcig if adcig is not None else (0, 0, 0)
     desc = RTM3DDesc(fd=fd, ns=ns, mute_tt=mute_tt, method=_RTM[method] if isinstance(method, str) else int(method),
-                     snap_every=snap_every, ae=codec._p if codec is not None else None)
+                     snap_every=snap_every, ae=codec._p if codec is not None else None, na=na, da=da, dcdp=dcdp)
     pv, pe, pd = b.inp(v), b.inp(e), b.inp(d)
     mig, pm = b.out((ny, nx, nz), v)
     lap, pl = b.out((ny, nx, nz), v) if laplace else (None, None)
     ill, pi = b.out((ny, nx, nz), v) if illum else (None, None)
-    check(lib().geo_rtm3d(C.byref(desc), pv, pe, pd, pm, pl, pi, b.mem, b.stream()), "geo_rtm3d")
-    out = [mig] + ([lap] if laplace else []) + ([ill] if illum else [])
+    ag, pa = b.out((ny // dcdp, nx // dcdp, na, nz), v) if adcig is not None else (None, None)
+    check(lib().geo_rtm3d_adcig(C.byref(desc), pv, pe, pd, pm, pl, pi, pa, b.mem, b.stream()), "geo_rtm3d_adcig")
+    out = [mig] + ([lap] if laplace else []) + ([ill] if illum else []) + ([ag] if adcig is not None else [])
     return out[0] if len(out) == 1 else tuple(out)
 
 

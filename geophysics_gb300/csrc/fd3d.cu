@@ -16,6 +16,7 @@
 #include "fd3d.cuh"
 #include "fd3d_fused.cuh"
 #include "ae.cuh"
+#include "adcig.cuh"
 #include <algorithm>
 #include <cstdlib>
 #include <cmath>
@@ -609,6 +610,48 @@ __global__ void k_snap_image(Grid3D g, const float *snap, const float *gP, float
     }
 }
 
+// Poynting angle gathers after a backward step (Poynting_Adcigs :618-661):
+// s, r are the source and receiver fields at their new time level; tab holds
+// the bin thresholds then cosf(ia*pi/180), kMaxAngles each.  One thread per
+// gather column point (iz fastest); each point adds to one bin of its own
+// column, so there are no write conflicts.
+__global__ void k_adcig3d(Grid3D s, Grid3D r, float *adcig, const float *tab, int na, int dcdp, int nxa, int nya) {
+    __shared__ float thr[kMaxAngles], cs[kMaxAngles];
+    for (int i = threadIdx.x; i < kMaxAngles; i += blockDim.x) {
+        thr[i] = tab[i];
+        cs[i] = tab[kMaxAngles + i];
+    }
+    __syncthreads();
+    const int nz = s.nz;
+    const long n = (long)nz * nxa * nya;
+    for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < n; k += (long)gridDim.x * blockDim.x) {
+        const int iz = (int)(k % nz);
+        const long c = k / nz;
+        const int ix = (int)(c % nxa), iy = (int)(c / nxa);
+        const long id = (s.npd + iz) + s.ldz * (long)(s.npd + ix * dcdp) + s.sxy * (long)(s.npd + iy * dcdp);
+        const float sP = s.P[id], gP = r.P[id];
+        const float Ssx = -sP * s.u[id], Ssy = -sP * s.v[id], Ssz = -s.Q[id] * s.w[id];
+        const float Sgx = gP * r.u[id], Sgy = gP * r.v[id], Sgz = r.Q[id] * r.w[id];
+        const float b1 = Ssx * Ssx + Ssy * Ssy + Ssz * Ssz, b2 = Sgx * Sgx + Sgy * Sgy + Sgz * Sgz;
+        const int ia = poynting_bin(Ssx * Sgx + Ssy * Sgy + Ssz * Sgz, b1, b2, thr, na);
+        if (ia < 0) continue;
+        const float w = cs[ia];
+        float *o = adcig + iz + (long)nz * (ia + (long)na * (ix + (long)nxa * iy));
+        *o = *o + sP * gP * w * w * w;
+    }
+}
+
+// adcigs_illum (:663-684): gathers /= illum at (iz, ix*dcdp, iy*dcdp) where non-zero.
+__global__ void k_adcig3d_illum(float *adcig, const float *ill, int nx, int nz, int na, int dcdp, int nxa, long n) {
+    for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < n; k += (long)gridDim.x * blockDim.x) {
+        const int iz = (int)(k % nz);
+        const long c = k / ((long)nz * na);
+        const int ix = (int)(c % nxa), iy = (int)(c / nxa);
+        const float w = ill[iz + (long)ix * dcdp * nz + (long)iy * dcdp * nx * nz];
+        if (w != 0.0f) adcig[k] = adcig[k] / w;
+    }
+}
+
 static int grid_blocks(long n) { return (int)std::min<long>((n + 255) / 256, 152L * 16); }
 
 }  // namespace geo
@@ -618,8 +661,9 @@ static int grid_blocks(long n) { return (int)std::min<long>((n + 255) / 256, 152
 // ring save in the forward pass, source re-propagation driven by the ring in
 // the backward pass.  GEO_RTM_SNAPSHOT and GEO_RTM_LEARNED keep snapshots of
 // the source P instead and propagate only the receiver field backwards.
-extern "C" int geo_rtm3d(const geo_rtm3d_desc *desc, const float *v, const float *e, const float *d, float *mig_out,
-                         float *lap_out, float *illum_out, int mem, void *stream) {
+extern "C" int geo_rtm3d_adcig(const geo_rtm3d_desc *desc, const float *v, const float *e, const float *d,
+                               float *mig_out, float *lap_out, float *illum_out, float *adcig_out, int mem,
+                               void *stream) {
     if (!desc || !v || !e || !d || !mig_out) return fail(GEO_ERR_ARG, "null argument");
     if (mem != GEO_MEM_HOST && mem != GEO_MEM_DEVICE) return fail(GEO_ERR_ARG, "bad mem kind");
     const geo_rtm3d_desc &R = *desc;
@@ -629,6 +673,13 @@ extern "C" int geo_rtm3d(const geo_rtm3d_desc *desc, const float *v, const float
         return fail(GEO_ERR_ARG, "unknown RTM method %d", method);
     if (method != GEO_RTM_BOUNDARY && R.snap_every < 1) return fail(GEO_ERR_ARG, "snap_every must be >= 1");
     if (method == GEO_RTM_LEARNED && !R.ae) return fail(GEO_ERR_ARG, "the learned method needs a codec");
+    // angle gathers: the program's na = 65, da = 1, dcdp = 1 by default
+    const int na = R.na > 0 ? R.na : 65, da = R.da > 0 ? R.da : 1, dcdp = R.dcdp > 0 ? R.dcdp : 1;
+    if (adcig_out) {
+        if (method != GEO_RTM_BOUNDARY) return fail(GEO_ERR_ARG, "angle gathers need the boundary method");
+        if (na > kMaxAngles) return fail(GEO_ERR_ARG, "na must be 1..%d", kMaxAngles);
+        if (dcdp > R.fd.nx || dcdp > R.fd.ny) return fail(GEO_ERR_ARG, "dcdp exceeds the model");
+    }
     geo_fd3d_desc D = R.fd;
     // every surface node records P+Q at z = npml (shot_record :319-334)
     D.rec_iz = D.npd; D.rx0 = 0; D.drx = 1; D.nrx = D.nx; D.ry0 = 0; D.dry = 1; D.nry = D.ny;
@@ -663,6 +714,18 @@ extern "C" int geo_rtm3d(const geo_rtm3d_desc *desc, const float *v, const float
     GEO_TRY(ill.alloc(nimg * 4));
     GEO_TRY(mig.zero(s));
     GEO_TRY(ill.zero(s));
+    const int nxa = D.nx / dcdp, nya = D.ny / dcdp;
+    const long nag = (long)D.nz * na * nxa * nya;
+    DevBuf ag, atab;
+    if (adcig_out) {
+        std::vector<float> tab(2 * kMaxAngles);
+        adcig_angle_tables(na, da, tab.data(), tab.data() + kMaxAngles);
+        GEO_TRY(ag.alloc(nag * 4));
+        GEO_TRY(ag.zero(s));
+        GEO_TRY(atab.alloc(tab.size() * 4));
+        GEO_CUDA(cudaMemcpyAsync(atab.p, tab.data(), tab.size() * 4, cudaMemcpyHostToDevice, s));
+        GEO_CUDA(cudaStreamSynchronize(s));
+    }
     float *bp = ring.as<float>(), *bq = bp + (size_t)D.nt * L;
     const int ntr = D.nx * D.ny;
     auto launch_ring = [&](int it, int save) -> int {
@@ -734,6 +797,11 @@ extern "C" int geo_rtm3d(const geo_rtm3d_desc *desc, const float *v, const float
             }
             if (method == GEO_RTM_BOUNDARY) gb.other_P = grid_of(p, 0).P;  // the source side's new level
             GEO_TRY(step3d(p, 1, gb, s));
+            if (adcig_out) {
+                k_adcig3d<<<grid_blocks((long)D.nz * nxa * nya), 256, 0, s>>>(
+                    grid_of(p, 0), grid_of(p, 1), ag.as<float>(), atab.as<float>(), na, dcdp, nxa, nya);
+                GEO_TRY(check_launch("adcig3d"));
+            }
             if (is_snap(it)) {
                 const Grid3D g = grid_of(p, 1);
                 const int j = it / k;
@@ -766,6 +834,12 @@ extern "C" int geo_rtm3d(const geo_rtm3d_desc *desc, const float *v, const float
     const cudaMemcpyKind kind = mem == GEO_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
     GEO_CUDA(cudaMemcpyAsync(mig_out, mig.p, nimg * 4, kind, s));
     if (illum_out) GEO_CUDA(cudaMemcpyAsync(illum_out, ill.p, nimg * 4, kind, s));
+    if (adcig_out) {
+        k_adcig3d_illum<<<grid_blocks(nag), 256, 0, s>>>(ag.as<float>(), ill.as<float>(), D.nx, D.nz, na, dcdp, nxa,
+                                                         nag);
+        GEO_TRY(check_launch("adcig3d_illum"));
+        GEO_CUDA(cudaMemcpyAsync(adcig_out, ag.p, nag * 4, kind, s));
+    }
     if (lap_out) {
         GEO_TRY(lap.alloc(nimg * 4));
         GEO_TRY(launch_laplace3d(D.nx, D.ny, D.nz, mig.as<float>(), lap.as<float>(), s));
@@ -773,4 +847,9 @@ extern "C" int geo_rtm3d(const geo_rtm3d_desc *desc, const float *v, const float
     }
     GEO_CUDA(cudaStreamSynchronize(s));
     return GEO_OK;
+}
+
+extern "C" int geo_rtm3d(const geo_rtm3d_desc *desc, const float *v, const float *e, const float *d, float *mig_out,
+                         float *lap_out, float *illum_out, int mem, void *stream) {
+    return geo_rtm3d_adcig(desc, v, e, d, mig_out, lap_out, illum_out, nullptr, mem, stream);
 }

@@ -86,6 +86,11 @@ void mute_window_3d_band(int nx, int ny, int nt, float dt, float favg, float dx,
                          int fsx, int fsy, int dsx, int dsy, int fsz, int is, float vp1, float eps1, int tt,
                          std::vector<int> &lo, std::vector<int> &hi);
 
+// Angle-gather tables of the GPU RTM programs' Poynting bin: thresholds
+// (largest cosine of bins >= k, -2 where none) and cosf(ia*pi/180), 128
+// entries each.
+void adcig_angle_tables(int nangle, int dangle, float *thr, float *cs);
+
 // Model sanity: finite, velocity > 0.
 int check_model(const float *v, const float *e, const float *d, size_t n);
 

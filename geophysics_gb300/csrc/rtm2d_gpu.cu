@@ -22,6 +22,7 @@
 // Fields are single buffers updated in place (the program's u0 = u1
 // pointer assignment).
 #include "geo_internal.h"
+#include "adcig.cuh"
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -141,17 +142,10 @@ __global__ void k_g_image(GRtm g, GField s, GField r, float *mig, float *adcig) 
         const float Ssx = -sP * s.u[id], Ssz = -s.Q[id] * s.w[id];
         const float Sgx = gP * r.u[id], Sgz = r.Q[id] * r.w[id];
         const float b1 = Ssx * Ssx + Ssz * Ssz, b2 = Sgx * Sgx + Sgz * Sgz;
-        const float a = (float)((double)(Ssx * Sgx + Ssz * Sgz) / ((double)sqrtf(b1 * b2) * (1 - 0.1)));
-        if (!(a >= -1.0f && a <= 1.0f)) continue;
-        int lo = 0, hi = g.nangle;          // bin = #thresholds at or above a
-        while (lo < hi) {
-            const int mid = (lo + hi + 1) >> 1;
-            if (a <= c_gthr[mid - 1]) lo = mid;
-            else hi = mid - 1;
-        }
-        if (lo >= g.nangle) continue;
-        const float c = c_gcos[lo];
-        float *ag = adcig + iz + (long)g.nz * lo + (long)g.nz * g.nangle * ix;
+        const int ia = poynting_bin(Ssx * Sgx + Ssz * Sgz, b1, b2, c_gthr, g.nangle);
+        if (ia < 0) continue;
+        const float c = c_gcos[ia];
+        float *ag = adcig + iz + (long)g.nz * ia + (long)g.nz * g.nangle * ix;
         *ag = *ag + sP * gP * c * c * c;
     }
 }
@@ -181,7 +175,7 @@ __global__ void k_g_stack_angles(const float *adcig, float *stk, int nx, int nz,
     }
 }
 
-// The program's bin of a cosine a: (int)((float)(0.5*acosf(a)*180.0/pi) / (dangle*1.0)).
+// The programs' bin of a cosine a: (int)((float)(0.5*acosf(a)*180.0/pi) / (dangle*1.0)).
 static int ref_gpu_bin(float a, int dangle) {
     const float deg = (float)(0.5 * std::acos(a) * 180.0 / kPiGui);
     return (int)(deg / (dangle * 1.0));
@@ -200,9 +194,12 @@ static float kfloat(uint32_t k) {
     return f;
 }
 
-static int gpu_adcig_tables(int nangle, int dangle, cudaStream_t s) {
-    std::vector<float> thr(128, -2.0f), cs(128, 0.0f);
+// thr[k-1] = largest float a in [-1,1] with bin(a) >= k (binary search over
+// the ordered float keys; bin is non-increasing in a), -2 where none is;
+// cs[ia] = cosf(ia*pi/180).  Both arrays hold kMaxAngles entries.
+void adcig_angle_tables(int nangle, int dangle, float *thr, float *cs) {
     const uint32_t lo = okey(-1.0f), hi = okey(1.0f);
+    for (int k = 0; k < kMaxAngles; k++) { thr[k] = -2.0f; cs[k] = 0.0f; }
     for (int k = 1; k <= nangle; k++) {
         if (ref_gpu_bin(-1.0f, dangle) < k) continue;
         uint32_t a = lo, b = hi;
@@ -214,8 +211,13 @@ static int gpu_adcig_tables(int nangle, int dangle, cudaStream_t s) {
         thr[k - 1] = kfloat(a);
     }
     for (int ia = 0; ia < nangle; ia++) cs[ia] = std::cos((float)(ia * kPiGui / 180.0));
-    GEO_CUDA(cudaMemcpyToSymbolAsync(c_gthr, thr.data(), 128 * 4, 0, cudaMemcpyHostToDevice, s));
-    GEO_CUDA(cudaMemcpyToSymbolAsync(c_gcos, cs.data(), 128 * 4, 0, cudaMemcpyHostToDevice, s));
+}
+
+static int gpu_adcig_tables(int nangle, int dangle, cudaStream_t s) {
+    std::vector<float> thr(kMaxAngles), cs(kMaxAngles);
+    adcig_angle_tables(nangle, dangle, thr.data(), cs.data());
+    GEO_CUDA(cudaMemcpyToSymbolAsync(c_gthr, thr.data(), kMaxAngles * 4, 0, cudaMemcpyHostToDevice, s));
+    GEO_CUDA(cudaMemcpyToSymbolAsync(c_gcos, cs.data(), kMaxAngles * 4, 0, cudaMemcpyHostToDevice, s));
     return GEO_OK;
 }
 

@@ -198,6 +198,8 @@ typedef struct geo_rtm3d_desc {
     int   method;            /* GEO_RTM_*                                    */
     int   snap_every;        /* snapshot interval (methods 1, 2)             */
     geo_ae *ae;              /* trained codec (method 2)                     */
+    int   na, da, dcdp;      /* angle gathers: bins, bin width in degrees,
+                                CDP decimation (0 = the program's 65, 1, 1)   */
 } geo_rtm3d_desc;
 
 /* v,e,d: nx*ny*nz.  mig: nx*ny*nz image divided by the illumination where
@@ -211,6 +213,17 @@ typedef struct geo_rtm3d_desc {
  * Illumination is the same as method 0 (every step, both fields). */
 int geo_rtm3d(const geo_rtm3d_desc *desc, const float *v, const float *e, const float *d,
               float *mig, float *mig_lap, float *illum, int mem, void *stream);
+
+/* geo_rtm3d plus the Poynting angle-domain common-image gathers of the 3D
+ * GPU RTM program (Poynting_Adcigs, 3D-vti-fd+rtm-cuda/
+ * Toa_gpu_3dvti_rtm_adcigs_1orderfunction.cu:618-661, after every backward
+ * step; adcigs_illum :663-684 after the shots).  Method 0 only: the gathers
+ * need the source particle velocities.  adcigs: nxa*nya*na*nz with
+ * nxa = nx/dcdp, nya = ny/dcdp, element iz + nz*(ia + na*(ixa + nxa*iya)),
+ * divided by the illumination at (iz, ixa*dcdp, iya*dcdp) where it is
+ * non-zero; NULL gives geo_rtm3d. */
+int geo_rtm3d_adcig(const geo_rtm3d_desc *desc, const float *v, const float *e, const float *d,
+                    float *mig, float *mig_lap, float *illum, float *adcigs, int mem, void *stream);
 
 /* 2D RTM with the MPI CPU program's semantics on per-shot aperture windows
  * (2D-vti-fd+rtm-mpi/Toa_rtm_vti_adcig_cdp.c:295-392 with

@@ -1175,9 +1175,18 @@ int orc_fd3d(const orc_fd3d_desc *d, const float *v, const float *e, const float
  * mig and illum (nx*ny*nz interior, iz + nz*(ix + nx*iy)) accumulate over
  * calls; the caller divides (migration_illum :539-553) and filters.  The
  * wavefields start from zero for every shot (the program zeroes them once
- * before its shot loop). */
+ * before its shot loop).
+ * adcigs (optional): after each backward step's image, the Poynting
+ * angle gathers (Poynting_Adcigs :618-661) over iy < ny/dcdp, ix < nx/dcdp,
+ * iz < nz at the padded point (iz, ix*dcdp, iy*dcdp) + npml:
+ *   Ss = -(sP*su, sP*sv, sQ*sw), Sg = (gP*gu, gP*gv, gQ*gw),
+ *   a = (Ss.Sg) / (sqrtf(|Ss|^2 |Sg|^2) * (1 - 0.1))  (double quotient, kept as float),
+ *   if -1 <= a <= 1: ia = (int)((float)(0.5*acosf(a)*180/pi) / (da*1.0)), and if ia < na
+ *   adcigs[iz + nz*(ia + na*(ix + nxa*iy))] += sP*gP*c*c*c, c = cosf(ia*pi/180)
+ * (velocities of the new time level: the program's u0 = u1 pointer
+ * assignment makes the update in place); the caller divides (adcigs_illum). */
 int orc_rtm3d_shot(const orc_fd3d_desc *d, int mute_tt, const float *v, const float *e, const float *dl,
-                   float *mig, float *illum, float *rec_out)
+                   float *mig, float *illum, float *rec_out, int na, int da, int dcdp, float *adcigs)
 {
     orc_g3d G; orc_f3d S, R;
     const int nx = d->nx, ny = d->ny, nz = d->nz, npd = d->npd, nt = d->nt;
@@ -1246,6 +1255,26 @@ int orc_rtm3d_shot(const orc_fd3d_desc *d, int mute_tt, const float *v, const fl
             REAL gp = R.P[gid], gq = R.Q[gid];
             illum[o] = (float)(illum[o] + (gp * gp + gq * gq));
             mig[o] = (float)(mig[o] + S.P[gid] * gp);
+        }
+        if (adcigs) {
+            const int nxa = nx / dcdp, nya = ny / dcdp;
+            for (iy = 0; iy < nya; iy++) for (ix = 0; ix < nxa; ix++) for (iz = 0; iz < nz; iz++) {
+                long gid = GID(npd + iz, npd + ix * dcdp, npd + iy * dcdp);
+                float sP = (float)S.P[gid], gP = (float)R.P[gid];
+                float Ssx = -sP * (float)S.u[gid], Ssy = -sP * (float)S.v[gid], Ssz = -(float)S.Q[gid] * (float)S.w[gid];
+                float Sgx = gP * (float)R.u[gid], Sgy = gP * (float)R.v[gid], Sgz = (float)R.Q[gid] * (float)R.w[gid];
+                float b1 = Ssx * Ssx + Ssy * Ssy + Ssz * Ssz, b2 = Sgx * Sgx + Sgy * Sgy + Sgz * Sgz;
+                float a = (Ssx * Sgx + Ssy * Sgy + Ssz * Sgz) / (sqrtf(b1 * b2) * (1 - 0.1));
+                if (a >= -1 && a <= 1) {
+                    int ia;
+                    a = 0.5 * acosf(a) * 180.0 / PI_GUI;
+                    ia = (int)(a / (da * 1.0));
+                    if (ia < na) {
+                        float c = cosf(ia * PI_GUI / 180.0);
+                        adcigs[iz + (long)nz * (ia + (long)na * (ix + (long)nxa * iy))] += sP * gP * c * c * c;
+                    }
+                }
+            }
         }
     }
 #undef RING
@@ -1327,6 +1356,19 @@ void orc_image_illum(long n, float *mig, const float *illum)
 {
     long k;
     for (k = 0; k < n; k++) if (illum[k] != 0) mig[k] = mig[k] / illum[k];
+}
+
+/* adcigs_illum (3D-vti-fd+rtm-cuda/Toa_gpu_3dvti_rtm_adcigs_1orderfunction.cu:663-684):
+ * gather element (iz, ia, ix, iy) /= illum at (iz, ix*dcdp, iy*dcdp) where that is non-zero. */
+void orc_adcig3d_illum(int nx, int ny, int nz, int na, int dcdp, float *adcigs, const float *illum)
+{
+    const int nxa = nx / dcdp, nya = ny / dcdp;
+    long iy, ix, ia, iz;
+    for (iy = 0; iy < nya; iy++) for (ix = 0; ix < nxa; ix++) for (ia = 0; ia < na; ia++) for (iz = 0; iz < nz; iz++) {
+        float w = illum[iz + (long)ix * dcdp * nz + (long)iy * dcdp * nx * nz];
+        long o = iz + (long)nz * (ia + (long)na * (ix + (long)nxa * iy));
+        if (w != 0) adcigs[o] /= w;
+    }
 }
 
 /* Direct-wave mute of a 3D record (mute_directwave3d, GPU_vti3dfd_kernels.cu:342-369):

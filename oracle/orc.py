@@ -64,7 +64,9 @@ def lib(prec=32):
             [C.c_float, C.c_int, C.POINTER(C.c_float)]
         L.orc_mute3d.argtypes = [C.c_int] * 3 + [C.c_float] * 5 + [C.c_int] * 6 + [C.c_float] * 2 + \
             [C.c_int, C.POINTER(C.c_float)]
-        L.orc_rtm3d_shot.argtypes = [C.POINTER(FD3DDesc), C.c_int] + [C.POINTER(C.c_float)] * 6
+        L.orc_rtm3d_shot.argtypes = [C.POINTER(FD3DDesc), C.c_int] + [C.POINTER(C.c_float)] * 6 + \
+            [C.c_int] * 3 + [C.POINTER(C.c_float)]
+        L.orc_adcig3d_illum.argtypes = [C.c_int] * 5 + [C.POINTER(C.c_float)] * 2
         L.orc_rtm3d_snap_shot.argtypes = [C.POINTER(FD3DDesc), C.c_int, C.c_int] + [C.POINTER(C.c_float)] * 5
         L.orc_rtm2d_gpu.argtypes = [C.c_int] * 4 + [C.c_float] * 5 + [C.c_int] * 8 + [C.POINTER(C.c_float)] * 8
         L.orc_image_illum.argtypes = [C.c_long, C.POINTER(C.c_float), C.POINTER(C.c_float)]
@@ -129,16 +131,25 @@ def fd3d(v, e, d, *, npd, nt, dx, dy, dz, dt, favg, pfac, fsx, fsy, fsz, dsx=0, 
 
 
 def rtm3d(v, e, d, *, npd, nt, dx, dy, dz, dt, favg, pfac, fsx, fsy, fsz, dsx=0, dsy=0, dsz=0,
-          ns=1, sv=0, wtype=1, mode=0, mute_tt=70, snap_every=0, prec=32):
+          ns=1, sv=0, wtype=1, mode=0, mute_tt=70, snap_every=0, prec=32, adcig=None):
     """3D boundary-saving RTM over shots 0..ns-1 (3D GPU RTM program
     semantics; with snap_every > 0 the stored-snapshot method instead);
     v,e,d shaped (ny, nx, nz).  Returns (mig divided by the illumination,
-    illum, last shot's muted record (ny, nx, nt); zeros for snap_every > 0)."""
+    illum, last shot's muted record (ny, nx, nt); zeros for snap_every > 0)
+    [+ the Poynting angle gathers (ny/dcdp, nx/dcdp, na, nz) divided by the
+    illumination, when adcig = (na, da, dcdp)]."""
     v, e, d = c32(v), c32(e), c32(d)
     ny, nx, nz = v.shape
     mig = np.zeros((ny, nx, nz), _f)
     ill = np.zeros((ny, nx, nz), _f)
     rec = np.zeros((ny, nx, nt), _f)
+    na = da = dcdp = 0
+    ag = None
+    if adcig is not None:
+        if snap_every:
+            raise ValueError("angle gathers need the boundary method")
+        na, da, dcdp = adcig
+        ag = np.zeros((ny // dcdp, nx // dcdp, na, nz), _f)
     for is_ in range(ns):
         desc = FD3DDesc(nx=nx, ny=ny, nz=nz, npd=npd, nt=nt, sv=sv, wtype=wtype, mode=mode,
                         dx=dx, dy=dy, dz=dz, dt=dt, favg=favg, pfac=pfac, fsx=fsx, fsy=fsy, fsz=fsz,
@@ -148,9 +159,13 @@ def rtm3d(v, e, d, *, npd, nt, dx, dy, dz, dt, favg, pfac, fsx, fsy, fsz, dsx=0,
             lib(prec).orc_rtm3d_snap_shot(C.byref(desc), mute_tt, snap_every, _fp(v), _fp(e), _fp(d), _fp(mig),
                                           _fp(ill))
         else:
-            lib(prec).orc_rtm3d_shot(C.byref(desc), mute_tt, _fp(v), _fp(e), _fp(d), _fp(mig), _fp(ill), _fp(rec))
+            lib(prec).orc_rtm3d_shot(C.byref(desc), mute_tt, _fp(v), _fp(e), _fp(d), _fp(mig), _fp(ill), _fp(rec),
+                                     na, da, dcdp, _fp(ag))
     lib(prec).orc_image_illum(mig.size, _fp(mig), _fp(ill))
-    return mig, ill, rec
+    if ag is None:
+        return mig, ill, rec
+    lib(prec).orc_adcig3d_illum(nx, ny, nz, na, dcdp, _fp(ag), _fp(ill))
+    return mig, ill, rec, ag
 
 
 def rtm2d_mpi_shot(v, e, d, *, npd, nt, dx, dz, dt_ms, favg, pfac, fs_sxd, ds_sxd, zs_sxd, is_, nxs,

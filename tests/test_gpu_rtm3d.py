@@ -38,3 +38,26 @@ def test_rtm3d_fast_close_to_exact(geo):
     a = geo.rtm3d(v, e, d, mode="exact", laplace=False, **KW)
     b = geo.rtm3d(v, e, d, mode="fast", laplace=False, **KW)
     assert rel_l2(b, a) < 1e-4
+
+
+@pytest.mark.parametrize("mode,adcig", [(0, (65, 1, 1)), (1, (65, 1, 1)), (1, (40, 2, 2)), (0, (7, 3, 3))])
+def test_rtm3d_adcig_bit_exact(geo, orc, mode, adcig):
+    """Poynting angle gathers (Poynting_Adcigs + adcigs_illum) bit-exact,
+    together with the image and the illumination of the same run."""
+    v, e, d = random_model_3d(20, 17, 23, seed=14)
+    mig_o, ill_o, _, ag_o = orc.rtm3d(v, e, d, mode=mode, adcig=adcig, **KW)
+    mig, ill, ag = geo.rtm3d(v, e, d, mode=mode, laplace=False, illum=True, adcig=adcig, **KW)
+    na, _, dcdp = adcig
+    assert ag.shape == (17 // dcdp, 20 // dcdp, na, 23)
+    filled = np.count_nonzero(np.abs(ag_o).sum(axis=(0, 1, 3)))
+    assert filled >= min(na, 5), filled          # several angle bins receive energy
+    assert np.array_equal(ill, ill_o)
+    assert np.array_equal(mig, mig_o)
+    assert np.array_equal(ag, ag_o), rel_l2(ag, ag_o)
+
+
+def test_rtm3d_adcig_needs_boundary_method(geo):
+    from geophysics_gb300 import GeoError
+    v, e, d = random_model_3d(16, 16, 16, seed=15)
+    with pytest.raises(GeoError):
+        geo.rtm3d(v, e, d, method="snapshot", snap_every=2, adcig=(65, 1, 1), **dict(KW, ns=1, nt=40))
