@@ -49,7 +49,7 @@ class RTM3DDesc(C.Structure):
 class RTM2DGpuDesc(C.Structure):
     _fields_ = [(n, C.c_int) for n in ("nx", "nz", "npml", "nt")] + \
                [(n, C.c_float) for n in ("dx", "dz", "dt", "favg", "pfac")] + \
-               [(n, C.c_int) for n in ("wtype", "ns", "fs", "ds", "zs", "mute_tt", "nangle", "dangle")]
+               [(n, C.c_int) for n in ("wtype", "ns", "fs", "ds", "zs", "mute_tt", "nangle", "dangle", "dcdp")]
 
 
 class RTM2DDesc(C.Structure):
@@ -96,6 +96,7 @@ def lib():
         "geo_su_write": (_i, [C.c_char_p, _i, _i, _f, _i, _vp, _vp]),
         "geo_su_replace_data": (_i, [C.c_char_p, C.c_char_p, C.c_char_p, _i, _i]),
         "geo_rtm2d_gpu": (_i, [C.POINTER(RTM2DGpuDesc)] + [_vp] * 9 + [_i, _vp]),
+        "geo_rtm2d_tti": (_i, [C.POINTER(RTM2DGpuDesc)] + [_vp] * 9 + [_i, _vp]),
         "geo_tti2d_shot": (_i, [C.POINTER(FD2DDesc), _vp, _vp, _vp, _vp, _vp, _vp, _i, _i, _vp]),
         "geo_ae_create": (_i, [C.POINTER(_vp), C.c_ulonglong]),
         "geo_ae_destroy": (_i, [_vp]),

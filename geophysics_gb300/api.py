@@ -248,6 +248,26 @@ def rtm2d_gpu(v, e, d, *, npml, nt, dx, dz, dt, favg, ns=1, fs=1, ds=0, zs=1, pf
     return out
 
 
+def rtm2d_tti(v, e, d, theta, *, npml, nt, dx, dz, dt, favg, ns=1, fs=1, ds=0, zs=1, pfac=10.0, wtype=1,
+              mute_tt=30, nangle=65, dangle=1, dcdp=1, obs=None):
+    """2D TTI RTM with the 2D TTI GPU RTM program's semantics; theta is the
+    tilt in degrees.  Returns a dict: "mig_lap" (nx,nz), "illum", "adcigs"
+    (nx//dcdp, nangle, nz), "shots" (ns,nx,nt)."""
+    b = _Bufs(v, e, d, theta, obs)
+    nx, nz = v.shape
+    desc = RTM2DGpuDesc(nx=nx, nz=nz, npml=npml, nt=nt, dx=dx, dz=dz, dt=dt, favg=favg, pfac=pfac, wtype=wtype,
+                        ns=ns, fs=fs, ds=ds, zs=zs, mute_tt=mute_tt, nangle=nangle, dangle=dangle, dcdp=dcdp)
+    pv, pe, pd, pt, po = b.inp(v), b.inp(e), b.inp(d), b.inp(theta), b.inp(obs)
+    out = {}
+    ptrs = []
+    for name, shape in (("mig_lap", (nx, nz)), ("illum", (nx, nz)), ("adcigs", (nx // dcdp, nangle, nz)),
+                        ("shots", (ns, nx, nt))):
+        out[name], p = b.out(shape, v)
+        ptrs.append(p)
+    check(lib().geo_rtm2d_tti(C.byref(desc), pv, pe, pd, pt, po, *ptrs, b.mem, b.stream()), "geo_rtm2d_tti")
+    return out
+
+
 def morton_order():
     """perm[m] = natural index (z + 16*x + 256*y) of Morton index m of a
     16^3 block (bit 3l = z bit l, 3l+1 = x bit l, 3l+2 = y bit l)."""

@@ -47,7 +47,9 @@ struct DevBuf {
 
 // ------------------------------------------------------------ host setup
 // Reference program whose arithmetic a run follows.
-enum Variant { V_CPU = GEO_VARIANT_CPU, V_GPU = GEO_VARIANT_GPU, V_MPI = GEO_VARIANT_MPI };
+// V_TTIRTM (internal): the 2D TTI GPU RTM program's sponge, which differs
+// from the other GPU programs' (sponge_d0, sponge_profiles).
+enum Variant { V_CPU = GEO_VARIANT_CPU, V_GPU = GEO_VARIANT_GPU, V_MPI = GEO_VARIANT_MPI, V_TTIRTM = 100 };
 
 // pi as each reference program spells it.
 constexpr double kPiGui = 3.141592653;      // CPU_vti2dfd_kernels.c:27, GPU_vti*_kernels.cu:31

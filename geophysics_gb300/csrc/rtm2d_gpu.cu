@@ -21,8 +21,23 @@
 // nnx*nnz threads on nx*nz arrays (an overrun); here they cover nx*nz.
 // Fields are single buffers updated in place (the program's u0 = u1
 // pointer assignment).
+//
+// The 2D TTI GPU RTM program (2D-tti-fd+rtm-cuda/
+// Toa_gpu_2dtti_rtm_adcigs_iorderfunciton.cu, main :500-800) has the same
+// shot structure and runs through the same driver with its own choices:
+// the TTI update_vel / update_stress (:126-228) over the tilt field, SV taper
+// R=15, r=4, a mute with a sample bound whose direct-wave velocity is
+// vp[1]*(1+(sqrtf(1+2 eps[1])-1)*cos(theta[1])) (:336-358, tt = 30 in the
+// program), its own sponge (d0 with 3.0 in place of 10.0, whole-cell
+// distances for both profile pairs; :230-233, :289-320), gathers at every
+// dcdp-th CDP (Poynting_Adcigs :454-486,
+// adcigs_illum :488-498), no angle stack and no readFile checks.  Where the
+// program's adcigs_illum bound ((nx*nz)/dcdp*na) runs past its gathers
+// array (nx not a multiple of dcdp) it divides floats beyond the array;
+// here only the nx/dcdp gathers are divided.
 #include "geo_internal.h"
 #include "adcig.cuh"
+#include "tti2d.cuh"
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -34,15 +49,31 @@ __constant__ float c_gthr[128];   // angle-bin thresholds (largest cosine of bin
 __constant__ float c_gcos[128];   // cosf(ia*pi/180) per bin
 
 struct GRtm {
-    int nnx, nnz, nx, nz, npml, nangle;
+    int nnx, nnz, nx, nz, npml, nangle, dcdp;
     float dtx, dtz;
     const float *cx1, *cx2, *cz1, *cz2, *ax1, *ax2, *az1, *az2;
     const float *vp;
+    const float *ct, *st;   // cos, sin of the tilt (TTI program)
 };
 
 struct GField {
     float *u, *w, *P, *Q, *px, *pz, *qx, *qz;
 };
+
+static TtiGrid tti_grid(const GRtm &g) {
+    TtiGrid t;
+    t.nnx = g.nnx; t.nnz = g.nnz; t.dtx = g.dtx; t.dtz = g.dtz;
+    t.cx1 = g.cx1; t.cx2 = g.cx2; t.cz1 = g.cz1; t.cz2 = g.cz2;
+    t.ax1 = g.ax1; t.ax2 = g.ax2; t.az1 = g.az1; t.az2 = g.az2;
+    t.vp = g.vp; t.ct = g.ct; t.st = g.st;
+    return t;
+}
+
+static TtiField tti_field(const GField &f) {
+    TtiField t;
+    t.u = f.u; t.w = f.w; t.px = f.px; t.pz = f.pz; t.qx = f.qx; t.qz = f.qz; t.P = f.P; t.Q = f.Q;
+    return t;
+}
 
 __global__ void k_g_src(GField f, long id, float amp) {
     f.P[id] += amp;
@@ -84,6 +115,25 @@ __global__ void k_g_stress(GRtm g, GField f, const float *e2, const float *d2) {
         f.px[id] = px; f.pz[id] = pz; f.qx[id] = qx; f.qz[id] = qz;
         f.P[id] = px + pz;
         f.Q[id] = qx + qz;
+    }
+}
+
+// The TTI program's update_vel / update_stress (Toa_gpu_2dtti_rtm_adcigs_iorderfunciton.cu:126-228).
+__global__ void k_g_vel_tti(TtiGrid g, TtiField f) {
+    const long n = (long)g.nnx * g.nnz;
+    for (long id = blockIdx.x * (long)blockDim.x + threadIdx.x; id < n; id += (long)gridDim.x * blockDim.x) {
+        const int ix = (int)(id / g.nnz), iz = (int)(id % g.nnz);
+        if (ix < 4 || ix >= g.nnx - 4 || iz < 4 || iz >= g.nnz - 4) continue;
+        tti_vel_at(g, f, c_grtm, id, ix, iz);
+    }
+}
+
+__global__ void k_g_stress_tti(TtiGrid g, TtiField f, const float *e2, const float *d2) {
+    const long n = (long)g.nnx * g.nnz;
+    for (long id = blockIdx.x * (long)blockDim.x + threadIdx.x; id < n; id += (long)gridDim.x * blockDim.x) {
+        const int ix = (int)(id / g.nnz), iz = (int)(id % g.nnz);
+        if (ix < 4 || ix >= g.nnx - 4 || iz < 4 || iz >= g.nnz - 4) continue;
+        tti_stress_at(g, f, e2, d2, c_grtm, id, ix, iz);
     }
 }
 
@@ -138,14 +188,14 @@ __global__ void k_g_image(GRtm g, GField s, GField r, float *mig, float *adcig) 
         const long id = iz + g.npml + (long)g.nnz * (ix + g.npml);
         const float sP = s.P[id], gP = r.P[id];
         mig[o] = mig[o] + sP * gP;
-        if (!adcig) continue;
+        if (!adcig || ix % g.dcdp != 0) continue;
         const float Ssx = -sP * s.u[id], Ssz = -s.Q[id] * s.w[id];
         const float Sgx = gP * r.u[id], Sgz = r.Q[id] * r.w[id];
         const float b1 = Ssx * Ssx + Ssz * Ssz, b2 = Sgx * Sgx + Sgz * Sgz;
         const int ia = poynting_bin(Ssx * Sgx + Ssz * Sgz, b1, b2, c_gthr, g.nangle);
         if (ia < 0) continue;
         const float c = c_gcos[ia];
-        float *ag = adcig + iz + (long)g.nz * ia + (long)g.nz * g.nangle * ix;
+        float *ag = adcig + iz + (long)g.nz * ia + (long)g.nz * g.nangle * (ix / g.dcdp);
         *ag = *ag + sP * gP * c * c * c;
     }
 }
@@ -155,11 +205,11 @@ __global__ void k_g_mask(float *rec, const uint8_t *keep, long n) {
         if (!keep[k]) rec[k] = 0.0f;
 }
 
-// gathers [ix][ia][iz] /= ill[ix][iz]
-__global__ void k_g_adcig_norm(float *adcig, const float *ill, int nx, int nz, int nangle) {
-    const long n = (long)nx * nz * nangle;
+// gathers [ixa][ia][iz] /= ill[ixa*dcdp][iz]
+__global__ void k_g_adcig_norm(float *adcig, const float *ill, int nxa, int nz, int nangle, int dcdp) {
+    const long n = (long)nxa * nz * nangle;
     for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < n; k += (long)gridDim.x * blockDim.x) {
-        const int ix = (int)(k / ((long)nz * nangle)), iz = (int)(k % nz);
+        const int ix = (int)(k / ((long)nz * nangle)) * dcdp, iz = (int)(k % nz);
         adcig[k] = adcig[k] / ill[iz + (long)nz * ix];
     }
 }
@@ -242,30 +292,42 @@ static int grid_of_n(long n) { return (int)std::min<long>((n + 255) / 256, 152L 
 
 }  // namespace geo
 
-using namespace geo;
+namespace geo {
 
-extern "C" int geo_rtm2d_gpu(const geo_rtm2d_gpu_desc *desc, const float *v, const float *e, const float *d,
-                             const float *obs, float *mig_lap, float *illum, float *adcigs, float *stk_lap,
-                             float *shots, int mem, void *stream) {
-    if (!desc || !v || !e || !d || !mig_lap) return fail(GEO_ERR_ARG, "null argument");
-    const geo_rtm2d_gpu_desc &D = *desc;
+// What differs between the two GPU RTM programs that share this driver.
+struct GpuRtmProgram {
+    bool tti;            // TTI stencil over a tilt field (theta, degrees)
+    int taper_R, taper_r;  // SV taper radii of the forward stress update
+    bool mute_overrun;   // the mute launch has no sample bound (VTI program)
+    bool checks;         // readFile's dispersion / stability checks (VTI program)
+};
+
+static int gpu_rtm_run(const GpuRtmProgram &prog, const geo_rtm2d_gpu_desc &D, const float *v, const float *e,
+                       const float *d, const float *theta, const float *obs, float *mig_lap, float *illum,
+                       float *adcigs, float *stk_lap, float *shots, int mem, void *stream) {
     if (D.nx < 2 || D.nz < 2 || D.npml < 5 || D.nt < 1 || D.ns < 1) return fail(GEO_ERR_ARG, "bad sizes");
     if (!(D.dt > 0) || !(D.dx > 0) || !(D.dz > 0) || !(D.favg > 0)) return fail(GEO_ERR_ARG, "bad spacing");
     if (D.nangle < 1 || D.nangle > 128 || D.dangle < 1) return fail(GEO_ERR_ARG, "nangle must be 1..128, dangle >= 1");
+    const int dcdp = D.dcdp > 0 ? D.dcdp : 1;
+    if (dcdp > D.nx) return fail(GEO_ERR_ARG, "dcdp exceeds nx");
+    if (dcdp != 1 && !prog.tti) return fail(GEO_ERR_ARG, "the VTI program forms gathers at every CDP (dcdp 0 or 1)");
     if (mem != GEO_MEM_HOST && mem != GEO_MEM_DEVICE) return fail(GEO_ERR_ARG, "bad mem kind");
     const int nx = D.nx, nz = D.nz, npml = D.npml, nt = D.nt, nnx = nx + 2 * npml, nnz = nz + 2 * npml;
     const size_t n0 = (size_t)nx * nz, n = (size_t)nnx * nnz;
     cudaStream_t s = (cudaStream_t)stream;
-    std::vector<float> hv(n0), he(n0), hd(n0);
-    const float *src[3] = {v, e, d};
-    float *dst[3] = {hv.data(), he.data(), hd.data()};
-    for (int k = 0; k < 3; k++) {
+    std::vector<float> hv(n0), he(n0), hd(n0), ht(prog.tti ? n0 : 0);
+    const float *src[4] = {v, e, d, theta};
+    float *dst[4] = {hv.data(), he.data(), hd.data(), ht.data()};
+    for (int k = 0; k < (prog.tti ? 4 : 3); k++) {
         if (mem == GEO_MEM_DEVICE) GEO_CUDA(cudaMemcpyAsync(dst[k], src[k], n0 * 4, cudaMemcpyDeviceToHost, s));
         else memcpy(dst[k], src[k], n0 * 4);
     }
     GEO_CUDA(cudaStreamSynchronize(s));
     GEO_TRY(check_model(hv.data(), he.data(), hd.data(), n0));
-    GEO_TRY(gpu_rtm_checks(D, hv));
+    if (prog.tti)
+        for (size_t k = 0; k < n0; k++)
+            if (!std::isfinite(ht[k])) return fail(GEO_ERR_MODEL, "theta[%zu] not finite", k);
+    if (prog.checks) GEO_TRY(gpu_rtm_checks(D, hv));
     for (int is = 1; is <= D.ns; is++) {
         const int ixs = D.fs + (is - 1) * D.ds + npml - 1, izs = D.zs + npml - 1;
         if (ixs < 4 || ixs >= nnx - 4 || izs < 4 || izs >= nnz - 4) return fail(GEO_ERR_ARG, "shot %d outside the grid", is);
@@ -274,12 +336,14 @@ extern "C" int geo_rtm2d_gpu(const geo_rtm2d_gpu_desc *desc, const float *v, con
     pad_model_2d(nx, nz, npml, hv.data(), pv.data());
     pad_model_2d(nx, nz, npml, he.data(), pe.data());
     pad_model_2d(nx, nz, npml, hd.data(), pd.data());
-    const float d0 = sponge_d0(V_GPU, 2, 0.0f, pv[n / 2], npml, D.dx, D.dx, D.dz);   // get_d0 :110-118
+    // get_d0 and initial_coffe of the program (VTI :110-118; TTI :230-233, :289-320)
+    const Variant sp = prog.tti ? V_TTIRTM : V_GPU;
+    const float d0 = sponge_d0(sp, 2, 0.0f, pv[n / 2], npml, D.dx, D.dx, D.dz);
     std::vector<float> prof(4 * (size_t)(nnx + nnz));
     float *q = prof.data();
-    sponge_profiles(V_GPU, nx, npml, D.dt, d0, q, q + nnx, q + 2 * nnx, q + 3 * nnx);
+    sponge_profiles(sp, nx, npml, D.dt, d0, q, q + nnx, q + 2 * nnx, q + 3 * nnx);
     q += 4 * nnx;
-    sponge_profiles(V_GPU, nz, npml, D.dt, d0, q, q + nnz, q + 2 * nnz, q + 3 * nnz);
+    sponge_profiles(sp, nz, npml, D.dt, d0, q, q + nnz, q + 2 * nnz, q + 3 * nnz);
     std::vector<float> amp;
     std::vector<uint8_t> on;
     source_amplitudes(V_GPU, nt, D.dt, D.favg, D.pfac, D.wtype, amp, on);
@@ -289,11 +353,32 @@ extern "C" int geo_rtm2d_gpu(const geo_rtm2d_gpu_desc *desc, const float *v, con
         e2[k] = 1 + 2 * pe[k];
         d2[k] = sqrtf(1 + 2 * pd[k]);
     }
-    const float mu_v = pv[1] * sqrtf(1 + 2 * pe[1]);
+    // tilt in radians as read_file converts it (theta *= pi/180), cos and sin tables
+    std::vector<float> ct, st;
+    float mu_v = pv[1] * sqrtf(1 + 2 * pe[1]);   // direct-wave velocity of the VTI program's mute
+    if (prog.tti) {
+        std::vector<float> pt(n);
+        pad_model_2d(nx, nz, npml, ht.data(), pt.data());
+        ct.resize(n);
+        st.resize(n);
+        for (size_t k = 0; k < n; k++) {
+            const float th = (float)((double)pt[k] * (kPiGui / 180.0));
+            ct[k] = std::cos(th);
+            st[k] = std::sin(th);
+        }
+        // mute_directwave of the TTI program: vp[1]*(1+(sqrtf(1+2 eps[1])-1)*cos(theta[1]))
+        mu_v = pv[1] * (1 + (sqrtf(1 + 2 * pe[1]) - 1) * ct[1]);
+    }
     const int L = 2 * nx + 2 * nz;
 
-    DevBuf dvp, dprof, de2, dd2, dte2, dtd2, fs_, fr_, ring, rec, mig, ill, ag, lap, stk, mkeep, trs;
+    DevBuf dvp, dprof, de2, dd2, dte2, dtd2, fs_, fr_, ring, rec, mig, ill, ag, lap, stk, mkeep, trs, dct, dst_;
     GEO_TRY(dvp.alloc(n * 4));
+    if (prog.tti) {
+        GEO_TRY(dct.alloc(n * 4));
+        GEO_TRY(dst_.alloc(n * 4));
+        GEO_CUDA(cudaMemcpyAsync(dct.p, ct.data(), n * 4, cudaMemcpyHostToDevice, s));
+        GEO_CUDA(cudaMemcpyAsync(dst_.p, st.data(), n * 4, cudaMemcpyHostToDevice, s));
+    }
     GEO_TRY(dprof.alloc(prof.size() * 4));
     GEO_TRY(de2.alloc(n * 4));
     GEO_TRY(dd2.alloc(n * 4));
@@ -306,8 +391,10 @@ extern "C" int geo_rtm2d_gpu(const geo_rtm2d_gpu_desc *desc, const float *v, con
     GEO_TRY(mig.alloc(n0 * 4));
     GEO_TRY(ill.alloc(n0 * 4));
     GEO_TRY(mkeep.alloc((size_t)nt * nx));
+    const int nxa = nx / dcdp;
+    const size_t nag = (size_t)D.nangle * nz * nxa;
     if (adcigs || stk_lap) {
-        GEO_TRY(ag.alloc((size_t)D.nangle * n0 * 4));
+        GEO_TRY(ag.alloc(nag * 4));
         GEO_TRY(ag.zero(s));
         GEO_TRY(gpu_adcig_tables(D.nangle, D.dangle, s));
     }
@@ -318,7 +405,9 @@ extern "C" int geo_rtm2d_gpu(const geo_rtm2d_gpu_desc *desc, const float *v, con
     GEO_TRY(mig.zero(s));
     GEO_TRY(ill.zero(s));
     GRtm g{};
-    g.nnx = nnx; g.nnz = nnz; g.nx = nx; g.nz = nz; g.npml = npml; g.nangle = D.nangle;
+    g.nnx = nnx; g.nnz = nnz; g.nx = nx; g.nz = nz; g.npml = npml; g.nangle = D.nangle; g.dcdp = dcdp;
+    g.ct = dct.as<float>();
+    g.st = dst_.as<float>();
     g.dtx = D.dt / D.dx;
     g.dtz = D.dt / D.dz;
     const float *pp = dprof.as<float>();
@@ -339,19 +428,33 @@ extern "C" int geo_rtm2d_gpu(const geo_rtm2d_gpu_desc *desc, const float *v, con
     const cudaMemcpyKind kout = mem == GEO_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
     const cudaMemcpyKind kin = mem == GEO_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
     if (shots || obs) GEO_TRY(trs.alloc((size_t)nt * nx * 4));
+    const TtiGrid tg = tti_grid(g);
+    auto step = [&](const GField &f, const float *e2p, const float *d2p) -> int {
+        if (prog.tti) {
+            k_g_vel_tti<<<gb, 256, 0, s>>>(tg, tti_field(f));
+            GEO_TRY(check_launch("grtm_vel_tti"));
+            k_g_stress_tti<<<gb, 256, 0, s>>>(tg, tti_field(f), e2p, d2p);
+            return check_launch("grtm_stress_tti");
+        }
+        k_g_vel<<<gb, 256, 0, s>>>(g, f);
+        GEO_TRY(check_launch("grtm_vel"));
+        k_g_stress<<<gb, 256, 0, s>>>(g, f, e2p, d2p);
+        return check_launch("grtm_stress");
+    };
     for (int is = 1; is <= D.ns; is++) {
-        // SV taper box of this shot (R=18, r=7; centre fs+(is-1)ds+npml, zs+npml)
+        // SV taper box of this shot (centre fs+(is-1)ds+npml, zs+npml)
         std::vector<float> te2(e2), td2(d2);
         {
-            const int cx = D.fs + (is - 1) * D.ds + npml, cz = D.zs + npml, R2 = 18 * 18, r2 = 7 * 7;
-            for (int ix = std::max(0, cx - 18); ix <= std::min(nnx - 1, cx + 18); ix++)
-                for (int iz = std::max(0, cz - 18); iz <= std::min(nnz - 1, cz + 18); iz++) {
+            const int TR = prog.taper_R, tr = prog.taper_r;
+            const int cx = D.fs + (is - 1) * D.ds + npml, cz = D.zs + npml, R2 = TR * TR, r2 = tr * tr;
+            for (int ix = std::max(0, cx - TR); ix <= std::min(nnx - 1, cx + TR); ix++)
+                for (int iz = std::max(0, cz - TR); iz <= std::min(nnz - 1, cz + TR); iz++) {
                     const int rx = ix - cx, rz = iz - cz, q2 = rx * rx + rz * rz;
                     if (q2 > R2) continue;
                     const size_t id = (size_t)ix * nnz + iz;
                     float ee = 0.0f, dd = 0.0f;
                     if (q2 > r2) {
-                        const double gq = 0.5 * (1 - std::cos(kPiGui * ((sqrtf((float)q2) - 7) * 4.0 / (18 * 3.0 - 1))));
+                        const double gq = 0.5 * (1 - std::cos(kPiGui * ((sqrtf((float)q2) - tr) * 4.0 / (TR * 3.0 - 1))));
                         ee = (float)(gq * pe[id]);
                         dd = (float)(gq * pd[id]);
                     }
@@ -371,10 +474,7 @@ extern "C" int geo_rtm2d_gpu(const geo_rtm2d_gpu_desc *desc, const float *v, con
                 k_g_src<<<1, 1, 0, s>>>(S, src, amp[it]);
                 GEO_TRY(check_launch("grtm_src"));
             }
-            k_g_vel<<<gb, 256, 0, s>>>(g, S);
-            GEO_TRY(check_launch("grtm_vel"));
-            k_g_stress<<<gb, 256, 0, s>>>(g, S, dte2.as<float>(), dtd2.as<float>());
-            GEO_TRY(check_launch("grtm_stress"));
+            GEO_TRY(step(S, dte2.as<float>(), dtd2.as<float>()));
             k_g_surface<<<(nx + 255) / 256, 256, 0, s>>>(g, S, rec.as<float>(), it, 0);
             GEO_TRY(check_launch("grtm_record"));
             k_g_ring<<<(L + 255) / 256, 256, 0, s>>>(g, S, bp, bq, it, 1);
@@ -383,12 +483,13 @@ extern "C" int geo_rtm2d_gpu(const geo_rtm2d_gpu_desc *desc, const float *v, con
             GEO_TRY(check_launch("grtm_illum"));
         }
         // direct-wave mute (GPU form, tt), exactly as the program's kernel
-        // writes it: thread it < nt rounded up to 512 zeroes flat sample
-        // ix*nt + it of the trace-major record for every trace ix whose
-        // window holds it -- past nt that lands on later traces
+        // writes it.  VTI program: thread it < nt rounded up to 512 zeroes
+        // flat sample ix*nt + it of the trace-major record for every trace
+        // ix whose window holds it -- past nt that lands on later traces.
+        // TTI program: one thread per sample, bounded.
         {
             std::vector<uint8_t> keep((size_t)nt * nx, 1);   // time-major
-            const int nt512 = (nt + 511) / 512 * 512;
+            const int nt512 = prog.mute_overrun ? (nt + 511) / 512 * 512 : nt;
             for (int ix = 0; ix < nx; ix++) {
                 const float mu_x = D.dx * std::abs(ix - D.fs - (is - 1) * D.ds), mu_z = D.dz * D.zs;
                 const float mu_t0 = sqrtf((float)(std::pow(mu_x, 2) + std::pow(mu_z, 2))) / mu_v;
@@ -418,16 +519,10 @@ extern "C" int geo_rtm2d_gpu(const geo_rtm2d_gpu_desc *desc, const float *v, con
         for (int it = nt - 1; it >= 0; it--) {
             k_g_ring<<<(L + 255) / 256, 256, 0, s>>>(g, S, bp, bq, it, 0);
             GEO_TRY(check_launch("grtm_ring"));
-            k_g_vel<<<gb, 256, 0, s>>>(g, S);
-            GEO_TRY(check_launch("grtm_vel"));
-            k_g_stress<<<gb, 256, 0, s>>>(g, S, de2.as<float>(), dd2.as<float>());
-            GEO_TRY(check_launch("grtm_stress"));
+            GEO_TRY(step(S, de2.as<float>(), dd2.as<float>()));
             k_g_surface<<<(nx + 255) / 256, 256, 0, s>>>(g, R, rec.as<float>(), it, 1);
             GEO_TRY(check_launch("grtm_inject"));
-            k_g_vel<<<gb, 256, 0, s>>>(g, R);
-            GEO_TRY(check_launch("grtm_vel"));
-            k_g_stress<<<gb, 256, 0, s>>>(g, R, de2.as<float>(), dd2.as<float>());
-            GEO_TRY(check_launch("grtm_stress"));
+            GEO_TRY(step(R, de2.as<float>(), dd2.as<float>()));
             k_g_image<<<gi, 256, 0, s>>>(g, S, R, mig.as<float>(), ag.p ? ag.as<float>() : nullptr);
             GEO_TRY(check_launch("grtm_image"));
         }
@@ -438,9 +533,9 @@ extern "C" int geo_rtm2d_gpu(const geo_rtm2d_gpu_desc *desc, const float *v, con
     GEO_CUDA(cudaMemcpyAsync(mig_lap, lap.p, n0 * 4, kout, s));
     if (illum) GEO_CUDA(cudaMemcpyAsync(illum, ill.p, n0 * 4, kout, s));
     if (ag.p) {
-        k_g_adcig_norm<<<grid_of_n((long)n0 * D.nangle), 256, 0, s>>>(ag.as<float>(), ill.as<float>(), nx, nz, D.nangle);
+        k_g_adcig_norm<<<grid_of_n((long)nag), 256, 0, s>>>(ag.as<float>(), ill.as<float>(), nxa, nz, D.nangle, dcdp);
         GEO_TRY(check_launch("grtm_adcig_norm"));
-        if (adcigs) GEO_CUDA(cudaMemcpyAsync(adcigs, ag.p, (size_t)D.nangle * n0 * 4, kout, s));
+        if (adcigs) GEO_CUDA(cudaMemcpyAsync(adcigs, ag.p, nag * 4, kout, s));
         if (stk_lap) {
             GEO_TRY(stk.alloc(n0 * 4));
             k_g_stack_angles<<<gi, 256, 0, s>>>(ag.as<float>(), stk.as<float>(), nx, nz, D.nangle);
@@ -451,4 +546,24 @@ extern "C" int geo_rtm2d_gpu(const geo_rtm2d_gpu_desc *desc, const float *v, con
     }
     GEO_CUDA(cudaStreamSynchronize(s));
     return GEO_OK;
+}
+
+}  // namespace geo
+
+using namespace geo;
+
+extern "C" int geo_rtm2d_gpu(const geo_rtm2d_gpu_desc *desc, const float *v, const float *e, const float *d,
+                             const float *obs, float *mig_lap, float *illum, float *adcigs, float *stk_lap,
+                             float *shots, int mem, void *stream) {
+    if (!desc || !v || !e || !d || !mig_lap) return fail(GEO_ERR_ARG, "null argument");
+    const GpuRtmProgram vti{false, 18, 7, true, true};
+    return gpu_rtm_run(vti, *desc, v, e, d, nullptr, obs, mig_lap, illum, adcigs, stk_lap, shots, mem, stream);
+}
+
+extern "C" int geo_rtm2d_tti(const geo_rtm2d_gpu_desc *desc, const float *v, const float *e, const float *d,
+                             const float *theta, const float *obs, float *mig_lap, float *illum, float *adcigs,
+                             float *shots, int mem, void *stream) {
+    if (!desc || !v || !e || !d || !theta || !mig_lap) return fail(GEO_ERR_ARG, "null argument");
+    const GpuRtmProgram tti{true, 15, 4, false, false};
+    return gpu_rtm_run(tti, *desc, v, e, d, theta, obs, mig_lap, illum, adcigs, nullptr, shots, mem, stream);
 }

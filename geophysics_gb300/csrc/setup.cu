@@ -94,6 +94,8 @@ void pad_model_3d(int nx, int ny, int nz, int npd, const float *in, float *out) 
 float sponge_d0(Variant v, int dims, float vpmax, float vcenter, int npd, float dx, float dy, float dz) {
     const double l = std::log(100000.0);
     if (v == V_CPU || v == V_MPI) return (float)(3.0 * vpmax * l / (2.0 * npd * dx));
+    // 2D TTI GPU RTM program, get_d0 (Toa_gpu_2dtti_rtm_adcigs_iorderfunciton.cu:230-233)
+    if (v == V_TTIRTM) return (float)(3.0 * vcenter * l / (2.0 * npd * ((dx + dz) / 2.0)));
     if (dims == 2) return (float)(10.0 * vcenter * l / (2.0 * npd * ((dx + dz) / 2.0)));
     return (float)(10.0 * vcenter * l / (2.0 * npd * ((dx + dy + dz) / 3.0)));
 }
@@ -104,7 +106,9 @@ float sponge_d0(Variant v, int dims, float vpmax, float vcenter, int npd, float 
 // program builds acoff2 from coff1 (CPU_vti2dfd_kernels.c:307-319), the MPI
 // program from acoff1 (Toa_rtm_vti_adcig_cdp.c:1497-1512), and the GPU
 // programs measure the far side from the interior edge itself
-// (GPU_vti2dfd_kernels.cu:132-136).
+// (GPU_vti2dfd_kernels.cu:132-136).  The 2D TTI GPU RTM program uses the
+// integer-cell distance for both pairs (initial_coffe,
+// Toa_gpu_2dtti_rtm_adcigs_iorderfunciton.cu:289-320).
 void sponge_profiles(Variant v, int n, int npd, float dt, float d0, float *coff1, float *coff2,
                      float *acoff1, float *acoff2) {
     const int nn = n + 2 * npd;
@@ -116,9 +120,11 @@ void sponge_profiles(Variant v, int n, int npd, float dt, float d0, float *coff1
         if (i < npd) {
             qh = (npd - 0.5 - i) / npd;
             qi = ((npd - i) * 1.0) / npd;
+            if (v == V_TTIRTM) qh = (npd - i) * 1.0 / npd;
         } else if (i >= npd + n) {
             qh = (0.5 + i - n - npd) / npd;
-            qi = (v == V_GPU) ? ((i - n - npd) * 1.0) / npd : ((1 + i - n - npd) * 1.0) / npd;
+            qi = (v == V_GPU || v == V_TTIRTM) ? ((i - n - npd) * 1.0) / npd : ((1 + i - n - npd) * 1.0) / npd;
+            if (v == V_TTIRTM) qh = (i - n - npd) * 1.0 / npd;
         } else {
             continue;
         }

@@ -14,6 +14,7 @@
 // cos and sin of the tilt are formed once on the host (cosf/sinf of the
 // angle in radians, theta * pi/180 as the program converts it).
 #include "geo_internal.h"
+#include "tti2d.cuh"
 #include <cmath>
 #include <vector>
 
@@ -21,64 +22,26 @@ namespace geo {
 
 __constant__ float c_tti[4] = {1.196289f, -0.0797526f, 0.009570313f, -0.0006975447f};
 
-struct Tti2D {
-    int nnx, nnz;
-    float dtx, dtz;
-    const float *cx1, *cx2, *cz1, *cz2, *ax1, *ax2, *az1, *az2;
-    const float *vp, *e2, *d2, *ct, *st;
-    float *u, *w, *px, *pz, *qx, *qz, *P, *Q;
-};
-
-__global__ void k_tti_src(Tti2D g, long id, float amp) {
-    g.P[id] += amp;
-    g.Q[id] += amp;
+__global__ void k_tti_src(TtiField f, long id, float amp) {
+    f.P[id] += amp;
+    f.Q[id] += amp;
 }
 
-__global__ void k_tti_vel(Tti2D g) {
+__global__ void k_tti_vel(TtiGrid g, TtiField f) {
     const long n = (long)g.nnx * g.nnz;
     for (long id = blockIdx.x * (long)blockDim.x + threadIdx.x; id < n; id += (long)gridDim.x * blockDim.x) {
         const int ix = (int)(id / g.nnz), iz = (int)(id % g.nnz);
         if (ix < 4 || ix >= g.nnx - 4 || iz < 4 || iz >= g.nnz - 4) continue;
-        const long s = g.nnz;
-        float Px = 0.0f, Pz = 0.0f, Qz = 0.0f, Qx = 0.0f;
-#pragma unroll
-        for (int im = 0; im < 4; im++) {
-            Px += c_tti[im] * (g.P[id + (im + 1) * s] - g.P[id - im * s]);
-            Pz += c_tti[im] * (g.P[id + im + 1] - g.P[id - im]);
-            Qz += c_tti[im] * (g.Q[id + im + 1] - g.Q[id - im]);
-            Qx += c_tti[im] * (g.Q[id + (im + 1) * s] - g.Q[id - im * s]);
-        }
-        const float ct = g.ct[id], st = g.st[id];
-        const float k2 = g.cx2[ix] * g.cz2[iz], k1 = g.cx1[ix] * g.cz1[iz];
-        g.u[id] = k2 * g.u[id] - k1 * (ct * g.dtx * Px - st * g.dtz * Pz);
-        g.w[id] = k2 * g.w[id] - k1 * (st * g.dtx * Qx + ct * g.dtz * Qz);
+        tti_vel_at(g, f, c_tti, id, ix, iz);
     }
 }
 
-__global__ void k_tti_stress(Tti2D g) {
+__global__ void k_tti_stress(TtiGrid g, TtiField f, const float *e2, const float *d2) {
     const long n = (long)g.nnx * g.nnz;
     for (long id = blockIdx.x * (long)blockDim.x + threadIdx.x; id < n; id += (long)gridDim.x * blockDim.x) {
         const int ix = (int)(id / g.nnz), iz = (int)(id % g.nnz);
         if (ix < 4 || ix >= g.nnx - 4 || iz < 4 || iz >= g.nnz - 4) continue;
-        const long s = g.nnz;
-        float ux = 0.0f, uz = 0.0f, wz = 0.0f, wx = 0.0f;
-#pragma unroll
-        for (int im = 0; im < 4; im++) {
-            ux += c_tti[im] * (g.u[id + im * s] - g.u[id - (im + 1) * s]);
-            uz += c_tti[im] * (g.u[id + im] - g.u[id - im - 1]);
-            wz += c_tti[im] * (g.w[id + im] - g.w[id - im - 1]);
-            wx += c_tti[im] * (g.w[id + im * s] - g.w[id - (im + 1) * s]);
-        }
-        const float ct = g.ct[id], st = g.st[id], vp = g.vp[id];
-        const float A = ct * g.dtx * ux - st * g.dtz * uz, B = st * g.dtx * wx + ct * g.dtz * wz;
-        const float k2 = g.ax2[ix] * g.az2[iz], k1 = g.ax1[ix] * g.az1[iz];
-        const float px = k2 * g.px[id] - k1 * vp * vp * g.e2[id] * A;
-        const float pz = k2 * g.pz[id] - k1 * vp * vp * g.d2[id] * B;
-        const float qx = k2 * g.qx[id] - k1 * vp * vp * g.d2[id] * A;
-        const float qz = k2 * g.qz[id] - k1 * vp * vp * B;
-        g.px[id] = px; g.pz[id] = pz; g.qx[id] = qx; g.qz[id] = qz;
-        g.P[id] = px + pz;
-        g.Q[id] = qx + qz;
+        tti_stress_at(g, f, e2, d2, c_tti, id, ix, iz);
     }
 }
 
@@ -166,7 +129,7 @@ extern "C" int geo_tti2d_shot(const geo_fd2d_desc *desc, const float *v, const f
     GEO_CUDA(cudaMemcpyAsync(dprof.p, prof.data(), prof.size() * 4, cudaMemcpyHostToDevice, s));
     GEO_TRY(df.zero(s));
     GEO_TRY(drec.zero(s));
-    Tti2D g{};
+    TtiGrid g{};
     g.nnx = nnx;
     g.nnz = nnz;
     g.dtx = D.dt / D.dx;
@@ -176,26 +139,28 @@ extern "C" int geo_tti2d_shot(const geo_fd2d_desc *desc, const float *v, const f
     pp += 4 * nnx;
     g.cz1 = pp; g.cz2 = pp + nnz; g.az1 = pp + 2 * nnz; g.az2 = pp + 3 * nnz;
     const float *m = dm.as<float>();
-    g.vp = m; g.e2 = m + n; g.d2 = m + 2 * n; g.ct = m + 3 * n; g.st = m + 4 * n;
-    float *f = df.as<float>();
-    g.u = f; g.w = f + n; g.px = f + 2 * n; g.pz = f + 3 * n; g.qx = f + 4 * n; g.qz = f + 5 * n;
-    g.P = f + 6 * n; g.Q = f + 7 * n;
+    g.vp = m; g.ct = m + 3 * n; g.st = m + 4 * n;
+    const float *e2 = m + n, *d2 = m + 2 * n;
+    float *fb = df.as<float>();
+    TtiField f;
+    f.u = fb; f.w = fb + n; f.px = fb + 2 * n; f.pz = fb + 3 * n; f.qx = fb + 4 * n; f.qz = fb + 5 * n;
+    f.P = fb + 6 * n; f.Q = fb + 7 * n;
     const int blocks = (int)std::min<size_t>((n + 255) / 256, 152 * 16);
     const long src_id = (long)ixs * nnz + izs;
     const cudaMemcpyKind kout = mem == GEO_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
     for (int it = 0; it < nt; it++) {
         if (on[it]) {
-            k_tti_src<<<1, 1, 0, s>>>(g, src_id, amp[it]);
+            k_tti_src<<<1, 1, 0, s>>>(f, src_id, amp[it]);
             GEO_TRY(check_launch("tti_src"));
         }
-        k_tti_vel<<<blocks, 256, 0, s>>>(g);
+        k_tti_vel<<<blocks, 256, 0, s>>>(g, f);
         GEO_TRY(check_launch("tti_vel"));
-        k_tti_stress<<<blocks, 256, 0, s>>>(g);
+        k_tti_stress<<<blocks, 256, 0, s>>>(g, f, e2, d2);
         GEO_TRY(check_launch("tti_stress"));
-        k_tti_rec<<<(nx + 255) / 256, 256, 0, s>>>(g.P, drec.as<float>(), nnz, nx, npd, D.rec_iz, it, nt);
+        k_tti_rec<<<(nx + 255) / 256, 256, 0, s>>>(f.P, drec.as<float>(), nnz, nx, npd, D.rec_iz, it, nt);
         GEO_TRY(check_launch("tti_rec"));
         if (snap && it % snap_every == 0 && it != 0)
-            GEO_CUDA(cudaMemcpyAsync(snap + (size_t)(it / snap_every - 1) * n, g.P, n * 4, kout, s));
+            GEO_CUDA(cudaMemcpyAsync(snap + (size_t)(it / snap_every - 1) * n, f.P, n * 4, kout, s));
     }
     GEO_CUDA(cudaMemcpyAsync(shot, drec.p, (size_t)nx * nt * 4, kout, s));
     GEO_CUDA(cudaStreamSynchronize(s));

@@ -274,11 +274,29 @@ typedef struct geo_rtm2d_gpu_desc {
     int   ns, fs, ds, zs;    /* shots; source x (1-based), step, depth       */
     int   mute_tt;           /* 20 in the program                            */
     int   nangle, dangle;    /* 70 and 1 in the program                      */
+    int   dcdp;              /* gathers at every dcdp-th CDP: TTI program
+                                only (0 = 1); the VTI program takes 0 or 1  */
 } geo_rtm2d_gpu_desc;
 
 int geo_rtm2d_gpu(const geo_rtm2d_gpu_desc *desc, const float *v, const float *e, const float *d,
                   const float *obs, float *mig_lap, float *illum, float *adcigs, float *stk_lap, float *shots,
                   int mem, void *stream);
+
+/* 2D TTI RTM with the 2D TTI GPU RTM program's semantics
+ * (2D-tti-fd+rtm-cuda/Toa_gpu_2dtti_rtm_adcigs_iorderfunciton.cu, main
+ * :500-800): the shot structure of geo_rtm2d_gpu with the TTI stencil
+ * (update_vel / update_stress :126-228) over theta (nx*nz tilt in degrees),
+ * SV taper R=15, r=4 in the forward pass, direct-wave mute with velocity
+ * vp*(1+(sqrtf(1+2 eps)-1)*cos(theta)) at the first model cell (:336-358;
+ * tt = 30 in the program), forward illumination (:430-442), and Poynting
+ * gathers at CDPs 0, dcdp, 2 dcdp, ... (:454-498): adcigs is
+ * (nx/dcdp)*nangle*nz, [ixa][ia][iz].  The program's defaults: nangle 65,
+ * dangle 1, dcdp 1.  No readFile checks, no angle stack.  mig_lap: the
+ * Laplacian-filtered image; illum, adcigs, shots (muted records
+ * ns*nx*nt): optional. */
+int geo_rtm2d_tti(const geo_rtm2d_gpu_desc *desc, const float *v, const float *e, const float *d,
+                  const float *theta, const float *obs, float *mig_lap, float *illum, float *adcigs,
+                  float *shots, int mem, void *stream);
 
 /* Adjoint first-difference Laplacian (laplac2_lop adj=1,
  * utils-Laplacian-filter/laplace.c:9-53; the in-program copy

@@ -456,6 +456,171 @@ int orc_fd2d(const orc_fd2d_desc *d, const float *v, const float *e, const float
     return 0;
 }
 
+/* A 2D TTI propagator of the GPU TTI programs: model (padded vp, 1+2eps and
+ * sqrtf(1+2del) with and without the SV taper, cosf/sinf of the tilt,
+ * x*z-product sponge profiles, source amplitudes) and in-place fields.
+ *   theta (degrees) -> theta * (pi/180.0) in double, stored float;
+ *   sponge: the TTI forward program's (get_d0 with 10.0, half-cell velocity
+ *   profiles; Toa_gpu_2dtti_fd_1orderfunction.cu:186-189, :227-271) or, with
+ *   rtm_sponge, the TTI RTM program's (get_d0 with 3.0 and whole-cell
+ *   distances for both pairs; Toa_gpu_2dtti_rtm_adcigs_iorderfunciton.cu:230-233,
+ *   :289-320). */
+typedef struct { REAL *u, *w, *P, *Q, *px, *pz, *qx, *qz; } orc_ttif;
+typedef struct {
+    int nnx, nnz; long n, src;
+    REAL *vp;
+    float *ct, *st, *e2, *d2, *e2t, *d2t;
+    float *cx1, *cx2, *ax1, *ax2, *cz1, *cz2, *az1, *az2;
+    float dtx, dtz, *amp;
+    unsigned char *act;
+} orc_ttim;
+
+static void ttif_alloc(orc_ttif *f, long n)
+{
+    f->u = calloc(n, sizeof(REAL)); f->w = calloc(n, sizeof(REAL)); f->P = calloc(n, sizeof(REAL)); f->Q = calloc(n, sizeof(REAL));
+    f->px = calloc(n, sizeof(REAL)); f->pz = calloc(n, sizeof(REAL)); f->qx = calloc(n, sizeof(REAL)); f->qz = calloc(n, sizeof(REAL));
+}
+
+static void ttif_free(orc_ttif *f)
+{
+    free(f->u); free(f->w); free(f->P); free(f->Q); free(f->px); free(f->pz); free(f->qx); free(f->qz);
+}
+
+static void ttim_free(orc_ttim *m)
+{
+    free(m->vp); free(m->ct); free(m->st); free(m->e2); free(m->d2); free(m->e2t); free(m->d2t);
+    free(m->cx1); free(m->cx2); free(m->ax1); free(m->ax2); free(m->cz1); free(m->cz2); free(m->az1); free(m->az2);
+    free(m->amp); free(m->act);
+}
+
+/* taper_R, taper_r: SV taper of e2t/d2t centred (fs+(is-1)ds+npd, zs+npd) (0: none) */
+static void ttim_init(orc_ttim *m, const orc_fd2d_desc *d, const float *v, const float *e, const float *dl,
+                      const float *theta, int rtm_sponge, int taper_R, int taper_r)
+{
+    const int nx = d->nx, nz = d->nz, npd = d->npd, nt = d->nt;
+    const int nnx = nx + 2 * npd, nnz = nz + 2 * npd;
+    const long n = (long)nnx * nnz;
+    long id, ix, iz;
+    REAL *ee = calloc(n, sizeof(REAL)), *dd = calloc(n, sizeof(REAL)), *th = calloc(n, sizeof(REAL));
+    m->nnx = nnx; m->nnz = nnz; m->n = n;
+    m->vp = calloc(n, sizeof(REAL));
+    m->ct = malloc(n * 4); m->st = malloc(n * 4); m->e2 = malloc(n * 4); m->d2 = malloc(n * 4);
+    m->e2t = malloc(n * 4); m->d2t = malloc(n * 4);
+    m->cx1 = malloc(nnx * 4); m->cx2 = malloc(nnx * 4); m->ax1 = malloc(nnx * 4); m->ax2 = malloc(nnx * 4);
+    m->cz1 = malloc(nnz * 4); m->cz2 = malloc(nnz * 4); m->az1 = malloc(nnz * 4); m->az2 = malloc(nnz * 4);
+    m->amp = malloc(nt * 4); m->act = malloc(nt);
+    for (ix = 0; ix < nx; ix++)
+        for (iz = 0; iz < nz; iz++) {
+            id = (ix + npd) * nnz + iz + npd;
+            m->vp[id] = v[ix * nz + iz]; ee[id] = e[ix * nz + iz]; dd[id] = dl[ix * nz + iz];
+            th[id] = (float)((double)theta[ix * nz + iz] * (PI_GUI / 180.0));
+        }
+    orc_pad2d(nx, nz, npd, m->vp); orc_pad2d(nx, nz, npd, ee); orc_pad2d(nx, nz, npd, dd); orc_pad2d(nx, nz, npd, th);
+    {
+        const float fsx = d->fs + (d->is - 1) * d->ds;
+        const int ixs = (int)(fsx + 0.5f) + npd - 1, izs = (int)(d->zs + 0.5f) + npd - 1;
+        const double k0 = rtm_sponge ? 3.0 : 10.0;
+        const float d0 = (float)(k0 * (float)m->vp[n / 2] * log(100000.0) / (2.0 * npd * ((d->dx + d->dz) / 2.0)));
+        const int cx = (int)d->fs + (d->is - 1) * (int)d->ds + npd, cz = (int)d->zs + npd;
+        m->src = (long)ixs * nnz + izs;
+        for (id = 0; id < n; id++) {
+            float thf = (float)th[id], te = (float)ee[id], td = (float)dd[id];
+            m->e2[id] = 1 + 2 * te;
+            m->d2[id] = sqrtf(1 + 2 * td);
+            m->ct[id] = cosf(thf);
+            m->st[id] = sinf(thf);
+            ix = id / nnz; iz = id % nnz;
+            if (taper_R > 0) {
+                int rx = (int)ix - cx, rz = (int)iz - cz;
+                if ((rx * rx + rz * rz) <= taper_R * taper_R) {
+                    if ((rx * rx + rz * rz) <= taper_r * taper_r) { te = 0.0f; td = 0.0f; }
+                    else {
+                        double g = 0.5 * (1 - cos(PI_GUI * ((sqrtf((float)(rx * rx + rz * rz)) - taper_r) * 4.0 / (taper_R * 3.0 - 1))));
+                        te = (float)(g * te);
+                        td = (float)(g * td);
+                    }
+                }
+            }
+            m->e2t[id] = 1 + 2 * te;
+            m->d2t[id] = sqrtf(1 + 2 * td);
+        }
+        if (rtm_sponge) {
+            /* integer-cell distance for both pairs, far side (i-n-npd)/npd */
+            int i, k;
+            for (k = 0; k < 2; k++) {
+                int nn = k ? nz : nx, nnn = nn + 2 * npd;
+                float *c1 = k ? m->cz1 : m->cx1, *c2 = k ? m->cz2 : m->cx2, *a1 = k ? m->az1 : m->ax1, *a2 = k ? m->az2 : m->ax2;
+                for (i = 0; i < nnn; i++) {
+                    double q;
+                    if (i < npd) q = (npd - i) * 1.0 / npd;
+                    else if (i >= npd + nn) q = (i - nn - npd) * 1.0 / npd;
+                    else { c1[i] = c2[i] = a1[i] = a2[i] = 1.0f; continue; }
+                    c1[i] = (float)(1.0 / (1.0 + (d->dt * d0 * pow(q, 2.0)) / 2.0));
+                    c2[i] = (float)(c1[i] * (1.0 - (d->dt * d0 * pow(q, 2.0)) / 2.0));
+                    a1[i] = c1[i];
+                    a2[i] = c2[i];
+                }
+            }
+        } else {
+            orc_sponge(ORC_V_GPU, nx, npd, d->dt, d0, m->cx1, m->cx2, m->ax1, m->ax2);
+            orc_sponge(ORC_V_GPU, nz, npd, d->dt, d0, m->cz1, m->cz2, m->az1, m->az2);
+        }
+        orc_source_amp(ORC_V_GPU, nt, d->dt, d->favg, d->pfac, d->wtype, m->amp, m->act);
+        m->dtx = d->dt / d->dx;
+        m->dtz = d->dt / d->dz;
+    }
+    free(ee); free(dd); free(th);
+}
+
+/* update_vel then update_stress, in place, with e2/d2 (tapered or not) */
+static void tti_step(const orc_ttim *m, orc_ttif *f, const float *e2, const float *d2)
+{
+    const int nnx = m->nnx, nnz = m->nnz;
+    const long s = nnz;
+    const float dtx = m->dtx, dtz = m->dtz;
+    REAL *u = f->u, *w = f->w, *P = f->P, *Q = f->Q;
+    long id, ix, iz;
+    int im;
+    for (ix = 4; ix < nnx - 4; ix++)
+        for (iz = 4; iz < nnz - 4; iz++) {
+            REAL Px = 0, Pz = 0, Qz = 0, Qx = 0, k1, k2;
+            id = ix * nnz + iz;
+            for (im = 0; im < 4; im++) {
+                Px += C8[im] * (P[id + (im + 1) * s] - P[id - im * s]);
+                Pz += C8[im] * (P[id + im + 1] - P[id - im]);
+                Qz += C8[im] * (Q[id + im + 1] - Q[id - im]);
+                Qx += C8[im] * (Q[id + (im + 1) * s] - Q[id - im * s]);
+            }
+            k2 = (REAL)m->cx2[ix] * m->cz2[iz];
+            k1 = (REAL)m->cx1[ix] * m->cz1[iz];
+            u[id] = k2 * u[id] - k1 * ((REAL)m->ct[id] * dtx * Px - (REAL)m->st[id] * dtz * Pz);
+            w[id] = k2 * w[id] - k1 * ((REAL)m->st[id] * dtx * Qx + (REAL)m->ct[id] * dtz * Qz);
+        }
+    for (ix = 4; ix < nnx - 4; ix++)
+        for (iz = 4; iz < nnz - 4; iz++) {
+            REAL ux = 0, uz = 0, wz = 0, wx = 0, A, B, k1, k2, a, b, c_, e_;
+            const REAL *vp = m->vp;
+            id = ix * nnz + iz;
+            for (im = 0; im < 4; im++) {
+                ux += C8[im] * (u[id + im * s] - u[id - (im + 1) * s]);
+                uz += C8[im] * (u[id + im] - u[id - im - 1]);
+                wz += C8[im] * (w[id + im] - w[id - im - 1]);
+                wx += C8[im] * (w[id + im * s] - w[id - (im + 1) * s]);
+            }
+            A = (REAL)m->ct[id] * dtx * ux - (REAL)m->st[id] * dtz * uz;
+            B = (REAL)m->st[id] * dtx * wx + (REAL)m->ct[id] * dtz * wz;
+            k2 = (REAL)m->ax2[ix] * m->az2[iz];
+            k1 = (REAL)m->ax1[ix] * m->az1[iz];
+            a = k2 * f->px[id] - k1 * vp[id] * vp[id] * e2[id] * A;
+            b = k2 * f->pz[id] - k1 * vp[id] * vp[id] * d2[id] * B;
+            c_ = k2 * f->qx[id] - k1 * vp[id] * vp[id] * d2[id] * A;
+            e_ = k2 * f->qz[id] - k1 * vp[id] * vp[id] * B;
+            f->px[id] = a; f->pz[id] = b; f->qx[id] = c_; f->qz[id] = e_;
+            P[id] = a + b;
+            Q[id] = c_ + e_;
+        }
+}
+
 /* 2D TTI forward modelling with the GPU TTI program's semantics
  * (2D-tti-fd+rtm-cuda/Toa_gpu_2dtti_fd_1orderfunction.cu):
  *   theta (degrees) -> theta * (pi/180.0) in double, stored float (:235);
@@ -473,99 +638,22 @@ int orc_fd2d(const orc_fd2d_desc *d, const float *v, const float *e, const float
 int orc_tti2d(const orc_fd2d_desc *d, const float *v, const float *e, const float *dl, const float *theta,
               float *shot, float *snaps, int snap_every)
 {
-    const int nx = d->nx, nz = d->nz, npd = d->npd, nt = d->nt;
-    const int nnx = nx + 2 * npd, nnz = nz + 2 * npd;
-    const long n = (long)nnx * nnz;
-    long id, ix, iz;
-    int it, im;
-    REAL *vp = calloc(n, sizeof(REAL)), *ee = calloc(n, sizeof(REAL)), *dd = calloc(n, sizeof(REAL));
-    REAL *th = calloc(n, sizeof(REAL));
-    float *ct = malloc(n * 4), *st = malloc(n * 4), *e2 = malloc(n * 4), *d2 = malloc(n * 4);
-    REAL *u = calloc(n, sizeof(REAL)), *w = calloc(n, sizeof(REAL)), *P = calloc(n, sizeof(REAL)), *Q = calloc(n, sizeof(REAL));
-    REAL *px = calloc(n, sizeof(REAL)), *pz = calloc(n, sizeof(REAL)), *qx = calloc(n, sizeof(REAL)), *qz = calloc(n, sizeof(REAL));
-    float *cx1 = malloc(nnx * 4), *cx2 = malloc(nnx * 4), *ax1 = malloc(nnx * 4), *ax2 = malloc(nnx * 4);
-    float *cz1 = malloc(nnz * 4), *cz2 = malloc(nnz * 4), *az1 = malloc(nnz * 4), *az2 = malloc(nnz * 4);
-    float *amp = malloc(nt * 4);
-    unsigned char *act = malloc(nt);
-    for (ix = 0; ix < nx; ix++)
-        for (iz = 0; iz < nz; iz++) {
-            id = (ix + npd) * nnz + iz + npd;
-            vp[id] = v[ix * nz + iz]; ee[id] = e[ix * nz + iz]; dd[id] = dl[ix * nz + iz];
-            th[id] = (float)((double)theta[ix * nz + iz] * (PI_GUI / 180.0));
-        }
-    orc_pad2d(nx, nz, npd, vp); orc_pad2d(nx, nz, npd, ee); orc_pad2d(nx, nz, npd, dd); orc_pad2d(nx, nz, npd, th);
-    {
-        const float fsx = d->fs + (d->is - 1) * d->ds;
-        const int ixs = (int)(fsx + 0.5f) + npd - 1, izs = (int)(d->zs + 0.5f) + npd - 1;
-        const float d0 = (float)(10.0 * (float)vp[n / 2] * log(100000.0) / (2.0 * npd * ((d->dx + d->dz) / 2.0)));
-        float *te = malloc(n * 4), *td = malloc(n * 4), *te2 = malloc(n * 4), *td2 = malloc(n * 4);
-        for (id = 0; id < n; id++) { te[id] = (float)ee[id]; td[id] = (float)dd[id]; }
-        if (d->sv) {
-            orc_sv_taper2d(ORC_V_GPU, nnx, nnz, npd, d->fs, d->ds, d->zs, d->is, te, td, te2, td2);
-            memcpy(te, te2, n * 4); memcpy(td, td2, n * 4);
-        }
-        for (id = 0; id < n; id++) {
-            float thf = (float)th[id];
-            e2[id] = 1 + 2 * te[id];
-            d2[id] = sqrtf(1 + 2 * td[id]);
-            ct[id] = cosf(thf);
-            st[id] = sinf(thf);
-        }
-        free(te); free(td); free(te2); free(td2);
-        orc_sponge(ORC_V_GPU, nx, npd, d->dt, d0, cx1, cx2, ax1, ax2);
-        orc_sponge(ORC_V_GPU, nz, npd, d->dt, d0, cz1, cz2, az1, az2);
-        orc_source_amp(ORC_V_GPU, nt, d->dt, d->favg, d->pfac, d->wtype, amp, act);
-        {
-            const float dtx = d->dt / d->dx, dtz = d->dt / d->dz;
-            const long s = nnz;
-            for (it = 0; it < nt; it++) {
-                if (act[it]) { P[(long)ixs * nnz + izs] += amp[it]; Q[(long)ixs * nnz + izs] += amp[it]; }
-                for (ix = 4; ix < nnx - 4; ix++)
-                    for (iz = 4; iz < nnz - 4; iz++) {
-                        REAL Px = 0, Pz = 0, Qz = 0, Qx = 0, k1, k2;
-                        id = ix * nnz + iz;
-                        for (im = 0; im < 4; im++) {
-                            Px += C8[im] * (P[id + (im + 1) * s] - P[id - im * s]);
-                            Pz += C8[im] * (P[id + im + 1] - P[id - im]);
-                            Qz += C8[im] * (Q[id + im + 1] - Q[id - im]);
-                            Qx += C8[im] * (Q[id + (im + 1) * s] - Q[id - im * s]);
-                        }
-                        k2 = (REAL)cx2[ix] * cz2[iz];
-                        k1 = (REAL)cx1[ix] * cz1[iz];
-                        u[id] = k2 * u[id] - k1 * ((REAL)ct[id] * dtx * Px - (REAL)st[id] * dtz * Pz);
-                        w[id] = k2 * w[id] - k1 * ((REAL)st[id] * dtx * Qx + (REAL)ct[id] * dtz * Qz);
-                    }
-                for (ix = 4; ix < nnx - 4; ix++)
-                    for (iz = 4; iz < nnz - 4; iz++) {
-                        REAL ux = 0, uz = 0, wz = 0, wx = 0, A, B, k1, k2, a, b, c_, e_;
-                        id = ix * nnz + iz;
-                        for (im = 0; im < 4; im++) {
-                            ux += C8[im] * (u[id + im * s] - u[id - (im + 1) * s]);
-                            uz += C8[im] * (u[id + im] - u[id - im - 1]);
-                            wz += C8[im] * (w[id + im] - w[id - im - 1]);
-                            wx += C8[im] * (w[id + im * s] - w[id - (im + 1) * s]);
-                        }
-                        A = (REAL)ct[id] * dtx * ux - (REAL)st[id] * dtz * uz;
-                        B = (REAL)st[id] * dtx * wx + (REAL)ct[id] * dtz * wz;
-                        k2 = (REAL)ax2[ix] * az2[iz];
-                        k1 = (REAL)ax1[ix] * az1[iz];
-                        a = k2 * px[id] - k1 * vp[id] * vp[id] * e2[id] * A;
-                        b = k2 * pz[id] - k1 * vp[id] * vp[id] * d2[id] * B;
-                        c_ = k2 * qx[id] - k1 * vp[id] * vp[id] * d2[id] * A;
-                        e_ = k2 * qz[id] - k1 * vp[id] * vp[id] * B;
-                        px[id] = a; pz[id] = b; qx[id] = c_; qz[id] = e_;
-                        P[id] = a + b;
-                        Q[id] = c_ + e_;
-                    }
-                for (ix = 0; ix < nx; ix++) shot[it + (long)nt * ix] = (float)P[d->rec_iz + (long)nnz * (ix + npd)];
-                if (snaps && snap_every > 0 && it % snap_every == 0 && it != 0)
-                    for (id = 0; id < n; id++) snaps[(long)(it / snap_every - 1) * n + id] = (float)P[id];
-            }
-        }
+    const int nx = d->nx, npd = d->npd, nt = d->nt;
+    orc_ttim m;
+    orc_ttif f;
+    long id;
+    int it, ix;
+    ttim_init(&m, d, v, e, dl, theta, 0, d->sv ? 15 : 0, 4);
+    ttif_alloc(&f, m.n);
+    for (it = 0; it < nt; it++) {
+        if (m.act[it]) { f.P[m.src] += m.amp[it]; f.Q[m.src] += m.amp[it]; }
+        tti_step(&m, &f, m.e2t, m.d2t);
+        for (ix = 0; ix < nx; ix++) shot[it + (long)nt * ix] = (float)f.P[d->rec_iz + (long)m.nnz * (ix + npd)];
+        if (snaps && snap_every > 0 && it % snap_every == 0 && it != 0)
+            for (id = 0; id < m.n; id++) snaps[(long)(it / snap_every - 1) * m.n + id] = (float)f.P[id];
     }
-    free(vp); free(ee); free(dd); free(th); free(ct); free(st); free(e2); free(d2);
-    free(u); free(w); free(P); free(Q); free(px); free(pz); free(qx); free(qz);
-    free(cx1); free(cx2); free(ax1); free(ax2); free(cz1); free(cz2); free(az1); free(az2); free(amp); free(act);
+    ttif_free(&f);
+    ttim_free(&m);
     return 0;
 }
 
@@ -858,6 +946,127 @@ int orc_rtm2d_gpu(int nx, int nz, int npml, int nt, float dx, float dz, float dt
     if (adcigs)
         for (size_t q = 0; q < n0 * nangle; q++) {
             size_t ixq = q / ((size_t)nz * nangle), izq = q % nz;
+            adcigs[q] /= ill[izq + (size_t)nz * ixq];
+        }
+    free(rec); free(bp); free(bq);
+    return 0;
+}
+
+/* 2D TTI RTM with the 2D TTI GPU RTM program's semantics
+ * (2D-tti-fd+rtm-cuda/Toa_gpu_2dtti_rtm_adcigs_iorderfunciton.cu, main
+ * :500-800), shots is = 1..ns at fs + (is-1)*ds:
+ *   forward: point source, TTI step with the SV taper (R=15, r=4), record P
+ *     at row npml, ring of P,Q (rows npml-1, npml+nz+1, columns npml-1,
+ *     npml+nx+1; wavefield_bndr :360-416), illumination ill += P*P + Q*Q,
+ *     == 0 -> 1 (:430-442);
+ *   mute (:336-358): zero (t0/dt - tt, t0/dt + 2/(dt f) + tt) with
+ *     t0 = offset / (vp[1]*(1+(sqrtf(1+2 eps[1])-1)*cos(theta[1])));
+ *   obs (optional) replaces the record;
+ *   backward: ring restore + untapered step of the source field, record
+ *     into P and Q of the receiver field at row npml + step, image
+ *     += sP*gP (:418-428), Poynting gathers at ix = 0, dcdp, 2 dcdp, ...
+ *     (:454-486).
+ * After the shots mig /= ill and gathers /= ill (:444-452, :488-498); the
+ * caller filters.  The model uses the RTM program's sponge (ttim_init with
+ * rtm_sponge).  mig, ill: nx*nz; adcigs (optional): (nx/dcdp)*nangle*nz;
+ * shots (optional): the muted records ns*nx*nt. */
+int orc_rtm2d_tti(int nx, int nz, int npml, int nt, float dx, float dz, float dt, float favg, float pfac,
+                  int wtype, int ns, int fs, int ds, int zs, int mute_tt, int nangle, int dangle, int dcdp,
+                  const float *v, const float *e, const float *dl, const float *theta, const float *obs,
+                  float *mig, float *ill, float *adcigs, float *shots)
+{
+    const int nnz = nz + 2 * npml, L = 2 * nx + 2 * nz, nxa = nx / dcdp;
+    const size_t n0 = (size_t)nx * nz;
+    int is, it, ix, iz, k;
+    float *rec = calloc((size_t)nt * nx, 4), *bp = calloc((size_t)nt * L, 4), *bq = calloc((size_t)nt * L, 4);
+    memset(mig, 0, n0 * 4);
+    memset(ill, 0, n0 * 4);
+    if (adcigs) memset(adcigs, 0, (size_t)nxa * nangle * nz * 4);
+    for (is = 1; is <= ns; is++) {
+        orc_fd2d_desc d;
+        orc_ttim m;
+        orc_ttif S, R;
+        memset(&d, 0, sizeof d);
+        d.nx = nx; d.nz = nz; d.npd = npml; d.nt = nt; d.variant = ORC_V_GPU; d.sv = 1; d.wtype = wtype;
+        d.dx = dx; d.dz = dz; d.dt = dt; d.favg = favg; d.pfac = pfac;
+        d.fs = (float)fs; d.ds = (float)ds; d.zs = (float)zs; d.is = is;
+        ttim_init(&m, &d, v, e, dl, theta, 1, 15, 4);
+        ttif_alloc(&S, m.n);
+        ttif_alloc(&R, m.n);
+#define RING_ID(k) ((k) < nx ? npml - 1 + (size_t)nnz * ((k) + npml) \
+                 : (k) < 2 * nx ? npml + nz + 1 + (size_t)nnz * ((k) - nx + npml) \
+                 : (k) < 2 * nx + nz ? (k) - 2 * nx + npml + (size_t)nnz * (npml - 1) \
+                 : (k) - 2 * nx - nz + npml + (size_t)nnz * (npml + nx + 1))
+        memset(rec, 0, (size_t)nt * nx * 4);
+        for (it = 0; it < nt; it++) {
+            if (m.act[it]) { S.P[m.src] += m.amp[it]; S.Q[m.src] += m.amp[it]; }
+            tti_step(&m, &S, m.e2t, m.d2t);
+            for (ix = 0; ix < nx; ix++) rec[(size_t)ix * nt + it] = (float)S.P[npml + (size_t)nnz * (ix + npml)];
+            for (k = 0; k < L; k++) {
+                bp[(size_t)it * L + k] = (float)S.P[RING_ID(k)];
+                bq[(size_t)it * L + k] = (float)S.Q[RING_ID(k)];
+            }
+            for (ix = 0; ix < nx; ix++)
+                for (iz = 0; iz < nz; iz++) {
+                    size_t id = iz + npml + (size_t)nnz * (ix + npml), o = (size_t)ix * nz + iz;
+                    float pp = (float)S.P[id], qq = (float)S.Q[id];
+                    ill[o] += pp * pp + qq * qq;
+                    if (ill[o] == 0.0f) ill[o] = 1.0f;
+                }
+        }
+        {
+            const float mu_v = (float)m.vp[1] * (1 + (sqrtf(1 + 2 * e[0]) - 1) * m.ct[1]);
+            for (ix = 0; ix < nx; ix++) {
+                float mu_x = dx * abs(ix - fs - (is - 1) * ds), mu_z = dz * zs;
+                float mu_t0 = sqrtf((float)(pow(mu_x, 2) + pow(mu_z, 2))) / mu_v;
+                int mu_t = (int)(2.0 / (dt * favg));
+                int mu_nt = (int)(mu_t0 / dt) + mu_t + mute_tt;
+                for (it = 0; it < nt; it++)
+                    if ((it > (int)(mu_t0 / dt) - mute_tt) && (it < mu_nt)) rec[(size_t)ix * nt + it] = 0.0f;
+            }
+        }
+        if (shots) memcpy(shots + (size_t)(is - 1) * nx * nt, rec, (size_t)nx * nt * 4);
+        if (obs) memcpy(rec, obs + (size_t)(is - 1) * nx * nt, (size_t)nx * nt * 4);
+        for (it = nt - 1; it >= 0; it--) {
+            for (k = 0; k < L; k++) {
+                S.P[RING_ID(k)] = (REAL)bp[(size_t)it * L + k];
+                S.Q[RING_ID(k)] = (REAL)bq[(size_t)it * L + k];
+            }
+            tti_step(&m, &S, m.e2, m.d2);
+            for (ix = 0; ix < nx; ix++) {
+                size_t id = npml + (size_t)nnz * (ix + npml);
+                R.P[id] = R.Q[id] = (REAL)rec[(size_t)ix * nt + it];
+            }
+            tti_step(&m, &R, m.e2, m.d2);
+            for (ix = 0; ix < nx; ix++)
+                for (iz = 0; iz < nz; iz++) {
+                    size_t id = iz + npml + (size_t)nnz * (ix + npml), o = (size_t)ix * nz + iz;
+                    float sP = (float)S.P[id], gP = (float)R.P[id];
+                    mig[o] += sP * gP;
+                    if (adcigs && ix % dcdp == 0 && ix / dcdp < nxa) {
+                        float Ssx = -sP * (float)S.u[id], Ssz = -(float)S.Q[id] * (float)S.w[id];
+                        float Sgx = gP * (float)R.u[id], Sgz = (float)R.Q[id] * (float)R.w[id];
+                        float b1 = Ssx * Ssx + Ssz * Ssz, b2 = Sgx * Sgx + Sgz * Sgz;
+                        float a = (Ssx * Sgx + Ssz * Sgz) / (sqrtf(b1 * b2) * (1 - 0.1));
+                        if (a >= -1 && a <= 1) {
+                            int ia;
+                            a = 0.5 * acosf(a) * 180.0 / PI_GUI;
+                            ia = (int)(a / (dangle * 1.0));
+                            if (ia < nangle) {
+                                float c = cosf(ia * PI_GUI / 180.0);
+                                adcigs[iz + (size_t)nz * ia + (size_t)nz * nangle * (ix / dcdp)] += sP * gP * c * c * c;
+                            }
+                        }
+                    }
+                }
+        }
+#undef RING_ID
+        ttif_free(&S); ttif_free(&R); ttim_free(&m);
+    }
+    for (size_t o = 0; o < n0; o++) mig[o] /= ill[o];
+    if (adcigs)
+        for (size_t q = 0; q < (size_t)nxa * nz * nangle; q++) {
+            size_t ixq = q / ((size_t)nz * nangle) * dcdp, izq = q % nz;
             adcigs[q] /= ill[izq + (size_t)nz * ixq];
         }
     free(rec); free(bp); free(bq);

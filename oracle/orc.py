@@ -69,6 +69,7 @@ def lib(prec=32):
         L.orc_adcig3d_illum.argtypes = [C.c_int] * 5 + [C.POINTER(C.c_float)] * 2
         L.orc_rtm3d_snap_shot.argtypes = [C.POINTER(FD3DDesc), C.c_int, C.c_int] + [C.POINTER(C.c_float)] * 5
         L.orc_rtm2d_gpu.argtypes = [C.c_int] * 4 + [C.c_float] * 5 + [C.c_int] * 8 + [C.POINTER(C.c_float)] * 8
+        L.orc_rtm2d_tti.argtypes = [C.c_int] * 4 + [C.c_float] * 5 + [C.c_int] * 9 + [C.POINTER(C.c_float)] * 9
         L.orc_image_illum.argtypes = [C.c_long, C.POINTER(C.c_float), C.POINTER(C.c_float)]
         _libs[key] = L
     return _libs[key]
@@ -196,6 +197,23 @@ def rtm2d_gpu(v, e, d, *, npml, nt, dx, dz, dt, favg, pfac, wtype=1, ns=1, fs=1,
     ob = c32(obs) if obs is not None else None
     lib(prec).orc_rtm2d_gpu(nx, nz, npml, nt, dx, dz, dt, favg, pfac, wtype, ns, fs, ds, zs, mute_tt, nangle,
                             dangle, _fp(v), _fp(e), _fp(d), _fp(ob), _fp(mig), _fp(ill), _fp(ag), _fp(shots))
+    return mig, ill, ag, shots
+
+
+def rtm2d_tti(v, e, d, theta, *, npml, nt, dx, dz, dt, favg, pfac, wtype=1, ns=1, fs=1, ds=0, zs=1, mute_tt=30,
+              nangle=65, dangle=1, dcdp=1, obs=None, prec=32):
+    """The 2D TTI GPU RTM program; theta in degrees.  Returns (mig/ill (nx,nz),
+    ill, adcigs (nx//dcdp,nangle,nz), muted modelled shots (ns,nx,nt))."""
+    v, e, d, theta = c32(v), c32(e), c32(d), c32(theta)
+    nx, nz = v.shape
+    mig = np.zeros((nx, nz), _f)
+    ill = np.zeros((nx, nz), _f)
+    ag = np.zeros((nx // dcdp, nangle, nz), _f)
+    shots = np.zeros((ns, nx, nt), _f)
+    ob = c32(obs) if obs is not None else None
+    lib(prec).orc_rtm2d_tti(nx, nz, npml, nt, dx, dz, dt, favg, pfac, wtype, ns, fs, ds, zs, mute_tt, nangle,
+                            dangle, dcdp, _fp(v), _fp(e), _fp(d), _fp(theta), _fp(ob), _fp(mig), _fp(ill), _fp(ag),
+                            _fp(shots))
     return mig, ill, ag, shots
 
 

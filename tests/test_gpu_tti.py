@@ -43,3 +43,37 @@ def test_tti2d_rejects_bad_input(geo):
     th[3, 4] = np.nan
     with pytest.raises(geo.GeoError):
         geo.tti2d_shot(v, e, d, th, **KW)
+
+
+TKW = dict(npml=20, nt=600, dx=10.0, dz=10.0, dt=np.float32(1e-3), favg=20.0, pfac=10.0, ns=2, fs=30, ds=30, zs=2,
+           mute_tt=30, nangle=65, dangle=1)
+
+
+@pytest.mark.parametrize("dcdp", [1, 3])
+def test_rtm2d_tti_program_bit_exact(geo, orc, dcdp):
+    """The 2D TTI GPU RTM program (TTI stencil, ring saving, forward-stepped
+    reconstruction, Poynting gathers at every dcdp-th CDP; nx = 91 is not a
+    multiple of 3): image, illumination, gathers and records equal the
+    oracle's."""
+    v, e, d, th = _model(nx=91, nz=60, seed=5)
+    mig, ill, ag, shots = orc.rtm2d_tti(v, e, d, th, dcdp=dcdp, **TKW)
+    out = geo.rtm2d_tti(v, e, d, th, dcdp=dcdp, **TKW)
+    assert np.abs(ill).max() > 0 and np.abs(ag).max() > 0
+    assert out["adcigs"].shape == (91 // dcdp, 65, 60)
+    assert np.array_equal(out["shots"], shots)
+    assert np.array_equal(out["illum"], ill)
+    assert np.array_equal(out["mig_lap"], orc.laplace2d_adj(mig))
+    assert np.array_equal(out["adcigs"], ag), rel_l2(out["adcigs"], ag)
+
+
+def test_rtm2d_tti_program_observed_shots_device(geo, orc):
+    import torch
+    v, e, d, th = _model(nx=80, nz=50, seed=6)
+    kw = dict(TKW, ns=1, nt=400)
+    obs = np.random.default_rng(7).standard_normal((1, 80, 400)).astype(np.float32) * 1e-3
+    mig, ill, ag, _ = orc.rtm2d_tti(v, e, d, th, obs=obs, **kw)
+    t = [torch.from_numpy(a).cuda() for a in (v, e, d, th, obs)]
+    out = geo.rtm2d_tti(*t[:4], obs=t[4], **kw)
+    assert out["mig_lap"].is_cuda
+    assert np.array_equal(out["mig_lap"].cpu().numpy(), orc.laplace2d_adj(mig))
+    assert np.array_equal(out["adcigs"].cpu().numpy(), ag)
