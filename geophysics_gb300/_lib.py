@@ -97,6 +97,12 @@ def lib():
         "geo_su_replace_data": (_i, [C.c_char_p, C.c_char_p, C.c_char_p, _i, _i]),
         "geo_rtm2d_gpu": (_i, [C.POINTER(RTM2DGpuDesc)] + [_vp] * 9 + [_i, _vp]),
         "geo_rtm2d_tti": (_i, [C.POINTER(RTM2DGpuDesc)] + [_vp] * 9 + [_i, _vp]),
+        "geo_smooth_lines": (_i, [_vp, _i, C.c_longlong, C.c_longlong, C.c_longlong, _i, _i, _vp]),
+        "geo_smooth2d": (_i, [_i, _i, _i, _i, _vp, _i, _vp]),
+        "geo_adcig_smooth_stack": (_i, [_i, _i, _i, _i, _vp, _vp, _i, _vp]),
+        "geo_mute_direct": (_i, [_i, _i, _f, _f, _f, _f, _i, _i, _i, _i, _f, _f, _i, _vp, _i, _vp]),
+        "geo_smooth_model3d": (_i, [_i, _i, _i, _i, _i, _vp, _i, _vp]),
+        "geo_smooth_model2d": (_i, [_i, _i, _i, _i, _vp, _i, _vp]),
         "geo_tti2d_shot": (_i, [C.POINTER(FD2DDesc), _vp, _vp, _vp, _vp, _vp, _vp, _i, _i, _vp]),
         "geo_ae_create": (_i, [C.POINTER(_vp), C.c_ulonglong]),
         "geo_ae_destroy": (_i, [_vp]),

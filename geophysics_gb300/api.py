@@ -268,6 +268,68 @@ def rtm2d_tti(v, e, d, theta, *, npml, nt, dx, dz, dt, favg, ns=1, fs=1, ds=0, z
     return out
 
 
+def _inplace_copy(b, a):
+    """A float32 contiguous copy of `a` on the same side, and its pointer."""
+    if b.dev:
+        c = a.to(_torch().float32).contiguous().clone()
+        return c, C.c_void_p(c.data_ptr())
+    c = np.array(a, dtype=np.float32, order="C", copy=True)
+    return c, C.c_void_p(c.ctypes.data)
+
+
+def smooth2d(v, rx, rz):
+    """smooth2float of the MPI RTM program on v (nx, nz): rx 3-point passes
+    along x, then rz along z.  Returns a new array."""
+    b = _Bufs(v)
+    nx, nz = v.shape
+    out, p = _inplace_copy(b, v)
+    check(lib().geo_smooth2d(nx, rx, nz, rz, p, b.mem, b.stream()), "geo_smooth2d")
+    return out
+
+
+def adcig_smooth_stack(adcig, passes=10):
+    """The MPI RTM program's smoothed angle gathers and their stack: adcig
+    shaped (na, nx, nz) as rtm2d_batch(adcig=True) returns it.  Returns
+    (smoothed gathers, stack (nx, nz))."""
+    b = _Bufs(adcig)
+    na, nx, nz = adcig.shape
+    g, pg = _inplace_copy(b, adcig)
+    stk, ps = b.out((nx, nz), adcig)
+    check(lib().geo_adcig_smooth_stack(nx, nz, na, passes, pg, ps, b.mem, b.stream()), "geo_adcig_smooth_stack")
+    return g, stk
+
+
+def mute_direct(shot, *, dt, favg, dx, dz, fs, ds, zs, is_, vp, epsilon=0.0, tt=190):
+    """The direct-wave mute utility on one trace-major record shot (nx, nt);
+    returns a new array."""
+    b = _Bufs(shot)
+    nx, nt = shot.shape
+    out, p = _inplace_copy(b, shot)
+    check(lib().geo_mute_direct(nx, nt, dt, favg, dx, dz, fs, ds, zs, is_, vp, epsilon, tt, p, b.mem, b.stream()),
+          "geo_mute_direct")
+    return out
+
+
+def smooth_model3d(v, passes=20, mmz=20):
+    """The 3D model smoother utility on v shaped (ny, nx, nz); returns a new
+    array (host sweep, see geo_smooth_model3d)."""
+    b = _Bufs(v)
+    ny, nx, nz = v.shape
+    out, p = _inplace_copy(b, v)
+    check(lib().geo_smooth_model3d(nx, ny, nz, passes, mmz, p, b.mem, b.stream()), "geo_smooth_model3d")
+    return out
+
+
+def smooth_model2d(v, passes=100, z0=31):
+    """The 2D model smoother utility on v shaped (nx, nz), rows z >= z0;
+    returns a new array."""
+    b = _Bufs(v)
+    nx, nz = v.shape
+    out, p = _inplace_copy(b, v)
+    check(lib().geo_smooth_model2d(nx, nz, z0, passes, p, b.mem, b.stream()), "geo_smooth_model2d")
+    return out
+
+
 def morton_order():
     """perm[m] = natural index (z + 16*x + 256*y) of Morton index m of a
     16^3 block (bit 3l = z bit l, 3l+1 = x bit l, 3l+2 = y bit l)."""

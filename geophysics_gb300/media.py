@@ -70,3 +70,47 @@ def layered_random_vti(nx, nz, seed=3, corr=40.0, amp=0.05, **kw):
     G = G / max(np.abs(G).max(), 1e-30)
     f = (1.0 + amp * G).astype(np.float32)
     return (v * f).astype(np.float32), (e * f).astype(np.float32), (d * f).astype(np.float32)
+
+
+def interface_model(nx, nz, tops, values, base, ny=None):
+    """Layered medium by interfaces, the rule of the reference's generators
+    (utils-getBinaryMedia-c/Toa_vtiMedia.c:27-60, 3D-vti-fd+rtm-cuda/
+    Toa_vel3.c:37-51): a cell takes `base`, then values[k] for every
+    interface k (in order, later ones win) whose depth it lies strictly below
+    (iz > top).  tops[k] is a depth in cells, or an array over x (a curved
+    interface such as `anticline_profile`).  Returns float32 (nx, nz), or
+    (ny, nx, nz) when ny is given (interfaces constant along y)."""
+    iz = np.arange(nz)[None, :]
+    a = np.full((nx, nz), base, np.float32)
+    for top, val in zip(tops, values):
+        t = np.broadcast_to(np.asarray(top, np.float64).reshape(-1, 1) if np.ndim(top) else top, (nx, 1))
+        a = np.where(iz > t, np.float32(val), a)
+    a = a.astype(np.float32)
+    return a if ny is None else np.ascontiguousarray(np.broadcast_to(a, (ny, nx, nz)))
+
+
+def anticline_profile(nx, x0, x1, x2, x3, z_flank, z_crest):
+    """Depth of an anticline-shaped interface over x, as the generators'
+    `layer` arrays (utils-getBinaryMedia-c/Toa_vel.c:27-34: 150 / rising
+    0.5 per cell / 200 / falling / 150 with breaks at x = 150, 250, 350,
+    450; Toa_vel3.c:29-35 the same at 25, 75, 125, 175 from 100 to 125):
+    z_flank before x0 and from x3 on, a linear ramp from x0 to x1 and back
+    down from x2 to x3, z_crest between x1 and x2.  float32 (nx,)."""
+    k = np.arange(nx, dtype=np.float64)
+    up = (z_crest - z_flank) / float(x1 - x0)
+    down = (z_crest - z_flank) / float(x3 - x2)
+    z = np.full(nx, float(z_flank))
+    z = np.where((k >= x0) & (k < x1), up * (k - x0) + z_flank, z)
+    z = np.where((k >= x1) & (k < x2), z_crest, z)
+    z = np.where((k >= x2) & (k < x3), -down * (k - x2) + z_crest, z)
+    return z.astype(np.float32)
+
+
+def vti_layers_media(nx, nz=2500):
+    """The VTI media generator's model (Toa_vtiMedia.c, 10000 x 2500 there):
+    interfaces below rows 500, 1000, 1500, 2000; vp 2000/2600/3300/3800/4500,
+    eps 0/0.07/0.12/0.19/0.25, del 0/0.02/0.05/0.08/0.1.  Returns v, e, d (nx, nz)."""
+    tops = (500, 1000, 1500, 2000)
+    return (interface_model(nx, nz, tops, (2600, 3300, 3800, 4500), 2000.0),
+            interface_model(nx, nz, tops, (0.07, 0.12, 0.19, 0.25), 0.0),
+            interface_model(nx, nz, tops, (0.02, 0.05, 0.08, 0.1), 0.0))

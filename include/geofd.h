@@ -306,6 +306,45 @@ int geo_laplace2d(int nx, int nz, const float *in, float *out, int mem, void *st
  * Toa_gpu_3dvti_rtm_adcigs_1orderfunction.cu:555-616). */
 int geo_laplace3d(int nx, int ny, int nz, const float *in, float *out, int mem, void *stream);
 
+/* ---- post-processing and model tools --------------------------------
+ * geo_smooth_lines: `passes` Jacobi passes of 3-point averaging along
+ *   nlines lines of n samples, sample k of line l at v[l*line_stride +
+ *   k*elem_stride] -- smooth1float of the MPI RTM program
+ *   (2D-vti-fd+rtm-mpi/Toa_rtm_vti_adcig_cdp.c:1642-1664): inside
+ *   (v[k-1]+v[k]+v[k+1])/3, ends (v[0]+v[1])/2 and (v[n-1]+v[n-2])/2.
+ *   n <= 24576.
+ * geo_smooth2d: smooth2float (:1607-1639) on v[ix*nz + iz]: rx passes along
+ *   x for every iz, then rz passes along z for every ix.
+ * geo_adcig_smooth_stack: the program's smoothed gathers and angle stack
+ *   (:416-437): adcig[ia][ix][iz] (na*nx*nz, the geo_rtm2d_batch_adcig
+ *   order) smoothed in place along ia with `passes` passes (10 in the
+ *   program); stack (optional, nx*nz) = sum over ia in order.
+ * geo_mute_direct: the direct-wave mute utility
+ *   (2D-vti-fd+rtm-cuda/functions/shot_muteDirect.c:11-33) on a trace-major
+ *   record shot[ix*nt + it]: zero (t0/dt - tt, t0/dt + 2/(dt favg) + tt),
+ *   t0 = sqrt(offset^2 + (dz zs)^2) / (vp sqrtf(1+2 epsilon)) in double,
+ *   offset = dx |ix - fs - (is-1) ds|. */
+int geo_smooth_lines(float *v, int n, long long nlines, long long line_stride, long long elem_stride, int passes,
+                     int mem, void *stream);
+int geo_smooth2d(int nx, int rx, int nz, int rz, float *v, int mem, void *stream);
+int geo_adcig_smooth_stack(int nx, int nz, int na, int passes, float *adcig, float *stack, int mem, void *stream);
+int geo_mute_direct(int nx, int nt, float dt, float favg, float dx, float dz, int fs, int ds, int zs, int is,
+                    float vp, float epsilon, int tt, float *shot, int mem, void *stream);
+
+/* In-place model smoothers.  Both sweep the model Gauss-Seidel fashion
+ * (each update reads neighbours already updated in the same pass), so the
+ * result depends on the visiting order; they run on the host in the
+ * programs' order (device buffers are copied through the host).
+ * geo_smooth_model3d: utils-3D-smooth-f95/Toa_smooth3D.c:50-161 on
+ *   v[iz + nz*(ix + nx*iy)]: `passes` passes over z >= mmz (1 <= mmz <= nz-2)
+ *   -- 27-point inner average, 18-point faces, 12-point edges, 8-point
+ *   corners; reads past a z column follow the program's memory layout.
+ * geo_smooth_model2d: utils-3D-smooth-f95/smooth.f95:44-70 on v[ix*nz + iz]:
+ *   `passes` passes of the 3x3 (1 2 1) weighted average over rows iz >= z0
+ *   (the program's nzs - 1), with its 9- and 12-point edge forms. */
+int geo_smooth_model3d(int nx, int ny, int nz, int passes, int mmz, float *v, int mem, void *stream);
+int geo_smooth_model2d(int nx, int nz, int z0, int passes, float *v, int mem, void *stream);
+
 /* ---- SU / SEG-Y traces ------------------------------------------------
  * A trace = 240-byte header (the segy struct of hc/cjbsegy.h) + ns floats.
  * geo_su_read: ntr traces into data[ntr*ns] (samples byte-swapped when

@@ -296,3 +296,54 @@ def ref_laplace2d_adj(img):
     nx, nz = img.shape
     L.laplac2_lop(1, nz, nx, _fp(img), _fp(out))
     return out
+
+
+def _rows(a):
+    """float** of the rows of a C-contiguous 2D float32 array."""
+    return (C.POINTER(C.c_float) * a.shape[0])(*[a[i].ctypes.data_as(C.POINTER(C.c_float)) for i in range(a.shape[0])])
+
+
+def ref_smooth2float(v, rx, rz):
+    """The MPI RTM program's smooth2float on a copy of v (nx, nz)."""
+    L = C.CDLL(os.path.join(REF, "librefrtm.so"))
+    L.smooth2float.restype = None
+    L.smooth2float.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p]
+    a = np.array(v, dtype=_f, copy=True, order="C")
+    rows = _rows(a)
+    L.smooth2float(a.shape[0], rx, a.shape[1], rz, rows)
+    return a
+
+
+def ref_mute_direct(shot, *, dt, favg, dx, dz, fs, ds, zs, is_, vp, epsilon=0.0, tt=190):
+    """The direct-wave mute utility's mute_directwave on a copy of shot (nx, nt)."""
+    L = C.CDLL(os.path.join(REF, "librefmute.so"))
+    L.mute_directwave.restype = None
+    L.mute_directwave.argtypes = [C.c_int, C.c_int, C.c_float, C.c_float, C.c_float, C.c_float] + [C.c_int] * 4 + \
+        [C.c_float, C.c_float, C.POINTER(C.c_float), C.c_int]
+    a = np.array(shot, dtype=_f, copy=True, order="C")
+    L.mute_directwave(a.shape[0], a.shape[1], dt, favg, dx, dz, fs, ds, zs, is_, vp, epsilon, _fp(a), tt)
+    return a
+
+
+_SMOOTH3D_RUN = r"""
+import ctypes as C, sys
+L = C.CDLL(sys.argv[1])
+L.ref_smooth3d_main()
+C.CDLL(None).fflush(None)   # the program leaves its output stream open
+"""
+
+
+def ref_smooth3d(v):
+    """The reference 3D model smoother (utils-3D-smooth-f95/Toa_smooth3D.c) run
+    through its file interface on v shaped (70, 70, 70) as (y, x, z): 20
+    passes from z = 20.  Runs in a child process (the program works in its
+    current directory and leaves its output file open)."""
+    import subprocess
+    import sys
+    v = c32(v)
+    assert v.shape == (70, 70, 70)
+    with tempfile.TemporaryDirectory() as td:
+        v.tofile(os.path.join(td, "vel707070.dat"))
+        subprocess.run([sys.executable, "-c", _SMOOTH3D_RUN, os.path.join(REF, "librefsmooth3d.so")], cwd=td,
+                       check=True, capture_output=True)
+        return np.fromfile(os.path.join(td, "vel707070initial.dat"), _f).reshape(70, 70, 70)
