@@ -1,0 +1,72 @@
+"""Parity at the benchmark workloads' full sizes.  The CPU oracle finishes
+the 2D shot at full size, so that one is compared bit for bit; the 3D shot
+and the 128-shot batch are checked through properties that hold at any size
+(the oracle would take hours there):
+
+* 2D VTI FD, 401x401 + 50 sponge, 2000 steps, CPU-program arithmetic:
+  the record equals the oracle's (itself pinned to the reference program);
+* 3D VTI FD, 400^3 + 40 sponge, 2500 steps (the headline shot): the fast
+  stress form's record is within rel-L2 1e-5 of the exact form's (the exact
+  form equals the oracle bit for bit at test sizes);
+* batched 2D RTM, 128 shots on 2401x601, widths 401-1199, 3000 steps: the
+  stack is the shot-ordered sum of the per-shot images, and a shot of the
+  batch equals the same shot run alone.
+"""
+import numpy as np
+import pytest
+
+from tests.util import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+
+def test_fd2d_401_fullsize_bit_exact(geo, orc):
+    from geophysics_gb300 import media
+    npd, nt = 50, 2000
+    v, e, d = media.layered_vti(401, 401, seed=1)
+    got = geo.fd2d_shot(v, e, d, npd=npd, nt=nt, dx=10.0, dz=10.0, dt=1e-3, favg=20.0, fs=200, zs=5,
+                        variant="cpu", rec_iz=npd + 4)
+    want = orc.fd2d(v, e, d, npd=npd, nt=nt, dx=10.0, dz=10.0, dt=np.float32(1e-3), favg=20.0, pfac=10.0, fs=200,
+                    zs=5, rec_iz=npd + 4)
+    assert np.abs(want).max() > 0
+    assert np.array_equal(got, want), rel_l2(got, want)
+
+
+def test_fd3d_400cube_fast_form_within_1e5_of_exact(geo):
+    import torch
+
+    from bench import make_model, plan_kwargs
+    v, e, d = make_model()
+    kw = {k: x for k, x in plan_kwargs().items() if k not in ("nx", "ny", "nz")}
+    exact = geo.fd3d_shot(v, e, d, **dict(kw, mode="exact"))
+    fast = geo.fd3d_shot(v, e, d, **dict(kw, mode="fast"))
+    assert fast.shape == exact.shape
+    a, b = exact.double(), fast.double()
+    assert torch.isfinite(b).all() and a.abs().max() > 0
+    rel = float(torch.linalg.vector_norm(b - a) / torch.linalg.vector_norm(a))
+    assert rel < 1e-5, rel
+
+
+def test_rtm2d_batch_128_shots_fullsize(geo):
+    import torch
+
+    from geophysics_gb300 import media
+    nx, nz, npd, nt, ns = 2401, 601, 50, 3000, 128
+    v, e, d = media.layered_random_vti(nx, nz, seed=3)
+    rng = np.random.default_rng(3)
+    widths = (rng.integers(200, 600, ns) * 2 + 1).astype(int)
+    xs = np.round(np.linspace(601, 1801, ns)).astype(int)
+    kw = dict(npd=npd, nt=nt, dx=10.0, dz=10.0, dt_ms=1.0, favg=20.0, pfac=10.0, zs=5, laplace=False, per_shot=True)
+    tv, te, td = (torch.from_numpy(a).cuda() for a in (v, e, d))
+    stack, per = geo.rtm2d_batch(tv, te, td, shot_x=xs, shot_nxs=widths, **kw)
+    stack = stack.cpu().numpy()
+    per = [p.cpu().numpy() for p in per]
+    acc = np.zeros((nx, nz), np.float32)
+    for k in range(ns):
+        off = int(xs[k]) - int(widths[k]) // 2 - 1          # window of shot k (model_vti_get_boundry)
+        acc[off:off + int(widths[k])] += per[k]
+    assert np.isfinite(stack).all() and np.abs(stack).max() > 0
+    assert np.array_equal(stack, acc)
+    for k in (0, 64, 127):
+        _, alone = geo.rtm2d_batch(tv, te, td, shot_x=[int(xs[k])], shot_nxs=[int(widths[k])], **kw)
+        assert np.array_equal(alone[0].cpu().numpy(), per[k]), k
