@@ -508,7 +508,7 @@ def run_rtm2d_case(args):
     from geophysics_gb300 import media
     from geophysics_gb300 import build as B
     B.build()
-    nx, nz, npd, nt, ns = 2401, 601, 50, 3000, 128
+    nx, nz, npd, nt, ns = 2401, 601, 50, args.nt, args.shots
     v, e, d = media.layered_random_vti(nx, nz, seed=3)
     rng = np.random.default_rng(3)
     widths = (rng.integers(200, 600, ns) * 2 + 1).astype(int)
@@ -539,7 +539,8 @@ def run_rtm2d_case(args):
     print(json.dumps({"case": "rtm2d", "metric": "shots/hr", "value": ns * 3600.0 / sec, "unit": "shots/hr",
                       "seconds": sec, "grid_pt_updates_per_s": upd / sec / 1e9,
                       "image_finite": bool(torch.isfinite(torch.as_tensor(img)).all()),
-                      "config": {"workload": "128-shot batched 2D VTI RTM, 2401x601, widths 401-1199, 3000 steps"},
+                      "config": {"workload": "%d-shot batched 2D VTI RTM, 2401x601, widths 401-1199, %d steps"
+                                             % (ns, nt)},
                       "cpu_baseline": cpu, "dtype": "f32"}), flush=True)
 
 
@@ -552,7 +553,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--case", default="full", choices=["full", "small", "traffic", "rtm-learned", "rtm-methods", "fd2d", "rtm2d"],
                     help="small / traffic: ncu profiling cases; rtm-learned: the learned-codec RTM comparison")
-    ap.add_argument("--nt", type=int, default=3000, help="rtm-learned: time steps")
+    ap.add_argument("--nt", type=int, default=3000, help="rtm-learned, rtm2d: time steps")
+    ap.add_argument("--shots", type=int, default=128, help="rtm2d: shots in the batch (the workload has 128)")
     ap.add_argument("--err-nt", type=int, default=1200, help="rtm-learned: steps of the image-error comparison")
     ap.add_argument("--train-iters", type=int, default=16000, help="rtm-learned: codec training steps")
     ap.add_argument("--escape", type=float, default=0.03, help="rtm-learned: escaped-block budget")
