@@ -575,3 +575,31 @@ class Par:
 
 def read_par(path):
     return Par(path)
+
+
+def _par_run(fn, path, out_shape, device, like):
+    """geo_fd2d / geo_fd3d / geo_rtm2d on a par file; with out_shape, also
+    into a fresh CUDA tensor of that shape (returned)."""
+    par = Par(path)
+    out, ptr, stream = None, None, None
+    if out_shape is not None:
+        t = _torch()
+        out = t.empty(out_shape, dtype=t.float32, device="cuda" if like is None else like)
+        ptr, stream = C.c_void_p(out.data_ptr()), C.c_void_p(t.cuda.current_stream().cuda_stream)
+    check(getattr(lib(), fn)(par._p, device, ptr, stream), fn)
+    return out
+
+
+def fd2d_par(path, device=-1, out_shape=None):
+    """The shots of GPU_vti2dfd / CPU_vti2dfd from a par file (see geo_fd2d)."""
+    return _par_run("geo_fd2d", path, out_shape, device, None)
+
+
+def fd3d_par(path, device=-1, out_shape=None):
+    """The shots of GPU_vti3dfd from a par file (see geo_fd3d)."""
+    return _par_run("geo_fd3d", path, out_shape, device, None)
+
+
+def rtm2d_par(path, device=-1, out_shape=None):
+    """The MPI RTM program from a par file (see geo_rtm2d)."""
+    return _par_run("geo_rtm2d", path, out_shape, device, None)

@@ -83,7 +83,9 @@ extern "C" int geo_laplace3d(int nx, int ny, int nz, const float *in, float *out
 }
 
 // ---------------------------------------------------------------- file I/O
-static int read_floats(const char *fn, size_t n, std::vector<float> &out) {
+namespace geo {
+
+int read_floats(const char *fn, size_t n, std::vector<float> &out) {
     FILE *fp = fopen(fn, "rb");
     if (!fp) return fail(GEO_ERR_IO, "cannot open <%s>", fn);
     out.resize(n);
@@ -93,11 +95,13 @@ static int read_floats(const char *fn, size_t n, std::vector<float> &out) {
     return GEO_OK;
 }
 
-static int write_at(FILE *fp, size_t offset_bytes, const float *a, size_t n) {
+int write_at(FILE *fp, size_t offset_bytes, const float *a, size_t n) {
     if (fseek(fp, (long)offset_bytes, SEEK_SET) != 0) return fail(GEO_ERR_IO, "seek failed");
     if (fwrite(a, 4, n, fp) != n) return fail(GEO_ERR_IO, "write failed");
     return GEO_OK;
 }
+
+}  // namespace geo
 
 static void report(const char *who, int st) {
     if (st != GEO_OK) fprintf(stderr, "%s: %s (%s)\n", who, geo_strerror(st), g_last_error);

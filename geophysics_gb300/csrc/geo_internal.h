@@ -93,6 +93,10 @@ void mute_window_3d_band(int nx, int ny, int nt, float dt, float favg, float dx,
 // entries each.
 void adcig_angle_tables(int nangle, int dangle, float *thr, float *cs);
 
+// Raw float32 files: read exactly n values; write n values at a byte offset.
+int read_floats(const char *fn, size_t n, std::vector<float> &out);
+int write_at(FILE *fp, size_t offset_bytes, const float *a, size_t n);
+
 // Model sanity: finite, velocity > 0.
 int check_model(const float *v, const float *e, const float *d, size_t n);
 

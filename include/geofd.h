@@ -420,6 +420,36 @@ int geo_par_get_float(const geo_par *par, const char *key, float *out);
 int geo_par_get_string(const geo_par *par, const char *key, char *out, int cap);
 void geo_par_free(geo_par *par);
 
+/* Runs driven by a loaded par file.  device >= 0 makes that GPU current for
+ * the call (the caller's current device is restored); -1 uses the current
+ * one.  The result goes to the par file's output files and, when the device
+ * pointer is not NULL, into that caller-owned device buffer as well.
+ *
+ * geo_fd2d: the shots of GPU_vti2dfd / CPU_vti2dfd
+ *   (2D-3D-vti-fd-cuda-gtk-GUI/GPU_vti2dfd_kernels.cu:301-444,
+ *   CPU_vti2dfd_kernels.c:366-510).  Keys, named after those functions'
+ *   arguments: nx nz dx dz npd nt dt (microseconds) favg ns fs ds zs FNv FNe
+ *   FNd; optional FNshot (ns records nx*nt, trace-major), FNsnap (padded P of
+ *   shot 1 every snap_every = 50 steps), SV, variant (gpu | cpu | mpi, default
+ *   gpu), pfac (10), wtype (1), rec_iz (npd), mute_tt (100 for gpu, else 0).
+ *   d_shots: ns*nx*nt.
+ * geo_fd3d: the shots of GPU_vti3dfd (GPU_vti3dfd_kernels.cu:371-573),
+ *   shots 0..ns-1.  Keys: nx ny nz dx dy dz npml nt dt (microseconds) favg ns
+ *   fsx fsy fsz FNv FNe FNd; optional dsx dsy dsz, FNshot, SV, mode (exact |
+ *   fast, default exact), pfac, wtype, rec_iz, rx0 drx nrx ry0 dry nry (every
+ *   surface node by default), mute_tt (100).  d_shots: ns*nt*nrx*nry.
+ * geo_rtm2d: the MPI RTM program (2D-vti-fd+rtm-mpi/Toa_rtm_vti_adcig_cdp.c:
+ *   59-481), shot is at fs_sxd + (is-1)*ds_sxd with an nxs-wide window.
+ *   Keys, its variable names: nx nz dx dz npd nt dt (ms) favg pfac ns_sxd
+ *   fs_sxd ds_sxd zs_sxd nxs FN1 FN2 FN3 (vp, epsilon, delta); optional seismic
+ *   (1 raw floats, 2 SU), laplace (0: the program's raw stack), FN6 (stacked
+ *   image), FN7 (per-shot images), FN8 (angle gathers, x-major), FN9
+ *   (smoothed gathers) and FN10 (their stack) as the program writes them.
+ *   d_image: nx*nz. */
+int geo_fd2d(const geo_par *par, int device, float *d_shots, void *stream);
+int geo_fd3d(const geo_par *par, int device, float *d_shots, void *stream);
+int geo_rtm2d(const geo_par *par, int device, float *d_image, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

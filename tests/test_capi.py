@@ -53,3 +53,21 @@ def test_missing_file_is_an_io_error(geo, tmp_path):
     with __import__("pytest").raises(geo.GeoError) as ei:
         geo.read_par(str(tmp_path / "nope.par"))
     assert ei.value.status == 3
+
+
+def test_par_runs_reject_incomplete_par_files(geo, tmp_path):
+    """geo_fd2d / geo_fd3d / geo_rtm2d check their keys before touching a
+    GPU: a missing key or an output nowhere to go is GEO_ERR_ARG."""
+    import pytest
+    p = tmp_path / "a.par"
+    p.write_text("nx= 10\nnz= 10\n")
+    for fn in (geo.fd2d_par, geo.fd3d_par, geo.rtm2d_par):
+        with pytest.raises(geo.GeoError) as ei:
+            fn(str(p))
+        assert ei.value.status == 1
+    q = tmp_path / "b.par"
+    q.write_text("nx= 10\nnz= 10\ndx= 10\ndz= 10\nnpd= 20\nnt= 10\ndt= 1000\nfavg= 20\nns= 1\nfs= 5\nds= 0\n"
+                 "zs= 1\nFNv= v\nFNe= e\nFNd= d\n")
+    with pytest.raises(geo.GeoError) as ei:
+        geo.fd2d_par(str(q))          # no FNshot and no device buffer
+    assert ei.value.status == 1

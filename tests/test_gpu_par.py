@@ -1,0 +1,100 @@
+"""Par-file runs (geo_fd2d, geo_fd3d, geo_rtm2d) against the same runs made
+through the library's descriptor entry points: files and device buffers
+bit-identical."""
+import numpy as np
+import pytest
+
+from tests.util import layered_model, random_model_3d
+
+pytestmark = pytest.mark.gpu
+
+
+def _write(tmp, name, a):
+    path = tmp / name
+    np.ascontiguousarray(a, np.float32).tofile(path)
+    return str(path)
+
+
+def _par(tmp, name, **kv):
+    path = tmp / name
+    path.write_text("".join("%12s= %s\n" % (k, v) for k, v in kv.items()))
+    return str(path)
+
+
+def test_fd2d_par(geo, tmp_path):
+    import torch
+    v, e, d = layered_model(61, 51, seed=2)
+    kw = dict(nx=61, nz=51, dx=10, dz=10, npd=20, nt=300, dt=1000, favg=20, ns=2, fs=20, ds=15, zs=3, SV=1,
+              FNv=_write(tmp_path, "v", v), FNe=_write(tmp_path, "e", e), FNd=_write(tmp_path, "d", d),
+              FNshot=str(tmp_path / "shot"), FNsnap=str(tmp_path / "snap"))
+    out = geo.fd2d_par(_par(tmp_path, "fd.par", **kw), device=0, out_shape=(2, 61, 300))
+    shots = np.fromfile(tmp_path / "shot", np.float32).reshape(2, 61, 300)
+    snaps = np.fromfile(tmp_path / "snap", np.float32).reshape(6, 101, 91)
+    for is_ in (1, 2):
+        ref = geo.fd2d_shot(v, e, d, npd=20, nt=300, dx=10.0, dz=10.0, dt=1e-3, favg=20.0, fs=20, ds=15, zs=3,
+                            is_=is_, variant="gpu", sv=1, mute_tt=100, snap_every=50 if is_ == 1 else 0)
+        rec = ref[0] if is_ == 1 else ref
+        assert np.abs(rec).max() > 0
+        assert np.array_equal(shots[is_ - 1], rec)
+        assert np.array_equal(out[is_ - 1].cpu().numpy(), rec)
+        if is_ == 1:
+            assert np.array_equal(snaps, ref[1])
+
+
+def test_fd3d_par(geo, tmp_path):
+    v, e, d = random_model_3d(20, 18, 22, seed=5)
+    kw = dict(nx=20, ny=18, nz=22, dx=10, dy=10, dz=10, npml=10, nt=200, dt=1000, favg=25, ns=2, fsx=6, fsy=8,
+              fsz=2, dsx=5, SV=1, mute_tt=5, FNv=_write(tmp_path, "v", v), FNe=_write(tmp_path, "e", e),
+              FNd=_write(tmp_path, "d", d), FNshot=str(tmp_path / "shot"))
+    out = geo.fd3d_par(_par(tmp_path, "fd3.par", **kw), out_shape=(2, 18, 20, 200))
+    shots = np.fromfile(tmp_path / "shot", np.float32).reshape(2, 18, 20, 200)
+    plan = geo.FD3DPlan(nx=20, ny=18, nz=22, npd=10, nt=200, dx=10.0, dy=10.0, dz=10.0, dt=1e-3, favg=25.0, fsx=6,
+                        fsy=8, fsz=2, dsx=5, sv=1, mode="exact", mute_tt=5)
+    try:
+        plan.set_model(v, e, d)
+        for is_ in (0, 1):
+            rec = plan.run_shot(is_)
+            assert np.abs(rec).max() > 0
+            assert np.array_equal(shots[is_], rec)
+            assert np.array_equal(out[is_].cpu().numpy(), rec)
+    finally:
+        plan.close()
+
+
+@pytest.mark.parametrize("seismic", [1, 2])
+def test_rtm2d_par(geo, tmp_path, seismic):
+    rng = np.random.default_rng(3)
+    v, e, d = layered_model(101, 50, seed=3, vlo=2000, vhi=2600)
+    v = v + rng.uniform(0, 40, v.shape).astype(np.float32)
+    names = {}
+    for k, a in (("FN1", v), ("FN2", e), ("FN3", d)):
+        if seismic == 2:
+            names[k] = str(tmp_path / (k + ".su"))
+            geo.su_write(names[k], a, dt_us=1000, big_endian=True)
+        else:
+            names[k] = _write(tmp_path, k, a)
+    outs = {k: str(tmp_path / k) for k in ("FN6", "FN7", "FN8", "FN9", "FN10")}
+    kw = dict(nx=101, nz=50, dx=10, dz=10, npd=15, nt=650, dt=1, favg=20, pfac=1000, ns_sxd=3, fs_sxd=35, ds_sxd=10,
+              zs_sxd=1, nxs=41, seismic=seismic, **names, **outs)
+    img_dev = geo.rtm2d_par(_par(tmp_path, "rtm.par", **kw), out_shape=(101, 50))
+    img, per, gathers = geo.rtm2d_batch(v, e, d, npd=15, nt=650, dx=10.0, dz=10.0, dt_ms=1.0, favg=20.0, pfac=1000.0,
+                                        zs=1, shot_x=[35, 45, 55], shot_nxs=[41] * 3, laplace=False, per_shot=True,
+                                        adcig=True)
+    sg, stk = geo.adcig_smooth_stack(gathers, 10)
+    f = lambda k: np.fromfile(outs[k], np.float32)
+    assert np.abs(img).max() > 0
+    assert np.array_equal(f("FN6").reshape(101, 50), img)
+    assert np.array_equal(img_dev.cpu().numpy(), img)
+    assert np.array_equal(f("FN7"), np.concatenate([p.ravel() for p in per]))
+    assert np.array_equal(f("FN8").reshape(101, 90, 50), gathers.transpose(1, 0, 2))
+    assert np.array_equal(f("FN9").reshape(101, 90, 50), sg.transpose(1, 0, 2))
+    assert np.array_equal(f("FN10").reshape(101, 50), stk)
+
+
+def test_par_device_out_of_range(geo, tmp_path):
+    v, e, d = layered_model(31, 31, seed=2)
+    kw = dict(nx=31, nz=31, dx=10, dz=10, npd=20, nt=50, dt=1000, favg=20, ns=1, fs=15, ds=0, zs=3,
+              FNv=_write(tmp_path, "v", v), FNe=_write(tmp_path, "e", e), FNd=_write(tmp_path, "d", d),
+              FNshot=str(tmp_path / "shot"))
+    with pytest.raises(geo.GeoError):
+        geo.fd2d_par(_par(tmp_path, "fd.par", **kw), device=4096)
