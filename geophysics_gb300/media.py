@@ -22,7 +22,7 @@ def random_vti(nx, ny, nz, seed=0, corr=40.0, vlo=1500.0, vhi=4500.0, jump=300.0
     fx = np.fft.fftfreq(nx)[None, :, None]
     fz = np.fft.rfftfreq(nz)[None, None, :]
     filt = np.exp(-2.0 * np.pi ** 2 * sig ** 2 * (fx ** 2 + fy ** 2 + fz ** 2))
-    G = np.fft.irfftn(np.fft.rfftn(noise) * filt, s=(ny, nx, nz))
+    G = np.fft.irfftn(np.fft.rfftn(noise) * filt, s=(ny, nx, nz), axes=(0, 1, 2))
     G = (G - G.min()) / max(G.max() - G.min(), 1e-30)
     span = vhi - vlo - interfaces * jump
     vp = vlo + span * G
