@@ -27,6 +27,7 @@
 #include "geo_internal.h"
 #include "fd3d.cuh"
 #include "fd3d_fused.cuh"
+#include "tc_util.cuh"
 #include <cudaTypedefs.h>
 
 namespace geo {
@@ -49,42 +50,12 @@ static_assert((OFF_V * 4) % 128 == 0 && (OFF_PH * 4) % 128 == 0 && (OFF_Q * 4) %
               "TMA destinations must stay 128-byte aligned");
 static_assert(kFusedSmem * 2 + 2048 <= 233472, "two blocks per SM must fit in shared memory");
 
-__device__ __forceinline__ uint32_t su32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(su32(bar)), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(su32(bar)), "r"(bytes) : "memory");
-}
-
-__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, 1000000;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(ok)
-        : "r"(su32(bar)), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-
-__device__ __forceinline__ uint64_t gtimer() {
-    uint64_t t;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-    return t;
-}
-
-// Wait for a stage with a 2 s limit; false on timeout.
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
-    if (mbar_try_wait(bar, parity)) return true;
-    const uint64_t t0 = gtimer();
-    while (!mbar_try_wait(bar, parity))
-        if (gtimer() - t0 > 2000000000ull) return false;
-    return true;
-}
+// mbarrier helpers with bounded waits (2 s), shared with the codec kernels
+using tc::gtimer;
+using tc::mbar_expect_tx;
+using tc::mbar_init;
+using tc::mbar_wait;
+using tc::su32;
 
 __device__ __forceinline__ void tma3(float *dst, const CUtensorMap *map, int c0, int c1, int c2, uint64_t *bar) {
     asm volatile(

@@ -37,12 +37,15 @@ __device__ __forceinline__ uint64_t gtimer() {
     return t;
 }
 
-// Wait for the phase of the given parity with a 2 s limit; false on timeout.
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
+// Wait for the phase of the given parity, giving up after limit_ns (2 s by
+// default); false on timeout.  Every pipeline wait in the library goes
+// through this, so a stage that never completes ends the kernel with an
+// error word the host reads instead of hanging the GPU.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, uint64_t limit_ns = 2000000000ull) {
     if (mbar_try_wait(bar, parity)) return true;
     const uint64_t t0 = gtimer();
     while (!mbar_try_wait(bar, parity))
-        if (gtimer() - t0 > 2000000000ull) return false;
+        if (gtimer() - t0 > limit_ns) return false;
     return true;
 }
 

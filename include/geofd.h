@@ -446,6 +446,14 @@ void geo_par_free(geo_par *par);
  *   image), FN7 (per-shot images), FN8 (angle gathers, x-major), FN9
  *   (smoothed gathers) and FN10 (their stack) as the program writes them.
  *   d_image: nx*nz. */
+/* Diagnostic without a reference counterpart: a kernel waits on a barrier
+ * that nothing arrives on, through the bounded wait every pipeline wait of
+ * the library uses, with a limit of limit_ms (1..2000).  *gave_up = 1 when
+ * the wait gave up and the kernel reported it; GEO_OK means the kernel ended
+ * and the context is usable -- what a stuck pipeline stage looks like to a
+ * caller of the 3D step or the codec (GEO_ERR_CUDA, "... timed out"). */
+int geo_selftest_bounded_wait(int limit_ms, int *gave_up, void *stream);
+
 int geo_fd2d(const geo_par *par, int device, float *d_shots, void *stream);
 int geo_fd3d(const geo_par *par, int device, float *d_shots, void *stream);
 int geo_rtm2d(const geo_par *par, int device, float *d_image, void *stream);
