@@ -350,7 +350,8 @@ extern "C" int geo_fd2d_shot(const geo_fd2d_desc *desc, const float *v, const fl
     B.S[0].rec_iz = D.rec_iz;
     B.S[0].rec_scale = D.rec_scale;
     B.S[0].rec_q = nullptr;
-    GEO_TRY(B.upload(8, 8, ss.cs));
+    const bool persistent = !(snap && snap_every > 0);
+    GEO_TRY(B.upload(persistent ? 16 : 8, 8, ss.cs));
     std::vector<float> amp;
     std::vector<uint8_t> on;
     source_amplitudes(var, D.nt, D.dt, D.favg, D.pfac, D.wtype, amp, on);
@@ -375,12 +376,27 @@ extern "C" int geo_fd2d_shot(const geo_fd2d_desc *desc, const float *v, const fl
             }
         }
     } else {
-        Graph G;
-        GEO_TRY(capture(G, ss.cs, [&]() -> int {
-            for (int it = 0; it < D.nt; it++) GEO_TRY(step(it));
-            return GEO_OK;
-        }));
-        GEO_TRY(G.launch(ss.cs));
+        // the whole shot in one cooperative launch (grid barriers between the
+        // half-steps, bounded waits reported through an error word)
+        DevBuf d_amp, d_on, d_sync;
+        GEO_TRY(d_amp.alloc((size_t)D.nt * 4));
+        GEO_TRY(d_on.alloc((size_t)D.nt));
+        GEO_TRY(d_sync.alloc(8));
+        GEO_TRY(d_sync.zero(ss.cs));
+        GEO_CUDA(cudaMemcpyAsync(d_amp.p, amp.data(), (size_t)D.nt * 4, cudaMemcpyHostToDevice, ss.cs));
+        GEO_CUDA(cudaMemcpyAsync(d_on.p, on.data(), (size_t)D.nt, cudaMemcpyHostToDevice, ss.cs));
+        Persist2D a{};
+        a.nt = D.nt;
+        a.taper = taper ? 1 : 0;
+        a.amp = d_amp.as<float>();
+        a.on = d_on.as<unsigned char>();
+        a.bar = d_sync.as<unsigned>();
+        a.err = d_sync.as<int>() + 1;
+        GEO_TRY(launch_fd2d_shot(var, B.d_S.as<Shot2D>(), B.d_items.as<int>(), (int)B.items.size(), B.by, a, ss.cs));
+        int err = 0;
+        GEO_CUDA(cudaMemcpyAsync(&err, a.err, 4, cudaMemcpyDeviceToHost, ss.cs));
+        GEO_CUDA(cudaStreamSynchronize(ss.cs));
+        if (err) return fail(GEO_ERR_CUDA, "2D shot: a grid barrier wait timed out");
     }
     DevBuf mlo, mhi, out;
     if (D.mute_tt > 0) {

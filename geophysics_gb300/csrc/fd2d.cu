@@ -13,6 +13,8 @@
 //             MPI program Toa_rtm_vti_adcig_cdp.c:1227-1327 (rho*vp^2 form,
 //             pz/qx chains in double after pow(1+2del, 0.5))
 #include "geo_internal.h"
+#include "tc_util.cuh"
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 
@@ -50,12 +52,21 @@ __device__ __forceinline__ bool locate(const Shot2D *shots, const int *item_shot
     return t.ix >= 4 && t.ix < sh->nnx - 4 && t.iz >= 4 && t.iz < sh->nnz - 4;
 }
 
+// Reads of neighbours' values.  Kernels of one half-step read fields that
+// no thread of the launch writes, through the read-only path (NC); the
+// persistent shot kernel reads values other blocks wrote before a grid
+// barrier, through L2 (the read-only path is not coherent with them).
+template <bool NC>
+__device__ __forceinline__ float ldf(const float *p) {
+    return NC ? __ldg(p) : __ldcg(p);
+}
+
 // P/Q read for the velocity update.  The GPU-form source (P,Q += amp at one
 // cell before the velocity update, GPU_vti2dfd_kernels.cu:423) is applied on
 // the fly to the taps that touch the source cell.
-template <bool PT_SRC>
+template <bool PT_SRC, bool NC>
 __device__ __forceinline__ float tap(const float *a, long idx, long src, float amp) {
-    float v = a[idx];
+    float v = NC ? a[idx] : __ldcg(a + idx);
     if (PT_SRC && idx == src) v = v + amp;
     return v;
 }
@@ -81,38 +92,145 @@ __device__ __forceinline__ int adcig_bin(float a1) {
     return lo == kAdcigAngles ? kAdcigAngles - 1 : lo;   // ia == 90 -> 89
 }
 
+// Velocity update of one updated point (ix, iz) of a shot, every field.
+template <int VARIANT, bool NC>
+__device__ __forceinline__ void vel_point(const Shot2D &sh, int ix, int iz, const Step2D &st) {
+    const int nnz = sh.nnz;
+    const long id = (long)ix * nnz + iz;
+    const bool pt_src = VARIANT == V_GPU && st.src_on;
+    const long src = (long)sh.ixs * nnz + sh.izs;
+    const bool near = pt_src && ((iz == sh.izs && abs(ix - sh.ixs) <= 4) || (ix == sh.ixs && abs(iz - sh.izs) <= 4));
+    for (int f = 0; f < st.nf; f++) {
+        const float *P = sh.P[f], *Q = sh.Q[f];
+        float xx = 0.0f, zz = 0.0f;
+        if (near) {
+#pragma unroll
+            for (int im = 0; im < 4; im++) {
+                xx += c_fd[im] * (tap<true, NC>(P, id + (im + 1) * nnz, src, st.amp) - tap<true, NC>(P, id - im * nnz, src, st.amp));
+                zz += c_fd[im] * (tap<true, NC>(Q, id + im + 1, src, st.amp) - tap<true, NC>(Q, id - im, src, st.amp));
+            }
+        } else {
+#pragma unroll
+            for (int im = 0; im < 4; im++) {
+                xx += c_fd[im] * (ldf<NC>(P + id + (im + 1) * nnz) - ldf<NC>(P + id - im * nnz));
+                zz += c_fd[im] * (ldf<NC>(Q + id + im + 1) - ldf<NC>(Q + id - im));
+            }
+        }
+        float *u = sh.u[f], *w = sh.w[f];
+        // u1 = coffx2*u0 - coffx1*dtx*xx (the MPI copy's extra *rho is *1.0f)
+        u[id] = sh.cx2[ix] * u[id] - sh.cx1[ix] * sh.dtx * xx;
+        w[id] = sh.cz2[iz] * w[id] - sh.cz1[iz] * sh.dtz * zz;
+    }
+}
+
 template <int VARIANT>
 __global__ void __launch_bounds__(256) k_vel2d(const Shot2D *__restrict__ shots, const int *__restrict__ item_shot,
                                                int nitems, Step2D st) {
     for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
         Tile2D t;
         if (!locate(shots, item_shot, item, t)) continue;
-        const Shot2D &sh = *t.sh;
-        const int nnz = sh.nnz;
-        const long id = (long)t.ix * nnz + t.iz;
-        const bool pt_src = VARIANT == V_GPU && st.src_on;
-        const long src = (long)sh.ixs * nnz + sh.izs;
-        const bool near = pt_src && ((t.iz == sh.izs && abs(t.ix - sh.ixs) <= 4) || (t.ix == sh.ixs && abs(t.iz - sh.izs) <= 4));
-        for (int f = 0; f < st.nf; f++) {
-            const float *P = sh.P[f], *Q = sh.Q[f];
-            float xx = 0.0f, zz = 0.0f;
-            if (near) {
+        vel_point<VARIANT, true>(*t.sh, t.ix, t.iz, st);
+    }
+}
+
+// Stress update of one updated point (ix, iz) of a shot, every field, and
+// the phase's epilogue (records and edge lines forward; image, illumination
+// and gathers backward).
+template <int VARIANT, int PHASE, bool NC>
+__device__ __forceinline__ void stress_point(const Shot2D &sh, int ix, int iz, const Step2D &st) {
+    const int nnz = sh.nnz;
+    const long id = (long)ix * nnz + iz;
+    const float vp = __ldg(sh.vp + id);
+    float e2 = __ldg(sh.e2 + id), d2 = 0.0f;
+    double pw = 0.0;
+    if (VARIANT == V_MPI) pw = __ldg(sh.pw + id);
+    else d2 = __ldg(sh.d2 + id);
+    if (st.taper) {
+        const int bx = ix - sh.tx0, bz = iz - sh.tz0;
+        if (bx >= 0 && bx < kTB && bz >= 0 && bz < kTB) {
+            e2 = sh.te2[bx * kTB + bz];
+            if (VARIANT == V_MPI) pw = sh.tpw[bx * kTB + bz];
+            else d2 = sh.td2[bx * kTB + bz];
+        }
+    }
+    const float ax1 = sh.ax1[ix], ax2 = sh.ax2[ix], az1 = sh.az1[iz], az2 = sh.az2[iz];
+    // Gaussian source window value (CPU/MPI forward), added after the split sum.
+    float s = 0.0f;
+    if ((VARIANT == V_CPU || VARIANT == V_MPI) && PHASE == PH_FWD && st.src_on) {
+        const int rx = ix - sh.ixs, rz = iz - sh.izs;
+        if (rx >= -3 && rx <= 3 && rz >= -3 && rz <= 3)
+            s = (float)((double)st.amp * c_gauss[(rx + 3) * 7 + (rz + 3)]);
+    }
+    float Pn[2], Qn[2];
+    for (int f = 0; f < st.nf; f++) {
+        const float *u = sh.u[f], *w = sh.w[f];
+        float xx = 0.0f, zz = 0.0f;
 #pragma unroll
-                for (int im = 0; im < 4; im++) {
-                    xx += c_fd[im] * (tap<true>(P, id + (im + 1) * nnz, src, st.amp) - tap<true>(P, id - im * nnz, src, st.amp));
-                    zz += c_fd[im] * (tap<true>(Q, id + im + 1, src, st.amp) - tap<true>(Q, id - im, src, st.amp));
-                }
-            } else {
-#pragma unroll
-                for (int im = 0; im < 4; im++) {
-                    xx += c_fd[im] * (__ldg(P + id + (im + 1) * nnz) - __ldg(P + id - im * nnz));
-                    zz += c_fd[im] * (__ldg(Q + id + im + 1) - __ldg(Q + id - im));
-                }
-            }
-            float *u = sh.u[f], *w = sh.w[f];
-            // u1 = coffx2*u0 - coffx1*dtx*xx (the MPI copy's extra *rho is *1.0f)
-            u[id] = sh.cx2[t.ix] * u[id] - sh.cx1[t.ix] * sh.dtx * xx;
-            w[id] = sh.cz2[t.iz] * w[id] - sh.cz1[t.iz] * sh.dtz * zz;
+        for (int im = 0; im < 4; im++) {
+            xx += c_fd[im] * (ldf<NC>(u + id + im * nnz) - ldf<NC>(u + id - (im + 1) * nnz));
+            zz += c_fd[im] * (ldf<NC>(w + id + im) - ldf<NC>(w + id - im - 1));
+        }
+        float px = sh.px[f][id], pz = sh.pz[f][id], qx = sh.qx[f][id], qz = sh.qz[f][id];
+        if (VARIANT == V_MPI) {
+            px = ax2 * px - ax1 * vp * e2 * sh.dtx * xx;
+            pz = (float)((double)(az2 * pz) - (double)(az1 * vp) * pw * (double)sh.dtz * (double)zz);
+            qx = (float)((double)(ax2 * qx) - (double)(ax1 * vp) * pw * (double)sh.dtx * (double)xx);
+            qz = az2 * qz - az1 * vp * sh.dtz * zz;
+        } else {
+            px = ax2 * px - ax1 * vp * vp * e2 * sh.dtx * xx;
+            pz = az2 * pz - az1 * vp * vp * d2 * sh.dtz * zz;
+            qx = ax2 * qx - ax1 * vp * vp * d2 * sh.dtx * xx;
+            qz = az2 * qz - az1 * vp * vp * sh.dtz * zz;
+        }
+        sh.px[f][id] = px; sh.pz[f][id] = pz; sh.qx[f][id] = qx; sh.qz[f][id] = qz;
+        float P, Q;
+        if ((VARIANT == V_CPU || VARIANT == V_MPI) && PHASE == PH_FWD) {
+            P = px + pz + s;
+            Q = qx + qz + s;
+        } else {
+            P = px + pz;
+            Q = qx + qz;
+        }
+        sh.P[f][id] = P;
+        sh.Q[f][id] = Q;
+        Pn[f] = P; Qn[f] = Q;
+    }
+    const int gx = ix - sh.npd, gz = iz - sh.npd;
+    if (PHASE == PH_FWD) {
+        // receiver gather at rec_iz, time-major
+        if (iz == sh.rec_iz && gx >= 0 && gx < sh.nx) {
+            const float r = sh.rec_scale == 2.0f ? Pn[0] + Pn[0] : Pn[0] * sh.rec_scale;
+            sh.rec_p[(long)st.it * sh.nx + gx] = r;
+            if (sh.rec_q) sh.rec_q[(long)st.it * sh.nx + gx] = Qn[0];
+        }
+        // interior-edge lines for the boundary-driven reconstruction
+        // (Toa_rtm_vti_adcig_cdp.c:668-683): top, bottom, left, right
+        if (sh.edge_p && gx >= 0 && gx < sh.nx && gz >= 0 && gz < sh.nz) {
+            const long L = 2L * sh.nx + 2L * sh.nz, b = (long)st.it * L;
+            if (gz == 0) { sh.edge_p[b + gx] = Pn[0]; sh.edge_q[b + gx] = Qn[0]; }
+            if (gz == sh.nz - 1) { sh.edge_p[b + sh.nx + gx] = Pn[0]; sh.edge_q[b + sh.nx + gx] = Qn[0]; }
+            if (gx == 0) { sh.edge_p[b + 2 * sh.nx + gz] = Pn[0]; sh.edge_q[b + 2 * sh.nx + gz] = Qn[0]; }
+            if (gx == sh.nx - 1) { sh.edge_p[b + 2 * sh.nx + sh.nz + gz] = Pn[0]; sh.edge_q[b + 2 * sh.nx + sh.nz + gz] = Qn[0]; }
+        }
+    } else if (st.nf == 2 && gx >= 0 && gx < sh.nx && gz >= 0 && gz < sh.nz) {
+        // zero-lag cross-correlation image and source illumination
+        // (Toa_rtm_vti_adcig_cdp.c:1067-1076): the illumination sum is
+        // formed in double, as pow() returns it, and a zero becomes 1
+        const long o = (long)gx * sh.nz + gz;
+        const float sv = Pn[0];
+        float ill = (float)((double)sh.ill[o] + (double)sv * (double)sv);
+        if (ill == 0.0f) ill = 1.0f;
+        sh.ill[o] = ill;
+        sh.mig[o] = sh.mig[o] + Pn[1] * sv;
+        if (sh.adcig) {
+            // Poynting vectors from the new P,Q and u,w of both fields
+            const float sx = -Pn[0] * sh.u[0][id], sz = -Qn[0] * sh.w[0][id];
+            const float gx = Pn[1] * sh.u[1][id], gz = Qn[1] * sh.w[1][id];
+            const float b1 = sx * sx + sz * sz, b2 = gx * gx + gz * gz, a = sx * gx + sz * gz;
+            const float a1 = (float)((double)a / ((double)sqrtf(b1 * b2) + 0.0000000000001));
+            const int ia = adcig_bin(a1);
+            float *ag = sh.adcig + (long)ia * sh.nx * sh.nz + o;
+            *ag = (float)((double)*ag + (double)(Pn[1] * sv) * c_adw[ia]);
         }
     }
 }
@@ -123,103 +241,94 @@ __global__ void __launch_bounds__(256) k_stress2d(const Shot2D *__restrict__ sho
     for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
         Tile2D t;
         if (!locate(shots, item_shot, item, t)) continue;
-        const Shot2D &sh = *t.sh;
-        const int nnz = sh.nnz, ix = t.ix, iz = t.iz;
-        const long id = (long)ix * nnz + iz;
-        const float vp = __ldg(sh.vp + id);
-        float e2 = __ldg(sh.e2 + id), d2 = 0.0f;
-        double pw = 0.0;
-        if (VARIANT == V_MPI) pw = __ldg(sh.pw + id);
-        else d2 = __ldg(sh.d2 + id);
-        if (st.taper) {
-            const int bx = ix - sh.tx0, bz = iz - sh.tz0;
-            if (bx >= 0 && bx < kTB && bz >= 0 && bz < kTB) {
-                e2 = sh.te2[bx * kTB + bz];
-                if (VARIANT == V_MPI) pw = sh.tpw[bx * kTB + bz];
-                else d2 = sh.td2[bx * kTB + bz];
-            }
-        }
-        const float ax1 = sh.ax1[ix], ax2 = sh.ax2[ix], az1 = sh.az1[iz], az2 = sh.az2[iz];
-        // Gaussian source window value (CPU/MPI forward), added after the split sum.
-        float s = 0.0f;
-        if ((VARIANT == V_CPU || VARIANT == V_MPI) && PHASE == PH_FWD && st.src_on) {
-            const int rx = ix - sh.ixs, rz = iz - sh.izs;
-            if (rx >= -3 && rx <= 3 && rz >= -3 && rz <= 3)
-                s = (float)((double)st.amp * c_gauss[(rx + 3) * 7 + (rz + 3)]);
-        }
-        float Pn[2], Qn[2];
-        for (int f = 0; f < st.nf; f++) {
-            const float *u = sh.u[f], *w = sh.w[f];
-            float xx = 0.0f, zz = 0.0f;
-#pragma unroll
-            for (int im = 0; im < 4; im++) {
-                xx += c_fd[im] * (__ldg(u + id + im * nnz) - __ldg(u + id - (im + 1) * nnz));
-                zz += c_fd[im] * (__ldg(w + id + im) - __ldg(w + id - im - 1));
-            }
-            float px = sh.px[f][id], pz = sh.pz[f][id], qx = sh.qx[f][id], qz = sh.qz[f][id];
-            if (VARIANT == V_MPI) {
-                px = ax2 * px - ax1 * vp * e2 * sh.dtx * xx;
-                pz = (float)((double)(az2 * pz) - (double)(az1 * vp) * pw * (double)sh.dtz * (double)zz);
-                qx = (float)((double)(ax2 * qx) - (double)(ax1 * vp) * pw * (double)sh.dtx * (double)xx);
-                qz = az2 * qz - az1 * vp * sh.dtz * zz;
-            } else {
-                px = ax2 * px - ax1 * vp * vp * e2 * sh.dtx * xx;
-                pz = az2 * pz - az1 * vp * vp * d2 * sh.dtz * zz;
-                qx = ax2 * qx - ax1 * vp * vp * d2 * sh.dtx * xx;
-                qz = az2 * qz - az1 * vp * vp * sh.dtz * zz;
-            }
-            sh.px[f][id] = px; sh.pz[f][id] = pz; sh.qx[f][id] = qx; sh.qz[f][id] = qz;
-            float P, Q;
-            if ((VARIANT == V_CPU || VARIANT == V_MPI) && PHASE == PH_FWD) {
-                P = px + pz + s;
-                Q = qx + qz + s;
-            } else {
-                P = px + pz;
-                Q = qx + qz;
-            }
-            sh.P[f][id] = P;
-            sh.Q[f][id] = Q;
-            Pn[f] = P; Qn[f] = Q;
-        }
-        const int gx = ix - sh.npd, gz = iz - sh.npd;
-        if (PHASE == PH_FWD) {
-            // receiver gather at rec_iz, time-major
-            if (iz == sh.rec_iz && gx >= 0 && gx < sh.nx) {
-                const float r = sh.rec_scale == 2.0f ? Pn[0] + Pn[0] : Pn[0] * sh.rec_scale;
-                sh.rec_p[(long)st.it * sh.nx + gx] = r;
-                if (sh.rec_q) sh.rec_q[(long)st.it * sh.nx + gx] = Qn[0];
-            }
-            // interior-edge lines for the boundary-driven reconstruction
-            // (Toa_rtm_vti_adcig_cdp.c:668-683): top, bottom, left, right
-            if (sh.edge_p && gx >= 0 && gx < sh.nx && gz >= 0 && gz < sh.nz) {
-                const long L = 2L * sh.nx + 2L * sh.nz, b = (long)st.it * L;
-                if (gz == 0) { sh.edge_p[b + gx] = Pn[0]; sh.edge_q[b + gx] = Qn[0]; }
-                if (gz == sh.nz - 1) { sh.edge_p[b + sh.nx + gx] = Pn[0]; sh.edge_q[b + sh.nx + gx] = Qn[0]; }
-                if (gx == 0) { sh.edge_p[b + 2 * sh.nx + gz] = Pn[0]; sh.edge_q[b + 2 * sh.nx + gz] = Qn[0]; }
-                if (gx == sh.nx - 1) { sh.edge_p[b + 2 * sh.nx + sh.nz + gz] = Pn[0]; sh.edge_q[b + 2 * sh.nx + sh.nz + gz] = Qn[0]; }
-            }
-        } else if (st.nf == 2 && gx >= 0 && gx < sh.nx && gz >= 0 && gz < sh.nz) {
-            // zero-lag cross-correlation image and source illumination
-            // (Toa_rtm_vti_adcig_cdp.c:1067-1076): the illumination sum is
-            // formed in double, as pow() returns it, and a zero becomes 1
-            const long o = (long)gx * sh.nz + gz;
-            const float sv = Pn[0];
-            float ill = (float)((double)sh.ill[o] + (double)sv * (double)sv);
-            if (ill == 0.0f) ill = 1.0f;
-            sh.ill[o] = ill;
-            sh.mig[o] = sh.mig[o] + Pn[1] * sv;
-            if (sh.adcig) {
-                // Poynting vectors from the new P,Q and u,w of both fields
-                const float sx = -Pn[0] * sh.u[0][id], sz = -Qn[0] * sh.w[0][id];
-                const float gx = Pn[1] * sh.u[1][id], gz = Qn[1] * sh.w[1][id];
-                const float b1 = sx * sx + sz * sz, b2 = gx * gx + gz * gz, a = sx * gx + sz * gz;
-                const float a1 = (float)((double)a / ((double)sqrtf(b1 * b2) + 0.0000000000001));
-                const int ia = adcig_bin(a1);
-                float *ag = sh.adcig + (long)ia * sh.nx * sh.nz + o;
-                *ag = (float)((double)*ag + (double)(Pn[1] * sv) * c_adw[ia]);
-            }
-        }
+        stress_point<VARIANT, PHASE, true>(*t.sh, t.ix, t.iz, st);
     }
+}
+
+// ------------------------------------------------------ persistent shot
+// Arrival counter read with acquire semantics at GPU scope.
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned *p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// Grid barrier of a cooperative launch: one arrival per block on a counter
+// that only grows (barrier k completes at k*gridDim.x arrivals).  The fence
+// before the arrival publishes the block's writes; the wait is bounded
+// (2 s) and a timeout sets the error word and ends the block, after which
+// every other block's next wait times out too.
+__device__ bool grid_barrier(unsigned *bar, unsigned target, int *err) {
+    __shared__ int s_ok;
+    __syncthreads();
+    if (threadIdx.x == 0 && threadIdx.y == 0) {
+        int ok = 1;
+        __threadfence();
+        atomicAdd(bar, 1u);
+        if (ld_acquire_u32(bar) < target) {
+            const uint64_t t0 = tc::gtimer();
+            while (ld_acquire_u32(bar) < target)
+                if (tc::gtimer() - t0 > 2000000000ull) {
+                    atomicExch(err, 1);
+                    ok = 0;
+                    break;
+                }
+        }
+        __threadfence();
+        s_ok = ok;
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
+// A whole single-shot forward run in one cooperative launch: per step the
+// velocity half-step over every tile, a grid barrier, the stress half-step
+// (records, edge lines), a grid barrier.  Same per-point arithmetic as the
+// per-half-step kernels; neighbours' values are read through L2.
+template <int VARIANT>
+__global__ void __launch_bounds__(512) k_fd2d_shot(const Shot2D *__restrict__ shots,
+                                                   const int *__restrict__ item_shot, int nitems, Persist2D a) {
+    unsigned k = 0;
+    for (int it = 0; it < a.nt; it++) {
+        Step2D st;
+        st.it = it;
+        st.amp = a.amp[it];
+        st.src_on = a.on[it];
+        st.taper = a.taper;
+        st.nf = 1;
+        for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
+            Tile2D t;
+            if (locate(shots, item_shot, item, t)) vel_point<VARIANT, false>(*t.sh, t.ix, t.iz, st);
+        }
+        if (!grid_barrier(a.bar, ++k * gridDim.x, a.err)) return;
+        for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
+            Tile2D t;
+            if (locate(shots, item_shot, item, t)) stress_point<VARIANT, PH_FWD, false>(*t.sh, t.ix, t.iz, st);
+        }
+        if (!grid_barrier(a.bar, ++k * gridDim.x, a.err)) return;
+    }
+}
+
+int launch_fd2d_shot(int variant, const Shot2D *d_shots, const int *d_item_shot, int nitems, int by, Persist2D a,
+                     cudaStream_t s) {
+    const void *fn = variant == V_CPU ? (const void *)k_fd2d_shot<V_CPU>
+                   : variant == V_GPU ? (const void *)k_fd2d_shot<V_GPU>
+                                      : (const void *)k_fd2d_shot<V_MPI>;
+    GEO_TRY(ensure_gauss());
+    int dev = 0, sms = 0, occ = 0, coop = 0;
+    GEO_CUDA(cudaGetDevice(&dev));
+    GEO_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    GEO_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
+    GEO_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, 32 * by, 0));
+    if (!coop || occ < 1) return fail(GEO_ERR_CUDA, "cooperative launch unavailable");
+    // every block resident at once (the barrier needs it; the cooperative
+    // launch checks it), blocks walking the tiles when there are more
+    const int grid = std::min(nitems, occ * sms);
+    if ((long long)grid * 2 * a.nt >= 4000000000LL) return fail(GEO_ERR_ARG, "too many steps for one launch");
+    dim3 block(32, by);
+    void *args[] = {(void *)&d_shots, (void *)&d_item_shot, (void *)&nitems, (void *)&a};
+    GEO_CUDA(cudaLaunchCooperativeKernel(fn, dim3(grid), block, args, 0, s));
+    return check_launch("fd2d_shot");
 }
 
 // Boundary-driven reconstruction and receiver injection before step it of

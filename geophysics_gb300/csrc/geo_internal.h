@@ -134,6 +134,17 @@ struct Step2D {
 
 enum Phase2D { PH_FWD = 0, PH_BWD = 1 };
 
+// A whole single-shot forward run in one cooperative launch (launch_fd2d_shot).
+struct Persist2D {
+    int nt, taper;
+    const float *amp;             // pfac*w(t) of every step
+    const unsigned char *on;      // source active at every step
+    unsigned *bar;                // grid-barrier arrival counter, zeroed
+    int *err;                     // set when a barrier wait gave up
+};
+int launch_fd2d_shot(int variant, const Shot2D *d_shots, const int *d_item_shot, int nitems, int by, Persist2D a,
+                     cudaStream_t s);
+
 int launch_vel2d(int variant, const Shot2D *d_shots, const int *d_item_shot, int nitems, int by,
                  int grid, Step2D st, cudaStream_t s);
 int launch_stress2d(int variant, int phase, const Shot2D *d_shots, const int *d_item_shot, int nitems,
