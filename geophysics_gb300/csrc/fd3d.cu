@@ -84,6 +84,66 @@ __global__ void k_image_illum(float *mig, const float *ill, long n) {
         if (ill[k] != 0.0f) mig[k] = mig[k] / ill[k];
 }
 
+static int grid_blocks(long n) { return (int)std::min<long>((n + 255) / 256, 152L * 16); }
+
+// Model set-up on the device.  First failing point of the host check
+// check_model (velocity, then eps/del finiteness, then 1+2 del >= 0), as
+// key = index*4 + kind; the smallest key is the host loop's first report.
+__global__ void k_check_model3d(const float *v, const float *e, const float *d, long n,
+                                unsigned long long *first) {
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+        int kind = 0;
+        if (!isfinite(v[i]) || !(v[i] > 0.0f)) kind = 1;
+        else if (!isfinite(e[i]) || !isfinite(d[i])) kind = 2;
+        else if (1 + 2 * d[i] < 0) kind = 3;
+        if (kind) atomicMin(first, (unsigned long long)i * 4 + (kind - 1));
+    }
+}
+
+// Edge-replicated padding (pad_vv3d, GPU_vti3dfd_kernels.cu:208-255: each
+// axis clamped to the interior) and the stencil's model arrays in
+// one pass, into the pitched layout: exact vp, 1+2eps, sqrtf(1+2del); fast
+// A = vp^2(1+2eps), B = vp^2 sqrtf(1+2del), C = vp^2 -- the host formulas,
+// float for float.
+__global__ void k_model3d(const float *v, const float *e, const float *d, int nx, int ny, int nz, int npd,
+                          int nnx, int nny, int nnz, int ldz, int fast, float *o0, float *o1, float *o2) {
+    const long n = (long)nnx * nny * nnz;
+    for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < n; k += (long)gridDim.x * blockDim.x) {
+        const int iz = (int)(k % nnz), ix = (int)((k / nnz) % nnx), iy = (int)(k / ((long)nnz * nnx));
+        const int sz = min(max(iz - npd, 0), nz - 1), sx = min(max(ix - npd, 0), nx - 1),
+                  sy = min(max(iy - npd, 0), ny - 1);
+        const long r = sz + (long)nz * (sx + (long)nx * sy);
+        const float pv = v[r], e2 = 1 + 2 * e[r], d2 = sqrtf(1 + 2 * d[r]);
+        const long o = iz + (long)ldz * (ix + (long)nnx * iy);
+        if (fast) {
+            const float c2 = pv * pv;
+            o0[o] = c2 * e2;
+            o1[o] = c2 * d2;
+            o2[o] = c2;
+        } else {
+            o0[o] = pv;
+            o1[o] = e2;
+            o2[o] = d2;
+        }
+    }
+}
+
+// The padded raw model on a B^3 box at (x0, y0, z0) (padded coordinates),
+// gathered from the unpadded arrays with the same edge replication; box
+// points outside the padded grid are left alone.
+__global__ void k_gather_box3d(const float *raw, int nx, int ny, int nz, int npd, int nnx, int nny, int nnz, long x0,
+                               long y0, long z0, int B, float *out) {
+    const long nb = (long)B * B * B, n0 = (long)nx * ny * nz;
+    for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < nb; k += (long)gridDim.x * blockDim.x) {
+        const long iz = z0 + k % B, ix = x0 + (k / B) % B, iy = y0 + k / ((long)B * B);
+        if (iz < 0 || iz >= nnz || ix < 0 || ix >= nnx || iy < 0 || iy >= nny) continue;
+        const long sz = min(max(iz - npd, 0L), (long)nz - 1), sx = min(max(ix - npd, 0L), (long)nx - 1),
+                   sy = min(max(iy - npd, 0L), (long)ny - 1);
+        const long r = sz + (long)nz * (sx + (long)nx * sy);
+        for (int a = 0; a < 3; a++) out[a * nb + k] = raw[a * n0 + r];
+    }
+}
+
 }  // namespace geo
 
 // One wavefield set: u,v,w,P,Q at two time levels (ping-pong), split stresses
@@ -109,7 +169,7 @@ struct geo_fd3d_plan {
     int chunk = 0, nitems = 0, ntz = 0, ntx = 0;
     std::vector<float> amp;
     std::vector<uint8_t> on;
-    std::vector<float> h_vp, h_eps, h_del;  // padded raw model, kept for the SV taper
+    DevBuf raw;                        // unpadded vp, eps, del (3 x nx*ny*nz), kept for the SV taper
     float vp1 = 0, eps1 = 0;           // padded model at linear index 1 (mute)
     bool model_set = false;
     bool tuned = false;
@@ -288,14 +348,19 @@ static int taper_box_3d(geo_fd3d_plan *p, int is, bool tapered, cudaStream_t s) 
                cz = D.fsz + (long)is * D.dsz + D.npd - 1;
     const int B = 31, R = 15, r = 4;
     const long n = (long)B * B * B;
-    std::vector<float> h(2 * n, 1.0f);
+    std::vector<float> h(2 * n, 1.0f), raw(3 * n, 0.0f);   // raw: padded vp, eps, del on the box
+    k_gather_box3d<<<(int)((n + 255) / 256), 256, 0, s>>>(p->raw.as<float>(), D.nx, D.ny, D.nz, D.npd, p->nnx, p->nny,
+                                                          p->nnz, cx - 15, cy - 15, cz - 15, B, p->box.as<float>());
+    GEO_TRY(check_launch("gather_box3d"));
+    GEO_CUDA(cudaMemcpyAsync(raw.data(), p->box.p, 3 * n * 4, cudaMemcpyDeviceToHost, s));
+    GEO_CUDA(cudaStreamSynchronize(s));
     for (int by = 0; by < B; by++)
         for (int bx = 0; bx < B; bx++)
             for (int bz = 0; bz < B; bz++) {
                 const long iz = cz - 15 + bz, ix = cx - 15 + bx, iy = cy - 15 + by;
                 if (iz < 0 || iz >= p->nnz || ix < 0 || ix >= p->nnx || iy < 0 || iy >= p->nny) continue;
-                const size_t id = iz + (size_t)p->nnz * (ix + (size_t)p->nnx * iy);
-                float ee = p->h_eps[id], dd = p->h_del[id];
+                const long k = bz + (long)B * (bx + (long)B * by);
+                float ee = raw[n + k], dd = raw[2 * n + k];
                 if (tapered) {
                     const int rx = (int)(ix - cx), ry = (int)(iy - cy), rz = (int)(iz - cz);
                     const int r2 = rx * rx + ry * ry + rz * rz;
@@ -308,10 +373,9 @@ static int taper_box_3d(geo_fd3d_plan *p, int is, bool tapered, cudaStream_t s) 
                         }
                     }
                 }
-                const long k = bz + (long)B * (bx + (long)B * by);
                 const float e2 = 1 + 2 * ee, d2 = sqrtf(1 + 2 * dd);
                 if (p->d.mode == GEO_MODE_FAST) {
-                    const float c2 = p->h_vp[id] * p->h_vp[id];
+                    const float c2 = raw[k] * raw[k];
                     h[k] = c2 * e2;
                     h[n + k] = c2 * d2;
                 } else {
@@ -436,7 +500,7 @@ int plan3d_create(geo_fd3d_plan **out, const geo_fd3d_desc *desc, int nfs) {
     if (st == GEO_OK) st = p->rec_tr.alloc(ntr * d.nt * 4);
     if (st == GEO_OK) st = p->mute_lo.alloc(ntr * 4);
     if (st == GEO_OK) st = p->mute_hi.alloc(ntr * 4);
-    if (st == GEO_OK) st = p->box.alloc((size_t)2 * 31 * 31 * 31 * 4);
+    if (st == GEO_OK) st = p->box.alloc((size_t)3 * 31 * 31 * 31 * 4);   // gathered raw box (3), tapered box (2)
     if (st == GEO_OK) st = p->err.alloc(16);
     if (st == GEO_OK) st = p->err.zero(nullptr);
     if (st != GEO_OK) {
@@ -461,11 +525,6 @@ extern "C" int geo_fd3d_plan_destroy(geo_fd3d_plan *p) {
 }
 
 // Copy a padded nnz-contiguous host volume into an ldz-strided device field.
-static int upload_pitched(geo_fd3d_plan *p, DevBuf &dst, const float *src, cudaStream_t s) {
-    GEO_CUDA(cudaMemcpy2DAsync(dst.p, (size_t)p->ldz * 4, src, (size_t)p->nnz * 4, (size_t)p->nnz * 4,
-                               (size_t)p->nnx * p->nny, cudaMemcpyHostToDevice, s));
-    return GEO_OK;
-}
 
 // Model upload: pad on the host, build the model arrays of the chosen form
 // and the sponge profiles (d0 from the padded centre velocity,
@@ -473,29 +532,57 @@ static int upload_pitched(geo_fd3d_plan *p, DevBuf &dst, const float *src, cudaS
 extern "C" int geo_fd3d_set_model(geo_fd3d_plan *p, const float *v, const float *e, const float *d, int mem,
                                   void *stream) {
     if (!p || !v || !e || !d) return fail(GEO_ERR_ARG, "null argument");
+    if (mem != GEO_MEM_HOST && mem != GEO_MEM_DEVICE) return fail(GEO_ERR_ARG, "bad mem kind");
     cudaStream_t s = (cudaStream_t)stream;
     const geo_fd3d_desc &D = p->d;
     const size_t n0 = (size_t)D.nx * D.ny * D.nz;
-    std::vector<float> hv, he, hd;
-    const float *sv = v, *se = e, *sd = d;
-    if (mem == GEO_MEM_DEVICE) {
-        hv.resize(n0); he.resize(n0); hd.resize(n0);
-        GEO_CUDA(cudaMemcpyAsync(hv.data(), v, n0 * 4, cudaMemcpyDeviceToHost, s));
-        GEO_CUDA(cudaMemcpyAsync(he.data(), e, n0 * 4, cudaMemcpyDeviceToHost, s));
-        GEO_CUDA(cudaMemcpyAsync(hd.data(), d, n0 * 4, cudaMemcpyDeviceToHost, s));
-        GEO_CUDA(cudaStreamSynchronize(s));
-        sv = hv.data(); se = he.data(); sd = hd.data();
-    } else if (mem != GEO_MEM_HOST) {
-        return fail(GEO_ERR_ARG, "bad mem kind");
+    // the unpadded model on the device (kept: the SV taper gathers from it)
+    if (p->raw.bytes != 3 * n0 * 4) GEO_TRY(p->raw.alloc(3 * n0 * 4));
+    float *raw = p->raw.as<float>();
+    const cudaMemcpyKind kin = mem == GEO_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    GEO_CUDA(cudaMemcpyAsync(raw, v, n0 * 4, kin, s));
+    GEO_CUDA(cudaMemcpyAsync(raw + n0, e, n0 * 4, kin, s));
+    GEO_CUDA(cudaMemcpyAsync(raw + 2 * n0, d, n0 * 4, kin, s));
+    // model check on the device, reported like check_model
+    GEO_CUDA(cudaMemsetAsync(p->box.p, 0xff, 8, s));
+    unsigned long long *first = reinterpret_cast<unsigned long long *>(p->box.p);
+    k_check_model3d<<<grid_blocks((long)n0), 256, 0, s>>>(raw, raw + n0, raw + 2 * n0, (long)n0, first);
+    GEO_TRY(check_launch("check_model3d"));
+    unsigned long long key = 0;
+    GEO_CUDA(cudaMemcpyAsync(&key, first, 8, cudaMemcpyDeviceToHost, s));
+    GEO_CUDA(cudaStreamSynchronize(s));
+    if (key != ~0ull) {
+        const size_t i = (size_t)(key >> 2);
+        float bad = 0;
+        GEO_CUDA(cudaMemcpy(&bad, raw + i, 4, cudaMemcpyDeviceToHost));
+        if ((key & 3) == 0) return fail(GEO_ERR_MODEL, "velocity[%zu]=%g", i, bad);
+        if ((key & 3) == 1) return fail(GEO_ERR_MODEL, "eps/del[%zu] not finite", i);
+        return fail(GEO_ERR_MODEL, "1+2*delta[%zu] < 0", i);
     }
-    GEO_TRY(check_model(sv, se, sd, n0));
-    std::vector<float> pv(p->n), pe(p->n), pd(p->n);
-    pad_model_3d(D.nx, D.ny, D.nz, D.npd, sv, pv.data());
-    pad_model_3d(D.nx, D.ny, D.nz, D.npd, se, pe.data());
-    pad_model_3d(D.nx, D.ny, D.nz, D.npd, sd, pd.data());
-    p->vp1 = pv[1];
-    p->eps1 = pe[1];
-    const float d0 = sponge_d0(V_GPU, 3, 0.0f, pv[(size_t)p->nny * p->nnx * p->nnz / 2], D.npd, D.dx, D.dy, D.dz);
+    // padded model arrays, written straight into the pitched layout
+    k_model3d<<<grid_blocks((long)p->n), 256, 0, s>>>(raw, raw + n0, raw + 2 * n0, D.nx, D.ny, D.nz, D.npd, p->nnx,
+                                                      p->nny, p->nnz, p->ldz, D.mode == GEO_MODE_FAST ? 1 : 0,
+                                                      p->vp.as<float>(), p->e2.as<float>(), p->d2.as<float>());
+    GEO_TRY(check_launch("model3d"));
+    // the few padded values the host set-up needs: vp, eps at padded index 1
+    // (the mute) and vp at the padded centre (d0); edge replication maps a
+    // padded index to the unpadded one
+    auto raw_index = [&](size_t k) {
+        const long iz = (long)(k % p->nnz), ix = (long)((k / p->nnz) % p->nnx), iy = (long)(k / ((size_t)p->nnz * p->nnx));
+        const long sz = std::min(std::max(iz - D.npd, 0L), (long)D.nz - 1);
+        const long sx = std::min(std::max(ix - D.npd, 0L), (long)D.nx - 1);
+        const long sy = std::min(std::max(iy - D.npd, 0L), (long)D.ny - 1);
+        return (size_t)(sz + (long)D.nz * (sx + (long)D.nx * sy));
+    };
+    float pick[3];
+    const size_t r1 = raw_index(1), rc = raw_index((size_t)p->nny * p->nnx * p->nnz / 2);
+    GEO_CUDA(cudaMemcpyAsync(&pick[0], raw + r1, 4, cudaMemcpyDeviceToHost, s));
+    GEO_CUDA(cudaMemcpyAsync(&pick[1], raw + n0 + r1, 4, cudaMemcpyDeviceToHost, s));
+    GEO_CUDA(cudaMemcpyAsync(&pick[2], raw + rc, 4, cudaMemcpyDeviceToHost, s));
+    GEO_CUDA(cudaStreamSynchronize(s));
+    p->vp1 = pick[0];
+    p->eps1 = pick[1];
+    const float d0 = sponge_d0(V_GPU, 3, 0.0f, pick[2], D.npd, D.dx, D.dy, D.dz);
     std::vector<float> prof((size_t)4 * (p->nnx + p->nny + p->nnz));
     float *q = prof.data();
     sponge_profiles(V_GPU, D.nx, D.npd, D.dt, d0, q, q + p->nnx, q + 2 * p->nnx, q + 3 * p->nnx);
@@ -503,28 +590,6 @@ extern "C" int geo_fd3d_set_model(geo_fd3d_plan *p, const float *v, const float 
     sponge_profiles(V_GPU, D.ny, D.npd, D.dt, d0, q, q + p->nny, q + 2 * p->nny, q + 3 * p->nny);
     q += 4 * p->nny;
     sponge_profiles(V_GPU, D.nz, D.npd, D.dt, d0, q, q + p->nnz, q + 2 * p->nnz, q + 3 * p->nnz);
-    if (D.sv) {
-        p->h_vp = pv;
-        p->h_eps = pe;
-        p->h_del = pd;
-    }
-    // exact: vp, 1+2eps, sqrtf(1+2del) in float, as the reference forms them;
-    // fast: A = vp^2(1+2eps), B = vp^2 sqrtf(1+2del), C = vp^2
-    for (size_t k = 0; k < p->n; k++) {
-        const float e2 = 1 + 2 * pe[k], d2 = sqrtf(1 + 2 * pd[k]);
-        if (D.mode == GEO_MODE_FAST) {
-            const float c2 = pv[k] * pv[k];
-            pv[k] = c2 * e2;
-            pe[k] = c2 * d2;
-            pd[k] = c2;
-        } else {
-            pe[k] = e2;
-            pd[k] = d2;
-        }
-    }
-    GEO_TRY(upload_pitched(p, p->vp, pv.data(), s));
-    GEO_TRY(upload_pitched(p, p->e2, pe.data(), s));
-    GEO_TRY(upload_pitched(p, p->d2, pd.data(), s));
     GEO_CUDA(cudaMemcpyAsync(p->prof.p, prof.data(), prof.size() * 4, cudaMemcpyHostToDevice, s));
     GEO_CUDA(cudaStreamSynchronize(s));
     if (!p->tuned) {
@@ -651,8 +716,6 @@ __global__ void k_adcig3d_illum(float *adcig, const float *ill, int nx, int nz, 
         if (w != 0.0f) adcig[k] = adcig[k] / w;
     }
 }
-
-static int grid_blocks(long n) { return (int)std::min<long>((n + 255) / 256, 152L * 16); }
 
 }  // namespace geo
 

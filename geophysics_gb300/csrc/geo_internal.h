@@ -58,7 +58,6 @@ constexpr double kPiMpi = 3.1415926535898;  // Toa_rtm_vti_adcig_cdp.c:39
 // Edge-replicate an nx*nz model into its padded (nx+2npd)*(nz+2npd) form.
 void pad_model_2d(int nx, int nz, int npd, const float *in, float *out);
 // Same for 3D, reference layout iz + nz*(ix + nx*iy).
-void pad_model_3d(int nx, int ny, int nz, int npd, const float *in, float *out);
 
 float sponge_d0(Variant v, int dims, float vpmax, float vcenter, int npd, float dx, float dy, float dz);
 // coff1/coff2 on half cells (velocities), acoff1/acoff2 on integer cells

@@ -71,23 +71,6 @@ void pad_model_2d(int nx, int nz, int npd, const float *in, float *out) {
     }
 }
 
-// pad_vv3d (GPU_vti3dfd_kernels.cu:208-255): clamp each axis to the interior.
-void pad_model_3d(int nx, int ny, int nz, int npd, const float *in, float *out) {
-    const size_t nnx = nx + 2 * npd, nny = ny + 2 * npd, nnz = nz + 2 * npd;
-    for (size_t iy = 0; iy < nny; iy++) {
-        long sy = (long)iy - npd; sy = sy < 0 ? 0 : (sy >= ny ? ny - 1 : sy);
-        for (size_t ix = 0; ix < nnx; ix++) {
-            long sx = (long)ix - npd; sx = sx < 0 ? 0 : (sx >= nx ? nx - 1 : sx);
-            const float *src = in + (size_t)nz * (sx + (size_t)nx * sy);
-            float *dst = out + nnz * (ix + nnx * iy);
-            for (size_t iz = 0; iz < nnz; iz++) {
-                long sz = (long)iz - npd; sz = sz < 0 ? 0 : (sz >= nz ? nz - 1 : sz);
-                dst[iz] = src[sz];
-            }
-        }
-    }
-}
-
 // ---------------------------------------------------------------- sponge
 // d0 (CPU_vti2dfd_kernels.c:192; Toa_rtm_vti_adcig_cdp.c:1346;
 // GPU_vti2dfd_kernels.cu:105; GPU_vti3dfd_kernels.cu:205).

@@ -71,3 +71,19 @@ def test_fd3d_chunks_and_ragged_extents(geo, orc, monkeypatch, chunks, shape):
         ref = orc.fd3d(v, e, d, mode=mode, **kw)
         out = geo.fd3d_shot(v, e, d, mode=mode, **kw)
         assert np.array_equal(out, ref), (mode, rel_l2(out, ref))
+
+
+def test_fd3d_model_checked_on_device(geo):
+    """The model is checked and padded on the GPU; a bad value is reported
+    with the first offending index, as the host check reports it."""
+    from tests.util import random_model_3d
+    v, e, d = random_model_3d(12, 10, 14, seed=9)
+    kw = dict(npd=8, nt=10, dx=10.0, dy=10.0, dz=10.0, dt=1e-3, favg=25.0, fsx=6, fsy=5, fsz=2)
+    for arr, idx, val, what in ((0, 57, np.nan, "velocity[57]"), (0, 3, -1.0, "velocity[3]"),
+                                (2, 90, -0.7, "1+2*delta[90]"), (1, 11, np.inf, "eps/del[11]")):
+        m = [v.copy(), e.copy(), d.copy()]
+        m[arr].reshape(-1)[idx] = val
+        m[arr].reshape(-1)[idx + 200] = val           # a later bad point is not the one reported
+        with pytest.raises(geo.GeoError) as ei:
+            geo.fd3d_shot(*m, **kw)
+        assert ei.value.status == 4 and what in str(ei.value), str(ei.value)
