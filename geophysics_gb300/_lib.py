@@ -56,7 +56,8 @@ class RTM2DDesc(C.Structure):
     _fields_ = [(n, C.c_int) for n in ("nx", "nz", "npd", "nt")] + \
                [(n, C.c_float) for n in ("dx", "dz", "dt_ms", "favg", "pfac")] + \
                [("zs", C.c_int), ("ns", C.c_int), ("shot_x", C.POINTER(C.c_int)),
-                ("shot_nxs", C.POINTER(C.c_int)), ("laplace", C.c_int), ("tile_z", C.c_int), ("tile_x", C.c_int)]
+                ("shot_nxs", C.POINTER(C.c_int)), ("laplace", C.c_int), ("tile_z", C.c_int), ("tile_x", C.c_int),
+                ("mode", C.c_int)]
 
 
 _lib = None

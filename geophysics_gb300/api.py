@@ -443,17 +443,20 @@ def tc_gemm_bf16(A, B, bias=None, act=False, out_f32=True):
 
 
 def rtm2d_batch(v, e, d, *, npd, nt, dx, dz, dt_ms, favg, pfac, zs, shot_x, shot_nxs, laplace=True,
-                per_shot=False, tile_x=0, adcig=False):
+                per_shot=False, tile_x=0, adcig=False, mode="exact"):
     """Batched 2D RTM with the MPI program's semantics; returns the stacked
     (Laplacian-filtered) image (nx, nz) [and the per-shot images] [and the
-    Poynting angle gathers (90, nx, nz) when `adcig`]."""
+    Poynting angle gathers (90, nx, nz) when `adcig`].  mode "exact" is the
+    program's arithmetic bit for bit; "fast" forms its double-precision
+    chains (two stress terms and the illumination sum) in FP32."""
     b = _Bufs(v, e, d)
     nx, nz = v.shape
     ns = len(shot_x)
     sx = (C.c_int * ns)(*[int(k) for k in shot_x])
     sw = (C.c_int * ns)(*[int(k) for k in shot_nxs])
     desc = RTM2DDesc(nx=nx, nz=nz, npd=npd, nt=nt, dx=dx, dz=dz, dt_ms=dt_ms, favg=favg, pfac=pfac, zs=zs, ns=ns,
-                     shot_x=sx, shot_nxs=sw, laplace=1 if laplace else 0, tile_z=0, tile_x=tile_x)
+                     shot_x=sx, shot_nxs=sw, laplace=1 if laplace else 0, tile_z=0, tile_x=tile_x,
+                     mode=_MODES[mode] if isinstance(mode, str) else int(mode))
     pv, pe, pd = b.inp(v), b.inp(e), b.inp(d)
     img, pi = b.out((nx, nz), v)
     shots = pshots = None

@@ -447,6 +447,8 @@ extern "C" int geo_rtm2d_batch_adcig(const geo_rtm2d_desc *desc, const float *v,
         if (kk < nxs / 2 + 1 || kk + nxs / 2 > D.nx) return fail(GEO_ERR_WINDOW, "shot %d window leaves model", k);
     }
     if (D.zs < 1 || D.zs + D.npd - 1 + 3 >= D.nz + 2 * D.npd) return fail(GEO_ERR_ARG, "bad source depth");
+    if (D.mode != GEO_MODE_EXACT && D.mode != GEO_MODE_FAST) return fail(GEO_ERR_ARG, "bad mode %d", D.mode);
+    const int fast = D.mode == GEO_MODE_FAST;
     cudaStream_t s = (cudaStream_t)stream;
     std::vector<float> hv, he, hd;
     GEO_TRY(host_model(v, e, d, (size_t)D.nx * D.nz, mem, s, hv, he, hd));
@@ -502,7 +504,7 @@ extern "C" int geo_rtm2d_batch_adcig(const geo_rtm2d_desc *desc, const float *v,
         GEO_TRY(capture(G, ss.cs, [&]() -> int {
             for (int it = 0; it < nt; it++) {
                 Step2D st{};
-                st.it = it; st.amp = amp[it]; st.src_on = on[it]; st.taper = 1; st.nf = 1;
+                st.it = it; st.amp = amp[it]; st.src_on = on[it]; st.taper = 1; st.nf = 1; st.fast = fast;
                 GEO_TRY(B.vel(st, ss.cs));
                 GEO_TRY(B.stress(PH_FWD, st, ss.cs));
             }
@@ -530,7 +532,7 @@ extern "C" int geo_rtm2d_batch_adcig(const geo_rtm2d_desc *desc, const float *v,
             for (int it = nt - 1; it >= 0; it--) {
                 GEO_TRY(launch_inject2d(B.d_S.as<Shot2D>(), D.ns, maxline, it, ss.cs));
                 Step2D st{};
-                st.it = it; st.nf = 2;
+                st.it = it; st.nf = 2; st.fast = fast;
                 GEO_TRY(B.vel(st, ss.cs));
                 GEO_TRY(B.stress(PH_BWD, st, ss.cs));
             }

@@ -136,20 +136,24 @@ __global__ void __launch_bounds__(256) k_vel2d(const Shot2D *__restrict__ shots,
 // Stress update of one updated point (ix, iz) of a shot, every field, and
 // the phase's epilogue (records and edge lines forward; image, illumination
 // and gathers backward).
-template <int VARIANT, int PHASE, bool NC>
+template <int VARIANT, int PHASE, bool NC, bool FAST = false>
 __device__ __forceinline__ void stress_point(const Shot2D &sh, int ix, int iz, const Step2D &st) {
     const int nnz = sh.nnz;
     const long id = (long)ix * nnz + iz;
     const float vp = __ldg(sh.vp + id);
+    // the MPI form's exact arithmetic carries pow(1+2del,0.5) in double;
+    // its fast form (FAST, a separate instantiation so that no double
+    // operation is issued) uses the FP32 sqrtf(1+2del) of the others
+    constexpr bool dpw = VARIANT == V_MPI && !FAST;
     float e2 = __ldg(sh.e2 + id), d2 = 0.0f;
     double pw = 0.0;
-    if (VARIANT == V_MPI) pw = __ldg(sh.pw + id);
+    if (dpw) pw = __ldg(sh.pw + id);
     else d2 = __ldg(sh.d2 + id);
     if (st.taper) {
         const int bx = ix - sh.tx0, bz = iz - sh.tz0;
         if (bx >= 0 && bx < kTB && bz >= 0 && bz < kTB) {
             e2 = sh.te2[bx * kTB + bz];
-            if (VARIANT == V_MPI) pw = sh.tpw[bx * kTB + bz];
+            if (dpw) pw = sh.tpw[bx * kTB + bz];
             else d2 = sh.td2[bx * kTB + bz];
         }
     }
@@ -173,8 +177,13 @@ __device__ __forceinline__ void stress_point(const Shot2D &sh, int ix, int iz, c
         float px = sh.px[f][id], pz = sh.pz[f][id], qx = sh.qx[f][id], qz = sh.qz[f][id];
         if (VARIANT == V_MPI) {
             px = ax2 * px - ax1 * vp * e2 * sh.dtx * xx;
-            pz = (float)((double)(az2 * pz) - (double)(az1 * vp) * pw * (double)sh.dtz * (double)zz);
-            qx = (float)((double)(ax2 * qx) - (double)(ax1 * vp) * pw * (double)sh.dtx * (double)xx);
+            if (dpw) {
+                pz = (float)((double)(az2 * pz) - (double)(az1 * vp) * pw * (double)sh.dtz * (double)zz);
+                qx = (float)((double)(ax2 * qx) - (double)(ax1 * vp) * pw * (double)sh.dtx * (double)xx);
+            } else {
+                pz = az2 * pz - az1 * vp * d2 * sh.dtz * zz;
+                qx = ax2 * qx - ax1 * vp * d2 * sh.dtx * xx;
+            }
             qz = az2 * qz - az1 * vp * sh.dtz * zz;
         } else {
             px = ax2 * px - ax1 * vp * vp * e2 * sh.dtx * xx;
@@ -218,7 +227,9 @@ __device__ __forceinline__ void stress_point(const Shot2D &sh, int ix, int iz, c
         // formed in double, as pow() returns it, and a zero becomes 1
         const long o = (long)gx * sh.nz + gz;
         const float sv = Pn[0];
-        float ill = (float)((double)sh.ill[o] + (double)sv * (double)sv);
+        float ill;
+        if (FAST) ill = sh.ill[o] + sv * sv;
+        else ill = (float)((double)sh.ill[o] + (double)sv * (double)sv);
         if (ill == 0.0f) ill = 1.0f;
         sh.ill[o] = ill;
         sh.mig[o] = sh.mig[o] + Pn[1] * sv;
@@ -235,13 +246,13 @@ __device__ __forceinline__ void stress_point(const Shot2D &sh, int ix, int iz, c
     }
 }
 
-template <int VARIANT, int PHASE>
+template <int VARIANT, int PHASE, bool FAST = false>
 __global__ void __launch_bounds__(256) k_stress2d(const Shot2D *__restrict__ shots, const int *__restrict__ item_shot,
                                                   int nitems, Step2D st) {
     for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
         Tile2D t;
         if (!locate(shots, item_shot, item, t)) continue;
-        stress_point<VARIANT, PHASE, true>(*t.sh, t.ix, t.iz, st);
+        stress_point<VARIANT, PHASE, true, FAST>(*t.sh, t.ix, t.iz, st);
     }
 }
 
@@ -296,6 +307,7 @@ __global__ void __launch_bounds__(512) k_fd2d_shot(const Shot2D *__restrict__ sh
         st.src_on = a.on[it];
         st.taper = a.taper;
         st.nf = 1;
+        st.fast = 0;  // the single-shot forms have no double chains
         for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
             Tile2D t;
             if (locate(shots, item_shot, item, t)) vel_point<VARIANT, false>(*t.sh, t.ix, t.iz, st);
@@ -383,19 +395,23 @@ int launch_stress2d(int variant, int phase, const Shot2D *d_shots, const int *d_
     GEO_TRY(ensure_gauss());
     dim3 block(32, by), g(grid);
 #define GEO_STRESS(V, PH) k_stress2d<V, PH><<<g, block, 0, s>>>(d_shots, d_item_shot, nitems, st)
+#define GEO_STRESS_MPI(PH) \
+    (st.fast ? k_stress2d<V_MPI, PH, true><<<g, block, 0, s>>>(d_shots, d_item_shot, nitems, st) \
+             : k_stress2d<V_MPI, PH, false><<<g, block, 0, s>>>(d_shots, d_item_shot, nitems, st))
     if (phase == PH_FWD) {
         switch (variant) {
             case V_CPU: GEO_STRESS(V_CPU, PH_FWD); break;
             case V_GPU: GEO_STRESS(V_GPU, PH_FWD); break;
-            default: GEO_STRESS(V_MPI, PH_FWD); break;
+            default: GEO_STRESS_MPI(PH_FWD); break;
         }
     } else {
         switch (variant) {
             case V_CPU: GEO_STRESS(V_CPU, PH_BWD); break;
             case V_GPU: GEO_STRESS(V_GPU, PH_BWD); break;
-            default: GEO_STRESS(V_MPI, PH_BWD); break;
+            default: GEO_STRESS_MPI(PH_BWD); break;
         }
     }
+#undef GEO_STRESS_MPI
 #undef GEO_STRESS
     return check_launch("stress2d");
 }

@@ -129,6 +129,7 @@ struct Step2D {
     int src_on;       // source active this step
     int taper;        // use the taper box for eps/del
     int nf;           // fields updated (1: s only, 2: s and g)
+    int fast;         // MPI form: double-precision chains in FP32
 };
 
 enum Phase2D { PH_FWD = 0, PH_BWD = 1 };

@@ -242,6 +242,10 @@ typedef struct geo_rtm2d_desc {
     const int *shot_nxs;     /* ns odd window widths, host                   */
     int   laplace;           /* apply the adjoint Laplacian to the stack     */
     int   tile_z, tile_x;    /* 0 = autotuned                                */
+    int   mode;              /* GEO_MODE_EXACT (0): the program's arithmetic,
+                                bit for bit, with its double-precision chains;
+                                GEO_MODE_FAST: those chains in FP32 (pz, qx
+                                with sqrtf(1+2del), the illumination sum)     */
 } geo_rtm2d_desc;
 
 /* v,e,d: nx*nz; image: nx*nz stacked (Laplacian-filtered if asked).

@@ -35,6 +35,31 @@ def test_rtm2d_batch_bit_exact(geo, orc, tile_x):
     assert np.array_equal(raw, acc)
 
 
+def test_rtm2d_batch_fast_mode_within_rounding(geo, orc):
+    """The fast mode forms the program's double-precision chains in FP32.
+    Both modes are FP32 roundings of one computation whose image is a small
+    residual of large correlations: the exact mode itself is 1.3e-3 to
+    5.3e-3 (rel-L2) from the oracle's FP64 build here.  Bound: the fast
+    image is no further from FP64 than 1.5x the exact one, and within 1e-2
+    of it."""
+    from tests.util import rel_l2
+    v, e, d = model()
+    xs, ws = [35, 55, 48], [41, 53, 31]
+    kw = dict(npd=15, nt=650, dx=10.0, dz=10.0, dt_ms=1.0, favg=20.0, pfac=1000.0)
+    run = dict(kw, zs=1, shot_x=xs, shot_nxs=ws, per_shot=True)
+    img, per = geo.rtm2d_batch(v, e, d, **run)
+    fimg, fper = geo.rtm2d_batch(v, e, d, mode="fast", **run)
+    assert np.isfinite(fimg).all() and np.abs(img).max() > 0
+    for k, (x, w) in enumerate(zip(xs, ws)):
+        ref = orc.rtm2d_mpi_shot(v, e, d, fs_sxd=x, ds_sxd=0, zs_sxd=1, is_=k + 1, nxs=w, prec=64, **kw)[0]
+        e_exact, e_fast = rel_l2(per[k], ref), rel_l2(fper[k], ref)
+        assert e_fast <= 1.5 * e_exact, (k, e_fast, e_exact)
+        assert rel_l2(fper[k], per[k]) < 1e-2, k
+    assert rel_l2(fimg, img) < 1e-2
+    with pytest.raises(geo.GeoError):
+        geo.rtm2d_batch(v, e, d, mode=7, **run)
+
+
 def test_rtm2d_golden(geo):
     import os
     r = np.load(os.path.join(os.path.dirname(__file__), "golden", "golden_rtm2d_mpi.npz"))
