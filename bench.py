@@ -288,23 +288,25 @@ def run_ours(args, rank, world):
 
 
 def run_profile_case(args):
-    """Small case for ncu captures: 192^3 + 40 sponge (272^3 padded, each
-    field 80 MB, the working set well above L2), a 20-step shot."""
+    """Small case for ncu captures: by default 192^3 + 40 sponge (272^3
+    padded, each field 80 MB, the working set well above L2), a 20-step
+    shot; --grid / --sponge change the cube (200 and 20 give the headline
+    case's sponge fraction)."""
     import torch
 
     import geophysics_gb300 as geo
     global NX, NY, NZ
-    NX = NY = NZ = 192
+    NX = NY = NZ = args.grid
     vp, eps, dl = make_model(device="cuda")
     kw = plan_kwargs()
-    kw.update(nt=20, nrx=96, nry=96)
+    kw.update(nt=20, nrx=args.grid // 2, nry=args.grid // 2, npd=args.sponge, rec_iz=args.sponge)
     plan = geo.FD3DPlan(**kw)
     plan.set_model(vp, eps, dl)
     for _ in range(args.steps):
         plan.run_shot(0, device="cuda")
     torch.cuda.synchronize()
     plan.close()
-    print(json.dumps({"case": "profile-small", "grid": 192, "nt": 20, "shots": args.steps}))
+    print(json.dumps({"case": "profile-small", "grid": args.grid, "sponge": args.sponge, "nt": 20, "shots": args.steps}))
 
 
 def run_traffic_case(args):
@@ -563,6 +565,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--case", default="full", choices=["full", "small", "traffic", "rtm-learned", "rtm-methods", "fd2d", "rtm2d"],
                     help="small / traffic: ncu profiling cases; rtm-learned: the learned-codec RTM comparison")
+    ap.add_argument("--grid", type=int, default=192, help="small: cube edge")
+    ap.add_argument("--sponge", type=int, default=40, help="small: sponge width")
     ap.add_argument("--nt", type=int, default=3000, help="rtm-learned, rtm2d: time steps")
     ap.add_argument("--shots", type=int, default=128, help="rtm2d: shots in the batch (the workload has 128)")
     ap.add_argument("--err-nt", type=int, default=1200, help="rtm-learned: steps of the image-error comparison")

@@ -43,7 +43,8 @@ class FD3DDesc(C.Structure):
 
 class RTM3DDesc(C.Structure):
     _fields_ = [("fd", FD3DDesc), ("ns", C.c_int), ("mute_tt", C.c_int), ("method", C.c_int),
-                ("snap_every", C.c_int), ("ae", C.c_void_p), ("na", C.c_int), ("da", C.c_int), ("dcdp", C.c_int)]
+                ("snap_every", C.c_int), ("ae", C.c_void_p), ("na", C.c_int), ("da", C.c_int), ("dcdp", C.c_int),
+                ("theta", C.c_void_p), ("phi", C.c_void_p)]
 
 
 class RTM2DGpuDesc(C.Structure):
@@ -85,6 +86,7 @@ def lib():
         "geo_fd3d_plan_create": (_i, [C.POINTER(_vp), C.POINTER(FD3DDesc)]),
         "geo_fd3d_plan_destroy": (_i, [_vp]),
         "geo_fd3d_set_model": (_i, [_vp, _vp, _vp, _vp, _i, _vp]),
+        "geo_fd3d_set_tilt": (_i, [_vp, _vp, _vp, _i, _vp]),
         "geo_fd3d_run_shot": (_i, [_vp, _i, _vp, _i, _vp]),
         "geo_fd3d_time_steps": (_i, [_vp, _i, C.POINTER(_f), _vp]),
         "geo_fd3d_get_fields": (_i, [_vp, _vp, _vp, _i, _vp]),

@@ -143,6 +143,13 @@ class FD3DPlan:
         check(lib().geo_fd3d_set_model(self._p, b.inp(v), b.inp(e), b.inp(d), b.mem, b.stream()),
               "geo_fd3d_set_model")
 
+    def set_tilt(self, theta, phi):
+        """3D TTI medium: tilt from the vertical and azimuth in degrees,
+        shaped like the model and smooth in space (geo_fd3d_set_tilt); the
+        plan must use mode "fast"."""
+        b = _Bufs(theta, phi)
+        check(lib().geo_fd3d_set_tilt(self._p, b.inp(theta), b.inp(phi), b.mem, b.stream()), "geo_fd3d_set_tilt")
+
     def run_shot(self, is_=0, device=None):
         """Shot `is_` (0-based); returns (nry, nrx, nt), on the GPU if device."""
         D = self.desc
@@ -183,12 +190,15 @@ class FD3DPlan:
             pass
 
 
-def fd3d_shot(v, e, d, is_=0, **kw):
-    """One-call 3D shot (create plan, set model, run, destroy)."""
+def fd3d_shot(v, e, d, is_=0, theta=None, phi=None, **kw):
+    """One-call 3D shot (create plan, set model, run, destroy); with theta
+    and phi (degrees) on the 3D TTI medium."""
     ny, nx, nz = v.shape
     plan = FD3DPlan(nx=nx, ny=ny, nz=nz, **kw)
     try:
         plan.set_model(v, e, d)
+        if theta is not None:
+            plan.set_tilt(theta, phi)
         return plan.run_shot(is_, device=v.device if _is_dev(v) else None)
     finally:
         plan.close()
@@ -199,8 +209,9 @@ _RTM = {"boundary": GEO_RTM_BOUNDARY, "snapshot": GEO_RTM_SNAPSHOT, "learned": G
 
 def rtm3d(v, e, d, *, npd, nt, dx, dy, dz, dt, favg, fsx, fsy, fsz, ns=1, dsx=0, dsy=0, dsz=0, mute_tt=70,
           pfac=10.0, wtype=1, sv=0, mode="fast", laplace=True, illum=False, method="boundary", snap_every=4,
-          codec=None, adcig=None):
-    """3D RTM over shots 0..ns-1; v,e,d shaped (ny, nx, nz).
+          codec=None, adcig=None, theta=None, phi=None):
+    """3D RTM over shots 0..ns-1; v,e,d shaped (ny, nx, nz); theta, phi
+    (degrees, same shape): the 3D TTI medium (mode "fast", no gathers).
 
     method "boundary": the 3D GPU RTM program's boundary-saving recompute;
     "snapshot": source P kept every snap_every steps (fp32);
@@ -209,7 +220,7 @@ def rtm3d(v, e, d, *, npd, nt, dx, dy, dz, dt, favg, fsx, fsy, fsz, ns=1, dsx=0,
     gathers, shaped (ny//dcdp, nx//dcdp, na, nz), illumination-divided.
     Returns the illumination-divided image, then the Laplacian-filtered image
     if `laplace`, then the illumination if `illum`, then the gathers."""
-    b = _Bufs(v, e, d)
+    b = _Bufs(v, e, d, theta, phi)
     ny, nx, nz = v.shape
     fd = FD3DDesc(nx=nx, ny=ny, nz=nz, npd=npd, nt=nt, dx=dx, dy=dy, dz=dz, dt=dt, favg=favg, pfac=pfac,
                   wtype=wtype, sv=sv, mode=_MODES[mode] if isinstance(mode, str) else int(mode),
@@ -219,6 +230,8 @@ def rtm3d(v, e, d, *, npd, nt, dx, dy, dz, dt, favg, fsx, fsy, fsz, ns=1, dsx=0,
     desc = RTM3DDesc(fd=fd, ns=ns, mute_tt=mute_tt, method=_RTM[method] if isinstance(method, str) else int(method),
                      snap_every=snap_every, ae=codec._p if codec is not None else None, na=na, da=da, dcdp=dcdp)
     pv, pe, pd = b.inp(v), b.inp(e), b.inp(d)
+    if theta is not None:
+        desc.theta, desc.phi = b.inp(theta), b.inp(phi)
     mig, pm = b.out((ny, nx, nz), v)
     lap, pl = b.out((ny, nx, nz), v) if laplace else (None, None)
     ill, pi = b.out((ny, nx, nz), v) if illum else (None, None)

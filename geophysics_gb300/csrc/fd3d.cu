@@ -23,6 +23,7 @@
 #include <cstring>
 #include <vector>
 #include <memory>
+#include <thread>
 
 using namespace geo;
 
@@ -128,6 +129,19 @@ __global__ void k_model3d(const float *v, const float *e, const float *d, int nx
     }
 }
 
+// Edge-replicated padding of one unpadded array into the pitched layout
+// (the same clamping as k_model3d).
+__global__ void k_pad3d(const float *src, int nx, int ny, int nz, int npd, int nnx, int nny, int nnz, int ldz,
+                        float *dst) {
+    const long n = (long)nnx * nny * nnz;
+    for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < n; k += (long)gridDim.x * blockDim.x) {
+        const int iz = (int)(k % nnz), ix = (int)((k / nnz) % nnx), iy = (int)(k / ((long)nnz * nnx));
+        const int sz = min(max(iz - npd, 0), nz - 1), sx = min(max(ix - npd, 0), nx - 1),
+                  sy = min(max(iy - npd, 0), ny - 1);
+        dst[iz + (long)ldz * (ix + (long)nnx * iy)] = src[sz + (long)nz * (sx + (long)nx * sy)];
+    }
+}
+
 // The padded raw model on a B^3 box at (x0, y0, z0) (padded coordinates),
 // gathered from the unpadded arrays with the same edge replication; box
 // points outside the padded grid are left alone.
@@ -173,6 +187,9 @@ struct geo_fd3d_plan {
     float vp1 = 0, eps1 = 0;           // padded model at linear index 1 (mute)
     bool model_set = false;
     bool tuned = false;
+    // 3D TTI medium (geo_fd3d_set_tilt): cos/sin of tilt and azimuth, 4 x nalloc
+    DevBuf tilt, save;
+    bool tti = false;
 };
 
 namespace geo {
@@ -274,8 +291,23 @@ static void choose_chunks(geo_fd3d_plan *p) {
 // One time step of field set f: the fused kernel reads level cur and writes
 // level 1-cur.
 static int step3d(geo_fd3d_plan *p, int f, const StepArgs3D &st, cudaStream_t s) {
-    const Fused3D r = make_fused(p, f);
-    GEO_TRY(launch_fused3d(p->fs[f].maps[p->fs[f].cur], r, p->d.mode, st, s));
+    if (p->tti) {
+        const FieldSet3D &F = p->fs[f];
+        const int c = F.cur, n = 1 - c;
+        Tti3DStep t;
+        t.g = grid_of(p, f);
+        t.u0 = F.lev[c][0].as<float>(); t.v0 = F.lev[c][1].as<float>(); t.w0 = F.lev[c][2].as<float>();
+        t.P0 = F.lev[c][3].as<float>(); t.Q0 = F.lev[c][4].as<float>();
+        t.u1 = F.lev[n][0].as<float>(); t.v1 = F.lev[n][1].as<float>(); t.w1 = F.lev[n][2].as<float>();
+        t.P1 = F.lev[n][3].as<float>(); t.Q1 = F.lev[n][4].as<float>();
+        const float *tl = p->tilt.as<float>();
+        t.ct = tl; t.st = tl + p->nalloc; t.cp = tl + 2 * p->nalloc; t.sp = tl + 3 * p->nalloc;
+        t.save = p->save.as<float>();
+        GEO_TRY(launch_tti3d(t, st, s));
+    } else {
+        const Fused3D r = make_fused(p, f);
+        GEO_TRY(launch_fused3d(p->fs[f].maps[p->fs[f].cur], r, p->d.mode, st, s));
+    }
     p->fs[f].cur ^= 1;
     return GEO_OK;
 }
@@ -529,6 +561,62 @@ extern "C" int geo_fd3d_plan_destroy(geo_fd3d_plan *p) {
 // Model upload: pad on the host, build the model arrays of the chosen form
 // and the sponge profiles (d0 from the padded centre velocity,
 // GPU_vti3dfd_kernels.cu:203-206).
+// Tilt and azimuth (degrees, interior layout) of a 3D TTI medium: from now
+// on the plan steps with the 3D TTI scheme (tti3d.cu).  Their cosines and
+// sines are formed on the host as cosf(deg * 0.017453292519943295f) and
+// padded by edge replication on the device.
+extern "C" int geo_fd3d_set_tilt(geo_fd3d_plan *p, const float *theta, const float *phi, int mem, void *stream) {
+    if (!p || !theta || !phi) return fail(GEO_ERR_ARG, "null argument");
+    if (mem != GEO_MEM_HOST && mem != GEO_MEM_DEVICE) return fail(GEO_ERR_ARG, "bad mem kind");
+    if (p->d.mode != GEO_MODE_FAST) return fail(GEO_ERR_ARG, "the TTI step needs the fast (premultiplied) model form");
+    cudaStream_t s = (cudaStream_t)stream;
+    const geo_fd3d_desc &D = p->d;
+    const size_t n0 = (size_t)D.nx * D.ny * D.nz;
+    std::vector<float> ang;
+    const float *th = theta, *ph = phi;
+    if (mem == GEO_MEM_DEVICE) {
+        ang.resize(2 * n0);
+        GEO_CUDA(cudaMemcpyAsync(ang.data(), theta, n0 * 4, cudaMemcpyDeviceToHost, s));
+        GEO_CUDA(cudaMemcpyAsync(ang.data() + n0, phi, n0 * 4, cudaMemcpyDeviceToHost, s));
+        GEO_CUDA(cudaStreamSynchronize(s));
+        th = ang.data();
+        ph = ang.data() + n0;
+    }
+    for (size_t k = 0; k < n0; k++)
+        if (!std::isfinite(th[k]) || !std::isfinite(ph[k])) return fail(GEO_ERR_MODEL, "tilt/azimuth[%zu] not finite", k);
+    std::vector<float> trig(4 * n0);
+    {
+        const unsigned nth = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+        std::vector<std::thread> pool;
+        const size_t chunk = (n0 + nth - 1) / nth;
+        for (unsigned t = 0; t < nth; t++)
+            pool.emplace_back([&, t]() {
+                const size_t lo = t * chunk, hi = std::min(n0, lo + chunk);
+                for (size_t k = lo; k < hi; k++) {
+                    const float a = th[k] * 0.017453292519943295f, b = ph[k] * 0.017453292519943295f;
+                    trig[k] = cosf(a);
+                    trig[n0 + k] = sinf(a);
+                    trig[2 * n0 + k] = cosf(b);
+                    trig[3 * n0 + k] = sinf(b);
+                }
+            });
+        for (auto &t : pool) t.join();
+    }
+    DevBuf tmp;
+    GEO_TRY(tmp.alloc(4 * n0 * 4));
+    GEO_CUDA(cudaMemcpyAsync(tmp.p, trig.data(), 4 * n0 * 4, cudaMemcpyHostToDevice, s));
+    if (p->tilt.bytes != 4 * p->nalloc * 4) GEO_TRY(p->tilt.alloc(4 * p->nalloc * 4));
+    if (!p->save.p) GEO_TRY(p->save.alloc(16));
+    for (int r = 0; r < 4; r++) {
+        k_pad3d<<<grid_blocks((long)p->n), 256, 0, s>>>(tmp.as<float>() + r * n0, D.nx, D.ny, D.nz, D.npd, p->nnx,
+                                                        p->nny, p->nnz, p->ldz, p->tilt.as<float>() + r * p->nalloc);
+        GEO_TRY(check_launch("pad3d"));
+    }
+    GEO_CUDA(cudaStreamSynchronize(s));
+    p->tti = true;
+    return GEO_OK;
+}
+
 extern "C" int geo_fd3d_set_model(geo_fd3d_plan *p, const float *v, const float *e, const float *d, int mem,
                                   void *stream) {
     if (!p || !v || !e || !d) return fail(GEO_ERR_ARG, "null argument");
@@ -738,7 +826,9 @@ extern "C" int geo_rtm3d_adcig(const geo_rtm3d_desc *desc, const float *v, const
     if (method == GEO_RTM_LEARNED && !R.ae) return fail(GEO_ERR_ARG, "the learned method needs a codec");
     // angle gathers: the program's na = 65, da = 1, dcdp = 1 by default
     const int na = R.na > 0 ? R.na : 65, da = R.da > 0 ? R.da : 1, dcdp = R.dcdp > 0 ? R.dcdp : 1;
+    if (R.theta && !R.phi) return fail(GEO_ERR_ARG, "tilt without azimuth");
     if (adcig_out) {
+        if (R.theta) return fail(GEO_ERR_ARG, "no angle gathers on a TTI medium");
         if (method != GEO_RTM_BOUNDARY) return fail(GEO_ERR_ARG, "angle gathers need the boundary method");
         if (na > kMaxAngles) return fail(GEO_ERR_ARG, "na must be 1..%d", kMaxAngles);
         if (dcdp > R.fd.nx || dcdp > R.fd.ny) return fail(GEO_ERR_ARG, "dcdp exceeds the model");
@@ -752,6 +842,7 @@ extern "C" int geo_rtm3d_adcig(const geo_rtm3d_desc *desc, const float *v, const
     GEO_TRY(plan3d_create(&p, &D, 2));
     std::unique_ptr<geo_fd3d_plan, int (*)(geo_fd3d_plan *)> guard(p, geo_fd3d_plan_destroy);
     GEO_TRY(geo_fd3d_set_model(p, v, e, d, mem, stream));
+    if (R.theta) GEO_TRY(geo_fd3d_set_tilt(p, R.theta, R.phi, mem, stream));
     const long nimg = (long)D.nx * D.ny * D.nz;
     const long L = 2L * D.nx * D.ny + 2L * D.nz * D.ny + 2L * D.nx * D.nz;
     const int k = method == GEO_RTM_BOUNDARY ? 1 : R.snap_every;

@@ -31,6 +31,19 @@ struct StepArgs3D {
     const float *other_P;       // the source-side field's P (same layout)
 };
 
+// One 3D TTI step (tti3d.cu): g describes the grid, its profiles and the
+// premultiplied model (vp, e2, d2 hold A, B, C); level c is read, level n
+// written; ct..sp are cos/sin of tilt and azimuth; save keeps the source
+// cell's P,Q of level c.
+struct Tti3DStep {
+    Grid3D g;
+    const float *u0, *v0, *w0, *P0, *Q0;
+    float *u1, *v1, *w1, *P1, *Q1;
+    const float *ct, *st, *cp, *sp;
+    float *save;
+};
+int launch_tti3d(const Tti3DStep &t, const StepArgs3D &st, cudaStream_t s);
+
 Grid3D make_grid(const geo_fd3d_plan *p);
 int run_shot_3d(geo_fd3d_plan *p, int is, cudaStream_t s, int (*on_step)(void *, int), void *ctx);
 int fetch_shot_3d(geo_fd3d_plan *p, float *shot, int mem, cudaStream_t s);

@@ -162,6 +162,13 @@ int geo_fd3d_plan_destroy(geo_fd3d_plan *plan);
 /* v,e,d: nx*ny*nz model in the reference layout. */
 int geo_fd3d_set_model(geo_fd3d_plan *plan, const float *v, const float *e, const float *d,
                        int mem, void *stream);
+/* 3D TTI medium (no reference counterpart: the 2D TTI GPU programs'
+ * rotated-derivative scheme, 2D-tti-fd+rtm-cuda/Toa_gpu_2dtti_fd_1orderfunction.cu:81-183,
+ * extended to a symmetry axis with tilt theta from the vertical and azimuth
+ * phi, both in degrees on the nx*ny*nz model layout and smooth in space).
+ * After this call the plan steps with the TTI scheme; the plan must use
+ * GEO_MODE_FAST (the premultiplied model). */
+int geo_fd3d_set_tilt(geo_fd3d_plan *plan, const float *theta, const float *phi, int mem, void *stream);
 /* Shot number `is` (0-based, as the reference's loop): shot is nt*nrx*nry. */
 int geo_fd3d_run_shot(geo_fd3d_plan *plan, int is, float *shot, int mem, void *stream);
 /* Runs nsteps bare time steps (no source or receivers) on the current
@@ -200,6 +207,9 @@ typedef struct geo_rtm3d_desc {
     geo_ae *ae;              /* trained codec (method 2)                     */
     int   na, da, dcdp;      /* angle gathers: bins, bin width in degrees,
                                 CDP decimation (0 = the program's 65, 1, 1)   */
+    const float *theta, *phi;/* 3D TTI medium (geo_fd3d_set_tilt; in `mem`
+                                like the model) or NULL for VTI; no angle
+                                gathers on a TTI medium                       */
 } geo_rtm3d_desc;
 
 /* v,e,d: nx*ny*nz.  mig: nx*ny*nz image divided by the illumination where

@@ -1140,6 +1140,7 @@ typedef struct {
     REAL dtx, dty, dtz;
     float *cx1, *cx2, *ax1, *ax2, *cy1, *cy2, *ay1, *ay2, *cz1, *cz2, *az1, *az2;
     REAL *vp, *e2, *d2, *mA, *mB, *mC;
+    REAL *tct, *tst, *tcp, *tsp;   /* 3D TTI: cos/sin of tilt and azimuth (NULL: VTI) */
     float *amp; unsigned char *act;
     long src;
 } orc_g3d;
@@ -1241,6 +1242,112 @@ static void g3d_free(orc_g3d *G)
     free(G->cx1); free(G->cx2); free(G->ax1); free(G->ax2); free(G->cy1); free(G->cy2); free(G->ay1); free(G->ay2);
     free(G->cz1); free(G->cz2); free(G->az1); free(G->az2);
     free(G->vp); free(G->e2); free(G->d2); free(G->mA); free(G->mB); free(G->mC); free(G->amp); free(G->act);
+    free(G->tct); free(G->tst); free(G->tcp); free(G->tsp);
+}
+
+/* 3D TTI: tilt theta (from the vertical) and azimuth phi in degrees on the
+ * interior, iz + nz*(ix + nx*iy); their cosines and sines on the padded grid
+ * (edge-replicated like the model).  The FP32 build forms them as the
+ * library does, cosf(deg * 0.017453292519943295f); the FP64 build in
+ * double. */
+static void g3d_tilt(orc_g3d *G, const float *theta, const float *phi)
+{
+    const long n = G->n, nnz = G->nnz, nxz = G->nxz;
+    const int npd = G->npd;
+    long ix, iy, iz, k;
+    REAL *t[4];
+    for (k = 0; k < 4; k++) t[k] = calloc(n, sizeof(REAL));
+    for (iy = 0; iy < G->ny; iy++) for (ix = 0; ix < G->nx; ix++) for (iz = 0; iz < G->nz; iz++) {
+        const long g = (iz + npd) + nnz * (ix + npd) + nxz * (iy + npd), q = iz + (long)G->nz * (ix + (long)G->nx * iy);
+#if defined(ORC_FP64)
+        const double a = (double)theta[q] * (3.14159265358979323846 / 180.0);
+        const double b = (double)phi[q] * (3.14159265358979323846 / 180.0);
+        t[0][g] = cos(a); t[1][g] = sin(a); t[2][g] = cos(b); t[3][g] = sin(b);
+#else
+        const float a = theta[q] * 0.017453292519943295f, b = phi[q] * 0.017453292519943295f;
+        t[0][g] = cosf(a); t[1][g] = sinf(a); t[2][g] = cosf(b); t[3][g] = sinf(b);
+#endif
+    }
+    for (k = 0; k < 4; k++) orc_pad3d(G->nx, G->ny, G->nz, npd, t[k]);
+    G->tct = t[0]; G->tst = t[1]; G->tcp = t[2]; G->tsp = t[3];
+}
+
+/* One 3D TTI time step (no reference counterpart: the 2D TTI GPU programs'
+ * rotated-derivative scheme, 2D-tti-fd+rtm-cuda/Toa_gpu_2dtti_fd_1orderfunction.cu:81-183,
+ * extended to a symmetry axis with tilt t and azimuth f).  With the rotated
+ * frame x' = (cos t cos f, cos t sin f, -sin t), y' = (-sin f, cos f, 0),
+ * z' = (sin t cos f, sin t sin f, cos t):
+ *   u <- k2 u - k1 d/dx' P,  v <- k2 v - k1 d/dy' P,  w <- k2 w - k1 d/dz' Q
+ *   P <- k2 P - k1 (A a + B b),  Q <- k2 Q - k1 (B a + C b)
+ * with a = du/dx' + dv/dy', b = dw/dz', A = vp^2(1+2eps),
+ * B = vp^2 sqrtf(1+2del), C = vp^2, and the 2D programs' product sponge
+ * (k = cx*cy*cz on the half grid for the velocities, ax*ay*az for the
+ * stresses).  Every axis derivative has the 2D programs' stagger: forward
+ * (+1/2) for the velocities, backward for the stresses.  P,Q are unsplit
+ * (the 2D programs' split pairs share one damping factor, so their sum is
+ * the same update).  The source is added to P,Q before the velocity update
+ * and only reaches the velocities, as in the VTI step. */
+static void g3d_step_tti(const orc_g3d *G, orc_f3d *F, int src_on, REAL amp)
+{
+    const long nnx = G->nnx, nny = G->nny, nnz = G->nnz, nxz = G->nxz, src = G->src;
+    const REAL dtx = G->dtx, dty = G->dty, dtz = G->dtz;
+    REAL *u = F->u, *vv_ = F->v, *w = F->w, *P = F->P, *Q = F->Q;
+    const float *cx1 = G->cx1, *cx2 = G->cx2, *cy1 = G->cy1, *cy2 = G->cy2, *cz1 = G->cz1, *cz2 = G->cz2;
+    const float *ax1 = G->ax1, *ax2 = G->ax2, *ay1 = G->ay1, *ay2 = G->ay2, *az1 = G->az1, *az2 = G->az2;
+    const REAL *mA = G->mA, *mB = G->mB, *mC = G->mC;
+    const REAL *tct = G->tct, *tst = G->tst, *tcp = G->tcp, *tsp = G->tsp;
+    long ix, iy, iz;
+    REAL P_src0 = P[src], Q_src0 = Q[src];
+    if (src_on) { P[src] += amp; Q[src] += amp; }
+#pragma omp parallel for schedule(static) private(ix, iz)
+    for (iy = 4; iy < nny - 4; iy++)
+        for (ix = 4; ix < nnx - 4; ix++)
+            for (iz = 4; iz < nnz - 4; iz++) {
+                const long id = iz + ix * nnz + iy * nxz; int im;
+                REAL Px = 0, Py = 0, Pz = 0, Qx = 0, Qy = 0, Qz = 0;
+                for (im = 0; im < 4; im++) {
+                    Px += (REAL)C8[im] * (P[id + (im + 1) * nnz] - P[id - im * nnz]);
+                    Py += (REAL)C8[im] * (P[id + (im + 1) * nxz] - P[id - im * nxz]);
+                    Pz += (REAL)C8[im] * (P[id + im + 1] - P[id - im]);
+                    Qx += (REAL)C8[im] * (Q[id + (im + 1) * nnz] - Q[id - im * nnz]);
+                    Qy += (REAL)C8[im] * (Q[id + (im + 1) * nxz] - Q[id - im * nxz]);
+                    Qz += (REAL)C8[im] * (Q[id + im + 1] - Q[id - im]);
+                }
+                const REAL a = tct[id], b = tst[id], c = tcp[id], sn = tsp[id];
+                const REAL k2 = (REAL)cx2[ix] * (REAL)cy2[iy] * (REAL)cz2[iz];
+                const REAL k1 = (REAL)cx1[ix] * (REAL)cy1[iy] * (REAL)cz1[iz];
+                const REAL gx = a * c * dtx * Px + a * sn * dty * Py - b * dtz * Pz;
+                const REAL gy = c * dty * Py - sn * dtx * Px;
+                const REAL gz = b * c * dtx * Qx + b * sn * dty * Qy + a * dtz * Qz;
+                u[id] = k2 * u[id] - k1 * gx;
+                vv_[id] = k2 * vv_[id] - k1 * gy;
+                w[id] = k2 * w[id] - k1 * gz;
+            }
+#pragma omp parallel for schedule(static) private(ix, iz)
+    for (iy = 4; iy < nny - 4; iy++)
+        for (ix = 4; ix < nnx - 4; ix++)
+            for (iz = 4; iz < nnz - 4; iz++) {
+                const long id = iz + ix * nnz + iy * nxz; int im;
+                REAL ux = 0, uy = 0, uz = 0, vx = 0, vy = 0, wx = 0, wy = 0, wz = 0;
+                for (im = 0; im < 4; im++) {
+                    ux += (REAL)C8[im] * (u[id + im * nnz] - u[id - (im + 1) * nnz]);
+                    uy += (REAL)C8[im] * (u[id + im * nxz] - u[id - (im + 1) * nxz]);
+                    uz += (REAL)C8[im] * (u[id + im] - u[id - im - 1]);
+                    vx += (REAL)C8[im] * (vv_[id + im * nnz] - vv_[id - (im + 1) * nnz]);
+                    vy += (REAL)C8[im] * (vv_[id + im * nxz] - vv_[id - (im + 1) * nxz]);
+                    wx += (REAL)C8[im] * (w[id + im * nnz] - w[id - (im + 1) * nnz]);
+                    wy += (REAL)C8[im] * (w[id + im * nxz] - w[id - (im + 1) * nxz]);
+                    wz += (REAL)C8[im] * (w[id + im] - w[id - im - 1]);
+                }
+                const REAL a = tct[id], b = tst[id], c = tcp[id], sn = tsp[id];
+                const REAL ha = (a * c * dtx * ux + a * sn * dty * uy - b * dtz * uz) + (c * dty * vy - sn * dtx * vx);
+                const REAL hb = b * c * dtx * wx + b * sn * dty * wy + a * dtz * wz;
+                const REAL k2 = (REAL)ax2[ix] * (REAL)ay2[iy] * (REAL)az2[iz];
+                const REAL k1 = (REAL)ax1[ix] * (REAL)ay1[iy] * (REAL)az1[iz];
+                const REAL p0 = (id == src) ? P_src0 : P[id], q0 = (id == src) ? Q_src0 : Q[id];
+                P[id] = k2 * p0 - k1 * (mA[id] * ha + mB[id] * hb);
+                Q[id] = k2 * q0 - k1 * (mB[id] * ha + mC[id] * hb);
+            }
 }
 
 /* One 3D time step of field set F; the point source (amp, when src_on) is
@@ -1248,6 +1355,7 @@ static void g3d_free(orc_g3d *G)
  * only affects the velocities (the stress update overwrites P,Q). */
 static void g3d_step(const orc_g3d *G, orc_f3d *F, int src_on, REAL amp)
 {
+    if (G->tct) { g3d_step_tti(G, F, src_on, amp); return; }
     const long nnx = G->nnx, nny = G->nny, nnz = G->nnz, nxz = G->nxz, src = G->src;
     const int npd = G->npd, fast = G->fast;
     const REAL dtx = G->dtx, dty = G->dty, dtz = G->dtz;
@@ -1348,12 +1456,13 @@ static void g3d_step(const orc_g3d *G, orc_f3d *F, int src_on, REAL amp)
  * centre velocity (:203-206).  shot is (nt x nrx*nry) trace-major,
  * shot[it + nt*(irx + nrx*iry)] = P[rec_iz, npd+rx0+irx*drx, npd+ry0+iry*dry].
  * final_P/final_Q (optional) receive the padded P, Q at the end. */
-int orc_fd3d(const orc_fd3d_desc *d, const float *v, const float *e, const float *dl,
-             float *shot, float *final_P, float *final_Q)
+static int fd3d_run(const orc_fd3d_desc *d, const float *v, const float *e, const float *dl, const float *theta,
+                    const float *phi, float *shot, float *final_P, float *final_Q)
 {
     orc_g3d G; orc_f3d F;
     int it; long k;
     g3d_init(&G, d, v, e, dl);
+    if (theta) g3d_tilt(&G, theta, phi);
     f3d_alloc(&F, G.n);
     for (it = 0; it < d->nt; it++) {
         g3d_step(&G, &F, G.act[it], (REAL)G.amp[it]);
@@ -1394,13 +1503,15 @@ int orc_fd3d(const orc_fd3d_desc *d, const float *v, const float *e, const float
  *   adcigs[iz + nz*(ia + na*(ix + nxa*iy))] += sP*gP*c*c*c, c = cosf(ia*pi/180)
  * (velocities of the new time level: the program's u0 = u1 pointer
  * assignment makes the update in place); the caller divides (adcigs_illum). */
-int orc_rtm3d_shot(const orc_fd3d_desc *d, int mute_tt, const float *v, const float *e, const float *dl,
-                   float *mig, float *illum, float *rec_out, int na, int da, int dcdp, float *adcigs)
+static int rtm3d_shot_run(const orc_fd3d_desc *d, int mute_tt, const float *v, const float *e, const float *dl,
+                          const float *theta, const float *phi, float *mig, float *illum, float *rec_out, int na,
+                          int da, int dcdp, float *adcigs)
 {
     orc_g3d G; orc_f3d S, R;
     const int nx = d->nx, ny = d->ny, nz = d->nz, npd = d->npd, nt = d->nt;
     long it, ix, iy, iz;
     g3d_init(&G, d, v, e, dl);
+    if (theta) g3d_tilt(&G, theta, phi);
     f3d_alloc(&S, G.n);
     f3d_alloc(&R, G.n);
     const long L = 2L * nx * ny + 2L * nz * ny + 2L * nx * nz;
@@ -1499,8 +1610,8 @@ int orc_rtm3d_shot(const orc_fd3d_desc *d, int mute_tt, const float *v, const fl
  * interior P of every step it with it % k == k-1; the backward pass
  * propagates only the receiver field (same injection and illumination) and
  * at those steps adds mig += (k * snap) * gP. */
-int orc_rtm3d_snap_shot(const orc_fd3d_desc *d, int mute_tt, int k, const float *v, const float *e, const float *dl,
-                        float *mig, float *illum)
+static int rtm3d_snap_run(const orc_fd3d_desc *d, int mute_tt, int k, const float *v, const float *e,
+                          const float *dl, const float *theta, const float *phi, float *mig, float *illum)
 {
     orc_g3d G; orc_f3d S, R;
     const int nx = d->nx, ny = d->ny, nz = d->nz, npd = d->npd, nt = d->nt;
@@ -1508,6 +1619,7 @@ int orc_rtm3d_snap_shot(const orc_fd3d_desc *d, int mute_tt, int k, const float 
     const int nsnap = nt / k;
     long it, ix, iy, iz;
     g3d_init(&G, d, v, e, dl);
+    if (theta) g3d_tilt(&G, theta, phi);
     f3d_alloc(&S, G.n);
     f3d_alloc(&R, G.n);
     float *snap = calloc((size_t)(nsnap > 0 ? nsnap : 1) * nimg, 4);
@@ -1558,6 +1670,54 @@ int orc_rtm3d_snap_shot(const orc_fd3d_desc *d, int mute_tt, int k, const float 
     free(snap); free(rec);
     f3d_free(&S); f3d_free(&R); g3d_free(&G);
     return 0;
+}
+
+int orc_fd3d(const orc_fd3d_desc *d, const float *v, const float *e, const float *dl,
+             float *shot, float *final_P, float *final_Q)
+{
+    return fd3d_run(d, v, e, dl, NULL, NULL, shot, final_P, final_Q);
+}
+
+int orc_rtm3d_shot(const orc_fd3d_desc *d, int mute_tt, const float *v, const float *e, const float *dl,
+                   float *mig, float *illum, float *rec_out, int na, int da, int dcdp, float *adcigs)
+{
+    return rtm3d_shot_run(d, mute_tt, v, e, dl, NULL, NULL, mig, illum, rec_out, na, da, dcdp, adcigs);
+}
+
+int orc_rtm3d_snap_shot(const orc_fd3d_desc *d, int mute_tt, int k, const float *v, const float *e, const float *dl,
+                        float *mig, float *illum)
+{
+    return rtm3d_snap_run(d, mute_tt, k, v, e, dl, NULL, NULL, mig, illum);
+}
+
+/* The same three runs on a 3D TTI medium (g3d_step_tti); theta and phi in
+ * degrees on the interior.  The model takes the premultiplied form. */
+static orc_fd3d_desc tti_desc(const orc_fd3d_desc *d)
+{
+    orc_fd3d_desc t = *d;
+    t.mode = 1;
+    return t;
+}
+
+int orc_tti3d(const orc_fd3d_desc *d, const float *v, const float *e, const float *dl, const float *theta,
+              const float *phi, float *shot, float *final_P, float *final_Q)
+{
+    const orc_fd3d_desc t = tti_desc(d);
+    return fd3d_run(&t, v, e, dl, theta, phi, shot, final_P, final_Q);
+}
+
+int orc_rtm3d_tti_shot(const orc_fd3d_desc *d, int mute_tt, const float *v, const float *e, const float *dl,
+                       const float *theta, const float *phi, float *mig, float *illum, float *rec_out)
+{
+    const orc_fd3d_desc t = tti_desc(d);
+    return rtm3d_shot_run(&t, mute_tt, v, e, dl, theta, phi, mig, illum, rec_out, 0, 1, 1, NULL);
+}
+
+int orc_rtm3d_tti_snap_shot(const orc_fd3d_desc *d, int mute_tt, int k, const float *v, const float *e,
+                            const float *dl, const float *theta, const float *phi, float *mig, float *illum)
+{
+    const orc_fd3d_desc t = tti_desc(d);
+    return rtm3d_snap_run(&t, mute_tt, k, v, e, dl, theta, phi, mig, illum);
 }
 
 /* migration_illum (:539-553): mig /= illum where illum != 0. */

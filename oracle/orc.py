@@ -55,6 +55,9 @@ def lib(prec=32):
         L.orc_fd2d.argtypes = [C.POINTER(FD2DDesc)] + [C.POINTER(C.c_float)] * 5 + [C.c_int]
         L.orc_tti2d.argtypes = [C.POINTER(FD2DDesc)] + [C.POINTER(C.c_float)] * 6 + [C.c_int]
         L.orc_fd3d.argtypes = [C.POINTER(FD3DDesc)] + [C.POINTER(C.c_float)] * 6
+        L.orc_tti3d.argtypes = [C.POINTER(FD3DDesc)] + [C.POINTER(C.c_float)] * 8
+        L.orc_rtm3d_tti_shot.argtypes = [C.POINTER(FD3DDesc), C.c_int] + [C.POINTER(C.c_float)] * 8
+        L.orc_rtm3d_tti_snap_shot.argtypes = [C.POINTER(FD3DDesc), C.c_int, C.c_int] + [C.POINTER(C.c_float)] * 7
         L.orc_rtm2d_mpi_shot.argtypes = [C.c_int] * 4 + [C.c_float] * 5 + [C.c_int] * 5 + \
             [C.POINTER(C.c_float)] * 4 + [C.POINTER(C.c_int), C.POINTER(C.c_float), C.POINTER(C.c_float)]
         L.orc_laplace2d_adj.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_float), C.POINTER(C.c_float)]
@@ -112,8 +115,10 @@ def tti2d(v, e, d, theta, *, npd, nt, dx, dz, dt, favg, pfac, fs, zs, ds=0.0, is
 
 def fd3d(v, e, d, *, npd, nt, dx, dy, dz, dt, favg, pfac, fsx, fsy, fsz, dsx=0, dsy=0, dsz=0,
          is_=0, sv=0, wtype=1, mode=0, rec_iz=None, rx0=0, drx=1, nrx=None, ry0=0, dry=1, nry=None,
-         final=False, prec=32):
-    """3D forward modelling (GUI GPU semantics); v,e,d shaped (ny, nx, nz)."""
+         final=False, prec=32, theta=None, phi=None):
+    """3D forward modelling (GUI GPU semantics); v,e,d shaped (ny, nx, nz).
+    With theta and phi (tilt and azimuth in degrees, same shape) the 3D TTI
+    step of orc_tti3d instead (premultiplied model, mode ignored)."""
     v, e, d = c32(v), c32(e), c32(d)
     ny, nx, nz = v.shape
     nrx = nx if nrx is None else nrx
@@ -127,19 +132,29 @@ def fd3d(v, e, d, *, npd, nt, dx, dy, dz, dt, favg, pfac, fsx, fsy, fsz, dsx=0, 
     if final:
         shape = (ny + 2 * npd, nx + 2 * npd, nz + 2 * npd)
         fp, fq = np.zeros(shape, _f), np.zeros(shape, _f)
-    lib(prec).orc_fd3d(C.byref(desc), _fp(v), _fp(e), _fp(d), _fp(shot), _fp(fp), _fp(fq))
+    if theta is not None:
+        th, ph = c32(theta), c32(phi)
+        lib(prec).orc_tti3d(C.byref(desc), _fp(v), _fp(e), _fp(d), _fp(th), _fp(ph), _fp(shot), _fp(fp), _fp(fq))
+    else:
+        lib(prec).orc_fd3d(C.byref(desc), _fp(v), _fp(e), _fp(d), _fp(shot), _fp(fp), _fp(fq))
     return (shot, fp, fq) if final else shot
 
 
 def rtm3d(v, e, d, *, npd, nt, dx, dy, dz, dt, favg, pfac, fsx, fsy, fsz, dsx=0, dsy=0, dsz=0,
-          ns=1, sv=0, wtype=1, mode=0, mute_tt=70, snap_every=0, prec=32, adcig=None):
+          ns=1, sv=0, wtype=1, mode=0, mute_tt=70, snap_every=0, prec=32, adcig=None, theta=None, phi=None):
     """3D boundary-saving RTM over shots 0..ns-1 (3D GPU RTM program
     semantics; with snap_every > 0 the stored-snapshot method instead);
     v,e,d shaped (ny, nx, nz).  Returns (mig divided by the illumination,
     illum, last shot's muted record (ny, nx, nt); zeros for snap_every > 0)
     [+ the Poynting angle gathers (ny/dcdp, nx/dcdp, na, nz) divided by the
-    illumination, when adcig = (na, da, dcdp)]."""
+    illumination, when adcig = (na, da, dcdp)].  theta/phi (degrees): the
+    3D TTI medium (no angle gathers)."""
     v, e, d = c32(v), c32(e), c32(d)
+    tti = theta is not None
+    if tti:
+        if adcig is not None:
+            raise ValueError("no angle gathers on the TTI medium")
+        th, ph = c32(theta), c32(phi)
     ny, nx, nz = v.shape
     mig = np.zeros((ny, nx, nz), _f)
     ill = np.zeros((ny, nx, nz), _f)
@@ -156,7 +171,13 @@ def rtm3d(v, e, d, *, npd, nt, dx, dy, dz, dt, favg, pfac, fsx, fsy, fsz, dsx=0,
                         dx=dx, dy=dy, dz=dz, dt=dt, favg=favg, pfac=pfac, fsx=fsx, fsy=fsy, fsz=fsz,
                         dsx=dsx, dsy=dsy, dsz=dsz, is_=is_, rec_iz=npd,
                         rx0=0, drx=1, nrx=nx, ry0=0, dry=1, nry=ny)
-        if snap_every:
+        if tti and snap_every:
+            lib(prec).orc_rtm3d_tti_snap_shot(C.byref(desc), mute_tt, snap_every, _fp(v), _fp(e), _fp(d), _fp(th),
+                                              _fp(ph), _fp(mig), _fp(ill))
+        elif tti:
+            lib(prec).orc_rtm3d_tti_shot(C.byref(desc), mute_tt, _fp(v), _fp(e), _fp(d), _fp(th), _fp(ph),
+                                         _fp(mig), _fp(ill), _fp(rec))
+        elif snap_every:
             lib(prec).orc_rtm3d_snap_shot(C.byref(desc), mute_tt, snap_every, _fp(v), _fp(e), _fp(d), _fp(mig),
                                           _fp(ill))
         else:

@@ -69,3 +69,14 @@ def wave_blocks(nb, seed):
         f *= np.exp(-((z - 8) ** 2 + (x - 8) ** 2 + (y - 8) ** 2) / rng.uniform(20, 80))
         out[b] = (rng.uniform(0.1, 10) * f)[zz, xx, yy]
     return out
+
+
+def smooth_angles(shape, seed=0):
+    """Smooth tilt 2.5-42.5 deg and azimuth 10-350 deg fields (ny, nx, nz)."""
+    ny, nx, nz = shape
+    rng = np.random.default_rng(seed)
+    a, b, c = rng.uniform(5, 12, 3)
+    Y, X, Z = np.meshgrid(np.arange(ny), np.arange(nx), np.arange(nz), indexing="ij")
+    theta = 22.5 + 20.0 * np.sin(X / a + Y / b) * np.cos(Z / c)
+    phi = 180.0 + 170.0 * np.sin(X / c - Y / a + Z / b)
+    return theta.astype(np.float32), phi.astype(np.float32)
