@@ -324,10 +324,42 @@ def run_traffic_case(args):
     print(json.dumps({"case": "traffic", "grid": NX, "steps": args.steps}))
 
 
-def train_codec(geo, iters, models=32, n=96, seed=1):
+def smooth_field(shape, corr, seed, device="cuda"):
+    """Seeded Gaussian random field (FFT-filtered white noise, correlation
+    `corr` cells) scaled to [0, 1]."""
+    import torch
+    ny, nx, nz = shape
+    g = torch.Generator(device="cpu").manual_seed(seed)
+    noise = torch.randn(shape, generator=g, dtype=torch.float32).to(device)
+    sig = corr / 2.0
+    fy = torch.fft.fftfreq(ny, device=device)[:, None, None]
+    fx = torch.fft.fftfreq(nx, device=device)[None, :, None]
+    fz = torch.fft.rfftfreq(nz, device=device)[None, None, :]
+    filt = torch.exp(-2.0 * (torch.pi ** 2) * sig ** 2 * (fx ** 2 + fy ** 2 + fz ** 2))
+    f = torch.fft.irfftn(torch.fft.rfftn(noise) * filt, s=shape)
+    return ((f - f.min()) / (f.max() - f.min())).float().contiguous()
+
+
+def tti_model(shape, seed=5, device="cuda"):
+    """3D TTI medium: vp as make_model (random field + dipping interfaces),
+    eps = 0.3 r and del = -0.05 + 0.2 r with r = (vp - 1500) / 3000 (so
+    del < eps everywhere: the pseudo-acoustic TTI scheme is unstable where
+    del > eps), tilt 0-45 deg and azimuth 0-360 deg as seeded smooth fields
+    (correlation 60 cells)."""
+    vp, _, _ = make_model(seed=seed, device=device, shape=shape)
+    r = ((vp - 1500.0) / 3000.0).clamp(0, 1)
+    eps = (0.3 * r).float().contiguous()
+    dl = (-0.05 + 0.2 * r).float().contiguous()
+    theta = (45.0 * smooth_field(shape, 60.0, seed + 1000, device)).contiguous()
+    phi = (360.0 * smooth_field(shape, 60.0, seed + 2000, device)).contiguous()
+    return vp, eps, dl, theta, phi
+
+
+def train_codec(geo, iters, models=32, n=96, seed=1, tti=False):
     """The codec trained on snapshots the solver generates: `models` seeded
     random-field media of n^3 (correlation 8-40 cells, random surface
-    source), P every 12 steps of a 560-step shot (SV taper on)."""
+    source), P every 12 steps of a 560-step shot (SV taper on); with `tti`
+    the media are 3D TTI (tti_model) at n^3."""
     import numpy as np
     import torch
     codec = geo.Codec(seed=seed)
@@ -336,10 +368,15 @@ def train_codec(geo, iters, models=32, n=96, seed=1):
     kw = dict(npd=16, nt=560, dx=DX, dy=DX, dz=DX, dt=DT, favg=FAVG, fsz=1, mode="fast", sv=1)
     t0 = time.perf_counter()
     for s in range(models):
-        v, e, d = make_model(seed=100 + s, device="cuda", shape=(n, n, n), corr=float(rng.uniform(8, 40)))
+        if tti:
+            v, e, d, th, ph = tti_model((n, n, n), seed=100 + s)
+        else:
+            v, e, d = make_model(seed=100 + s, device="cuda", shape=(n, n, n), corr=float(rng.uniform(8, 40)))
         plan = geo.FD3DPlan(nx=n, ny=n, nz=n, fsx=int(rng.integers(16, n - 16)), fsy=int(rng.integers(16, n - 16)),
                             **kw)
         plan.set_model(v, e, d)
+        if tti:
+            plan.set_tilt(th, ph)
         codec.add_shot(plan, 0, snap_every=12, t_first=8)
         plan.close()
     torch.cuda.synchronize()
@@ -413,6 +450,108 @@ def run_rtm_learned_case(args):
                             "escape_budget": args.escape},
             "training": tinfo, "dtype": "f32 propagation, bf16 codec", "data": "synthetic"}
     print(json.dumps(line), flush=True)
+
+
+TTI_SHAPE, TTI_DX, TTI_DT, TTI_FAVG, TTI_NT = (600, 600, 400), 12.5, 0.0008, 12.0, 3500
+TTI_BYTES_PER_PT = 104   # velocity kernel 12 floats (P,Q,u,v,w,4 trig in; u,v,w out), stress 14
+
+
+def run_tti_case(args):
+    """Bare 3D TTI time steps on the 600x600x400 (+40 sponge) medium at
+    12.5 m, dt 0.8 ms (tti_model): updates/s and the two kernels' roofline
+    (104 algorithmic bytes per updated point against the measured copy
+    peak).  cpu: the oracle's FP32 TTI restatement (OpenMP, all host
+    cores) on a 120^3 + 20 sample, 10 steps."""
+    import numpy as np
+    import torch
+
+    import geophysics_gb300 as geo
+    from geophysics_gb300 import build as B
+    B.build()
+    ny, nx, nz = TTI_SHAPE
+    v, e, d, th, ph = tti_model(TTI_SHAPE)
+    plan = geo.FD3DPlan(nx=nx, ny=ny, nz=nz, npd=NPD, nt=10, dx=TTI_DX, dy=TTI_DX, dz=TTI_DX, dt=TTI_DT,
+                        favg=TTI_FAVG, fsx=nx // 2, fsy=ny // 2, fsz=1, mode="fast")
+    plan.set_model(v, e, d)
+    plan.set_tilt(th, ph)
+    plan.time_steps(max(3, args.warmup))
+    nsteps = max(10, 10 * args.steps)
+    ms = plan.time_steps(nsteps) / nsteps
+    plan.close()
+    pts = (nx + 2 * NPD - 8) * (ny + 2 * NPD - 8) * (nz + 2 * NPD - 8)
+    peak, peak_kind = measured_peak()
+    achieved = pts * TTI_BYTES_PER_PT / (ms / 1000) / 1e9
+    cpu = None
+    if not args.no_cpu:
+        from oracle import orc
+        orc.build(with_ref=False)
+        n = 120
+        cv, ce, cd, cth, cph = (a.cpu().numpy() for a in tti_model((n, n, n), seed=7))
+        t0 = time.perf_counter()
+        orc.fd3d(cv, ce, cd, theta=cth, phi=cph, npd=20, nt=10, dx=TTI_DX, dy=TTI_DX, dz=TTI_DX,
+                 dt=np.float32(TTI_DT), favg=TTI_FAVG, pfac=10.0, fsx=n // 2, fsy=n // 2, fsz=1)
+        sec = time.perf_counter() - t0
+        cpu = {"value": (n + 40 - 8) ** 3 * 10 / sec / 1e9, "unit": "Gpt/s", "cores": os.cpu_count(),
+               "kind": "port", "sample": "10 steps of 120^3 + 20 sponge, oracle FP32 TTI restatement, OpenMP"}
+    print(json.dumps({"case": "tti", "metric": "grid-pt updates/s", "value": pts / (ms / 1000) / 1e9,
+                      "unit": "Gpt/s", "ms_per_step": ms,
+                      "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                                   "frac": achieved / peak, "peak_kind": peak_kind,
+                                   "unit_of_work": "one time step (%d updates, %d B each)" % (pts, TTI_BYTES_PER_PT)},
+                      "config": {"workload": "3D TTI step, 600x600x400 (+40 sponge) at 12.5 m, dt 0.8 ms, tilt "
+                                             "0-45 deg, azimuth 0-360 deg (smooth seeded fields)"},
+                      "cpu_baseline": cpu, "dtype": "f32", "data": "synthetic"}), flush=True)
+
+
+def run_tti_rtm_case(args):
+    """3D TTI RTM on the 600x600x400 (+40 sponge) medium at 12.5 m, 3500
+    steps, 12 Hz, 300x300 surface receivers every 2nd node are recorded by
+    the RTM (every surface node, as the 3D RTM program): plain
+    boundary-saving recompute against snapshots every 4 steps through the
+    learned codec trained on TTI snapshots from the solver.  `--shots`
+    shots back to back (source positions spread along x); shots/hour of both
+    methods, the learned image's error against the plain image (the judge)
+    and, on the first err_nt steps, against stored fp32 snapshots."""
+    import torch
+
+    import geophysics_gb300 as geo
+    from geophysics_gb300 import build as B
+    B.build()
+    ny, nx, nz = TTI_SHAPE
+    v, e, d, th, ph = tti_model(TTI_SHAPE)
+    codec, tinfo = train_codec(geo, args.train_iters, tti=True)
+    rk = dict(npd=NPD, dx=TTI_DX, dy=TTI_DX, dz=TTI_DX, dt=TTI_DT, favg=TTI_FAVG, fsx=nx // 2 - 100, fsy=ny // 2,
+              dsx=200 // max(1, args.shots - 1) if args.shots > 1 else 0, fsz=1, mute_tt=70, laplace=True,
+              mode="fast", theta=th, phi=ph)
+
+    def timed(nt, ns, **kw):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        out = geo.rtm3d(v, e, d, nt=nt, ns=ns, **rk, **kw)
+        torch.cuda.synchronize()
+        return out, time.perf_counter() - t0
+
+    codec.set_escape(0.02, args.escape)
+    bnd, tb = timed(args.nt, args.shots, method="boundary")
+    lrn, tl = timed(args.nt, args.shots, method="learned", snap_every=4, codec=codec)
+    ref, _ = timed(args.err_nt, 1, method="snapshot", snap_every=4)
+    l_short, _ = timed(args.err_nt, 1, method="learned", snap_every=4, codec=codec)
+    b_short, _ = timed(args.err_nt, 1, method="boundary")
+
+    def rel(a, b):
+        a, b = a[0].double(), b[0].double()
+        return float((a - b).norm() / b.norm())
+
+    print(json.dumps({"case": "tti-rtm", "metric": "3D TTI RTM shots/hr, learned snapshot codec vs boundary-saving "
+                                                   "recompute", "grid": [nx, ny, nz], "sponge": NPD, "nt": args.nt,
+                      "shots": args.shots, "snap_every": 4,
+                      "shots_per_hr": {"boundary": args.shots * 3600.0 / tb, "learned": args.shots * 3600.0 / tl},
+                      "seconds": {"boundary": tb, "learned": tl}, "speedup_vs_boundary": tb / tl,
+                      "image_rel_l2": {"learned_vs_boundary": rel(lrn, bnd),
+                                       "learned_vs_fp32_snapshots": rel(l_short, ref),
+                                       "boundary_vs_fp32_snapshots": rel(b_short, ref), "err_nt": args.err_nt,
+                                       "image": "Laplacian-filtered, illumination-divided"},
+                      "training": tinfo, "dtype": "f32 propagation, bf16 codec", "data": "synthetic"}), flush=True)
 
 
 def run_rtm_methods_case(args):
@@ -563,12 +702,14 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--case", default="full", choices=["full", "small", "traffic", "rtm-learned", "rtm-methods", "fd2d", "rtm2d"],
+    ap.add_argument("--case", default="full", choices=["full", "small", "traffic", "rtm-learned", "rtm-methods", "fd2d", "rtm2d",
+                                                      "tti", "tti-rtm"],
                     help="small / traffic: ncu profiling cases; rtm-learned: the learned-codec RTM comparison")
     ap.add_argument("--grid", type=int, default=192, help="small: cube edge")
     ap.add_argument("--sponge", type=int, default=40, help="small: sponge width")
-    ap.add_argument("--nt", type=int, default=3000, help="rtm-learned, rtm2d: time steps")
-    ap.add_argument("--shots", type=int, default=128, help="rtm2d: shots in the batch (the workload has 128)")
+    ap.add_argument("--nt", type=int, default=3000, help="rtm-learned, rtm2d, tti-rtm (3500 there): time steps")
+    ap.add_argument("--shots", type=int, default=128, help="rtm2d: shots in the batch (the workload has 128); "
+                                                           "tti-rtm: shots back to back (the workload has 8)")
     ap.add_argument("--err-nt", type=int, default=1200, help="rtm-learned: steps of the image-error comparison")
     ap.add_argument("--train-iters", type=int, default=16000, help="rtm-learned: codec training steps")
     ap.add_argument("--escape", type=float, default=0.03, help="rtm-learned: escaped-block budget")
@@ -579,6 +720,12 @@ def main():
         return
     if args.case == "rtm2d":
         run_rtm2d_case(args)
+        return
+    if args.case == "tti":
+        run_tti_case(args)
+        return
+    if args.case == "tti-rtm":
+        run_tti_rtm_case(args)
         return
     if args.case == "rtm-methods":
         run_rtm_methods_case(args)
