@@ -505,13 +505,15 @@ def run_tti_case(args):
 
 def run_tti_rtm_case(args):
     """3D TTI RTM on the 600x600x400 (+40 sponge) medium at 12.5 m, 3500
-    steps, 12 Hz, 300x300 surface receivers every 2nd node are recorded by
-    the RTM (every surface node, as the 3D RTM program): plain
-    boundary-saving recompute against snapshots every 4 steps through the
-    learned codec trained on TTI snapshots from the solver.  `--shots`
-    shots back to back (source positions spread along x); shots/hour of both
-    methods, the learned image's error against the plain image (the judge)
-    and, on the first err_nt steps, against stored fp32 snapshots."""
+    steps, 12 Hz, every surface node recorded (the 3D RTM program's
+    receivers; the 300x300 2-node grid is a subset): plain checkpoint
+    recompute (full wavefield every K steps, segments re-propagated; the
+    stored-snapshot image bit for bit) against snapshots every 4 steps
+    through the learned codec trained on TTI snapshots from the solver.
+    `--shots` shots back to back (sources spread along x); shots/hour of
+    both and the learned image's error against the plain one (the judge).
+    The reference programs' boundary re-propagation is not the judge here:
+    it diverges on the TTI medium."""
     import torch
 
     import geophysics_gb300 as geo
@@ -522,35 +524,35 @@ def run_tti_rtm_case(args):
     codec, tinfo = train_codec(geo, args.train_iters, tti=True)
     rk = dict(npd=NPD, dx=TTI_DX, dy=TTI_DX, dz=TTI_DX, dt=TTI_DT, favg=TTI_FAVG, fsx=nx // 2 - 100, fsy=ny // 2,
               dsx=200 // max(1, args.shots - 1) if args.shots > 1 else 0, fsz=1, mute_tt=70, laplace=True,
-              mode="fast", theta=th, phi=ph)
+              mode="fast", theta=th, phi=ph, nt=args.nt, ns=args.shots, snap_every=4)
 
-    def timed(nt, ns, **kw):
+    def timed(**kw):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        out = geo.rtm3d(v, e, d, nt=nt, ns=ns, **rk, **kw)
+        out = geo.rtm3d(v, e, d, **rk, **kw)
         torch.cuda.synchronize()
         return out, time.perf_counter() - t0
 
     codec.set_escape(0.02, args.escape)
-    bnd, tb = timed(args.nt, args.shots, method="boundary")
-    lrn, tl = timed(args.nt, args.shots, method="learned", snap_every=4, codec=codec)
-    ref, _ = timed(args.err_nt, 1, method="snapshot", snap_every=4)
-    l_short, _ = timed(args.err_nt, 1, method="learned", snap_every=4, codec=codec)
-    b_short, _ = timed(args.err_nt, 1, method="boundary")
+    b0, e0 = codec.stats()
+    plain, tp = timed(method="checkpoint")
+    lrn, tl = timed(method="learned", codec=codec)
+    b1, e1 = codec.stats()
 
     def rel(a, b):
         a, b = a[0].double(), b[0].double()
         return float((a - b).norm() / b.norm())
 
-    print(json.dumps({"case": "tti-rtm", "metric": "3D TTI RTM shots/hr, learned snapshot codec vs boundary-saving "
-                                                   "recompute", "grid": [nx, ny, nz], "sponge": NPD, "nt": args.nt,
-                      "shots": args.shots, "snap_every": 4,
-                      "shots_per_hr": {"boundary": args.shots * 3600.0 / tb, "learned": args.shots * 3600.0 / tl},
-                      "seconds": {"boundary": tb, "learned": tl}, "speedup_vs_boundary": tb / tl,
-                      "image_rel_l2": {"learned_vs_boundary": rel(lrn, bnd),
-                                       "learned_vs_fp32_snapshots": rel(l_short, ref),
-                                       "boundary_vs_fp32_snapshots": rel(b_short, ref), "err_nt": args.err_nt,
-                                       "image": "Laplacian-filtered, illumination-divided"},
+    esc = (e1 - e0) / max(1, b1 - b0)
+    print(json.dumps({"case": "tti-rtm", "metric": "3D TTI RTM shots/hr, learned snapshot codec vs plain "
+                                                   "checkpoint recompute", "grid": [nx, ny, nz], "sponge": NPD,
+                      "nt": args.nt, "shots": args.shots, "snap_every": 4,
+                      "shots_per_hr": {"checkpoint": args.shots * 3600.0 / tp, "learned": args.shots * 3600.0 / tl},
+                      "seconds": {"checkpoint": tp, "learned": tl}, "speedup_vs_plain": tp / tl,
+                      "image_rel_l2_learned_vs_plain": rel(lrn, plain),
+                      "image": "Laplacian-filtered, illumination-divided",
+                      "compression": {"escaped_block_frac": esc, "ratio": 16384 / (1024 + 4 + 4 + esc * 8192),
+                                      "escape_budget": args.escape},
                       "training": tinfo, "dtype": "f32 propagation, bf16 codec", "data": "synthetic"}), flush=True)
 
 

@@ -13,7 +13,7 @@ GEO_OK = 0
 GEO_MEM_HOST, GEO_MEM_DEVICE = 0, 1
 GEO_VARIANT_CPU, GEO_VARIANT_GPU, GEO_VARIANT_MPI = 0, 1, 2
 GEO_MODE_EXACT, GEO_MODE_FAST = 0, 1
-GEO_RTM_BOUNDARY, GEO_RTM_SNAPSHOT, GEO_RTM_LEARNED = 0, 1, 2
+GEO_RTM_BOUNDARY, GEO_RTM_SNAPSHOT, GEO_RTM_LEARNED, GEO_RTM_CHECKPOINT = 0, 1, 2, 3
 
 STATUS = {0: "GEO_OK", 1: "GEO_ERR_ARG", 2: "GEO_ERR_CUDA", 3: "GEO_ERR_IO", 4: "GEO_ERR_MODEL",
           5: "GEO_ERR_CFL", 6: "GEO_ERR_WINDOW", 7: "GEO_ERR_NOMEM", 8: "GEO_ERR_NAN"}
@@ -44,7 +44,7 @@ class FD3DDesc(C.Structure):
 class RTM3DDesc(C.Structure):
     _fields_ = [("fd", FD3DDesc), ("ns", C.c_int), ("mute_tt", C.c_int), ("method", C.c_int),
                 ("snap_every", C.c_int), ("ae", C.c_void_p), ("na", C.c_int), ("da", C.c_int), ("dcdp", C.c_int),
-                ("theta", C.c_void_p), ("phi", C.c_void_p)]
+                ("theta", C.c_void_p), ("phi", C.c_void_p), ("ckpt_every", C.c_int)]
 
 
 class RTM2DGpuDesc(C.Structure):

@@ -10,7 +10,7 @@ import ctypes as C
 import numpy as np
 
 from ._lib import (FD2DDesc, FD3DDesc, GEO_MEM_DEVICE, GEO_MEM_HOST, GEO_MODE_EXACT, GEO_MODE_FAST,
-                   GEO_RTM_BOUNDARY, GEO_RTM_LEARNED, GEO_RTM_SNAPSHOT, GEO_VARIANT_CPU, GEO_VARIANT_GPU,
+                   GEO_RTM_BOUNDARY, GEO_RTM_CHECKPOINT, GEO_RTM_LEARNED, GEO_RTM_SNAPSHOT, GEO_VARIANT_CPU, GEO_VARIANT_GPU,
                    GEO_VARIANT_MPI, RTM2DDesc, RTM2DGpuDesc, RTM3DDesc, check, lib)
 
 _VARIANTS = {"cpu": GEO_VARIANT_CPU, "gpu": GEO_VARIANT_GPU, "mpi": GEO_VARIANT_MPI}
@@ -204,18 +204,22 @@ def fd3d_shot(v, e, d, is_=0, theta=None, phi=None, **kw):
         plan.close()
 
 
-_RTM = {"boundary": GEO_RTM_BOUNDARY, "snapshot": GEO_RTM_SNAPSHOT, "learned": GEO_RTM_LEARNED}
+_RTM = {"boundary": GEO_RTM_BOUNDARY, "snapshot": GEO_RTM_SNAPSHOT, "learned": GEO_RTM_LEARNED,
+        "checkpoint": GEO_RTM_CHECKPOINT}
 
 
 def rtm3d(v, e, d, *, npd, nt, dx, dy, dz, dt, favg, fsx, fsy, fsz, ns=1, dsx=0, dsy=0, dsz=0, mute_tt=70,
           pfac=10.0, wtype=1, sv=0, mode="fast", laplace=True, illum=False, method="boundary", snap_every=4,
-          codec=None, adcig=None, theta=None, phi=None):
+          codec=None, adcig=None, theta=None, phi=None, ckpt_every=0):
     """3D RTM over shots 0..ns-1; v,e,d shaped (ny, nx, nz); theta, phi
     (degrees, same shape): the 3D TTI medium (mode "fast", no gathers).
 
     method "boundary": the 3D GPU RTM program's boundary-saving recompute;
     "snapshot": source P kept every snap_every steps (fp32);
-    "learned": the same snapshots through `codec` (a trained Codec).
+    "learned": the same snapshots through `codec` (a trained Codec);
+    "checkpoint": exact recompute from full wavefields saved every
+    ckpt_every steps (0: the interval minimising states plus segment
+    snapshots); same image as "snapshot" in bounded memory.
     adcig = (na, da, dcdp) (boundary method): also the Poynting angle
     gathers, shaped (ny//dcdp, nx//dcdp, na, nz), illumination-divided.
     Returns the illumination-divided image, then the Laplacian-filtered image
@@ -228,7 +232,8 @@ def rtm3d(v, e, d, *, npd, nt, dx, dy, dz, dt, favg, fsx, fsy, fsz, ns=1, dsx=0,
                   ry0=0, dry=1, nry=ny, mute_tt=0)
     na, da, dcdp = adcig if adcig is not None else (0, 0, 0)
     desc = RTM3DDesc(fd=fd, ns=ns, mute_tt=mute_tt, method=_RTM[method] if isinstance(method, str) else int(method),
-                     snap_every=snap_every, ae=codec._p if codec is not None else None, na=na, da=da, dcdp=dcdp)
+                     snap_every=snap_every, ae=codec._p if codec is not None else None, na=na, da=da, dcdp=dcdp,
+                     ckpt_every=ckpt_every)
     pv, pe, pd = b.inp(v), b.inp(e), b.inp(d)
     if theta is not None:
         desc.theta, desc.phi = b.inp(theta), b.inp(phi)

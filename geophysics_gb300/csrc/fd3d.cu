@@ -812,6 +812,11 @@ __global__ void k_adcig3d_illum(float *adcig, const float *ill, int nx, int nz, 
 // ring save in the forward pass, source re-propagation driven by the ring in
 // the backward pass.  GEO_RTM_SNAPSHOT and GEO_RTM_LEARNED keep snapshots of
 // the source P instead and propagate only the receiver field backwards.
+// GEO_RTM_CHECKPOINT saves the source field's full state every K steps and,
+// in the backward pass, re-propagates each K-step segment from its
+// checkpoint to hold that segment's snapshots: three propagations per step
+// like the boundary method, the snapshot method's image bit for bit, and
+// memory of K/snap_every snapshots plus nt/K states.
 extern "C" int geo_rtm3d_adcig(const geo_rtm3d_desc *desc, const float *v, const float *e, const float *d,
                                float *mig_out, float *lap_out, float *illum_out, float *adcig_out, int mem,
                                void *stream) {
@@ -820,7 +825,8 @@ extern "C" int geo_rtm3d_adcig(const geo_rtm3d_desc *desc, const float *v, const
     const geo_rtm3d_desc &R = *desc;
     if (R.ns < 1) return fail(GEO_ERR_ARG, "ns must be >= 1");
     const int method = R.method;
-    if (method != GEO_RTM_BOUNDARY && method != GEO_RTM_SNAPSHOT && method != GEO_RTM_LEARNED)
+    if (method != GEO_RTM_BOUNDARY && method != GEO_RTM_SNAPSHOT && method != GEO_RTM_LEARNED &&
+        method != GEO_RTM_CHECKPOINT)
         return fail(GEO_ERR_ARG, "unknown RTM method %d", method);
     if (method != GEO_RTM_BOUNDARY && R.snap_every < 1) return fail(GEO_ERR_ARG, "snap_every must be >= 1");
     if (method == GEO_RTM_LEARNED && !R.ae) return fail(GEO_ERR_ARG, "the learned method needs a codec");
@@ -847,13 +853,30 @@ extern "C" int geo_rtm3d_adcig(const geo_rtm3d_desc *desc, const float *v, const
     const long L = 2L * D.nx * D.ny + 2L * D.nz * D.ny + 2L * D.nx * D.nz;
     const int k = method == GEO_RTM_BOUNDARY ? 1 : R.snap_every;
     const int nsnap = method == GEO_RTM_BOUNDARY ? 0 : D.nt / k;
-    DevBuf ring, mig, ill, lap, snaps, codes, scales, escs, resid, nesc;
+    // checkpoint method: the full state of the source field every K steps
+    // (u,v,w,P,Q of the current level, plus the six split stresses of the
+    // VTI step), a segment's snapshots at a time in the backward pass
+    int K = 0, nck = 0, narr = 0;
+    if (method == GEO_RTM_CHECKPOINT) {
+        narr = R.theta ? 5 : 11;
+        // automatic interval: minimises nt/K states (narr padded arrays each)
+        // plus K/snap_every snapshots (interior arrays)
+        const double ratio = (double)narr * p->nalloc / (double)((long)D.nx * D.ny * D.nz);
+        K = R.ckpt_every;
+        if (K <= 0) K = k * std::max(1, (int)std::lround(std::sqrt((double)D.nt / k * ratio)));
+        if (K % k) return fail(GEO_ERR_ARG, "ckpt_every must be a multiple of snap_every");
+        nck = (D.nt + K - 1) / K;
+    }
+    DevBuf ring, mig, ill, lap, snaps, codes, scales, escs, resid, nesc, ckpt;
     const Grid3D g0 = grid_of(p, 0);
     const AeVolume box = ae_volume(nullptr, g0.ldz, g0.sxy, D.npd, D.npd, D.npd, D.nz, D.nx, D.ny);
     const int crow = ae_code_rows(box);
     const int ecap = method == GEO_RTM_LEARNED ? ae_escape_cap(R.ae, box) : 0;
     if (method == GEO_RTM_BOUNDARY) {
         GEO_TRY(ring.alloc((size_t)2 * D.nt * L * 4));
+    } else if (method == GEO_RTM_CHECKPOINT) {
+        GEO_TRY(ckpt.alloc((size_t)nck * narr * p->nalloc * 4));
+        GEO_TRY(snaps.alloc((size_t)std::max(K / k, 1) * nimg * 4));
     } else if (method == GEO_RTM_SNAPSHOT) {
         GEO_TRY(snaps.alloc((size_t)std::max(nsnap, 1) * nimg * 4));
     } else {
@@ -888,6 +911,20 @@ extern "C" int geo_rtm3d_adcig(const geo_rtm3d_desc *desc, const float *v, const
         return check_launch("ring3d");
     };
     auto is_snap = [&](int it) { return method != GEO_RTM_BOUNDARY && it % k == k - 1 && it / k < nsnap; };
+    // copy the source field's state into checkpoint c (save) or back
+    auto state_copy = [&](int c, bool save) -> int {
+        FieldSet3D &F = p->fs[0];
+        DevBuf *arr[11] = {&F.lev[F.cur][0], &F.lev[F.cur][1], &F.lev[F.cur][2], &F.lev[F.cur][3], &F.lev[F.cur][4],
+                           &F.px, &F.py, &F.pz, &F.qx, &F.qy, &F.qz};
+        for (int a = 0; a < narr; a++) {
+            float *slot = ckpt.as<float>() + ((size_t)c * narr + a) * p->nalloc;
+            if (save)
+                GEO_CUDA(cudaMemcpyAsync(slot, arr[a]->p, p->nalloc * 4, cudaMemcpyDeviceToDevice, s));
+            else
+                GEO_CUDA(cudaMemcpyAsync(arr[a]->p, slot, p->nalloc * 4, cudaMemcpyDeviceToDevice, s));
+        }
+        return GEO_OK;
+    };
     for (int is = 0; is < R.ns; is++) {
         StepArgs3D st{};
         GEO_TRY(source_cell(p, is, st));
@@ -904,10 +941,11 @@ extern "C" int geo_rtm3d_adcig(const geo_rtm3d_desc *desc, const float *v, const
             st.it = it;
             st.src_on = p->on[it];
             st.amp = p->amp[it];
+            if (method == GEO_RTM_CHECKPOINT && it % K == 0) GEO_TRY(state_copy(it / K, true));
             GEO_TRY(step3d(p, 0, st, s));
             if (method == GEO_RTM_BOUNDARY) {
                 GEO_TRY(launch_ring(it, 1));
-            } else if (is_snap(it)) {
+            } else if (is_snap(it) && method != GEO_RTM_CHECKPOINT) {
                 const Grid3D g = grid_of(p, 0);
                 const int j = it / k;
                 if (method == GEO_RTM_SNAPSHOT) {
@@ -944,6 +982,27 @@ extern "C" int geo_rtm3d_adcig(const geo_rtm3d_desc *desc, const float *v, const
                 GEO_TRY(launch_ring(it, 0));
                 GEO_TRY(step3d(p, 0, sb, s));
             }
+            if (method == GEO_RTM_CHECKPOINT && (it == D.nt - 1 || it % K == K - 1)) {
+                // entering segment c from its end: restore its checkpoint and
+                // re-propagate it (source on, nothing recorded), keeping
+                // its snapshots
+                const int c = it / K;
+                GEO_TRY(state_copy(c, false));
+                StepArgs3D sr{};
+                sr.ixs = st.ixs; sr.iys = st.iys; sr.izs = st.izs;
+                for (int j = c * K; j <= it; j++) {
+                    sr.it = j;
+                    sr.src_on = p->on[j];
+                    sr.amp = p->amp[j];
+                    GEO_TRY(step3d(p, 0, sr, s));
+                    if (is_snap(j)) {
+                        const Grid3D g = grid_of(p, 0);
+                        k_snap_store<<<grid_blocks(nimg), 256, 0, s>>>(
+                            g, g.P, snaps.as<float>() + (size_t)((j - c * K) / k) * nimg);
+                        GEO_TRY(check_launch("snap_store"));
+                    }
+                }
+            }
             {
                 Grid3D gg = grid_of(p, 1);
                 k_inject3d<<<grid_blocks(ntr), 256, 0, s>>>(gg, gg.P, gg.Q, p->rec_tm.as<float>(), it);
@@ -959,8 +1018,9 @@ extern "C" int geo_rtm3d_adcig(const geo_rtm3d_desc *desc, const float *v, const
             if (is_snap(it)) {
                 const Grid3D g = grid_of(p, 1);
                 const int j = it / k;
-                if (method == GEO_RTM_SNAPSHOT) {
-                    k_snap_image<<<grid_blocks(nimg), 256, 0, s>>>(g, snaps.as<float>() + (size_t)j * nimg, g.P,
+                if (method == GEO_RTM_SNAPSHOT || method == GEO_RTM_CHECKPOINT) {
+                    const size_t slot = method == GEO_RTM_SNAPSHOT ? (size_t)j : (size_t)((it % K) / k);
+                    k_snap_image<<<grid_blocks(nimg), 256, 0, s>>>(g, snaps.as<float>() + slot * nimg, g.P,
                                                                     mig.as<float>(), (float)k);
                     GEO_TRY(check_launch("snap_image"));
                 } else {

@@ -195,7 +195,11 @@ typedef struct geo_ae geo_ae;
 enum {
     GEO_RTM_BOUNDARY = 0,    /* the program's boundary-saving recompute      */
     GEO_RTM_SNAPSHOT = 1,    /* source P stored every snap_every steps       */
-    GEO_RTM_LEARNED  = 2     /* same snapshots through the learned codec     */
+    GEO_RTM_LEARNED  = 2,    /* same snapshots through the learned codec     */
+    GEO_RTM_CHECKPOINT = 3   /* exact recompute: the full wavefield saved
+                                every ckpt_every steps, each segment
+                                re-propagated in the backward pass; image
+                                bit-identical to GEO_RTM_SNAPSHOT's          */
 };
 
 typedef struct geo_rtm3d_desc {
@@ -210,6 +214,9 @@ typedef struct geo_rtm3d_desc {
     const float *theta, *phi;/* 3D TTI medium (geo_fd3d_set_tilt; in `mem`
                                 like the model) or NULL for VTI; no angle
                                 gathers on a TTI medium                       */
+    int   ckpt_every;        /* checkpoint interval in steps (method 3; a
+                                multiple of snap_every; 0 = the interval that
+                                minimises states plus segment snapshots)      */
 } geo_rtm3d_desc;
 
 /* v,e,d: nx*ny*nz.  mig: nx*ny*nz image divided by the illumination where

@@ -22,6 +22,25 @@ def test_rtm3d_bit_exact(geo, orc, mode, sv):
     assert np.array_equal(lap, lap_o), rel_l2(lap, lap_o)
 
 
+@pytest.mark.parametrize("mode,sv,ck", [(0, 0, 12), (1, 1, 20), (1, 0, 0)])
+def test_rtm3d_checkpoint_equals_snapshot(geo, orc, mode, sv, ck):
+    """Checkpoint recompute (full state every ck steps, ck not dividing nt;
+    0 = automatic) images exactly what the stored-snapshot method does, and
+    both equal the oracle's snapshot RTM."""
+    v, e, d = random_model_3d(20, 17, 23, seed=15)
+    mig_o, ill_o, _ = orc.rtm3d(v, e, d, mode=mode, sv=sv, snap_every=4, **KW)
+    rk = dict(KW, mode=mode, sv=sv, snap_every=4, laplace=False, illum=True)
+    mig_s, ill_s = geo.rtm3d(v, e, d, method="snapshot", **rk)
+    mig_c, ill_c = geo.rtm3d(v, e, d, method="checkpoint", ckpt_every=ck, **rk)
+    assert np.abs(mig_o).max() > 0
+    assert np.array_equal(mig_s, mig_o)
+    assert np.array_equal(ill_s, ill_o)
+    assert np.array_equal(mig_c, mig_s)
+    assert np.array_equal(ill_c, ill_s)
+    with pytest.raises(geo.GeoError):
+        geo.rtm3d(v, e, d, method="checkpoint", ckpt_every=6, **rk)   # not a multiple of snap_every
+
+
 def test_rtm3d_device_buffers(geo, orc):
     import torch
     v, e, d = random_model_3d(18, 16, 20, seed=12)

@@ -76,16 +76,16 @@ def test_tti3d_needs_fast_form_and_angles(geo):
                       fsx=6, fsy=5, fsz=2, mode="fast")
 
 
-@pytest.mark.parametrize("method", ["boundary", "snapshot"])
+@pytest.mark.parametrize("method", ["boundary", "snapshot", "checkpoint"])
 def test_tti3d_rtm_bit_exact(geo, orc, method):
     v, e, d = random_model_3d(18, 16, 20, seed=12, vlo=2000, vhi=2600)
     th, ph = smooth_angles(v.shape, seed=4)
     kw = dict(npd=8, nt=160, dx=10.0, dy=10.0, dz=10.0, dt=np.float32(1e-3), favg=25.0, pfac=10.0, fsx=9, fsy=8,
               fsz=1, mute_tt=5)
-    snap = 4 if method == "snapshot" else 0
+    snap = 0 if method == "boundary" else 4   # checkpoint recompute images as the snapshot method
     mig_ref, ill_ref, _ = orc.rtm3d(v, e, d, theta=th, phi=ph, snap_every=snap, **kw)
-    mig, ill = geo.rtm3d(v, e, d, theta=th, phi=ph, mode="fast", method=method, snap_every=4, laplace=False,
-                         illum=True, **kw)
+    mig, ill = geo.rtm3d(v, e, d, theta=th, phi=ph, mode="fast", method=method, snap_every=4, ckpt_every=12,
+                         laplace=False, illum=True, **kw)
     assert np.abs(mig_ref).max() > 0
     assert np.array_equal(ill, ill_ref)
     assert np.array_equal(mig, mig_ref), rel_l2(mig, mig_ref)
