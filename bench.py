@@ -9,8 +9,8 @@ del = 0.15*(vp-1500)/3000.  Synthetic, generated on the fly.
 
 Metric: grid-point updates per second, counting the points the step
 updates ((nn-8)^3 per time step).  `value` runs shots with the model and
-wavefields resident in HBM; `e2e` goes through the C ABI with host buffers
-(model upload and record download inside the timed region).  The working
+wavefields resident in HBM; `e2e` goes through the C ABI with pinned host
+buffers (model upload and record download inside the timed region).  The working
 set (~10 GB) is far larger than L2, so no flush is needed between steps.
 
 --impl reference times the CPU restatement of the same step (the reference
@@ -237,17 +237,24 @@ def run_ours(args, rank, world):
             if line.startswith("bytes_per_step:"):
                 traffic = int(line.split(":")[1])
 
-    # end to end through the C ABI with host buffers
-    hv, he, hd = (a.cpu().numpy() for a in (vp, eps, dl))
+    # end to end through the C ABI with host buffers: the model from pinned
+    # host memory, the record read back into pinned host memory
+    pinned = [torch.empty(a.shape, dtype=torch.float32, pin_memory=True) for a in (vp, eps, dl)]
+    for h, a in zip(pinned, (vp, eps, dl)):
+        h.copy_(a)
+    hv, he, hd = (h.numpy() for h in pinned)
     del vp, eps, dl
+    D = plan.desc
+    rec_pin = torch.empty((D.nry, D.nrx, D.nt), dtype=torch.float32, pin_memory=True)
+    rec = rec_pin.numpy()
     plan.set_model(hv, he, hd)
-    plan.run_shot(0)
+    plan.run_shot(0, out=rec)
     barrier()
     e2e_steps = max(1, args.steps)
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         plan.set_model(hv, he, hd)
-        rec = plan.run_shot(0)
+        plan.run_shot(0, out=rec)
     barrier()
     e2e_s = (time.perf_counter() - t0) / e2e_steps
     if world > 1:
@@ -390,10 +397,11 @@ def train_codec(geo, iters, models=32, n=96, seed=1, tti=False):
 
 def run_rtm_learned_case(args):
     """3D VTI RTM, one shot, 512x512x384 at 10 m (+40 sponge), dt 0.8 ms,
-    15 Hz: plain boundary-saving recompute against snapshots every 4 steps
-    through the learned codec (shots/hour), and the codec's image error
-    against stored fp32 snapshots (on the first err_nt steps: all 3000
-    steps of fp32 snapshots would need 302 GB)."""
+    15 Hz: the plain recomputes (the program's boundary re-propagation and
+    the exact checkpoint recompute) against snapshots every 4 steps through
+    the learned codec (shots/hour), and the codec's image error against
+    stored fp32 snapshots (on the first err_nt steps: all 3000 steps of fp32
+    snapshots would need 302 GB; the checkpoint image equals them)."""
     import numpy as np
     import torch
 
@@ -415,6 +423,7 @@ def run_rtm_learned_case(args):
 
     res = {}
     _, res["boundary"] = timed(nt=args.nt, method="boundary")
+    _, res["checkpoint"] = timed(nt=args.nt, method="checkpoint", snap_every=4)
     codec.set_escape(0.02, 0.0)
     _, res["learned16"] = timed(nt=args.nt, method="learned", snap_every=4, codec=codec)
     codec.set_escape(0.02, args.escape)
@@ -442,6 +451,8 @@ def run_rtm_learned_case(args):
             "shots_per_hr": {k: 3600.0 / v for k, v in res.items()}, "seconds": res,
             "speedup_vs_boundary": {"learned16": res["boundary"] / res["learned16"],
                                     "learned_esc": res["boundary"] / res["learned_esc"]},
+            "speedup_vs_checkpoint": {"learned16": res["checkpoint"] / res["learned16"],
+                                      "learned_esc": res["checkpoint"] / res["learned_esc"]},
             "image_rel_l2_vs_fp32_snapshots": {"learned16": rel(l16, ref), "learned_esc": rel(les, ref),
                                                "boundary": rel(bnd, ref), "err_nt": args.err_nt,
                                                "image": "Laplacian-filtered, illumination-divided"},
@@ -533,26 +544,31 @@ def run_tti_rtm_case(args):
         torch.cuda.synchronize()
         return out, time.perf_counter() - t0
 
-    codec.set_escape(0.02, args.escape)
-    b0, e0 = codec.stats()
     plain, tp = timed(method="checkpoint")
-    lrn, tl = timed(method="learned", codec=codec)
-    b1, e1 = codec.stats()
+    # two escape settings: (block error threshold, escaped-block budget)
+    out = {}
+    for name, tol, budget in (("learned", 0.02, args.escape), ("learned_tight", 0.01, 3 * args.escape)):
+        codec.set_escape(tol, budget)
+        b0, e0 = codec.stats()
+        img, sec = timed(method="learned", codec=codec)
+        b1, e1 = codec.stats()
+        out[name] = (img, sec, (e1 - e0) / max(1, b1 - b0), tol, budget)
 
     def rel(a, b):
         a, b = a[0].double(), b[0].double()
         return float((a - b).norm() / b.norm())
 
-    esc = (e1 - e0) / max(1, b1 - b0)
     print(json.dumps({"case": "tti-rtm", "metric": "3D TTI RTM shots/hr, learned snapshot codec vs plain "
                                                    "checkpoint recompute", "grid": [nx, ny, nz], "sponge": NPD,
                       "nt": args.nt, "shots": args.shots, "snap_every": 4,
-                      "shots_per_hr": {"checkpoint": args.shots * 3600.0 / tp, "learned": args.shots * 3600.0 / tl},
-                      "seconds": {"checkpoint": tp, "learned": tl}, "speedup_vs_plain": tp / tl,
-                      "image_rel_l2_learned_vs_plain": rel(lrn, plain),
+                      "shots_per_hr": dict({"checkpoint": args.shots * 3600.0 / tp},
+                                           **{k: args.shots * 3600.0 / o[1] for k, o in out.items()}),
+                      "seconds": dict({"checkpoint": tp}, **{k: o[1] for k, o in out.items()}),
+                      "speedup_vs_plain": {k: tp / o[1] for k, o in out.items()},
+                      "image_rel_l2_vs_plain": {k: rel(o[0], plain) for k, o in out.items()},
                       "image": "Laplacian-filtered, illumination-divided",
-                      "compression": {"escaped_block_frac": esc, "ratio": 16384 / (1024 + 4 + 4 + esc * 8192),
-                                      "escape_budget": args.escape},
+                      "compression": {k: {"escape_tol": o[3], "escape_budget": o[4], "escaped_block_frac": o[2],
+                                          "ratio": 16384 / (1024 + 4 + 4 + o[2] * 8192)} for k, o in out.items()},
                       "training": tinfo, "dtype": "f32 propagation, bf16 codec", "data": "synthetic"}), flush=True)
 
 

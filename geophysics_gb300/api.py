@@ -150,10 +150,18 @@ class FD3DPlan:
         b = _Bufs(theta, phi)
         check(lib().geo_fd3d_set_tilt(self._p, b.inp(theta), b.inp(phi), b.mem, b.stream()), "geo_fd3d_set_tilt")
 
-    def run_shot(self, is_=0, device=None):
-        """Shot `is_` (0-based); returns (nry, nrx, nt), on the GPU if device."""
+    def run_shot(self, is_=0, device=None, out=None):
+        """Shot `is_` (0-based); returns (nry, nrx, nt), on the GPU if device;
+        `out` (host float32 array of that shape, e.g. a view of pinned
+        memory) receives the record instead of a new array."""
         D = self.desc
         shape = (D.nry, D.nrx, D.nt)
+        if out is not None:
+            if out.shape != shape or out.dtype != np.float32 or not out.flags.c_contiguous:
+                raise ValueError("out must be a C-contiguous float32 array of shape %s" % (shape,))
+            check(lib().geo_fd3d_run_shot(self._p, is_, C.c_void_p(out.ctypes.data), GEO_MEM_HOST, None),
+                  "geo_fd3d_run_shot")
+            return out
         if device:
             t = _torch()
             out = t.empty(shape, dtype=t.float32, device=device)
