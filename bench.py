@@ -522,9 +522,9 @@ def run_tti_rtm_case(args):
     stored-snapshot image bit for bit) against snapshots every 4 steps
     through the learned codec trained on TTI snapshots from the solver.
     `--shots` shots back to back (sources spread along x); shots/hour of
-    both and the learned image's error against the plain one (the judge).
-    The reference programs' boundary re-propagation is not the judge here:
-    it diverges on the TTI medium."""
+    both and the learned image's error against the plain one (the image
+    the codec is measured against).  The reference programs' boundary
+    re-propagation is not that image here: it diverges on the TTI medium."""
     import torch
 
     import geophysics_gb300 as geo
