@@ -247,6 +247,15 @@ extern "C" int geo_fd3d(const geo_par *par, int device, float *d_shots, void *st
     GEO_TRY(geo_fd3d_plan_create(&plan, &D));
     std::unique_ptr<geo_fd3d_plan, int (*)(geo_fd3d_plan *)> guard(plan, geo_fd3d_plan_destroy);
     GEO_TRY(geo_fd3d_set_model(plan, m[0].data(), m[1].data(), m[2].data(), GEO_MEM_HOST, stream));
+    // optional 3D TTI medium: tilt and azimuth files in degrees (FNtheta, FNphi)
+    const std::string fth = opt_s(par, "FNtheta"), fph = opt_s(par, "FNphi");
+    if (fth.empty() != fph.empty()) return fail(GEO_ERR_ARG, "par: FNtheta and FNphi go together");
+    if (!fth.empty()) {
+        std::vector<float> th, ph;
+        GEO_TRY(read_floats(fth.c_str(), (size_t)D.nx * D.ny * D.nz, th));
+        GEO_TRY(read_floats(fph.c_str(), (size_t)D.nx * D.ny * D.nz, ph));
+        GEO_TRY(geo_fd3d_set_tilt(plan, th.data(), ph.data(), GEO_MEM_HOST, stream));
+    }
     const size_t nrec = (size_t)D.nt * D.nrx * D.nry;
     File f;
     if (!fshot.empty()) GEO_TRY(open_out(fshot, f));

@@ -458,7 +458,9 @@ void geo_par_free(geo_par *par);
  *   shots 0..ns-1.  Keys: nx ny nz dx dy dz npml nt dt (microseconds) favg ns
  *   fsx fsy fsz FNv FNe FNd; optional dsx dsy dsz, FNshot, SV, mode (exact |
  *   fast, default exact), pfac, wtype, rec_iz, rx0 drx nrx ry0 dry nry (every
- *   surface node by default), mute_tt (100).  d_shots: ns*nt*nrx*nry.
+ *   surface node by default), mute_tt (100), FNtheta FNphi (a 3D TTI medium:
+ *   tilt and azimuth files in degrees, with mode fast; geo_fd3d_set_tilt).
+ *   d_shots: ns*nt*nrx*nry.
  * geo_rtm2d: the MPI RTM program (2D-vti-fd+rtm-mpi/Toa_rtm_vti_adcig_cdp.c:
  *   59-481), shot is at fs_sxd + (is-1)*ds_sxd with an nxs-wide window.
  *   Keys, its variable names: nx nz dx dz npd nt dt (ms) favg pfac ns_sxd

@@ -61,6 +61,34 @@ def test_fd3d_par(geo, tmp_path):
         plan.close()
 
 
+def test_fd3d_par_tti(geo, tmp_path):
+    """The par run on a 3D TTI medium (FNtheta, FNphi) equals the plan with
+    set_tilt."""
+    from tests.util import smooth_angles
+    v, e, d = random_model_3d(20, 18, 22, seed=6)
+    th, ph = smooth_angles(v.shape, seed=5)
+    kw = dict(nx=20, ny=18, nz=22, dx=10, dy=10, dz=10, npml=10, nt=160, dt=1000, favg=25, ns=1, fsx=6, fsy=8,
+              fsz=2, mode="fast", mute_tt=5, FNv=_write(tmp_path, "v", v), FNe=_write(tmp_path, "e", e),
+              FNd=_write(tmp_path, "d", d), FNtheta=_write(tmp_path, "th", th), FNphi=_write(tmp_path, "ph", ph),
+              FNshot=str(tmp_path / "shot"))
+    geo.fd3d_par(_par(tmp_path, "fd3t.par", **kw))
+    shot = np.fromfile(tmp_path / "shot", np.float32).reshape(18, 20, 160)
+    plan = geo.FD3DPlan(nx=20, ny=18, nz=22, npd=10, nt=160, dx=10.0, dy=10.0, dz=10.0, dt=1e-3, favg=25.0, fsx=6,
+                        fsy=8, fsz=2, mode="fast", mute_tt=5)
+    try:
+        plan.set_model(v, e, d)
+        plan.set_tilt(th, ph)
+        rec = plan.run_shot(0)
+        assert np.abs(rec).max() > 0
+        assert np.array_equal(shot, rec)
+    finally:
+        plan.close()
+    bad = dict(kw, FNphi="")
+    del bad["FNphi"]
+    with pytest.raises(geo.GeoError):
+        geo.fd3d_par(_par(tmp_path, "fd3bad.par", **bad))
+
+
 @pytest.mark.parametrize("seismic", [1, 2])
 def test_rtm2d_par(geo, tmp_path, seismic):
     rng = np.random.default_rng(3)
