@@ -289,8 +289,12 @@ def run_ours(args, rank, world):
                          "step_ms": step_ms},
             "cpu_baseline": cpu,
             "exact_form": {"step_ms": exact_ms, "value": updates_per_step() / (exact_ms / 1000) / 1e9,
-                           "unit": "Gpt/s", "note": "bare steps of the reference-arithmetic form; the headline "
-                           "fast form's record is 1.08e-5 rel-L2 from it after 2500 steps"}}
+                           "unit": "Gpt/s",
+                           # split stresses everywhere: 84 algorithmic bytes at every updated point
+                           "roofline_frac": updates_per_step() * 84 / (exact_ms / 1000) / 1e9 / peak,
+                           "note": "bare steps of the reference-arithmetic form (84 B per update: split "
+                           "stresses everywhere); the headline fast form's record is 1.08e-5 rel-L2 from it "
+                           "after 2500 steps"}}
     print(json.dumps(line), flush=True)
 
 
