@@ -307,7 +307,7 @@ def run_profile_case(args):
 
     import geophysics_gb300 as geo
     global NX, NY, NZ
-    NX = NY = NZ = args.grid
+    NX = NY = NZ = args.grid = args.grid or 192
     vp, eps, dl = make_model(device="cuda")
     kw = plan_kwargs()
     kw.update(nt=20, nrx=args.grid // 2, nry=args.grid // 2, npd=args.sponge, rec_iz=args.sponge)
@@ -483,8 +483,9 @@ def run_tti_case(args):
     import geophysics_gb300 as geo
     from geophysics_gb300 import build as B
     B.build()
-    ny, nx, nz = TTI_SHAPE
-    v, e, d, th, ph = tti_model(TTI_SHAPE)
+    shape = (args.grid,) * 3 if args.grid else TTI_SHAPE
+    ny, nx, nz = shape
+    v, e, d, th, ph = tti_model(shape)
     plan = geo.FD3DPlan(nx=nx, ny=ny, nz=nz, npd=NPD, nt=10, dx=TTI_DX, dy=TTI_DX, dz=TTI_DX, dt=TTI_DT,
                         favg=TTI_FAVG, fsx=nx // 2, fsy=ny // 2, fsz=1, mode="fast")
     plan.set_model(v, e, d)
@@ -513,8 +514,8 @@ def run_tti_case(args):
                       "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                                    "frac": achieved / peak, "peak_kind": peak_kind,
                                    "unit_of_work": "one time step (%d updates, %d B each)" % (pts, TTI_BYTES_PER_PT)},
-                      "config": {"workload": "3D TTI step, 600x600x400 (+40 sponge) at 12.5 m, dt 0.8 ms, tilt "
-                                             "0-45 deg, azimuth 0-360 deg (smooth seeded fields)"},
+                      "config": {"workload": "3D TTI step, %dx%dx%d (+40 sponge) at 12.5 m, dt 0.8 ms, tilt "
+                                             "0-45 deg, azimuth 0-360 deg (smooth seeded fields)" % (nx, ny, nz)},
                       "cpu_baseline": cpu, "dtype": "f32", "data": "synthetic"}), flush=True)
 
 
@@ -727,7 +728,8 @@ def main():
     ap.add_argument("--case", default="full", choices=["full", "small", "traffic", "rtm-learned", "rtm-methods", "fd2d", "rtm2d",
                                                       "tti", "tti-rtm"],
                     help="small / traffic: ncu profiling cases; rtm-learned: the learned-codec RTM comparison")
-    ap.add_argument("--grid", type=int, default=192, help="small: cube edge")
+    ap.add_argument("--grid", type=int, default=None, help="small (192 by default), tti (600x600x400 by "
+                                                           "default): cube edge, for profiling cases")
     ap.add_argument("--sponge", type=int, default=40, help="small: sponge width")
     ap.add_argument("--nt", type=int, default=3000, help="rtm-learned, rtm2d, tti-rtm (3500 there): time steps")
     ap.add_argument("--shots", type=int, default=128, help="rtm2d: shots in the batch (the workload has 128); "
