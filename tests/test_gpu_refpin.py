@@ -1,0 +1,120 @@
+"""The library's drop-ins GPU_vti3dfd and GPU_vti2dfd against the
+reference's own GPU programs (2D-3D-vti-fd-cuda-gtk-GUI/GPU_vti3dfd_kernels.cu,
+GPU_vti2dfd_kernels.cu), whose device code was compiled unmodified and run
+on a GPU: the golden records of tests/golden/make_golden_refgpu.py, and, where
+the cubins are present (oracle/_ref), the 400^3 headline shot run through the
+reference program itself.
+
+Tolerances: the exact 3D form and the 2D GPU-program form are bit-identical
+to the program built with contraction to FMA off.  The fast 3D form (FMAs at
+fixed places, unsplit interior) is held to the distance between the
+reference program's own two builds (default FMA contraction against none),
+with a margin of 1.5x: that distance is what rounding alone does to this
+computation."""
+import os
+
+import numpy as np
+import pytest
+
+from tests.test_oracle_pin_gpuprog import M, _load
+from tests.util import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+
+def _files(tmp_path, tag, v, e, d):
+    names = []
+    for name, a in (("v", v), ("e", e), ("d", d)):
+        p = tmp_path / ("%s_%s.bin" % (name, tag))
+        a.tofile(p)
+        names.append(str(p))
+    return names
+
+
+def _run3d(geo, tmp_path, g, case, mode, monkeypatch):
+    v, e, d = g["v"], g["e"], g["d"]
+    ny, nx, nz = v.shape
+    kw = M.CASES3[case]
+    monkeypatch.setenv("GEO_FD3D_MODE", mode)
+    fv, fe, fd = _files(tmp_path, case, v, e, d)
+    shot, snap = str(tmp_path / ("shot3_%s_%s.bin" % (case, mode))), str(tmp_path / ("snap3_%s_%s.bin" % (case, mode)))
+    geo.GPU_vti3dfd(nx, ny, nz, kw["dx"], kw["dy"], kw["dz"], kw["npml"], kw["sv"], fv, fe, fd, kw["favg"], kw["ns"],
+                    kw["fsx"], kw["dsx"], kw["fsy"], kw["dsy"], kw["fsz"], kw["dsz"], shot, snap, kw["nt"], kw["dt_us"])
+    out = np.fromfile(shot, np.float32).reshape(kw["ns"], ny, nx, kw["nt"])
+    sn = np.fromfile(snap, np.float32) if os.path.getsize(snap) else None
+    return out, sn
+
+
+@pytest.mark.parametrize("case", sorted(M.CASES3))
+def test_GPU_vti3dfd_exact_form_bit_exact_vs_reference_program(geo, tmp_path, monkeypatch, case):
+    g = _load("golden_fd3d_gpu.npz")
+    out, sn = _run3d(geo, tmp_path, g, case, "exact", monkeypatch)
+    ref = g["shot_%s_nofma" % case]
+    assert np.abs(out).max() > 0
+    assert np.array_equal(out, ref), rel_l2(out, ref)
+    if "snap_%s_nofma" % case in g:
+        rs = g["snap_%s_nofma" % case].reshape(-1)
+        assert sn is not None and np.array_equal(sn[:rs.size], rs)
+
+
+@pytest.mark.parametrize("case", sorted(M.CASES3))
+def test_GPU_vti3dfd_fast_form_within_the_reference_builds_distance(geo, tmp_path, monkeypatch, case):
+    g = _load("golden_fd3d_gpu.npz")
+    out, _ = _run3d(geo, tmp_path, g, case, "fast", monkeypatch)
+    fma, nofma = g["shot_%s_fma" % case], g["shot_%s_nofma" % case]
+    own = rel_l2(fma, nofma)
+    assert rel_l2(out, nofma) <= 1.5 * own, (rel_l2(out, nofma), own)
+    assert rel_l2(out, fma) <= 1.5 * own, (rel_l2(out, fma), own)
+
+
+@pytest.mark.parametrize("case", sorted(M.CASES2))
+def test_GPU_vti2dfd_bit_exact_vs_reference_program(geo, tmp_path, case):
+    g = _load("golden_fd2d_gpu.npz")
+    v, e, d = g["v"], g["e"], g["d"]
+    nx, nz = v.shape
+    kw = M.CASES2[case]
+    fv, fe, fd = _files(tmp_path, "2d" + case, v, e, d)
+    shot, snap = str(tmp_path / "shot2.bin"), str(tmp_path / "snap2.bin")
+    geo.GPU_vti2dfd(nx, nz, kw["dx"], kw["dz"], kw["npd"], kw["sv"], fv, fe, fd, kw["favg"], kw["ns"], kw["fs"], kw["ds"],
+                    kw["zs"], shot, snap, kw["nt"], kw["dt_us"])
+    out = np.fromfile(shot, np.float32).reshape(kw["ns"], nx, kw["nt"])
+    ref = g["shot_%s_nofma" % case]
+    assert np.abs(out).max() > 0
+    assert np.array_equal(out, ref), rel_l2(out, ref)
+    if "snap_%s_nofma" % case in g:
+        rs = g["snap_%s_nofma" % case].reshape(-1)
+        assert np.array_equal(np.fromfile(snap, np.float32)[:rs.size], rs)
+
+
+def test_headline_shot_against_reference_program(geo):
+    """The 400^3 + 40 headline shot (2500 steps, dt 0.8 ms, 15 Hz, the
+    bench's random-field model), every surface node recorded and muted as
+    GPU_vti3dfd records it: the exact form is bit-identical to the reference
+    program built without contraction; the fast form is held to the
+    distance between the reference program's two builds."""
+    from oracle import refgpu
+    if not refgpu.available("vti3d"):
+        pytest.skip("reference program cubins not built (oracle/_ref)")
+    import bench
+    v, e, d = (a.cpu().numpy() for a in bench.make_model(device="cpu"))
+    n, npd, nt = bench.NX, bench.NPD, bench.NT
+    rkw = dict(dx=10, dy=10, dz=10, npml=npd, sv=0, favg=15, ns=1, fsx=n // 2, dsx=0, fsy=n // 2, dsy=0, fsz=1,
+               dsz=0, nt=nt, dt_us=800)
+    ref_nofma, _, ms_nofma = refgpu.vti3d(v, e, d, fma=False, **rkw)
+    ref_fma, _, ms_fma = refgpu.vti3d(v, e, d, fma=True, **rkw)
+    out = {}
+    for mode in ("exact", "fast"):
+        plan = geo.FD3DPlan(nx=n, ny=n, nz=n, npd=npd, nt=nt, dx=10.0, dy=10.0, dz=10.0, dt=np.float32(0.0008),
+                            favg=15.0, pfac=10.0, fsx=n // 2, fsy=n // 2, fsz=1, mode=mode, mute_tt=100)
+        plan.set_model(v, e, d)
+        out[mode] = plan.run_shot(0)
+        plan.close()
+    own = rel_l2(ref_fma[0], ref_nofma[0])
+    res = {"exact_vs_nofma": rel_l2(out["exact"], ref_nofma[0]), "exact_vs_fma": rel_l2(out["exact"], ref_fma[0]),
+           "fast_vs_nofma": rel_l2(out["fast"], ref_nofma[0]), "fast_vs_fma": rel_l2(out["fast"], ref_fma[0]),
+           "fast_vs_exact": rel_l2(out["fast"], out["exact"]), "fma_vs_nofma": own,
+           "ref_ms_per_step_fma": ms_fma, "ref_ms_per_step_nofma": ms_nofma}
+    print("HEADLINE_VS_REFERENCE", res)
+    assert np.abs(out["exact"]).max() > 0
+    assert np.array_equal(out["exact"], ref_nofma[0])
+    assert res["fast_vs_nofma"] <= 1.5 * own and res["fast_vs_fma"] <= 1.5 * own
