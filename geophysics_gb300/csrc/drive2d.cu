@@ -332,6 +332,10 @@ extern "C" int geo_fd2d_shot(const geo_fd2d_desc *desc, const float *v, const fl
     std::vector<float> hv, he, hd;
     GEO_TRY(host_model(v, e, d, (size_t)D.nx * D.nz, mem, s, hv, he, hd));
     const Variant var = (Variant)D.variant;
+    {
+        const auto mm = std::minmax_element(hv.begin(), hv.end());
+        GEO_TRY(check_stability(var, 2, *mm.first, *mm.second, D.dt, D.dx, D.dx, D.dz, D.favg));
+    }
     const float fsx = D.fs + (D.is - 1) * D.ds;
     ShotHost h;
     const bool taper = var == V_MPI || D.sv;
@@ -366,6 +370,8 @@ extern "C" int geo_fd2d_shot(const geo_fd2d_desc *desc, const float *v, const fl
         return B.stress(PH_FWD, st, ss.cs);
     };
     const size_t nn = (size_t)nnx * nnz;
+    Watchdog wd;
+    GEO_TRY(wd.open());
     if (snap && snap_every > 0) {
         for (int it = 0; it < D.nt; it++) {
             GEO_TRY(step(it));
@@ -373,6 +379,10 @@ extern "C" int geo_fd2d_shot(const geo_fd2d_desc *desc, const float *v, const fl
                 float *dst = snap + (size_t)(it / snap_every) * nn;
                 GEO_CUDA(cudaMemcpyAsync(dst, B.S[0].P[0], nn * 4,
                                          mem == GEO_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, ss.cs));
+            }
+            if (wd.every > 0 && ((it + 1) % wd.every == 0 || it == D.nt - 1)) {
+                GEO_TRY(launch_watch_shots(B.d_S.as<Shot2D>(), 1, 1, wd.d, it + 1, ss.cs));
+                if (wd.tripped()) break;
             }
         }
     } else {
@@ -397,7 +407,13 @@ extern "C" int geo_fd2d_shot(const geo_fd2d_desc *desc, const float *v, const fl
         GEO_CUDA(cudaMemcpyAsync(&err, a.err, 4, cudaMemcpyDeviceToHost, ss.cs));
         GEO_CUDA(cudaStreamSynchronize(ss.cs));
         if (err) return fail(GEO_ERR_CUDA, "2D shot: a grid barrier wait timed out");
+        // the shot ran in one launch: scan its final P and its record
+        if (wd.every > 0) {
+            GEO_TRY(launch_watch_shots(B.d_S.as<Shot2D>(), 1, 1, wd.d, D.nt, ss.cs));
+            GEO_TRY(wd.scan(B.S[0].rec_p, (size_t)D.nx * D.nt, D.nt, ss.cs));
+        }
     }
+    GEO_TRY(wd.verdict(ss.cs, "2D shot"));
     DevBuf mlo, mhi, out;
     if (D.mute_tt > 0) {
         std::vector<int> lo, hi;
@@ -456,6 +472,10 @@ extern "C" int geo_rtm2d_batch_adcig(const geo_rtm2d_desc *desc, const float *v,
     GEO_TRY(ss.open(s));
     const float dt = D.dt_ms / 1000;
     const int nt = D.nt, nz = D.nz, npd = D.npd;
+    {
+        const auto mm = std::minmax_element(hv.begin(), hv.end());
+        GEO_TRY(check_stability(V_MPI, 2, *mm.first, *mm.second, dt, D.dx, D.dx, D.dz, D.favg));
+    }
     std::vector<std::unique_ptr<ShotHost>> H(D.ns);
     Batch2D B;
     B.variant = V_MPI;
@@ -498,6 +518,14 @@ extern "C" int geo_rtm2d_batch_adcig(const geo_rtm2d_desc *desc, const float *v,
     std::vector<float> amp;
     std::vector<uint8_t> on;
     source_amplitudes(V_MPI, nt, dt, D.favg, D.pfac, 1, amp, on);
+    // non-finite detector: every wd.every steps (and the last) the graphs
+    // scan every shot's P; the verdict follows each pass
+    Watchdog wd;
+    GEO_TRY(wd.open());
+    auto watch = [&](int k, bool last, int nf) -> int {
+        if (wd.every <= 0 || ((k + 1) % wd.every && !last)) return GEO_OK;
+        return launch_watch_shots(B.d_S.as<Shot2D>(), D.ns, nf, wd.d, k + 1, ss.cs);
+    };
     // forward: source side only, with records and edge lines
     {
         Graph G;
@@ -507,11 +535,13 @@ extern "C" int geo_rtm2d_batch_adcig(const geo_rtm2d_desc *desc, const float *v,
                 st.it = it; st.amp = amp[it]; st.src_on = on[it]; st.taper = 1; st.nf = 1; st.fast = fast;
                 GEO_TRY(B.vel(st, ss.cs));
                 GEO_TRY(B.stress(PH_FWD, st, ss.cs));
+                GEO_TRY(watch(it, it == nt - 1, 1));
             }
             return GEO_OK;
         }));
         GEO_TRY(G.launch(ss.cs));
     }
+    GEO_TRY(wd.verdict(ss.cs, "batched 2D RTM forward pass"));
     // mute both records (tt = 285) and restart the source side from zero
     std::vector<DevBuf> mute(D.ns);
     for (int k = 0; k < D.ns; k++) {
@@ -535,11 +565,13 @@ extern "C" int geo_rtm2d_batch_adcig(const geo_rtm2d_desc *desc, const float *v,
                 st.it = it; st.nf = 2; st.fast = fast;
                 GEO_TRY(B.vel(st, ss.cs));
                 GEO_TRY(B.stress(PH_BWD, st, ss.cs));
+                GEO_TRY(watch(nt - 1 - it, it == 0, 2));
             }
             return GEO_OK;
         }));
         GEO_TRY(G.launch(ss.cs));
     }
+    GEO_TRY(wd.verdict(ss.cs, "batched 2D RTM backward pass"));
     // normalise per shot, stack in shot order, Laplacian
     std::vector<const float *> imgs(D.ns);
     std::vector<int> offs(D.ns), wid(D.ns);

@@ -15,6 +15,7 @@
 #include "geo_internal.h"
 #include "tc_util.cuh"
 #include <algorithm>
+#include <cfloat>
 #include <cmath>
 #include <cstring>
 
@@ -377,6 +378,26 @@ template <int V>
 static void vel_dispatch(const Shot2D *d_shots, const int *d_item_shot, int nitems, dim3 grid, dim3 block,
                          Step2D st, cudaStream_t s) {
     k_vel2d<V><<<grid, block, 0, s>>>(d_shots, d_item_shot, nitems, st);
+}
+
+// Wavefield watchdog over a batch: block row y scans shot y's P of sides
+// 0..nf-1 and sets *flag to tag (first writer wins) on a NaN or +-Inf.
+__global__ void k_watch_shots(const Shot2D *__restrict__ S, int nf, int *flag, int tag) {
+    const Shot2D &sh = S[blockIdx.y];
+    const size_t n = (size_t)sh.nnx * sh.nnz;
+    bool bad = false;
+    for (int f = 0; f < nf; f++) {
+        const float *P = sh.P[f];
+        for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x)
+            bad |= !(fabsf(P[k]) <= FLT_MAX);
+    }
+    if (__syncthreads_or(bad) && threadIdx.x == 0) atomicCAS(flag, 0, tag);
+}
+
+int launch_watch_shots(const Shot2D *d_shots, int ns, int nf, int *flag, int tag, cudaStream_t s) {
+    if (!flag || ns < 1) return GEO_OK;
+    k_watch_shots<<<dim3(64, ns), 256, 0, s>>>(d_shots, nf, flag, tag);
+    return check_launch("watch_shots");
 }
 
 int launch_vel2d(int variant, const Shot2D *d_shots, const int *d_item_shot, int nitems, int by, int grid,

@@ -190,6 +190,7 @@ struct geo_fd3d_plan {
     // 3D TTI medium (geo_fd3d_set_tilt): cos/sin of tilt and azimuth, 4 x nalloc
     DevBuf tilt, save;
     bool tti = false;
+    geo::Watchdog wd;                  // non-finite wavefield detector
 };
 
 namespace geo {
@@ -311,6 +312,9 @@ static int step3d(geo_fd3d_plan *p, int f, const StepArgs3D &st, cudaStream_t s)
     p->fs[f].cur ^= 1;
     return GEO_OK;
 }
+
+// Current level of P of field set f (the watchdog's input, nalloc floats).
+static const float *cur_P(const geo_fd3d_plan *p, int f) { return p->fs[f].lev[p->fs[f].cur][3].as<float>(); }
 
 static int zero_state(geo_fd3d_plan *p, int f, cudaStream_t s) {
     FieldSet3D &F = p->fs[f];
@@ -447,13 +451,19 @@ int run_shot_3d(geo_fd3d_plan *p, int is, cudaStream_t s, int (*on_step)(void *,
     if (D.sv) GEO_TRY(taper_box_3d(p, is, true, s));
     st.rec = p->rec_tm.as<float>();
     st.rec_iz = D.rec_iz; st.rx0 = D.rx0; st.drx = D.drx; st.nrx = D.nrx; st.ry0 = D.ry0; st.dry = D.dry; st.nry = D.nry;
+    GEO_TRY(p->wd.open());
+    p->wd.arm();
     for (int it = 0; it < D.nt; it++) {
         st.it = it;
         st.src_on = p->on[it];
         st.amp = p->amp[it];
         GEO_TRY(step3d(p, 0, st, s));
         if (on_step) GEO_TRY(on_step(ctx, it));
+        const int w = p->wd.check(cur_P(p, 0), p->nalloc, it, it == D.nt - 1, s);
+        if (w == GEO_ERR_NAN) break;
+        GEO_TRY(w);
     }
+    GEO_TRY(p->wd.verdict(s, "3D shot"));
     if (D.sv) GEO_TRY(taper_box_3d(p, is, false, s));
     GEO_TRY(check_err(p, s));
     const int ntr = D.nrx * D.nry;
@@ -646,6 +656,18 @@ extern "C" int geo_fd3d_set_model(geo_fd3d_plan *p, const float *v, const float 
         if ((key & 3) == 0) return fail(GEO_ERR_MODEL, "velocity[%zu]=%g", i, bad);
         if ((key & 3) == 1) return fail(GEO_ERR_MODEL, "eps/del[%zu] not finite", i);
         return fail(GEO_ERR_MODEL, "1+2*delta[%zu] < 0", i);
+    }
+    // the stability number of the set-up code (dt*vmax*sqrt(sum 1/d^2) < 0.777)
+    {
+        unsigned *mm = reinterpret_cast<unsigned *>(p->box.p) + 4;
+        GEO_TRY(launch_minmax(raw, n0, mm, s));
+        unsigned b[2];
+        GEO_CUDA(cudaMemcpyAsync(b, mm, 8, cudaMemcpyDeviceToHost, s));
+        GEO_CUDA(cudaStreamSynchronize(s));
+        float vmin, vmax;
+        memcpy(&vmin, &b[0], 4);
+        memcpy(&vmax, &b[1], 4);
+        GEO_TRY(check_stability(V_GPU, 3, vmin, vmax, D.dt, D.dx, D.dy, D.dz, D.favg));
     }
     // padded model arrays, written straight into the pitched layout
     k_model3d<<<grid_blocks((long)p->n), 256, 0, s>>>(raw, raw + n0, raw + 2 * n0, D.nx, D.ny, D.nz, D.npd, p->nnx,
@@ -937,7 +959,10 @@ extern "C" int geo_rtm3d_adcig(const geo_rtm3d_desc *desc, const float *v, const
         st.rec_iz = D.rec_iz; st.rx0 = 0; st.drx = 1; st.nrx = D.nx; st.ry0 = 0; st.dry = 1; st.nry = D.ny;
         st.rec_pq = 1;
         st.ill = ill.as<float>();
-        for (int it = 0; it < D.nt; it++) {
+        GEO_TRY(p->wd.open());
+        p->wd.arm();
+        bool diverged = false;
+        for (int it = 0; it < D.nt && !diverged; it++) {
             st.it = it;
             st.src_on = p->on[it];
             st.amp = p->amp[it];
@@ -960,7 +985,11 @@ extern "C" int geo_rtm3d_adcig(const geo_rtm3d_desc *desc, const float *v, const
                                              nesc.as<int>() + j, s));
                 }
             }
+            const int w = p->wd.check(cur_P(p, 0), p->nalloc, it, it == D.nt - 1, s);
+            if (w == GEO_ERR_NAN) diverged = true;
+            else GEO_TRY(w);
         }
+        GEO_TRY(p->wd.verdict(s, "3D RTM forward pass"));
         // direct-wave mute, window form (mute_directwave :352-390)
         if (R.mute_tt > 0) {
             std::vector<int> lo, hi;
@@ -976,7 +1005,7 @@ extern "C" int geo_rtm3d_adcig(const geo_rtm3d_desc *desc, const float *v, const
         sb.ixs = gb.ixs = st.ixs; sb.iys = gb.iys = st.iys; sb.izs = gb.izs = st.izs;
         gb.ill = ill.as<float>();
         if (method == GEO_RTM_BOUNDARY) gb.mig = mig.as<float>();
-        for (int it = D.nt - 1; it >= 0; it--) {
+        for (int it = D.nt - 1; it >= 0 && !diverged; it--) {
             sb.it = gb.it = it;
             if (method == GEO_RTM_BOUNDARY) {
                 GEO_TRY(launch_ring(it, 0));
@@ -1030,7 +1059,11 @@ extern "C" int geo_rtm3d_adcig(const geo_rtm3d_desc *desc, const float *v, const
                                              mig.as<float>(), (float)k, s));
                 }
             }
+            const int w = p->wd.check(cur_P(p, 1), p->nalloc, D.nt - 1 - it, it == 0, s);
+            if (w == GEO_ERR_NAN) diverged = true;
+            else GEO_TRY(w);
         }
+        GEO_TRY(p->wd.verdict(s, "3D RTM backward pass"));
         if (D.sv) GEO_TRY(taper_box_3d(p, is, false, s));
         GEO_TRY(check_err(p, s));
         if (method == GEO_RTM_LEARNED) {

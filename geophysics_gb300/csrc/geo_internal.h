@@ -55,6 +55,42 @@ enum Variant { V_CPU = GEO_VARIANT_CPU, V_GPU = GEO_VARIANT_GPU, V_MPI = GEO_VAR
 constexpr double kPiGui = 3.141592653;      // CPU_vti2dfd_kernels.c:27, GPU_vti*_kernels.cu:31
 constexpr double kPiMpi = 3.1415926535898;  // Toa_rtm_vti_adcig_cdp.c:39
 
+// ------------------------------------------------------------ failure detection (guard.cu)
+// The Madagascar-derived stability limit of the 8th-order staggered operator
+// (Toa_gpu2DvtiFdRtmAdcigsLaplace.cu:941-965, mm = 4).
+constexpr double kStabilityC = 0.777;
+double stability_number(int dims, float vmax, float dt, float dx, float dy, float dz);
+// GEO_ERR_CFL when dt*vmax*sqrt(sum 1/d^2) >= kStabilityC; for the CPU
+// program also its get_constant limits (dx, dz <= vmin/favg*0.2 and
+// dt <= 0.5*min(dx,dz)/vmax).
+int check_stability(Variant v, int dims, float vmin, float vmax, float dt, float dx, float dy, float dz,
+                    float favg);
+// min and max of n positive finite floats into out[0], out[1] (float bits;
+// out is written, not accumulated)
+int launch_minmax(const float *a, size_t n, unsigned *out, cudaStream_t s);
+// Interval of the wavefield watchdog (GEO_WATCH_EVERY, default 100; 0 = off).
+int watch_every();
+// Non-finite detector: a word of mapped pinned memory that k_watch sets to
+// the tag of the first scan that found NaN/Inf.  check() scans every
+// `every` steps (and on the last) and returns GEO_ERR_NAN, without a
+// message, once the word is seen set, so the caller stops queueing steps;
+// verdict() drains the stream and turns a set word into the error.
+struct Watchdog {
+    int *h = nullptr, *d = nullptr;
+    int every = 100;
+    Watchdog() = default;
+    Watchdog(const Watchdog &) = delete;
+    Watchdog &operator=(const Watchdog &) = delete;
+    ~Watchdog() { close(); }
+    int open();
+    void close();
+    void arm();
+    bool tripped() const;
+    int check(const float *a, size_t n, int it, bool last, cudaStream_t s);
+    int scan(const float *a, size_t n, int tag, cudaStream_t s);
+    int verdict(cudaStream_t s, const char *what);
+};
+
 // Edge-replicate an nx*nz model into its padded (nx+2npd)*(nz+2npd) form.
 void pad_model_2d(int nx, int nz, int npd, const float *in, float *out);
 // Same for 3D, reference layout iz + nz*(ix + nx*iy).
@@ -151,6 +187,8 @@ int launch_stress2d(int variant, int phase, const Shot2D *d_shots, const int *d_
                     int by, int grid, Step2D st, cudaStream_t s);
 int launch_inject2d(const Shot2D *d_shots, int nshots, int maxline, int it, cudaStream_t s);
 int launch_mute_records(float *rec, int nx, int nt, const int *lo, const int *hi, cudaStream_t s);
+// Watchdog scan of the P fields (sides 0..nf-1) of ns shots (fd2d.cu).
+int launch_watch_shots(const Shot2D *d_shots, int ns, int nf, int *flag, int tag, cudaStream_t s);
 int launch_transpose_records(const float *tm, float *out, int ntr, int nt, cudaStream_t s);
 int launch_normalize_image(float *mig, const float *ill, size_t n, cudaStream_t s);
 // a[p*n + k] /= ill[k] for p < planes.

@@ -441,6 +441,8 @@ static int gpu_rtm_run(const GpuRtmProgram &prog, const geo_rtm2d_gpu_desc &D, c
         k_g_stress<<<gb, 256, 0, s>>>(g, f, e2p, d2p);
         return check_launch("grtm_stress");
     };
+    Watchdog wd;
+    GEO_TRY(wd.open());
     for (int is = 1; is <= D.ns; is++) {
         // SV taper box of this shot (centre fs+(is-1)ds+npml, zs+npml)
         std::vector<float> te2(e2), td2(d2);
@@ -481,7 +483,11 @@ static int gpu_rtm_run(const GpuRtmProgram &prog, const geo_rtm2d_gpu_desc &D, c
             GEO_TRY(check_launch("grtm_ring"));
             k_g_illum<<<gi, 256, 0, s>>>(g, S, ill.as<float>());
             GEO_TRY(check_launch("grtm_illum"));
+            const int w = wd.check(S.P, n, it, it == nt - 1, s);
+            if (w == GEO_ERR_NAN) break;
+            GEO_TRY(w);
         }
+        GEO_TRY(wd.verdict(s, "2D RTM forward pass"));
         // direct-wave mute (GPU form, tt), exactly as the program's kernel
         // writes it.  VTI program: thread it < nt rounded up to 512 zeroes
         // flat sample ix*nt + it of the trace-major record for every trace
@@ -525,7 +531,11 @@ static int gpu_rtm_run(const GpuRtmProgram &prog, const geo_rtm2d_gpu_desc &D, c
             GEO_TRY(step(R, de2.as<float>(), dd2.as<float>()));
             k_g_image<<<gi, 256, 0, s>>>(g, S, R, mig.as<float>(), ag.p ? ag.as<float>() : nullptr);
             GEO_TRY(check_launch("grtm_image"));
+            const int w = wd.check(R.P, n, nt - 1 - it, it == 0, s);
+            if (w == GEO_ERR_NAN) break;
+            GEO_TRY(w);
         }
+        GEO_TRY(wd.verdict(s, "2D RTM backward pass"));
     }
     GEO_TRY(launch_normalize_image(mig.as<float>(), ill.as<float>(), n0, s));
     GEO_TRY(lap.alloc(n0 * 4));

@@ -14,6 +14,7 @@
 // cos and sin of the tilt are formed once on the host (cosf/sinf of the
 // angle in radians, theta * pi/180 as the program converts it).
 #include "geo_internal.h"
+#include <algorithm>
 #include "tti2d.cuh"
 #include <cmath>
 #include <vector>
@@ -109,6 +110,10 @@ extern "C" int geo_tti2d_shot(const geo_fd2d_desc *desc, const float *v, const f
         model[3 * n + k] = std::cos(th);
         model[4 * n + k] = std::sin(th);
     }
+    {
+        const auto mm = std::minmax_element(pv.begin(), pv.end());
+        GEO_TRY(check_stability(V_GPU, 2, *mm.first, *mm.second, D.dt, D.dx, D.dx, D.dz, D.favg));
+    }
     // sponge (get_d0 :186-189 from the padded centre velocity; initial_coffe :227-271)
     const float d0 = sponge_d0(V_GPU, 2, 0.0f, pv[n / 2], npd, D.dx, D.dx, D.dz);
     std::vector<float> prof(4 * (size_t)(nnx + nnz));
@@ -148,6 +153,8 @@ extern "C" int geo_tti2d_shot(const geo_fd2d_desc *desc, const float *v, const f
     const int blocks = (int)std::min<size_t>((n + 255) / 256, 152 * 16);
     const long src_id = (long)ixs * nnz + izs;
     const cudaMemcpyKind kout = mem == GEO_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+    Watchdog wd;
+    GEO_TRY(wd.open());
     for (int it = 0; it < nt; it++) {
         if (on[it]) {
             k_tti_src<<<1, 1, 0, s>>>(f, src_id, amp[it]);
@@ -161,7 +168,11 @@ extern "C" int geo_tti2d_shot(const geo_fd2d_desc *desc, const float *v, const f
         GEO_TRY(check_launch("tti_rec"));
         if (snap && it % snap_every == 0 && it != 0)
             GEO_CUDA(cudaMemcpyAsync(snap + (size_t)(it / snap_every - 1) * n, f.P, n * 4, kout, s));
+        const int w = wd.check(f.P, n, it, it == nt - 1, s);
+        if (w == GEO_ERR_NAN) break;
+        GEO_TRY(w);
     }
+    GEO_TRY(wd.verdict(s, "2D TTI shot"));
     GEO_CUDA(cudaMemcpyAsync(shot, drec.p, (size_t)nx * nt * 4, kout, s));
     GEO_CUDA(cudaStreamSynchronize(s));
     return GEO_OK;
