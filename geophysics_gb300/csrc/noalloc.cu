@@ -12,10 +12,15 @@
 // no graph instantiation, no allocating library routine) and nothing on the
 // host heap.  Its work memory is one file-scope device array, kScratchBytes
 // long, that every GPU which loads the library holds until the process
-// exits.  Host-side set-up quantities live in fixed-size static host arrays.
+// exits.  Host-side set-up quantities live in fixed-size static host arrays,
+// one set per process, so concurrent calls (other threads, other devices)
+// wait for one another on a mutex while they set up.  The array's device
+// address is looked up once per device and kept: a process that resets a
+// device (cudaDeviceReset) must not call this entry point on it afterwards.
 #include "geo_internal.h"
 #include <cmath>
 #include <cstring>
+#include <mutex>
 
 namespace geo {
 
@@ -32,14 +37,15 @@ static __device__ __align__(256) unsigned char g_scratch[kScratchBytes];
 
 static void *g_scratch_addr[kMaxDevices];     // per device, filled once
 
-// Host-side working storage (fixed size: no heap use).
+// Host-side working storage (fixed size: no heap use).  One set for the
+// process, so g_host_mu serialises the calls (from any thread, on any
+// device) for as long as they use it.
 static float h_prof[8 * kMaxN];
 static float h_amp[kMaxNt];
 static uint8_t h_on[kMaxNt];
-static float h_box_e[kTB * kTB], h_box_d[kTB * kTB], h_taper[2 * kTB * kTB];
+static float h_box[2 * kTB * kTB], h_taper[2 * kTB * kTB];
 static int h_mute[2 * kMaxN];
-static Shot2D h_shot;
-static float h_scalars[4];
+static std::mutex g_host_mu;
 
 // Device address of the scratch array on the current device.  The first
 // call on a device resolves it; that first call must come before any stream
@@ -73,6 +79,26 @@ __global__ void k_pad_model(int nx, int nz, int npd, const float *__restrict__ v
         vp[k] = v[s];
         e2[k] = 1 + 2 * e[s];
         d2[k] = sqrtf(1 + 2 * d[s]);
+    }
+}
+
+// The raw eps/del values of the SV taper box (kTB x kTB points from padded
+// cell (tx0, tz0)), read through the same edge clamp as the padded model;
+// z outside the padded grid gives 0 (those taper entries are never read).
+__global__ void k_gather_box(int nx, int nz, int npd, int tx0, int tz0, const float *__restrict__ e,
+                             const float *__restrict__ d, float *out) {
+    const int nnz = nz + 2 * npd;
+    for (int k = threadIdx.x; k < kTB * kTB; k += blockDim.x) {
+        const int bx = k / kTB, bz = k % kTB, ix = tx0 + bx, iz = tz0 + bz;
+        float ev = 0.0f, dv = 0.0f;
+        if (iz >= 0 && iz < nnz) {
+            const int sx = ix < npd ? 0 : (ix >= npd + nx ? nx - 1 : ix - npd);
+            const int sz = iz < npd ? 0 : (iz >= npd + nz ? nz - 1 : iz - npd);
+            ev = e[(size_t)sx * nz + sz];
+            dv = d[(size_t)sx * nz + sz];
+        }
+        out[k] = ev;
+        out[kTB * kTB + k] = dv;
     }
 }
 
@@ -141,6 +167,7 @@ extern "C" int geo_fd2d_shot_noalloc(const geo_fd2d_desc *desc, const float *v, 
         return fail(GEO_ERR_ARG, "shot needs %zu bytes of work memory; the no-allocation limit is %zu", off,
                     kScratchBytes);
 
+    std::lock_guard<std::mutex> host_lock(g_host_mu);
     void *base = nullptr;
     GEO_TRY(scratch_address(&base));
     unsigned char *S = static_cast<unsigned char *>(base);
@@ -156,6 +183,7 @@ extern "C" int geo_fd2d_shot_noalloc(const geo_fd2d_desc *desc, const float *v, 
     GEO_TRY(check_launch("pad_model"));
     k_model_stats<<<1, 256, 0, s>>>((long)D.nx * D.nz, v, e, stats);
     GEO_TRY(check_launch("model_stats"));
+    float h_scalars[4];
     GEO_CUDA(cudaMemcpyAsync(h_scalars, stats, 3 * 4, cudaMemcpyDeviceToHost, s));
     GEO_CUDA(cudaMemcpyAsync(h_scalars + 3, vp + n / 2, 4, cudaMemcpyDeviceToHost, s));
     GEO_CUDA(cudaStreamSynchronize(s));
@@ -200,23 +228,14 @@ extern "C" int geo_fd2d_shot_noalloc(const geo_fd2d_desc *desc, const float *v, 
         const int cx = var == V_GPU ? ixs + 1 : ixs, cz = var == V_GPU ? izs + 1 : izs;
         tx0 = cx - kTB / 2;
         tz0 = cz - kTB / 2;
-        for (int bx = 0; bx < kTB; bx++) {
-            const int ix = tx0 + bx;
-            const int sx = ix < D.npd ? 0 : (ix >= D.npd + D.nx ? D.nx - 1 : ix - D.npd);
-            const int z0 = tz0 < 0 ? 0 : tz0, z1 = tz0 + kTB > nnz ? nnz : tz0 + kTB;
-            for (int iz = z0; iz < z1; iz++) {
-                const int sz = iz < D.npd ? 0 : (iz >= D.npd + D.nz ? D.nz - 1 : iz - D.npd);
-                GEO_CUDA(cudaMemcpyAsync(&h_box_e[bx * kTB + iz - tz0], e + (size_t)sx * D.nz + sz, 4,
-                                         cudaMemcpyDeviceToHost, s));
-                GEO_CUDA(cudaMemcpyAsync(&h_box_d[bx * kTB + iz - tz0], d + (size_t)sx * D.nz + sz, 4,
-                                         cudaMemcpyDeviceToHost, s));
-            }
-        }
+        k_gather_box<<<1, 256, 0, s>>>(D.nx, D.nz, D.npd, tx0, tz0, e, d, taper);
+        GEO_TRY(check_launch("gather_box"));
+        GEO_CUDA(cudaMemcpyAsync(h_box, taper, 2 * kTB * kTB * 4, cudaMemcpyDeviceToHost, s));
         GEO_CUDA(cudaStreamSynchronize(s));
         for (int bx = 0; bx < kTB; bx++)
             for (int bz = 0; bz < kTB; bz++) {
                 const int rx = tx0 + bx - cx, rz = tz0 + bz - cz, r2 = rx * rx + rz * rz;
-                float ee = h_box_e[bx * kTB + bz], dd = h_box_d[bx * kTB + bz];
+                float ee = h_box[bx * kTB + bz], dd = h_box[kTB * kTB + bx * kTB + bz];
                 if (var == V_CPU) {
                     const int CR = 15;
                     if (r2 <= CR * CR) {
@@ -249,8 +268,8 @@ extern "C" int geo_fd2d_shot_noalloc(const geo_fd2d_desc *desc, const float *v, 
     GEO_CUDA(cudaMemsetAsync(rec, 0, (size_t)D.nt * D.nx * 4, s));
     GEO_CUDA(cudaMemsetAsync(items, 0, (size_t)ntiles * 4, s));
 
-    memset(&h_shot, 0, sizeof h_shot);
-    Shot2D &H = h_shot;
+    Shot2D H;
+    memset(&H, 0, sizeof H);
     H.nnx = nnx; H.nnz = nnz; H.npd = D.npd; H.nx = D.nx; H.nz = D.nz;
     H.dtx = D.dt / D.dx; H.dtz = D.dt / D.dz;
     H.cx1 = prof; H.cx2 = prof + nnx; H.ax1 = prof + 2 * nnx; H.ax2 = prof + 3 * nnx;
@@ -264,7 +283,8 @@ extern "C" int geo_fd2d_shot_noalloc(const geo_fd2d_desc *desc, const float *v, 
     H.rec_iz = D.rec_iz; H.rec_scale = D.rec_scale;
     H.rec_p = rec; H.rec_q = nullptr;
     H.tile_base = 0; H.ntz = (nnz + 31) / 32;
-    GEO_CUDA(cudaMemcpyAsync(dshot, &h_shot, sizeof(Shot2D), cudaMemcpyHostToDevice, s));
+    // from pageable memory: the copy has taken H before it returns
+    GEO_CUDA(cudaMemcpyAsync(dshot, &H, sizeof(Shot2D), cudaMemcpyHostToDevice, s));
 
     int sms = 1, dev = 0;
     GEO_CUDA(cudaGetDevice(&dev));

@@ -124,8 +124,14 @@ int geo_fd2d_shot(const geo_fd2d_desc *desc, const float *v, const float *e, con
  *     snapshots;
  *   - the first call on a device resolves the array's device address, so
  *     make that first call before any stream capture on that device;
- *   - all calls share the array: calls that overlap on the GPU (other
- *     streams, other host threads) race and corrupt each other's results. */
+ *   - the device address of the array is kept for the life of the
+ *     process: do not call this on a device after cudaDeviceReset;
+ *   - the host-side set-up is one fixed set of static arrays guarded by a
+ *     mutex: calls from several host threads (on one or several devices)
+ *     take turns for it;
+ *   - all calls on one device share the array: calls that overlap on the
+ *     GPU (other streams, other host threads) race and corrupt each
+ *     other's results. */
 int geo_fd2d_shot_noalloc(const geo_fd2d_desc *desc, const float *v, const float *e, const float *d,
                           float *shot, void *stream);
 size_t geo_fd2d_noalloc_limit(void);
