@@ -353,21 +353,15 @@ static int gpu_rtm_run(const GpuRtmProgram &prog, const geo_rtm2d_gpu_desc &D, c
         e2[k] = 1 + 2 * pe[k];
         d2[k] = sqrtf(1 + 2 * pd[k]);
     }
-    // tilt in radians as read_file converts it (theta *= pi/180), cos and sin tables
-    std::vector<float> ct, st;
+    // tilt in radians as read_file converts it (theta *= pi/180); its cos and
+    // sin are formed on the device below, as the program's kernels form them
+    std::vector<float> ct;
     float mu_v = pv[1] * sqrtf(1 + 2 * pe[1]);   // direct-wave velocity of the VTI program's mute
     if (prog.tti) {
         std::vector<float> pt(n);
         pad_model_2d(nx, nz, npml, ht.data(), pt.data());
         ct.resize(n);
-        st.resize(n);
-        for (size_t k = 0; k < n; k++) {
-            const float th = (float)((double)pt[k] * (kPiGui / 180.0));
-            ct[k] = std::cos(th);
-            st[k] = std::sin(th);
-        }
-        // mute_directwave of the TTI program: vp[1]*(1+(sqrtf(1+2 eps[1])-1)*cos(theta[1]))
-        mu_v = pv[1] * (1 + (sqrtf(1 + 2 * pe[1]) - 1) * ct[1]);
+        for (size_t k = 0; k < n; k++) ct[k] = (float)((double)pt[k] * (kPiGui / 180.0));
     }
     const int L = 2 * nx + 2 * nz;
 
@@ -377,7 +371,12 @@ static int gpu_rtm_run(const GpuRtmProgram &prog, const geo_rtm2d_gpu_desc &D, c
         GEO_TRY(dct.alloc(n * 4));
         GEO_TRY(dst_.alloc(n * 4));
         GEO_CUDA(cudaMemcpyAsync(dct.p, ct.data(), n * 4, cudaMemcpyHostToDevice, s));
-        GEO_CUDA(cudaMemcpyAsync(dst_.p, st.data(), n * 4, cudaMemcpyHostToDevice, s));
+        GEO_TRY(launch_tilt_trig(dct.as<float>(), dst_.as<float>(), n, s));
+        // mute_directwave of the TTI program: vp[1]*(1+(sqrtf(1+2 eps[1])-1)*cos(theta[1]))
+        float c1 = 0.0f;
+        GEO_CUDA(cudaMemcpyAsync(&c1, dct.as<float>() + 1, 4, cudaMemcpyDeviceToHost, s));
+        GEO_CUDA(cudaStreamSynchronize(s));
+        mu_v = pv[1] * (1 + (sqrtf(1 + 2 * pe[1]) - 1) * c1);
     }
     GEO_TRY(dprof.alloc(prof.size() * 4));
     GEO_TRY(de2.alloc(n * 4));

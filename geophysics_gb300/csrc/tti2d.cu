@@ -21,6 +21,27 @@
 
 namespace geo {
 
+// cos and sin of the tilt (radians, in place: th -> cos, sin into sn).  The
+// 2D TTI programs evaluate cos(theta[id]) and sin(theta[id]) of their float
+// tilt inside their kernels (Toa_gpu_2dtti_fd_1orderfunction.cu:106-107,
+// :168-175; Toa_gpu_2dtti_rtm_adcigs_iorderfunciton.cu:155-156, :216-222),
+// i.e. the device's single-precision cosf and sinf; the tables are formed
+// here with the same device functions, so they hold the programs' values.
+__global__ void k_tilt_trig(float *th_cos, float *sn, size_t n) {
+    for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x) {
+        const float t = th_cos[k];
+        th_cos[k] = cosf(t);
+        sn[k] = sinf(t);
+    }
+}
+
+int launch_tilt_trig(float *th_cos, float *sn, size_t n, cudaStream_t s) {
+    const int grid = (int)std::min<size_t>((n + 255) / 256, 152 * 8);
+    k_tilt_trig<<<grid, 256, 0, s>>>(th_cos, sn, n);
+    return check_launch("tilt_trig");
+}
+
+
 __constant__ float c_tti[4] = {1.196289f, -0.0797526f, 0.009570313f, -0.0006975447f};
 
 __global__ void k_tti_src(TtiField f, long id, float amp) {
@@ -100,15 +121,15 @@ extern "C" int geo_tti2d_shot(const geo_fd2d_desc *desc, const float *v, const f
                 pd[(size_t)ix * nnz + iz] = tp.d[bx * tp.n + bz];
             }
     }
-    // model arrays: vp, 1+2eps, sqrtf(1+2del), cos and sin of the tilt
+    // model arrays: vp, 1+2eps, sqrtf(1+2del), and the tilt in radians as
+    // read_file converts it (:235), whose cos and sin are then formed on the
+    // device (launch_tilt_trig) as the program's kernels form them
     std::vector<float> model(5 * n);
     for (size_t k = 0; k < n; k++) {
-        const float th = (float)((double)pt[k] * (kPiGui / 180.0));   // read_file :235
         model[k] = pv[k];
         model[n + k] = 1 + 2 * pe[k];
         model[2 * n + k] = sqrtf(1 + 2 * pd[k]);
-        model[3 * n + k] = std::cos(th);
-        model[4 * n + k] = std::sin(th);
+        model[3 * n + k] = (float)((double)pt[k] * (kPiGui / 180.0));
     }
     {
         const auto mm = std::minmax_element(pv.begin(), pv.end());
@@ -131,6 +152,7 @@ extern "C" int geo_tti2d_shot(const geo_fd2d_desc *desc, const float *v, const f
     GEO_TRY(df.alloc(8 * n * 4));
     GEO_TRY(drec.alloc((size_t)nx * nt * 4));
     GEO_CUDA(cudaMemcpyAsync(dm.p, model.data(), 5 * n * 4, cudaMemcpyHostToDevice, s));
+    GEO_TRY(launch_tilt_trig(dm.as<float>() + 3 * n, dm.as<float>() + 4 * n, n, s));
     GEO_CUDA(cudaMemcpyAsync(dprof.p, prof.data(), prof.size() * 4, cudaMemcpyHostToDevice, s));
     GEO_TRY(df.zero(s));
     GEO_TRY(drec.zero(s));

@@ -493,6 +493,19 @@ static void ttim_free(orc_ttim *m)
     free(m->amp); free(m->act);
 }
 
+/* cos and sin of the tilt.  The GPU TTI programs evaluate them inside their
+ * kernels with the device's cosf/sinf; a CPU cannot reproduce those bit for
+ * bit, so the caller may hand over the device's values for the model's
+ * nx*nz angles (padded here like the angles); without them the oracle uses
+ * the host's cosf/sinf. */
+static const float *g_tilt_cos, *g_tilt_sin;
+
+void orc_set_tilt_trig(const float *ct, const float *st)
+{
+    g_tilt_cos = ct;
+    g_tilt_sin = st;
+}
+
 /* taper_R, taper_r: SV taper of e2t/d2t centred (fs+(is-1)ds+npd, zs+npd) (0: none) */
 static void ttim_init(orc_ttim *m, const orc_fd2d_desc *d, const float *v, const float *e, const float *dl,
                       const float *theta, int rtm_sponge, int taper_R, int taper_r)
@@ -516,6 +529,19 @@ static void ttim_init(orc_ttim *m, const orc_fd2d_desc *d, const float *v, const
             th[id] = (float)((double)theta[ix * nz + iz] * (PI_GUI / 180.0));
         }
     orc_pad2d(nx, nz, npd, m->vp); orc_pad2d(nx, nz, npd, ee); orc_pad2d(nx, nz, npd, dd); orc_pad2d(nx, nz, npd, th);
+    REAL *tc = NULL, *ts = NULL;
+    if (g_tilt_cos && g_tilt_sin) {
+        tc = calloc(n, sizeof(REAL));
+        ts = calloc(n, sizeof(REAL));
+        for (ix = 0; ix < nx; ix++)
+            for (iz = 0; iz < nz; iz++) {
+                id = (ix + npd) * nnz + iz + npd;
+                tc[id] = g_tilt_cos[ix * nz + iz];
+                ts[id] = g_tilt_sin[ix * nz + iz];
+            }
+        orc_pad2d(nx, nz, npd, tc);
+        orc_pad2d(nx, nz, npd, ts);
+    }
     {
         const float fsx = d->fs + (d->is - 1) * d->ds;
         const int ixs = (int)(fsx + 0.5f) + npd - 1, izs = (int)(d->zs + 0.5f) + npd - 1;
@@ -527,8 +553,8 @@ static void ttim_init(orc_ttim *m, const orc_fd2d_desc *d, const float *v, const
             float thf = (float)th[id], te = (float)ee[id], td = (float)dd[id];
             m->e2[id] = 1 + 2 * te;
             m->d2[id] = sqrtf(1 + 2 * td);
-            m->ct[id] = cosf(thf);
-            m->st[id] = sinf(thf);
+            m->ct[id] = tc ? (float)tc[id] : cosf(thf);
+            m->st[id] = ts ? (float)ts[id] : sinf(thf);
             ix = id / nnz; iz = id % nnz;
             if (taper_R > 0) {
                 int rx = (int)ix - cx, rz = (int)iz - cz;
@@ -569,7 +595,7 @@ static void ttim_init(orc_ttim *m, const orc_fd2d_desc *d, const float *v, const
         m->dtx = d->dt / d->dx;
         m->dtz = d->dt / d->dz;
     }
-    free(ee); free(dd); free(th);
+    free(ee); free(dd); free(th); free(tc); free(ts);
 }
 
 /* update_vel then update_stress, in place, with e2/d2 (tapered or not) */
@@ -1509,14 +1535,20 @@ static int rtm3d_shot_run(const orc_fd3d_desc *d, int mute_tt, const float *v, c
 {
     orc_g3d G; orc_f3d S, R;
     const int nx = d->nx, ny = d->ny, nz = d->nz, npd = d->npd, nt = d->nt;
-    long it, ix, iy, iz;
+    /* receivers (record at z = npd, re-inject at npd - 1): the grid
+     * (rx0 + jx drx, ry0 + jy dry); every surface node is the program's
+     * (shot_record :319-334) */
+    const int nrx = d->nrx, nry = d->nry;
+    long it, ix, iy, iz, jx, jy;
+#define RX(j) (d->rx0 + (long)(j) * d->drx)
+#define RY(j) (d->ry0 + (long)(j) * d->dry)
     g3d_init(&G, d, v, e, dl);
     if (theta) g3d_tilt(&G, theta, phi);
     f3d_alloc(&S, G.n);
     f3d_alloc(&R, G.n);
     const long L = 2L * nx * ny + 2L * nz * ny + 2L * nx * nz;
     float *bp = calloc((size_t)nt * L, 4), *bq = calloc((size_t)nt * L, 4);
-    float *rec = calloc((size_t)nt * nx * ny, 4);
+    float *rec = calloc((size_t)nt * nrx * nry, 4);
 #define GID(z, x, y) ((long)(z) + G.nnz * (long)(x) + G.nxz * (long)(y))
     /* ring position of entry k (the program's face order) */
 #define RING(k, gid) do { long k_ = (k); \
@@ -1533,9 +1565,9 @@ static int rtm3d_shot_run(const orc_fd3d_desc *d, int mute_tt, const float *v, c
             long gid; RING(k, gid);
             bp[it * L + k] = (float)S.P[gid]; bq[it * L + k] = (float)S.Q[gid];
         }
-        for (iy = 0; iy < ny; iy++) for (ix = 0; ix < nx; ix++) {
-            long gid = GID(npd, npd + ix, npd + iy);
-            rec[it + (long)nt * ix + (long)nt * nx * iy] = (float)(S.P[gid] + S.Q[gid]);
+        for (jy = 0; jy < nry; jy++) for (jx = 0; jx < nrx; jx++) {
+            long gid = GID(npd, npd + RX(jx), npd + RY(jy));
+            rec[it + (long)nt * jx + (long)nt * nrx * jy] = (float)(S.P[gid] + S.Q[gid]);
         }
         for (iy = 0; iy < ny; iy++) for (ix = 0; ix < nx; ix++) for (iz = 0; iz < nz; iz++) {
             long gid = GID(npd + iz, npd + ix, npd + iy), o = iz + (long)nz * ix + (long)nz * nx * iy;
@@ -1547,17 +1579,18 @@ static int rtm3d_shot_run(const orc_fd3d_desc *d, int mute_tt, const float *v, c
     {
         /* vp[1], eps[1] of the padded model = the model's first cell */
         const float eps1 = e[0], vp1 = v[0];
-        for (iy = 0; iy < ny; iy++) for (ix = 0; ix < nx; ix++) {
+        for (jy = 0; jy < nry; jy++) for (jx = 0; jx < nrx; jx++) {
+            ix = RX(jx); iy = RY(jy);
             float mu_x = d->dx * abs((int)ix - d->fsx - d->is * d->dsx), mu_y = d->dy * abs((int)iy - d->fsy - d->is * d->dsy);
             float mu_z = d->dz * d->fsz;
             float mu_t0 = sqrtf((float)(pow(mu_x, 2) + pow(mu_y, 2) + pow(mu_z, 2))) / (vp1 * sqrtf(1 + 2 * eps1));
             int mu_t = (int)(2.0 / (d->dt * d->favg));
             int mu_nt = (int)(mu_t0 / d->dt) + mu_t + mute_tt;
             for (it = 0; it < nt; it++)
-                if ((it > (int)(mu_t0 / d->dt) - mute_tt) && (it < mu_nt)) rec[it + (long)nt * ix + (long)nt * nx * iy] = 0.0f;
+                if ((it > (int)(mu_t0 / d->dt) - mute_tt) && (it < mu_nt)) rec[it + (long)nt * jx + (long)nt * nrx * jy] = 0.0f;
         }
     }
-    if (rec_out) memcpy(rec_out, rec, (size_t)nt * nx * ny * 4);
+    if (rec_out) memcpy(rec_out, rec, (size_t)nt * nrx * nry * 4);
     for (it = nt - 1; it >= 0; it--) {
         long k;
         for (k = 0; k < L; k++) {
@@ -1565,9 +1598,9 @@ static int rtm3d_shot_run(const orc_fd3d_desc *d, int mute_tt, const float *v, c
             S.P[gid] = (REAL)bp[it * L + k]; S.Q[gid] = (REAL)bq[it * L + k];
         }
         g3d_step(&G, &S, 0, 0);
-        for (iy = 0; iy < ny; iy++) for (ix = 0; ix < nx; ix++) {
-            long gid = GID(npd - 1, npd + ix, npd + iy);
-            R.P[gid] = R.Q[gid] = (REAL)rec[it + (long)nt * ix + (long)nt * nx * iy];
+        for (jy = 0; jy < nry; jy++) for (jx = 0; jx < nrx; jx++) {
+            long gid = GID(npd - 1, npd + RX(jx), npd + RY(jy));
+            R.P[gid] = R.Q[gid] = (REAL)rec[it + (long)nt * jx + (long)nt * nrx * jy];
         }
         g3d_step(&G, &R, 0, 0);
         for (iy = 0; iy < ny; iy++) for (ix = 0; ix < nx; ix++) for (iz = 0; iz < nz; iz++) {
@@ -1617,19 +1650,20 @@ static int rtm3d_snap_run(const orc_fd3d_desc *d, int mute_tt, int k, const floa
     const int nx = d->nx, ny = d->ny, nz = d->nz, npd = d->npd, nt = d->nt;
     const long nimg = (long)nx * ny * nz;
     const int nsnap = nt / k;
-    long it, ix, iy, iz;
+    const int nrx = d->nrx, nry = d->nry;   /* receiver grid, as in rtm3d_shot_run */
+    long it, ix, iy, iz, jx, jy;
     g3d_init(&G, d, v, e, dl);
     if (theta) g3d_tilt(&G, theta, phi);
     f3d_alloc(&S, G.n);
     f3d_alloc(&R, G.n);
     float *snap = calloc((size_t)(nsnap > 0 ? nsnap : 1) * nimg, 4);
-    float *rec = calloc((size_t)nt * nx * ny, 4);
+    float *rec = calloc((size_t)nt * nrx * nry, 4);
 #define GID(z, x, y) ((long)(z) + G.nnz * (long)(x) + G.nxz * (long)(y))
     for (it = 0; it < nt; it++) {
         g3d_step(&G, &S, G.act[it], (REAL)G.amp[it]);
-        for (iy = 0; iy < ny; iy++) for (ix = 0; ix < nx; ix++) {
-            long gid = GID(npd, npd + ix, npd + iy);
-            rec[it + (long)nt * ix + (long)nt * nx * iy] = (float)(S.P[gid] + S.Q[gid]);
+        for (jy = 0; jy < nry; jy++) for (jx = 0; jx < nrx; jx++) {
+            long gid = GID(npd, npd + RX(jx), npd + RY(jy));
+            rec[it + (long)nt * jx + (long)nt * nrx * jy] = (float)(S.P[gid] + S.Q[gid]);
         }
         for (iy = 0; iy < ny; iy++) for (ix = 0; ix < nx; ix++) for (iz = 0; iz < nz; iz++) {
             long gid = GID(npd + iz, npd + ix, npd + iy), o = iz + (long)nz * ix + (long)nz * nx * iy;
@@ -1640,20 +1674,21 @@ static int rtm3d_snap_run(const orc_fd3d_desc *d, int mute_tt, int k, const floa
     }
     {
         const float eps1 = e[0], vp1 = v[0];
-        for (iy = 0; iy < ny; iy++) for (ix = 0; ix < nx; ix++) {
+        for (jy = 0; jy < nry; jy++) for (jx = 0; jx < nrx; jx++) {
+            ix = RX(jx); iy = RY(jy);
             float mu_x = d->dx * abs((int)ix - d->fsx - d->is * d->dsx), mu_y = d->dy * abs((int)iy - d->fsy - d->is * d->dsy);
             float mu_z = d->dz * d->fsz;
             float mu_t0 = sqrtf((float)(pow(mu_x, 2) + pow(mu_y, 2) + pow(mu_z, 2))) / (vp1 * sqrtf(1 + 2 * eps1));
             int mu_t = (int)(2.0 / (d->dt * d->favg));
             int mu_nt = (int)(mu_t0 / d->dt) + mu_t + mute_tt;
             for (it = 0; it < nt; it++)
-                if ((it > (int)(mu_t0 / d->dt) - mute_tt) && (it < mu_nt)) rec[it + (long)nt * ix + (long)nt * nx * iy] = 0.0f;
+                if ((it > (int)(mu_t0 / d->dt) - mute_tt) && (it < mu_nt)) rec[it + (long)nt * jx + (long)nt * nrx * jy] = 0.0f;
         }
     }
     for (it = nt - 1; it >= 0; it--) {
-        for (iy = 0; iy < ny; iy++) for (ix = 0; ix < nx; ix++) {
-            long gid = GID(npd - 1, npd + ix, npd + iy);
-            R.P[gid] = R.Q[gid] = (REAL)rec[it + (long)nt * ix + (long)nt * nx * iy];
+        for (jy = 0; jy < nry; jy++) for (jx = 0; jx < nrx; jx++) {
+            long gid = GID(npd - 1, npd + RX(jx), npd + RY(jy));
+            R.P[gid] = R.Q[gid] = (REAL)rec[it + (long)nt * jx + (long)nt * nrx * jy];
         }
         g3d_step(&G, &R, 0, 0);
         for (iy = 0; iy < ny; iy++) for (ix = 0; ix < nx; ix++) for (iz = 0; iz < nz; iz++) {
@@ -1667,6 +1702,8 @@ static int rtm3d_snap_run(const orc_fd3d_desc *d, int mute_tt, int k, const floa
         }
     }
 #undef GID
+#undef RX
+#undef RY
     free(snap); free(rec);
     f3d_free(&S); f3d_free(&R); g3d_free(&G);
     return 0;

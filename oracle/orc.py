@@ -54,6 +54,7 @@ def lib(prec=32):
         L = C.CDLL(path)
         L.orc_fd2d.argtypes = [C.POINTER(FD2DDesc)] + [C.POINTER(C.c_float)] * 5 + [C.c_int]
         L.orc_tti2d.argtypes = [C.POINTER(FD2DDesc)] + [C.POINTER(C.c_float)] * 6 + [C.c_int]
+        L.orc_set_tilt_trig.argtypes = [C.POINTER(C.c_float)] * 2
         L.orc_fd3d.argtypes = [C.POINTER(FD3DDesc)] + [C.POINTER(C.c_float)] * 6
         L.orc_tti3d.argtypes = [C.POINTER(FD3DDesc)] + [C.POINTER(C.c_float)] * 8
         L.orc_rtm3d_tti_shot.argtypes = [C.POINTER(FD3DDesc), C.c_int] + [C.POINTER(C.c_float)] * 8
@@ -100,16 +101,36 @@ def fd2d(v, e, d, *, npd, nt, dx, dz, dt, favg, pfac, fs, zs, ds=0.0, is_=1, var
     return (shot, snaps) if snap_every else shot
 
 
+class _TiltTrig:
+    """Hand the device's cos/sin of the tilt (nx*nz each) to the oracle for
+    one call (orc_set_tilt_trig); None keeps the host's cosf/sinf."""
+
+    def __init__(self, prec, trig):
+        self.L = lib(prec)
+        self.trig = None if trig is None else (c32(trig[0]), c32(trig[1]))
+
+    def __enter__(self):
+        if self.trig is not None:
+            self.L.orc_set_tilt_trig(_fp(self.trig[0]), _fp(self.trig[1]))
+        return self
+
+    def __exit__(self, *a):
+        self.L.orc_set_tilt_trig(None, None)
+
+
 def tti2d(v, e, d, theta, *, npd, nt, dx, dz, dt, favg, pfac, fs, zs, ds=0.0, is_=1, sv=0, wtype=1, rec_iz=None,
-          snap_every=0, prec=32):
-    """2D TTI forward modelling (GPU TTI program semantics); theta in degrees."""
+          snap_every=0, prec=32, trig=None):
+    """2D TTI forward modelling (GPU TTI program semantics); theta in degrees.
+    trig: (cos, sin) of the tilt as the GPU forms them (refgpu.cuda_trig);
+    without it the host's cosf/sinf."""
     v, e, d, theta = c32(v), c32(e), c32(d), c32(theta)
     nx, nz = v.shape
     desc = FD2DDesc(nx=nx, nz=nz, npd=npd, nt=nt, variant=V_GPU, sv=sv, wtype=wtype, dx=dx, dz=dz, dt=dt, favg=favg,
                     pfac=pfac, fs=fs, ds=ds, zs=zs, is_=is_, rec_iz=npd if rec_iz is None else rec_iz, rec_scale=1.0)
     shot = np.zeros((nx, nt), _f)
     snaps = np.zeros(((nt - 1) // snap_every, nx + 2 * npd, nz + 2 * npd), _f) if snap_every else None
-    lib(prec).orc_tti2d(C.byref(desc), _fp(v), _fp(e), _fp(d), _fp(theta), _fp(shot), _fp(snaps), snap_every)
+    with _TiltTrig(prec, trig):
+        lib(prec).orc_tti2d(C.byref(desc), _fp(v), _fp(e), _fp(d), _fp(theta), _fp(shot), _fp(snaps), snap_every)
     return (shot, snaps) if snap_every else shot
 
 
@@ -141,7 +162,8 @@ def fd3d(v, e, d, *, npd, nt, dx, dy, dz, dt, favg, pfac, fsx, fsy, fsz, dsx=0, 
 
 
 def rtm3d(v, e, d, *, npd, nt, dx, dy, dz, dt, favg, pfac, fsx, fsy, fsz, dsx=0, dsy=0, dsz=0,
-          ns=1, sv=0, wtype=1, mode=0, mute_tt=70, snap_every=0, prec=32, adcig=None, theta=None, phi=None):
+          ns=1, sv=0, wtype=1, mode=0, mute_tt=70, snap_every=0, prec=32, adcig=None, theta=None, phi=None,
+          receivers=None):
     """3D boundary-saving RTM over shots 0..ns-1 (3D GPU RTM program
     semantics; with snap_every > 0 the stored-snapshot method instead);
     v,e,d shaped (ny, nx, nz).  Returns (mig divided by the illumination,
@@ -158,7 +180,7 @@ def rtm3d(v, e, d, *, npd, nt, dx, dy, dz, dt, favg, pfac, fsx, fsy, fsz, dsx=0,
     ny, nx, nz = v.shape
     mig = np.zeros((ny, nx, nz), _f)
     ill = np.zeros((ny, nx, nz), _f)
-    rec = np.zeros((ny, nx, nt), _f)
+    rec = np.zeros((int(receivers[5]), int(receivers[2]), nt) if receivers is not None else (ny, nx, nt), _f)
     na = da = dcdp = 0
     ag = None
     if adcig is not None:
@@ -166,11 +188,12 @@ def rtm3d(v, e, d, *, npd, nt, dx, dy, dz, dt, favg, pfac, fsx, fsy, fsz, dsx=0,
             raise ValueError("angle gathers need the boundary method")
         na, da, dcdp = adcig
         ag = np.zeros((ny // dcdp, nx // dcdp, na, nz), _f)
+    rx0, drx, nrx, ry0, dry, nry = receivers if receivers is not None else (0, 1, nx, 0, 1, ny)
     for is_ in range(ns):
         desc = FD3DDesc(nx=nx, ny=ny, nz=nz, npd=npd, nt=nt, sv=sv, wtype=wtype, mode=mode,
                         dx=dx, dy=dy, dz=dz, dt=dt, favg=favg, pfac=pfac, fsx=fsx, fsy=fsy, fsz=fsz,
                         dsx=dsx, dsy=dsy, dsz=dsz, is_=is_, rec_iz=npd,
-                        rx0=0, drx=1, nrx=nx, ry0=0, dry=1, nry=ny)
+                        rx0=rx0, drx=drx, nrx=nrx, ry0=ry0, dry=dry, nry=nry)
         if tti and snap_every:
             lib(prec).orc_rtm3d_tti_snap_shot(C.byref(desc), mute_tt, snap_every, _fp(v), _fp(e), _fp(d), _fp(th),
                                               _fp(ph), _fp(mig), _fp(ill))
@@ -222,9 +245,10 @@ def rtm2d_gpu(v, e, d, *, npml, nt, dx, dz, dt, favg, pfac, wtype=1, ns=1, fs=1,
 
 
 def rtm2d_tti(v, e, d, theta, *, npml, nt, dx, dz, dt, favg, pfac, wtype=1, ns=1, fs=1, ds=0, zs=1, mute_tt=30,
-              nangle=65, dangle=1, dcdp=1, obs=None, prec=32):
+              nangle=65, dangle=1, dcdp=1, obs=None, prec=32, trig=None):
     """The 2D TTI GPU RTM program; theta in degrees.  Returns (mig/ill (nx,nz),
-    ill, adcigs (nx//dcdp,nangle,nz), muted modelled shots (ns,nx,nt))."""
+    ill, adcigs (nx//dcdp,nangle,nz), muted modelled shots (ns,nx,nt)).
+    trig: as for tti2d."""
     v, e, d, theta = c32(v), c32(e), c32(d), c32(theta)
     nx, nz = v.shape
     mig = np.zeros((nx, nz), _f)
@@ -232,9 +256,10 @@ def rtm2d_tti(v, e, d, theta, *, npml, nt, dx, dz, dt, favg, pfac, wtype=1, ns=1
     ag = np.zeros((nx // dcdp, nangle, nz), _f)
     shots = np.zeros((ns, nx, nt), _f)
     ob = c32(obs) if obs is not None else None
-    lib(prec).orc_rtm2d_tti(nx, nz, npml, nt, dx, dz, dt, favg, pfac, wtype, ns, fs, ds, zs, mute_tt, nangle,
-                            dangle, dcdp, _fp(v), _fp(e), _fp(d), _fp(theta), _fp(ob), _fp(mig), _fp(ill), _fp(ag),
-                            _fp(shots))
+    with _TiltTrig(prec, trig):
+        lib(prec).orc_rtm2d_tti(nx, nz, npml, nt, dx, dz, dt, favg, pfac, wtype, ns, fs, ds, zs, mute_tt, nangle,
+                                dangle, dcdp, _fp(v), _fp(e), _fp(d), _fp(theta), _fp(ob), _fp(mig), _fp(ill),
+                                _fp(ag), _fp(shots))
     return mig, ill, ag, shots
 
 

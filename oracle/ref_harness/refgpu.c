@@ -1,6 +1,7 @@
 /* Runs the reference's own GPU kernels, compiled unmodified from
- * 2D-3D-vti-fd-cuda-gtk-GUI/GPU_vti3dfd_kernels.cu and GPU_vti2dfd_kernels.cu
- * into cubins by oracle/Makefile, through the CUDA driver API.
+ * 2D-3D-vti-fd-cuda-gtk-GUI/GPU_vti3dfd_kernels.cu, GPU_vti2dfd_kernels.cu and
+ * 2D-tti-fd+rtm-cuda/Toa_gpu_2dtti_fd_1orderfunction.cu into cubins by
+ * oracle/Makefile, through the CUDA driver API.
  *
  * Test infrastructure only (the parity pin of the oracle and of the
  * library's 3D and 2D GPU-variant paths); nothing in the product links it.
@@ -15,6 +16,8 @@
  *
  *   refgpu_vti3d  GPU_vti3dfd  (GPU_vti3dfd_kernels.cu:371-574)
  *   refgpu_vti2d  GPU_vti2dfd  (GPU_vti2dfd_kernels.cu:301-484)
+ *   refgpu_tti2d  the 2D TTI forward program's main()
+ *                 (2D-tti-fd+rtm-cuda/Toa_gpu_2dtti_fd_1orderfunction.cu:312-470)
  *
  * Kernels are looked up by their C++ names in the module (the mangled name
  * starts with "_Z<len><name>").  Every index the launched kernels form was
@@ -414,5 +417,170 @@ done:
     if (ev1) cuEventDestroy(ev1);
     rt_close(&rt);
     free(v); free(e); free(d);
+    return rc;
+}
+
+/* The 2D TTI GPU program (2D-tti-fd+rtm-cuda/Toa_gpu_2dtti_fd_1orderfunction.cu:
+ * main, :312-470) with arrays: v, e, d, theta (degrees, converted as its
+ * read_file does, :235) hold nx*nz floats, z fastest; shot receives ns
+ * records of nt*nx floats (not muted: the program's mute call is commented
+ * out); snap, when not NULL, receives the padded P of shot 1 at it = 100,
+ * 200, ... ((nt-1)/100 fields).  dx, dz, dt, favg, pfac are the program's
+ * float parameters; SV is its update_stress flag (the program passes false). */
+int refgpu_tti2d(const char *cubin, int nx, int nz, float dx, float dz, int npml, int SV, const float *v_in,
+                 const float *e_in, const float *d_in, const float *th_in, float favg, float pfac, int ns, int fs,
+                 int ds, int zs, int nt, float dt, float *shot, float *snap, float *ms_per_step) {
+    int rc = 0, is, it, ix, iz, wtype = 1;
+    int nnx = nx + 2 * npml, nnz = nz + 2 * npml;
+    size_t nn = (size_t)nnx * nnz, nb = nn * sizeof(float);
+    float t, xsn = (float)fs, zsn = (float)zs;
+    unsigned char sv = SV ? 1 : 0;
+    float *v = 0, *e = 0, *d = 0, *b = 0;
+    Rt rt;
+    CUfunction f_src, f_vel, f_str, f_d0, f_coff, f_rec;
+    CUdeviceptr vp = 0, eps = 0, del = 0, th = 0, P = 0, Q = 0, shotd = 0;
+    CUdeviceptr u[2] = {0, 0}, w[2] = {0, 0}, px[2] = {0, 0}, pz[2] = {0, 0}, qx[2] = {0, 0}, qz[2] = {0, 0};
+    CUdeviceptr cf[8] = {0};
+    CUevent ev0 = 0, ev1 = 0;
+    float tot_ms = 0.f;
+    CUdeviceptr *all[] = {&vp, &eps, &del, &th, &P, &Q, &u[0], &u[1], &w[0], &w[1], &px[0], &px[1],
+                          &pz[0], &pz[1], &qx[0], &qx[1], &qz[0], &qz[1]};
+    size_t nall = sizeof all / sizeof all[0], k;
+
+    if (rt_open(&rt, cubin)) {
+        rt_close(&rt);
+        return 1;
+    }
+    if (find_fn(rt.mod, "add_source", &f_src) || find_fn(rt.mod, "update_vel", &f_vel) ||
+        find_fn(rt.mod, "update_stress", &f_str) || find_fn(rt.mod, "get_d0", &f_d0) ||
+        find_fn(rt.mod, "initial_coffe", &f_coff) || find_fn(rt.mod, "shot_record", &f_rec)) {
+        rc = 1;
+        goto done;
+    }
+    v = (float *)calloc(nn, sizeof(float));
+    e = (float *)calloc(nn, sizeof(float));
+    d = (float *)calloc(nn, sizeof(float));
+    b = (float *)calloc(nn, sizeof(float));
+    if (!v || !e || !d || !b) {
+        rc = 1;
+        goto done;
+    }
+    /* read_file (:206-236): theta in degrees *= pi/180 (pi = 3.141592653) */
+    k = 0;
+    for (ix = npml; ix < nx + npml; ix++)
+        for (iz = npml; iz < nz + npml; iz++, k++) {
+            v[ix * nnz + iz] = v_in[k];
+            e[ix * nnz + iz] = e_in[k];
+            d[ix * nnz + iz] = d_in[k];
+            b[ix * nnz + iz] = (float)(th_in[k] * (3.141592653 / 180.0));
+        }
+    pad2(nnx, nnz, npml, e);
+    pad2(nnx, nnz, npml, d);
+    pad2(nnx, nnz, npml, v);
+    pad2(nnx, nnz, npml, b);
+
+    for (k = 0; k < nall; k++) CK(cuMemAlloc(all[k], nb));
+    CK(cuMemAlloc(&cf[0], nnx * 4)); CK(cuMemAlloc(&cf[1], nnx * 4)); /* coffx1/2 */
+    CK(cuMemAlloc(&cf[2], nnz * 4)); CK(cuMemAlloc(&cf[3], nnz * 4)); /* coffz1/2 */
+    CK(cuMemAlloc(&cf[4], nnx * 4)); CK(cuMemAlloc(&cf[5], nnx * 4)); /* acoffx1/2 */
+    CK(cuMemAlloc(&cf[6], nnz * 4)); CK(cuMemAlloc(&cf[7], nnz * 4)); /* acoffz1/2 */
+    CK(cuMemAlloc(&shotd, (size_t)nt * nx * 4));
+    CK(cuMemcpyHtoD(vp, v, nb));
+    CK(cuMemcpyHtoD(eps, e, nb));
+    CK(cuMemcpyHtoD(del, d, nb));
+    CK(cuMemcpyHtoD(th, b, nb));
+    CK(cuEventCreate(&ev0, CU_EVENT_DEFAULT));
+    CK(cuEventCreate(&ev1, CU_EVENT_DEFAULT));
+    {
+        void *a[] = {&dx, &dz, &nnx, &nnz, &npml, &vp};
+        CK(launch(f_d0, 1, 1, 1, 1, a));
+    }
+    {
+        void *ax[] = {&dt, &nx, &cf[0], &cf[1], &cf[4], &cf[5], &npml};
+        void *az[] = {&dt, &nz, &cf[2], &cf[3], &cf[6], &cf[7], &npml};
+        CK(launch(f_coff, (nnx + 511) / 512, 1, 512, 1, ax));
+        CK(launch(f_coff, (nnz + 511) / 512, 1, 512, 1, az));
+    }
+    {
+        CUdeviceptr u0 = u[0], u1 = u[1], w0 = w[0], w1 = w[1];
+        CUdeviceptr px0 = px[0], px1 = px[1], pz0 = pz[0], pz1 = pz[1];
+        CUdeviceptr qx0 = qx[0], qx1 = qx[1], qz0 = qz[0], qz1 = qz[1];
+        unsigned g = (unsigned)((nn + 511) / 512);
+        for (is = 1; is <= ns; is++) {
+            for (k = 4; k < nall; k++) CK(cuMemsetD32(*all[k], 0, nn));
+            CK(cuMemsetD32(shotd, 0, (size_t)nt * nx));
+            CK(cuEventRecord(ev0, 0));
+            for (it = 0, t = dt; it < nt; it++, t += dt) {
+                void *as[] = {&pfac, &xsn, &zsn, &nx, &nz, &nnx, &nnz, &dt, &t, &favg, &wtype, &npml, &is, &ds,
+                              &P, &Q};
+                void *av[] = {&nx, &nz, &nnx, &nnz, &npml, &dt, &dx, &dz, &u0, &w0, &u1, &w1, &P, &Q,
+                              &cf[0], &cf[1], &cf[2], &cf[3], &th};
+                void *ap[] = {&nx, &nz, &nnx, &nnz, &dt, &dx, &dz, &u1, &w1, &P, &Q, &vp, &npml, &px1, &px0,
+                              &pz1, &pz0, &qx1, &qx0, &qz1, &qz0, &cf[4], &cf[5], &cf[6], &cf[7], &del, &eps,
+                              &th, &fs, &ds, &zs, &is, &sv};
+                void *ar[] = {&nnx, &nnz, &nx, &nz, &npml, &it, &nt, &P, &shotd};
+                CK(launch(f_src, 1, 1, 1, 1, as));
+                CK(launch(f_vel, g, 1, 512, 1, av));
+                CK(launch(f_str, g, 1, 512, 1, ap));
+                u0 = u1; w0 = w1; px0 = px1; pz0 = pz1; qx0 = qx1; qz0 = qz1;
+                CK(launch(f_rec, (nx + 511) / 512, 1, 512, 1, ar));
+                if (snap && is == 1 && it % 100 == 0 && it != 0)
+                    CK(cuMemcpyDtoH(snap + (size_t)(it / 100 - 1) * nn, P, nb));
+            }
+            CK(cuEventRecord(ev1, 0));
+            CK(cuEventSynchronize(ev1));
+            {
+                float ms = 0.f;
+                CK(cuEventElapsedTime(&ms, ev0, ev1));
+                tot_ms += ms;
+            }
+            CK(cuMemcpyDtoH(shot + (size_t)(is - 1) * nt * nx, shotd, (size_t)nt * nx * 4));
+        }
+    }
+    CK(cuCtxSynchronize());
+    if (ms_per_step) *ms_per_step = tot_ms / (float)(ns * nt);
+done:
+    for (k = 0; k < nall; k++)
+        if (*all[k]) cuMemFree(*all[k]);
+    for (k = 0; k < 8; k++)
+        if (cf[k]) cuMemFree(cf[k]);
+    if (shotd) cuMemFree(shotd);
+    if (ev0) cuEventDestroy(ev0);
+    if (ev1) cuEventDestroy(ev1);
+    rt_close(&rt);
+    free(v); free(e); free(d); free(b);
+    return rc;
+}
+
+
+/* cos and sin of n angles (radians) by the device (k_ref_trig of
+ * oracle/ref_harness/trig.cu, loaded from `cubin`). */
+int refgpu_cuda_trig(const char *cubin, const float *th, float *c, float *s, long n) {
+    int rc = 0;
+    Rt rt;
+    CUfunction f;
+    CUdeviceptr dth = 0, dc = 0, ds = 0;
+    size_t nb = (size_t)n * sizeof(float);
+    if (rt_open(&rt, cubin)) {
+        rt_close(&rt);
+        return 1;
+    }
+    CK(cuModuleGetFunction(&f, rt.mod, "k_ref_trig"));
+    CK(cuMemAlloc(&dth, nb));
+    CK(cuMemAlloc(&dc, nb));
+    CK(cuMemAlloc(&ds, nb));
+    CK(cuMemcpyHtoD(dth, th, nb));
+    {
+        void *a[] = {&dth, &dc, &ds, &n};
+        unsigned g = (unsigned)((n + 255) / 256);
+        CK(launch(f, g > 1024 ? 1024 : g, 1, 256, 1, a));
+    }
+    CK(cuMemcpyDtoH(c, dc, nb));
+    CK(cuMemcpyDtoH(s, ds, nb));
+done:
+    if (dth) cuMemFree(dth);
+    if (dc) cuMemFree(dc);
+    if (ds) cuMemFree(ds);
+    rt_close(&rt);
     return rc;
 }

@@ -20,7 +20,19 @@ golden_fd2d_gpu.npz  GPU_vti2dfd (GPU_vti2dfd_kernels.cu:301) on a 61x51
                      case a: SV off, 2 shots (ds = 5), 300 steps, with the
                              padded P snapshots of shot 1 every 50 steps
                      case b: SV taper on, 1 shot, 300 steps
-Records are muted (tt = 100) as the programs write them.
+golden_tti2d_gpu.npz the 2D TTI forward program
+                     (2D-tti-fd+rtm-cuda/Toa_gpu_2dtti_fd_1orderfunction.cu,
+                     main :312) on a 61x51 layered VTI model with a smooth
+                     tilt field (5-40 degrees), npml 20:
+                     case a: SV off (as its main), 2 shots (ds = 5), 300
+                             steps, with the padded P snapshots of shot 1
+                             every 100 steps
+                     case b: SV taper on, 1 shot, 300 steps
+                     plus cos_dev, sin_dev: the device's cosf/sinf of the
+                     tilt in radians (what the program's kernels evaluate),
+                     which the CPU oracle is given
+The VTI programs' records are muted (tt = 100) as the programs write them;
+the TTI program's mute call is commented out in its main.
 """
 import hashlib
 import os
@@ -44,6 +56,19 @@ CASES2 = {
     "a": dict(dx=10, dz=10, npd=20, sv=0, favg=20, ns=2, fs=30, ds=5, zs=5, nt=300, dt_us=1000),
     "b": dict(dx=10, dz=10, npd=20, sv=1, favg=20, ns=1, fs=28, ds=0, zs=6, nt=300, dt_us=1000),
 }
+
+
+CASEST = {
+    "a": dict(dx=10.0, dz=10.0, npml=20, sv=0, favg=20.0, pfac=10.0, ns=2, fs=30, ds=5, zs=5, nt=300, dt=1e-3),
+    "b": dict(dx=10.0, dz=10.0, npml=20, sv=1, favg=20.0, pfac=10.0, ns=1, fs=27, ds=0, zs=6, nt=300, dt=1e-3),
+}
+
+
+def model_tti():
+    v, e, d = layered_model(61, 51, seed=9)
+    x, z = np.meshgrid(np.arange(61), np.arange(51), indexing="ij")
+    th = (22.5 + 17.5 * np.sin(x / 9.0) * np.cos(z / 13.0)).astype(np.float32)
+    return v, e, d, th
 
 
 def model3():
@@ -86,6 +111,18 @@ def main(out):
                 res["snap_" + tag] = snap
             print("2D case %s: max|shot| %.4g, %.3f ms/step" % (tag, np.abs(shot).max(), ms))
     np.savez_compressed(os.path.join(out, "golden_fd2d_gpu.npz"), **res)
+    v, e, d, th = model_tti()
+    ct, st = refgpu.cuda_trig(th)     # the device's cos/sin of the tilt, for the CPU oracle
+    res = dict(v=v, e=e, d=d, theta=th, cos_dev=ct, sin_dev=st)
+    for name, kw in CASEST.items():
+        for fma in (True, False):
+            shot, snap, ms = refgpu.tti2d(v, e, d, th, fma=fma, snaps=(name == "a"), **kw)
+            tag = "%s_%s" % (name, "fma" if fma else "nofma")
+            res["shot_" + tag] = shot
+            if snap is not None:
+                res["snap_" + tag] = snap
+            print("TTI case %s: max|shot| %.4g, %.3f ms/step" % (tag, np.abs(shot).max(), ms))
+    np.savez_compressed(os.path.join(out, "golden_tti2d_gpu.npz"), **res)
     write_sums(out)
 
 

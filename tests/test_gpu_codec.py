@@ -39,14 +39,19 @@ def test_codec_forward_and_gradients_match_oracle(geo):
     acts = A.forward(p, blocks)
     lo, go = A.backward(p, blocks)
     assert np.isfinite(rec).all()
-    # bf16 activations: GPU and oracle agree to rounding (tolerances 1e-2)
-    assert rel_l2(rec, acts["recon"]) < 1e-2
-    assert abs(loss - lo) <= 1e-2 * lo
+    # bf16 activations: GPU and oracle agree to rounding (the tensor cores'
+    # fp32 accumulation order is not specified); measured about 1e-3
+    tol = 3e-3
+    assert rel_l2(rec, acts["recon"]) < tol, rel_l2(rec, acts["recon"])
+    assert abs(loss - lo) <= tol * lo, (loss, lo)
     offs, _ = A.offsets()
+    worst = 0.0
     for l, (ow, ob) in enumerate(offs):
         N, K, _, _ = A.LAYERS[l]
-        assert rel_l2(g[ow:ow + N * K], go[ow:ow + N * K]) < 1e-2, l
-        assert rel_l2(g[ob:ob + N], go[ob:ob + N]) < 1e-2, l
+        rw, rb = rel_l2(g[ow:ow + N * K], go[ow:ow + N * K]), rel_l2(g[ob:ob + N], go[ob:ob + N])
+        worst = max(worst, rw, rb)
+        assert rw < tol and rb < tol, (l, rw, rb)
+    print("codec gradient worst rel-L2 per tensor: %.3g" % worst)
 
 
 @pytest.mark.parametrize("mode", [0, 1])

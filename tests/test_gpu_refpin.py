@@ -1,6 +1,8 @@
-"""The library's drop-ins GPU_vti3dfd and GPU_vti2dfd against the
-reference's own GPU programs (2D-3D-vti-fd-cuda-gtk-GUI/GPU_vti3dfd_kernels.cu,
-GPU_vti2dfd_kernels.cu), whose device code was compiled unmodified and run
+"""The library's drop-ins GPU_vti3dfd and GPU_vti2dfd and its 2D TTI shot
+against the reference's own GPU programs
+(2D-3D-vti-fd-cuda-gtk-GUI/GPU_vti3dfd_kernels.cu, GPU_vti2dfd_kernels.cu,
+2D-tti-fd+rtm-cuda/Toa_gpu_2dtti_fd_1orderfunction.cu), whose device code
+was compiled unmodified and run
 on a GPU: the golden records of tests/golden/make_golden_refgpu.py, and, where
 the cubins are present (oracle/_ref), the 400^3 headline shot run through the
 reference program itself.
@@ -84,6 +86,26 @@ def test_GPU_vti2dfd_bit_exact_vs_reference_program(geo, tmp_path, case):
     if "snap_%s_nofma" % case in g:
         rs = g["snap_%s_nofma" % case].reshape(-1)
         assert np.array_equal(np.fromfile(snap, np.float32)[:rs.size], rs)
+
+
+@pytest.mark.parametrize("case", sorted(M.CASEST))
+def test_tti2d_shot_bit_exact_vs_reference_program(geo, case):
+    """geo_tti2d_shot against the 2D TTI forward program
+    (2D-tti-fd+rtm-cuda/Toa_gpu_2dtti_fd_1orderfunction.cu:312-470)."""
+    g = _load("golden_tti2d_gpu.npz")
+    v, e, d, th = g["v"], g["e"], g["d"], g["theta"]
+    kw = M.CASEST[case]
+    snap_every = 100 if "snap_%s_nofma" % case in g else 0
+    for is_ in range(1, kw["ns"] + 1):
+        out = geo.tti2d_shot(v, e, d, th, npd=kw["npml"], nt=kw["nt"], dx=kw["dx"], dz=kw["dz"], dt=kw["dt"],
+                             favg=kw["favg"], pfac=kw["pfac"], fs=float(kw["fs"]), ds=float(kw["ds"]),
+                             zs=float(kw["zs"]), is_=is_, sv=kw["sv"], snap_every=snap_every)
+        shot, snaps = out if snap_every else (out, None)
+        ref = g["shot_%s_nofma" % case][is_ - 1]
+        assert np.abs(shot).max() > 0
+        assert np.array_equal(shot, ref), rel_l2(shot, ref)
+        if snaps is not None and is_ == 1:
+            assert np.array_equal(snaps, g["snap_%s_nofma" % case])
 
 
 def test_headline_shot_against_reference_program(geo):

@@ -1,7 +1,10 @@
-"""2D TTI on the GPU against the oracle (bit-exact)."""
+"""2D TTI on the GPU against the oracle (bit-exact).  The GPU TTI programs
+form cos and sin of their tilt on the device; the oracle is given the
+device's values (oracle.refgpu.cuda_trig) and restates the rest."""
 import numpy as np
 import pytest
 
+from oracle.refgpu import cuda_trig
 from tests.util import layered_model, rel_l2
 
 pytestmark = pytest.mark.gpu
@@ -19,7 +22,7 @@ def _model(nx=90, nz=67, seed=3):
 @pytest.mark.parametrize("sv", [0, 1])
 def test_tti2d_bit_exact(geo, orc, sv):
     v, e, d, th = _model()
-    ref, rs = orc.tti2d(v, e, d, th, sv=sv, snap_every=100, **KW)
+    ref, rs = orc.tti2d(v, e, d, th, sv=sv, snap_every=100, trig=cuda_trig(th), **KW)
     out, snaps = geo.tti2d_shot(v, e, d, th, sv=sv, snap_every=100, **KW)
     assert np.abs(ref).max() > 0
     assert np.array_equal(out, ref), rel_l2(out, ref)
@@ -31,7 +34,7 @@ def test_tti2d_device_buffers_and_second_shot(geo, orc):
     import torch
     v, e, d, th = _model(seed=4)
     kw = dict(KW, ds=7.0, is_=2, rec_iz=22)
-    ref = orc.tti2d(v, e, d, th, **kw)
+    ref = orc.tti2d(v, e, d, th, trig=cuda_trig(th), **kw)
     t = [torch.from_numpy(a).cuda() for a in (v, e, d, th)]
     out = geo.tti2d_shot(*t, **kw)
     assert out.is_cuda
@@ -56,7 +59,7 @@ def test_rtm2d_tti_program_bit_exact(geo, orc, dcdp):
     multiple of 3): image, illumination, gathers and records equal the
     oracle's."""
     v, e, d, th = _model(nx=91, nz=60, seed=5)
-    mig, ill, ag, shots = orc.rtm2d_tti(v, e, d, th, dcdp=dcdp, **TKW)
+    mig, ill, ag, shots = orc.rtm2d_tti(v, e, d, th, dcdp=dcdp, trig=cuda_trig(th), **TKW)
     out = geo.rtm2d_tti(v, e, d, th, dcdp=dcdp, **TKW)
     assert np.abs(ill).max() > 0 and np.abs(ag).max() > 0
     assert out["adcigs"].shape == (91 // dcdp, 65, 60)
@@ -71,7 +74,7 @@ def test_rtm2d_tti_program_observed_shots_device(geo, orc):
     v, e, d, th = _model(nx=80, nz=50, seed=6)
     kw = dict(TKW, ns=1, nt=400)
     obs = np.random.default_rng(7).standard_normal((1, 80, 400)).astype(np.float32) * 1e-3
-    mig, ill, ag, _ = orc.rtm2d_tti(v, e, d, th, obs=obs, **kw)
+    mig, ill, ag, _ = orc.rtm2d_tti(v, e, d, th, obs=obs, trig=cuda_trig(th), **kw)
     t = [torch.from_numpy(a).cuda() for a in (v, e, d, th, obs)]
     out = geo.rtm2d_tti(*t[:4], obs=t[4], **kw)
     assert out["mig_lap"].is_cuda

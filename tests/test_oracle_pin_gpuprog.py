@@ -1,8 +1,10 @@
 """The oracle's GPU-program restatements against the reference's own GPU
 programs: golden records made by running GPU_vti3dfd and GPU_vti2dfd
 (2D-3D-vti-fd-cuda-gtk-GUI/GPU_vti3dfd_kernels.cu:371,
-GPU_vti2dfd_kernels.cu:301), their device code compiled unmodified,
-on a GPU (tests/golden/make_golden_refgpu.py).  CPU only.
+GPU_vti2dfd_kernels.cu:301) and the 2D TTI forward program
+(2D-tti-fd+rtm-cuda/Toa_gpu_2dtti_fd_1orderfunction.cu:312), their device
+code compiled unmodified, on a GPU (tests/golden/make_golden_refgpu.py).
+CPU only.
 
 The programs were built twice: with contraction to FMA off ("nofma"), which
 the oracle reproduces bit for bit, and with the compiler's defaults ("fma",
@@ -89,11 +91,31 @@ def test_fd2d_gpu_variant_oracle_bit_exact_vs_GPU_vti2dfd(orc, case):
             assert np.array_equal(snaps, g["snap_%s_nofma" % case])
 
 
+@pytest.mark.parametrize("case", sorted(M.CASEST))
+def test_tti2d_oracle_bit_exact_vs_reference_program(orc, case):
+    g = _load("golden_tti2d_gpu.npz")
+    v, e, d, th = g["v"], g["e"], g["d"], g["theta"]
+    kw = M.CASEST[case]
+    ref = g["shot_%s_nofma" % case]
+    snap_every = 100 if "snap_%s_nofma" % case in g else 0
+    for is_ in range(1, kw["ns"] + 1):
+        out = orc.tti2d(v, e, d, th, npd=kw["npml"], nt=kw["nt"], dx=kw["dx"], dz=kw["dz"], dt=np.float32(kw["dt"]),
+                        favg=kw["favg"], pfac=kw["pfac"], fs=float(kw["fs"]), ds=float(kw["ds"]), zs=float(kw["zs"]),
+                        is_=is_, sv=kw["sv"], snap_every=snap_every, trig=(g["cos_dev"], g["sin_dev"]))
+        mine, snaps = out if snap_every else (out, None)
+        assert np.abs(mine).max() > 0
+        assert np.array_equal(mine, ref[is_ - 1]), (is_, rel_l2(mine, ref[is_ - 1]))
+        assert rel_l2(mine, g["shot_%s_fma" % case][is_ - 1]) < 1e-4
+        if snaps is not None and is_ == 1:
+            assert np.array_equal(snaps, g["snap_%s_nofma" % case])
+
+
 def test_reference_builds_differ_by_rounding_only():
     """The reference program's two builds agree to FP32 rounding, and no
     closer: the target 'within 1e-5 of the reference' is met by the
     reference's own no-FMA build only up to this distance."""
-    for name, cases in (("golden_fd3d_gpu.npz", M.CASES3), ("golden_fd2d_gpu.npz", M.CASES2)):
+    for name, cases in (("golden_fd3d_gpu.npz", M.CASES3), ("golden_fd2d_gpu.npz", M.CASES2),
+                        ("golden_tti2d_gpu.npz", M.CASEST)):
         g = _load(name)
         for c in cases:
             a, b = g["shot_%s_fma" % c], g["shot_%s_nofma" % c]
