@@ -30,19 +30,20 @@ struct ShotHost {
     int nx, nz, npd, nnx, nnz;
     Variant var;
     std::vector<float> vp, e2, d2, cx1, cx2, cz1, cz2, ax1, ax2, az1, az2;
-    std::vector<double> pw;
+    std::vector<double> kz, kx;     // MPI exact form: the chains' double factors per point
     Taper2D taper;
     std::vector<float> te2, td2;
-    std::vector<double> tpw;
+    std::vector<double> tkz, tkx;   // the same on the taper box
     int ixs, izs;
     float mu_v;
-    DevBuf d_model, d_pw, d_prof, d_taper, d_tpw, d_fields, d_rec, d_edge, d_img, d_adcig;
+    DevBuf d_model, d_k, d_prof, d_taper, d_tk, d_fields, d_rec, d_edge, d_img, d_adcig;
 };
 
 // Build the propagation coefficients of one (padded) window from its
 // unpadded model; Variant picks the reference program's formulas.
 static void build_shot_host(ShotHost &h, Variant var, int nx, int nz, int npd, float dx, float dz, float dt,
-                            const float *v, const float *e, const float *d, float srcx, float srcz, bool taper) {
+                            const float *v, const float *e, const float *d, float srcx, float srcz, bool taper,
+                            bool fast = false) {
     h.var = var;
     h.nx = nx; h.nz = nz; h.npd = npd;
     h.nnx = nx + 2 * npd; h.nnz = nz + 2 * npd;
@@ -62,13 +63,29 @@ static void build_shot_host(ShotHost &h, Variant var, int nx, int nz, int npd, f
     h.ixs = (int)(srcx + 0.5) + npd - 1;
     h.izs = (int)(srcz + 0.5) + npd - 1;
     h.vp.resize(n); h.e2.resize(n); h.d2.resize(n);
-    if (var == V_MPI) h.pw.resize(n);
+    // the MPI program's pz and qx chains are
+    //   (double)(az2*pz) - (double)(az1*vp) * pow(1+2del,0.5) * (double)dtz * (double)zz
+    // (and with ax, dtx, xx for qx), evaluated left to right; every factor but
+    // zz is fixed for the shot, so the product of the first three is formed
+    // here once, in the same order and precision, and the kernel issues one
+    // double multiply and one double subtraction per chain
+    const bool kchain = var == V_MPI && !fast;
+    const double ddtx = (double)(dt / dx), ddtz = (double)(dt / dz);
+    if (kchain) {
+        h.kz.resize(n);
+        h.kx.resize(n);
+    }
     for (size_t k = 0; k < n; k++) {
         // MPI program: vp <- rho*vp^2 with rho == 1 (Toa_rtm_vti_adcig_cdp.c:641)
         h.vp[k] = (var == V_MPI) ? 1.0f * (pv[k] * pv[k]) : pv[k];
         h.e2[k] = 1 + 2 * pe[k];
         h.d2[k] = sqrtf(1 + 2 * pd[k]);
-        if (var == V_MPI) h.pw[k] = std::pow((double)(1 + 2 * pd[k]), 0.5);
+        if (kchain) {
+            const double pw = std::pow((double)(1 + 2 * pd[k]), 0.5);
+            const size_t ix = k / h.nnz, iz = k % h.nnz;
+            h.kz[k] = (double)(h.az1[iz] * h.vp[k]) * pw * ddtz;
+            h.kx[k] = (double)(h.ax1[ix] * h.vp[k]) * pw * ddtx;
+        }
     }
     h.mu_v = pv[(size_t)(1 + npd) * h.nnz + 1 + npd] * sqrtf(1 + 2 * pe[(size_t)(1 + npd) * h.nnz + 1 + npd]);
     if (taper) {
@@ -76,12 +93,22 @@ static void build_shot_host(ShotHost &h, Variant var, int nx, int nz, int npd, f
         // (fs+(is-1)ds+npd, zs+npd), one cell right/down of it
         const int cx = (var == V_GPU) ? h.ixs + 1 : h.ixs, cz = (var == V_GPU) ? h.izs + 1 : h.izs;
         sv_taper_2d(var, h.nnx, h.nnz, npd, cx, cz, pe.data(), pd.data(), h.taper);
-        h.te2.assign(kTB * kTB, 1.0f); h.td2.assign(kTB * kTB, 1.0f); h.tpw.assign(kTB * kTB, 1.0);
+        h.te2.assign(kTB * kTB, 1.0f); h.td2.assign(kTB * kTB, 1.0f);
+        if (kchain) {
+            h.tkz.assign(kTB * kTB, 0.0);
+            h.tkx.assign(kTB * kTB, 0.0);
+        }
         for (int k = 0; k < kTB * kTB; k++) {
             const float ee = h.taper.e[k], dd = h.taper.d[k];
             h.te2[k] = 1 + 2 * ee;
             h.td2[k] = sqrtf(1 + 2 * dd);
-            h.tpw[k] = std::pow((double)(1 + 2 * dd), 0.5);
+            const int ix = h.taper.x0 + k / kTB, iz = h.taper.z0 + k % kTB;
+            if (kchain && ix >= 0 && ix < h.nnx && iz >= 0 && iz < h.nnz) {
+                const double pw = std::pow((double)(1 + 2 * dd), 0.5);
+                const float vpk = h.vp[(size_t)ix * h.nnz + iz];
+                h.tkz[k] = (double)(h.az1[iz] * vpk) * pw * ddtz;
+                h.tkx[k] = (double)(h.ax1[ix] * vpk) * pw * ddtx;
+            }
         }
     }
 }
@@ -95,9 +122,10 @@ static int upload_shot(ShotHost &h, Shot2D &S, int nfields, int nt, bool records
     GEO_CUDA(cudaMemcpyAsync(m, h.vp.data(), n * 4, cudaMemcpyHostToDevice, s));
     GEO_CUDA(cudaMemcpyAsync(m + n, h.e2.data(), n * 4, cudaMemcpyHostToDevice, s));
     GEO_CUDA(cudaMemcpyAsync(m + 2 * n, h.d2.data(), n * 4, cudaMemcpyHostToDevice, s));
-    if (!h.pw.empty()) {
-        GEO_TRY(h.d_pw.alloc(n * 8));
-        GEO_CUDA(cudaMemcpyAsync(h.d_pw.p, h.pw.data(), n * 8, cudaMemcpyHostToDevice, s));
+    if (!h.kz.empty()) {
+        GEO_TRY(h.d_k.alloc(2 * n * 8));
+        GEO_CUDA(cudaMemcpyAsync(h.d_k.p, h.kz.data(), n * 8, cudaMemcpyHostToDevice, s));
+        GEO_CUDA(cudaMemcpyAsync(h.d_k.as<double>() + n, h.kx.data(), n * 8, cudaMemcpyHostToDevice, s));
     }
     const size_t np = 4 * (size_t)h.nnx + 4 * (size_t)h.nnz;
     GEO_TRY(h.d_prof.alloc(np * 4));
@@ -115,15 +143,23 @@ static int upload_shot(ShotHost &h, Shot2D &S, int nfields, int nt, bool records
     S.dtx = dtx; S.dtz = dtz;
     S.cx1 = dp[0]; S.cx2 = dp[1]; S.ax1 = dp[2]; S.ax2 = dp[3];
     S.cz1 = dp[4]; S.cz2 = dp[5]; S.az1 = dp[6]; S.az2 = dp[7];
-    S.vp = m; S.e2 = m + n; S.d2 = m + 2 * n; S.pw = h.d_pw.as<double>();
+    S.vp = m; S.e2 = m + n; S.d2 = m + 2 * n;
+    S.kz = h.kz.empty() ? nullptr : h.d_k.as<double>();
+    S.kx = h.kz.empty() ? nullptr : h.d_k.as<double>() + n;
     if (!h.te2.empty()) {
         GEO_TRY(h.d_taper.alloc(2 * kTB * kTB * 4));
-        GEO_TRY(h.d_tpw.alloc(kTB * kTB * 8));
         GEO_CUDA(cudaMemcpyAsync(h.d_taper.p, h.te2.data(), kTB * kTB * 4, cudaMemcpyHostToDevice, s));
         GEO_CUDA(cudaMemcpyAsync(h.d_taper.as<float>() + kTB * kTB, h.td2.data(), kTB * kTB * 4, cudaMemcpyHostToDevice, s));
-        GEO_CUDA(cudaMemcpyAsync(h.d_tpw.p, h.tpw.data(), kTB * kTB * 8, cudaMemcpyHostToDevice, s));
+        if (!h.tkz.empty()) {
+            GEO_TRY(h.d_tk.alloc(2 * kTB * kTB * 8));
+            GEO_CUDA(cudaMemcpyAsync(h.d_tk.p, h.tkz.data(), kTB * kTB * 8, cudaMemcpyHostToDevice, s));
+            GEO_CUDA(cudaMemcpyAsync(h.d_tk.as<double>() + kTB * kTB, h.tkx.data(), kTB * kTB * 8,
+                                     cudaMemcpyHostToDevice, s));
+        }
         S.tx0 = h.taper.x0; S.tz0 = h.taper.z0;
-        S.te2 = h.d_taper.as<float>(); S.td2 = h.d_taper.as<float>() + kTB * kTB; S.tpw = h.d_tpw.as<double>();
+        S.te2 = h.d_taper.as<float>(); S.td2 = h.d_taper.as<float>() + kTB * kTB;
+        S.tkz = h.tkz.empty() ? nullptr : h.d_tk.as<double>();
+        S.tkx = h.tkz.empty() ? nullptr : h.d_tk.as<double>() + kTB * kTB;
     } else {
         S.tx0 = -100000; S.tz0 = -100000;
     }
@@ -495,7 +531,7 @@ extern "C" int geo_rtm2d_batch_adcig(const geo_rtm2d_desc *desc, const float *v,
         H[k].reset(new ShotHost());
         // shot position inside its window: fs = nxs/2+1, ds = 0
         build_shot_host(*H[k], V_MPI, nxs, nz, npd, D.dx, D.dz, dt, wv.data(), we.data(), wd.data(),
-                        (float)(nxs / 2 + 1), (float)D.zs, true);
+                        (float)(nxs / 2 + 1), (float)D.zs, true, fast != 0);
         GEO_TRY(upload_shot(*H[k], B.S[k], 2, nt, true, true, true, dt / D.dx, dt / D.dz, ss.cs));
         if (adcig) {
             GEO_TRY(H[k]->d_adcig.alloc((size_t)kAdcigAngles * nxs * nz * 4));

@@ -142,20 +142,30 @@ __device__ __forceinline__ void stress_point(const Shot2D &sh, int ix, int iz, c
     const int nnz = sh.nnz;
     const long id = (long)ix * nnz + iz;
     const float vp = __ldg(sh.vp + id);
-    // the MPI form's exact arithmetic carries pow(1+2del,0.5) in double;
-    // its fast form (FAST, a separate instantiation so that no double
-    // operation is issued) uses the FP32 sqrtf(1+2del) of the others
+    // the MPI form's exact arithmetic carries its pz and qx chains in double
+    // (their fixed factors kz, kx formed per shot on the host in the
+    // program's order); its fast form (FAST, a separate instantiation so
+    // that no double operation is issued) uses the FP32 sqrtf(1+2del) of
+    // the others
     constexpr bool dpw = VARIANT == V_MPI && !FAST;
     float e2 = __ldg(sh.e2 + id), d2 = 0.0f;
-    double pw = 0.0;
-    if (dpw) pw = __ldg(sh.pw + id);
-    else d2 = __ldg(sh.d2 + id);
+    double kz = 0.0, kx = 0.0;
+    if (dpw) {
+        kz = __ldg(sh.kz + id);
+        kx = __ldg(sh.kx + id);
+    } else {
+        d2 = __ldg(sh.d2 + id);
+    }
     if (st.taper) {
         const int bx = ix - sh.tx0, bz = iz - sh.tz0;
         if (bx >= 0 && bx < kTB && bz >= 0 && bz < kTB) {
             e2 = sh.te2[bx * kTB + bz];
-            if (dpw) pw = sh.tpw[bx * kTB + bz];
-            else d2 = sh.td2[bx * kTB + bz];
+            if (dpw) {
+                kz = sh.tkz[bx * kTB + bz];
+                kx = sh.tkx[bx * kTB + bz];
+            } else {
+                d2 = sh.td2[bx * kTB + bz];
+            }
         }
     }
     const float ax1 = sh.ax1[ix], ax2 = sh.ax2[ix], az1 = sh.az1[iz], az2 = sh.az2[iz];
@@ -179,8 +189,8 @@ __device__ __forceinline__ void stress_point(const Shot2D &sh, int ix, int iz, c
         if (VARIANT == V_MPI) {
             px = ax2 * px - ax1 * vp * e2 * sh.dtx * xx;
             if (dpw) {
-                pz = (float)((double)(az2 * pz) - (double)(az1 * vp) * pw * (double)sh.dtz * (double)zz);
-                qx = (float)((double)(ax2 * qx) - (double)(ax1 * vp) * pw * (double)sh.dtx * (double)xx);
+                pz = (float)((double)(az2 * pz) - kz * (double)zz);
+                qx = (float)((double)(ax2 * qx) - kx * (double)xx);
             } else {
                 pz = az2 * pz - az1 * vp * d2 * sh.dtz * zz;
                 qx = ax2 * qx - ax1 * vp * d2 * sh.dtx * xx;

@@ -144,10 +144,13 @@ struct Shot2D {
     float dtx, dtz;
     const float *cx1, *cx2, *cz1, *cz2, *ax1, *ax2, *az1, *az2;
     const float *vp, *e2, *d2;      // vp (or rho*vp^2), 1+2eps, sqrtf(1+2del)
-    const double *pw;               // pow(1+2del, 0.5) (MPI form)
-    int tx0, tz0;                   // taper box origin; te2/td2/tpw on kTB*kTB
+    // MPI form, exact arithmetic: the double factors of its pz and qx
+    // chains, ((double)(az1*vp)*pow(1+2del,0.5))*(double)dtz and the same
+    // with ax1, dtx, formed once per shot in the program's order
+    const double *kz, *kx;
+    int tx0, tz0;                   // taper box origin; te2/td2/tkz/tkx on kTB*kTB
     const float *te2, *td2;
-    const double *tpw;
+    const double *tkz, *tkx;
     int ixs, izs;                   // source cell (padded)
     float *u[2], *w[2], *P[2], *Q[2], *px[2], *pz[2], *qx[2], *qz[2];
     int rec_iz;                     // receiver row
@@ -187,6 +190,9 @@ int launch_stress2d(int variant, int phase, const Shot2D *d_shots, const int *d_
                     int by, int grid, Step2D st, cudaStream_t s);
 int launch_inject2d(const Shot2D *d_shots, int nshots, int maxline, int it, cudaStream_t s);
 int launch_mute_records(float *rec, int nx, int nt, const int *lo, const int *hi, cudaStream_t s);
+// cos and sin of n tilt angles in radians on the device, as the 2D TTI
+// programs form them (in place: th_cos holds the angles, then the cosines).
+int launch_tilt_trig(float *th_cos, float *sn, size_t n, cudaStream_t s);
 // Watchdog scan of the P fields (sides 0..nf-1) of ns shots (fd2d.cu).
 int launch_watch_shots(const Shot2D *d_shots, int ns, int nf, int *flag, int tag, cudaStream_t s);
 int launch_transpose_records(const float *tm, float *out, int ntr, int nt, cudaStream_t s);

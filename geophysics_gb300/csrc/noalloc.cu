@@ -275,8 +275,8 @@ extern "C" int geo_fd2d_shot_noalloc(const geo_fd2d_desc *desc, const float *v, 
     H.cx1 = prof; H.cx2 = prof + nnx; H.ax1 = prof + 2 * nnx; H.ax2 = prof + 3 * nnx;
     float *pz = prof + 4 * nnx;
     H.cz1 = pz; H.cz2 = pz + nnz; H.az1 = pz + 2 * nnz; H.az2 = pz + 3 * nnz;
-    H.vp = vp; H.e2 = e2; H.d2 = d2; H.pw = nullptr;
-    H.tx0 = tx0; H.tz0 = tz0; H.te2 = taper; H.td2 = taper + kTB * kTB; H.tpw = nullptr;
+    H.vp = vp; H.e2 = e2; H.d2 = d2; H.kz = nullptr; H.kx = nullptr;
+    H.tx0 = tx0; H.tz0 = tz0; H.te2 = taper; H.td2 = taper + kTB * kTB; H.tkz = nullptr; H.tkx = nullptr;
     H.ixs = ixs; H.izs = izs;
     H.u[0] = fields; H.w[0] = fields + n; H.P[0] = fields + 2 * n; H.Q[0] = fields + 3 * n;
     H.px[0] = fields + 4 * n; H.pz[0] = fields + 5 * n; H.qx[0] = fields + 6 * n; H.qz[0] = fields + 7 * n;
