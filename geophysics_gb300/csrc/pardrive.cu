@@ -22,9 +22,22 @@
 // Everything runs through the library's own entry points (geo_fd2d_shot,
 // the 3D plan, geo_rtm2d_batch_adcig, geo_adcig_smooth_stack); this file
 // only reads parameters and files and writes results.
+//
+// Resume by shot (geo_fd2d, geo_fd3d; key resume= 1).  The reference writes
+// every shot's record at its own offset of the shot file
+// (GPU_vti2dfd_kernels.cu:441, GPU_vti3dfd_kernels.cu:560), so a run can be
+// continued shot by shot.  With resume on, the shot file is updated in place
+// and a manifest (key FNdone, default <FNshot>.done) gets one line per shot
+// once that shot's record (and, for shot 1, its snapshots) is on disk
+// (fflush + fsync before the line is written).  A rerun with the same par
+// file skips the shots the manifest lists -- their records are read back
+// from the shot file when a device buffer is given -- and runs the rest.
+// The manifest's first line holds the run's parameters; a manifest from a
+// different run is refused (GEO_ERR_ARG).
 #include "geo_internal.h"
 #include <cstring>
 #include <memory>
+#include <unistd.h>
 #include <string>
 #include <vector>
 
@@ -87,6 +100,71 @@ using File = std::unique_ptr<FILE, FileCloser>;
 static int open_out(const std::string &fn, File &f) {
     f.reset(fopen(fn.c_str(), "wb"));
     if (!f) return fail(GEO_ERR_IO, "cannot create <%s>", fn.c_str());
+    return GEO_OK;
+}
+
+// Open for update in place (resume), creating the file when absent.
+static int open_update(const std::string &fn, File &f) {
+    f.reset(fopen(fn.c_str(), "r+b"));
+    if (!f) f.reset(fopen(fn.c_str(), "w+b"));
+    if (!f) return fail(GEO_ERR_IO, "cannot open <%s> for update", fn.c_str());
+    return GEO_OK;
+}
+
+static int flush_to_disk(FILE *f, const char *what) {
+    if (fflush(f) != 0 || fsync(fileno(f)) != 0) return fail(GEO_ERR_IO, "cannot flush %s", what);
+    return GEO_OK;
+}
+
+// Manifest of completed shots: header line = the run's parameters, then one
+// "shot <is>" line per completed shot.
+struct Manifest {
+    std::string path, header;
+    std::vector<char> done;        // by shot index (0-based)
+    File f;
+    int open(const std::string &p, const std::string &hdr, int ns) {
+        path = p;
+        header = hdr;
+        done.assign(ns, 0);
+        FILE *r = fopen(p.c_str(), "r");
+        if (r) {
+            char line[4096];
+            bool first = true, ok = true;
+            while (fgets(line, sizeof line, r)) {
+                std::string l(line);
+                while (!l.empty() && (l.back() == '\n' || l.back() == '\r')) l.pop_back();
+                if (first) {
+                    ok = l == hdr;
+                    first = false;
+                    continue;
+                }
+                int k = -1;
+                if (sscanf(l.c_str(), "shot %d", &k) == 1 && k >= 0 && k < ns) done[k] = 1;
+            }
+            fclose(r);
+            if (!first && !ok) return fail(GEO_ERR_ARG, "manifest <%s> belongs to another run", p.c_str());
+            if (first) r = nullptr;   // empty file: start over
+        }
+        f.reset(fopen(p.c_str(), r ? "a" : "w"));
+        if (!f) return fail(GEO_ERR_IO, "cannot write manifest <%s>", p.c_str());
+        if (!r) {
+            fprintf(f.get(), "%s\n", hdr.c_str());
+            GEO_TRY(flush_to_disk(f.get(), "manifest"));
+        }
+        return GEO_OK;
+    }
+    int mark(int k) {
+        fprintf(f.get(), "shot %d\n", k);
+        GEO_TRY(flush_to_disk(f.get(), "manifest"));
+        done[k] = 1;
+        return GEO_OK;
+    }
+};
+
+// Read n floats at a byte offset (a completed shot's record on resume).
+static int read_at(FILE *fp, size_t offset_bytes, float *a, size_t n) {
+    if (fseeko(fp, (off_t)offset_bytes, SEEK_SET) != 0 || fread(a, 4, n, fp) != n)
+        return fail(GEO_ERR_IO, "short read of a completed shot's record");
     return GEO_OK;
 }
 
@@ -158,9 +236,23 @@ extern "C" int geo_fd2d(const geo_par *par, int device, float *d_shots, void *st
     const size_t n0 = (size_t)D.nx * D.nz, nrec = (size_t)D.nx * D.nt;
     const size_t nsnap = snap_every > 0 ? (size_t)((D.nt - 1) / snap_every + 1) * (D.nx + 2 * D.npd) * (D.nz + 2 * D.npd)
                                         : 0;
+    const int resume = opt_i(par, "resume", 0);
+    if (resume && fshot.empty()) return fail(GEO_ERR_ARG, "par: resume needs FNshot");
     File fs_, fsn;
-    if (!fshot.empty()) GEO_TRY(open_out(fshot, fs_));
-    if (!fsnap.empty()) GEO_TRY(open_out(fsnap, fsn));
+    Manifest man;
+    if (resume) {
+        char hdr[512];
+        snprintf(hdr, sizeof hdr, "geo_fd2d nx=%d nz=%d npd=%d nt=%d ns=%d variant=%d dx=%g dz=%g dt=%g favg=%g "
+                 "fs=%g ds=%g zs=%g SV=%d", D.nx, D.nz, D.npd, D.nt, ns, D.variant, D.dx, D.dz, D.dt, D.favg, D.fs,
+                 D.ds, D.zs, D.sv);
+        std::string dn = opt_s(par, "FNdone");
+        GEO_TRY(man.open(dn.empty() ? fshot + ".done" : dn, hdr, ns));
+        GEO_TRY(open_update(fshot, fs_));
+        if (!fsnap.empty()) GEO_TRY(open_update(fsnap, fsn));
+    } else {
+        if (!fshot.empty()) GEO_TRY(open_out(fshot, fs_));
+        if (!fsnap.empty()) GEO_TRY(open_out(fsnap, fsn));
+    }
     std::vector<float> rec(fshot.empty() ? 0 : nrec), snap(fsnap.empty() ? 0 : nsnap);
     DevBuf dm;
     if (d_shots) {   // the model on the device, as geo_fd2d_shot takes one memory kind
@@ -170,6 +262,15 @@ extern "C" int geo_fd2d(const geo_par *par, int device, float *d_shots, void *st
     }
     for (int is = 1; is <= ns; is++) {
         D.is = is;
+        if (resume && man.done[is - 1]) {
+            if (d_shots) {
+                GEO_TRY(read_at(fs_.get(), (size_t)(is - 1) * nrec * 4, rec.data(), nrec));
+                GEO_CUDA(cudaMemcpyAsync(d_shots + (size_t)(is - 1) * nrec, rec.data(), nrec * 4,
+                                         cudaMemcpyHostToDevice, s));
+                GEO_CUDA(cudaStreamSynchronize(s));
+            }
+            continue;
+        }
         const bool want_snap = is == 1 && !fsnap.empty() && snap_every > 0;
         if (d_shots) {
             float *out = d_shots + (size_t)(is - 1) * nrec;
@@ -190,6 +291,11 @@ extern "C" int geo_fd2d(const geo_par *par, int device, float *d_shots, void *st
         }
         if (fs_) GEO_TRY(write_at(fs_.get(), (size_t)(is - 1) * nrec * 4, rec.data(), nrec));
         if (want_snap) GEO_TRY(write_at(fsn.get(), 0, snap.data(), snap.size()));
+        if (resume) {
+            if (want_snap) GEO_TRY(flush_to_disk(fsn.get(), "snapshot file"));
+            GEO_TRY(flush_to_disk(fs_.get(), "shot file"));
+            GEO_TRY(man.mark(is - 1));
+        }
     }
     if (d_shots) GEO_CUDA(cudaStreamSynchronize(s));
     return GEO_OK;
@@ -257,11 +363,34 @@ extern "C" int geo_fd3d(const geo_par *par, int device, float *d_shots, void *st
         GEO_TRY(geo_fd3d_set_tilt(plan, th.data(), ph.data(), GEO_MEM_HOST, stream));
     }
     const size_t nrec = (size_t)D.nt * D.nrx * D.nry;
+    const int resume = opt_i(par, "resume", 0);
+    if (resume && fshot.empty()) return fail(GEO_ERR_ARG, "par: resume needs FNshot");
     File f;
-    if (!fshot.empty()) GEO_TRY(open_out(fshot, f));
+    Manifest man;
+    if (resume) {
+        char hdr[512];
+        snprintf(hdr, sizeof hdr, "geo_fd3d nx=%d ny=%d nz=%d npml=%d nt=%d ns=%d mode=%d dx=%g dy=%g dz=%g dt=%g "
+                 "favg=%g fsx=%d fsy=%d fsz=%d dsx=%d dsy=%d dsz=%d SV=%d rec=%d,%d,%d,%d,%d,%d,%d tilt=%d",
+                 D.nx, D.ny, D.nz, D.npd, D.nt, ns, D.mode, D.dx, D.dy, D.dz, D.dt, D.favg, D.fsx, D.fsy, D.fsz,
+                 D.dsx, D.dsy, D.dsz, D.sv, D.rec_iz, D.rx0, D.drx, D.nrx, D.ry0, D.dry, D.nry, fth.empty() ? 0 : 1);
+        std::string dn = opt_s(par, "FNdone");
+        GEO_TRY(man.open(dn.empty() ? fshot + ".done" : dn, hdr, ns));
+        GEO_TRY(open_update(fshot, f));
+    } else if (!fshot.empty()) {
+        GEO_TRY(open_out(fshot, f));
+    }
     std::vector<float> rec(f ? nrec : 0);
     cudaStream_t s = (cudaStream_t)stream;
     for (int is = 0; is < ns; is++) {   // 0-based shots, as the 3D program counts them
+        if (resume && man.done[is]) {
+            if (d_shots) {
+                GEO_TRY(read_at(f.get(), (size_t)is * nrec * 4, rec.data(), nrec));
+                GEO_CUDA(cudaMemcpyAsync(d_shots + (size_t)is * nrec, rec.data(), nrec * 4, cudaMemcpyHostToDevice,
+                                         s));
+                GEO_CUDA(cudaStreamSynchronize(s));
+            }
+            continue;
+        }
         if (d_shots) {
             float *out = d_shots + (size_t)is * nrec;
             GEO_TRY(geo_fd3d_run_shot(plan, is, out, GEO_MEM_DEVICE, stream));
@@ -273,6 +402,10 @@ extern "C" int geo_fd3d(const geo_par *par, int device, float *d_shots, void *st
             GEO_TRY(geo_fd3d_run_shot(plan, is, rec.data(), GEO_MEM_HOST, stream));
         }
         if (f) GEO_TRY(write_at(f.get(), (size_t)is * nrec * 4, rec.data(), nrec));
+        if (resume) {
+            GEO_TRY(flush_to_disk(f.get(), "shot file"));
+            GEO_TRY(man.mark(is));
+        }
     }
     GEO_CUDA(cudaStreamSynchronize(s));
     return GEO_OK;

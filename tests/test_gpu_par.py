@@ -126,3 +126,65 @@ def test_par_device_out_of_range(geo, tmp_path):
               FNshot=str(tmp_path / "shot"))
     with pytest.raises(geo.GeoError):
         geo.fd2d_par(_par(tmp_path, "fd.par", **kw), device=4096)
+
+
+def _resume_case(geo, tmp_path, run, nrec, ns, shot_file, done_file):
+    """Run to completion, then make the state of a run stopped after shot 0:
+    the manifest lists shot 0 only, the later records are overwritten with
+    junk, and shot 0's record is overwritten with a marker.  A rerun must
+    leave the marker (shot 0 is not recomputed) and restore the rest bit for
+    bit."""
+    run()
+    full = np.fromfile(shot_file, np.float32).copy()
+    lines = open(done_file).read().splitlines()
+    assert lines[0].startswith("geo_fd") and lines[1:] == ["shot %d" % k for k in range(ns)]
+    # a second run with everything done recomputes nothing
+    run()
+    assert np.array_equal(np.fromfile(shot_file, np.float32), full)
+    # stopped after the first shot
+    open(done_file, "w").write("\n".join(lines[:2]) + "\n")
+    junk = full.copy()
+    junk[:nrec] = 7.0
+    junk[nrec:] = np.nan
+    junk.tofile(shot_file)
+    run()
+    got = np.fromfile(shot_file, np.float32)
+    assert np.all(got[:nrec] == 7.0)
+    assert np.array_equal(got[nrec:], full[nrec:])
+    assert open(done_file).read().splitlines()[1:] == ["shot %d" % k for k in range(ns)]
+    return full
+
+
+def test_fd2d_par_resume(geo, tmp_path):
+    v, e, d = layered_model(61, 51, seed=2)
+    kw = dict(nx=61, nz=51, dx=10, dz=10, npd=20, nt=200, dt=1000, favg=20, ns=3, fs=20, ds=10, zs=3,
+              FNv=_write(tmp_path, "v", v), FNe=_write(tmp_path, "e", e), FNd=_write(tmp_path, "d", d),
+              FNshot=str(tmp_path / "shot"), resume=1)
+    par = _par(tmp_path, "fd.par", **kw)
+    full = _resume_case(geo, tmp_path, lambda: geo.fd2d_par(par), 61 * 200, 3, tmp_path / "shot",
+                        tmp_path / "shot.done")
+    # the same as a run without resume
+    kw.pop("resume")
+    kw["FNshot"] = str(tmp_path / "plain")
+    geo.fd2d_par(_par(tmp_path, "plain.par", **kw))
+    assert np.array_equal(np.fromfile(tmp_path / "plain", np.float32), full)
+    # a manifest from another run is refused
+    kw.update(FNshot=str(tmp_path / "shot"), resume=1, nt=150)
+    with pytest.raises(geo.GeoError) as ei:
+        geo.fd2d_par(_par(tmp_path, "other.par", **kw))
+    assert ei.value.status == 1 and "another run" in str(ei.value)
+
+
+def test_fd3d_par_resume(geo, tmp_path):
+    v, e, d = random_model_3d(20, 18, 22, seed=5)
+    kw = dict(nx=20, ny=18, nz=22, dx=10, dy=10, dz=10, npml=10, nt=120, dt=1000, favg=25, ns=3, fsx=6, fsy=8,
+              fsz=2, dsx=4, mute_tt=5, FNv=_write(tmp_path, "v", v), FNe=_write(tmp_path, "e", e),
+              FNd=_write(tmp_path, "d", d), FNshot=str(tmp_path / "shot"), FNdone=str(tmp_path / "m.txt"),
+              resume=1)
+    par = _par(tmp_path, "fd3.par", **kw)
+    nrec = 18 * 20 * 120
+    full = _resume_case(geo, tmp_path, lambda: geo.fd3d_par(par), nrec, 3, tmp_path / "shot", tmp_path / "m.txt")
+    # with a device buffer the completed shots come back from the file
+    out = geo.fd3d_par(par, out_shape=(3, 18, 20, 120)).cpu().numpy().reshape(-1)
+    assert np.array_equal(out, np.fromfile(tmp_path / "shot", np.float32))
+    assert np.array_equal(out[nrec:], full[nrec:])
