@@ -44,7 +44,7 @@ class FD3DDesc(C.Structure):
 class RTM3DDesc(C.Structure):
     _fields_ = [("fd", FD3DDesc), ("ns", C.c_int), ("mute_tt", C.c_int), ("method", C.c_int),
                 ("snap_every", C.c_int), ("ae", C.c_void_p), ("na", C.c_int), ("da", C.c_int), ("dcdp", C.c_int),
-                ("theta", C.c_void_p), ("phi", C.c_void_p), ("ckpt_every", C.c_int)]
+                ("theta", C.c_void_p), ("phi", C.c_void_p), ("ckpt_every", C.c_int), ("rec_grid", C.c_int)]
 
 
 class RTM2DGpuDesc(C.Structure):

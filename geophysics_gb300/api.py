@@ -218,7 +218,7 @@ _RTM = {"boundary": GEO_RTM_BOUNDARY, "snapshot": GEO_RTM_SNAPSHOT, "learned": G
 
 def rtm3d(v, e, d, *, npd, nt, dx, dy, dz, dt, favg, fsx, fsy, fsz, ns=1, dsx=0, dsy=0, dsz=0, mute_tt=70,
           pfac=10.0, wtype=1, sv=0, mode="fast", laplace=True, illum=False, method="boundary", snap_every=4,
-          codec=None, adcig=None, theta=None, phi=None, ckpt_every=0):
+          codec=None, adcig=None, theta=None, phi=None, ckpt_every=0, receivers=None):
     """3D RTM over shots 0..ns-1; v,e,d shaped (ny, nx, nz); theta, phi
     (degrees, same shape): the 3D TTI medium (mode "fast", no gathers).
 
@@ -230,6 +230,9 @@ def rtm3d(v, e, d, *, npd, nt, dx, dy, dz, dt, favg, fsx, fsy, fsz, ns=1, dsx=0,
     snapshots); same image as "snapshot" in bounded memory.
     adcig = (na, da, dcdp) (boundary method): also the Poynting angle
     gathers, shaped (ny//dcdp, nx//dcdp, na, nz), illumination-divided.
+    receivers = (rx0, drx, nrx, ry0, dry, nry): only that surface grid
+    records and takes the record back (default: every surface node, the
+    program's receivers).
     Returns the illumination-divided image, then the Laplacian-filtered image
     if `laplace`, then the illumination if `illum`, then the gathers."""
     b = _Bufs(v, e, d, theta, phi)
@@ -238,10 +241,12 @@ def rtm3d(v, e, d, *, npd, nt, dx, dy, dz, dt, favg, fsx, fsy, fsz, ns=1, dsx=0,
                   wtype=wtype, sv=sv, mode=_MODES[mode] if isinstance(mode, str) else int(mode),
                   fsx=fsx, fsy=fsy, fsz=fsz, dsx=dsx, dsy=dsy, dsz=dsz, rec_iz=npd, rx0=0, drx=1, nrx=nx,
                   ry0=0, dry=1, nry=ny, mute_tt=0)
+    if receivers is not None:
+        fd.rx0, fd.drx, fd.nrx, fd.ry0, fd.dry, fd.nry = (int(x) for x in receivers)
     na, da, dcdp = adcig if adcig is not None else (0, 0, 0)
     desc = RTM3DDesc(fd=fd, ns=ns, mute_tt=mute_tt, method=_RTM[method] if isinstance(method, str) else int(method),
                      snap_every=snap_every, ae=codec._p if codec is not None else None, na=na, da=da, dcdp=dcdp,
-                     ckpt_every=ckpt_every)
+                     ckpt_every=ckpt_every, rec_grid=1 if receivers is not None else 0)
     pv, pe, pd = b.inp(v), b.inp(e), b.inp(d)
     if theta is not None:
         desc.theta, desc.phi = b.inp(theta), b.inp(phi)

@@ -67,11 +67,14 @@ __global__ void k_ring3d(Grid3D g, float *P, float *Q, float *bp, float *bq, lon
 
 // Receiver injection before a backward step: the muted record into P and Q
 // of the receiver field at z = npml-1 (shot_record, flag false, :319-334).
-__global__ void k_inject3d(Grid3D g, float *P, float *Q, const float *rec_tm, int it) {
-    const int nx = g.nx, ny = g.ny, npd = g.npd;
-    const long n = (long)nx * ny;
+// Receivers (rx0 + jx*drx, ry0 + jy*dry), jx < nrx, jy < nry, take the
+// time-major record back at depth npml-1.
+__global__ void k_inject3d(Grid3D g, float *P, float *Q, const float *rec_tm, int it, int rx0, int drx, int nrx,
+                           int ry0, int dry, int nry) {
+    const int npd = g.npd;
+    const long n = (long)nrx * nry;
     for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < n; k += (long)gridDim.x * blockDim.x) {
-        const int ix = (int)(k % nx), iy = (int)(k / nx);
+        const int ix = rx0 + (int)(k % nrx) * drx, iy = ry0 + (int)(k / nrx) * dry;
         const long id = (npd - 1) + (long)g.ldz * (npd + ix) + g.sxy * (npd + iy);
         const float r = rec_tm[(long)it * n + k];
         P[id] = r;
@@ -862,8 +865,12 @@ extern "C" int geo_rtm3d_adcig(const geo_rtm3d_desc *desc, const float *v, const
         if (dcdp > R.fd.nx || dcdp > R.fd.ny) return fail(GEO_ERR_ARG, "dcdp exceeds the model");
     }
     geo_fd3d_desc D = R.fd;
-    // every surface node records P+Q at z = npml (shot_record :319-334)
-    D.rec_iz = D.npd; D.rx0 = 0; D.drx = 1; D.nrx = D.nx; D.ry0 = 0; D.dry = 1; D.nry = D.ny;
+    // every surface node records P+Q at z = npml (shot_record :319-334), or
+    // the caller's receiver grid (checked with the plan)
+    D.rec_iz = D.npd;
+    if (!R.rec_grid) {
+        D.rx0 = 0; D.drx = 1; D.nrx = D.nx; D.ry0 = 0; D.dry = 1; D.nry = D.ny;
+    }
     D.mute_tt = 0;
     cudaStream_t s = (cudaStream_t)stream;
     geo_fd3d_plan *p = nullptr;
@@ -926,7 +933,7 @@ extern "C" int geo_rtm3d_adcig(const geo_rtm3d_desc *desc, const float *v, const
         GEO_CUDA(cudaStreamSynchronize(s));
     }
     float *bp = ring.as<float>(), *bq = bp + (size_t)D.nt * L;
-    const int ntr = D.nx * D.ny;
+    const int ntr = D.nrx * D.nry;
     auto launch_ring = [&](int it, int save) -> int {
         Grid3D g = grid_of(p, 0);
         k_ring3d<<<grid_blocks(L), 256, 0, s>>>(g, g.P, g.Q, bp, bq, L, it, save);
@@ -956,7 +963,8 @@ extern "C" int geo_rtm3d_adcig(const geo_rtm3d_desc *desc, const float *v, const
         if (method == GEO_RTM_LEARNED) GEO_TRY(nesc.zero(s));
         // forward: record P+Q, source illumination, keep the ring or the snapshots
         st.rec = p->rec_tm.as<float>();
-        st.rec_iz = D.rec_iz; st.rx0 = 0; st.drx = 1; st.nrx = D.nx; st.ry0 = 0; st.dry = 1; st.nry = D.ny;
+        st.rec_iz = D.rec_iz; st.rx0 = D.rx0; st.drx = D.drx; st.nrx = D.nrx; st.ry0 = D.ry0; st.dry = D.dry;
+        st.nry = D.nry;
         st.rec_pq = 1;
         st.ill = ill.as<float>();
         GEO_TRY(p->wd.open());
@@ -992,9 +1000,16 @@ extern "C" int geo_rtm3d_adcig(const geo_rtm3d_desc *desc, const float *v, const
         GEO_TRY(p->wd.verdict(s, "3D RTM forward pass"));
         // direct-wave mute, window form (mute_directwave :352-390)
         if (R.mute_tt > 0) {
-            std::vector<int> lo, hi;
+            std::vector<int> flo, fhi, lo(ntr), hi(ntr);
             mute_window_3d_band(D.nx, D.ny, D.nt, D.dt, D.favg, D.dx, D.dy, D.dz, D.fsx, D.fsy, D.dsx, D.dsy, D.fsz,
-                                is, p->vp1, p->eps1, R.mute_tt, lo, hi);
+                                is, p->vp1, p->eps1, R.mute_tt, flo, fhi);
+            // the window of each receiver of the grid, by its model cell
+            for (int jy = 0; jy < D.nry; jy++)
+                for (int jx = 0; jx < D.nrx; jx++) {
+                    const size_t c = (size_t)(D.ry0 + jy * D.dry) * D.nx + (D.rx0 + jx * D.drx);
+                    lo[(size_t)jy * D.nrx + jx] = flo[c];
+                    hi[(size_t)jy * D.nrx + jx] = fhi[c];
+                }
             GEO_CUDA(cudaMemcpyAsync(p->mute_lo.p, lo.data(), lo.size() * 4, cudaMemcpyHostToDevice, s));
             GEO_CUDA(cudaMemcpyAsync(p->mute_hi.p, hi.data(), hi.size() * 4, cudaMemcpyHostToDevice, s));
             GEO_TRY(launch_mute_records(p->rec_tm.as<float>(), ntr, D.nt, p->mute_lo.as<int>(), p->mute_hi.as<int>(), s));
@@ -1034,7 +1049,8 @@ extern "C" int geo_rtm3d_adcig(const geo_rtm3d_desc *desc, const float *v, const
             }
             {
                 Grid3D gg = grid_of(p, 1);
-                k_inject3d<<<grid_blocks(ntr), 256, 0, s>>>(gg, gg.P, gg.Q, p->rec_tm.as<float>(), it);
+                k_inject3d<<<grid_blocks(ntr), 256, 0, s>>>(gg, gg.P, gg.Q, p->rec_tm.as<float>(), it, D.rx0, D.drx,
+                                                             D.nrx, D.ry0, D.dry, D.nry);
                 GEO_TRY(check_launch("inject3d"));
             }
             if (method == GEO_RTM_BOUNDARY) gb.other_P = grid_of(p, 0).P;  // the source side's new level

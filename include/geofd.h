@@ -223,6 +223,12 @@ typedef struct geo_rtm3d_desc {
     int   ckpt_every;        /* checkpoint interval in steps (method 3; a
                                 multiple of snap_every; 0 = the interval that
                                 minimises states plus segment snapshots)      */
+    int   rec_grid;          /* 0: every surface node records P+Q at z = npml
+                                and takes the record back at npml-1 (the
+                                program's receivers, shot_record :319-334);
+                                1: only the nodes of fd's grid rx0+k*drx
+                                (k < nrx), ry0+j*dry (j < nry) do (an
+                                addition: decimated receiver grids)          */
 } geo_rtm3d_desc;
 
 /* v,e,d: nx*ny*nz.  mig: nx*ny*nz image divided by the illumination where

@@ -80,3 +80,27 @@ def test_rtm3d_adcig_needs_boundary_method(geo):
     v, e, d = random_model_3d(16, 16, 16, seed=15)
     with pytest.raises(GeoError):
         geo.rtm3d(v, e, d, method="snapshot", snap_every=2, adcig=(65, 1, 1), **dict(KW, ns=1, nt=40))
+
+
+@pytest.mark.parametrize("method", ["boundary", "snapshot", "checkpoint"])
+def test_rtm3d_receiver_grid(geo, orc, method):
+    """A decimated surface grid (every 2nd node from x 1, y 0) records and
+    takes the record back instead of every node; image and illumination
+    equal the oracle's run with the same grid, on VTI and (checkpoint) TTI."""
+    from tests.util import smooth_angles
+    v, e, d = random_model_3d(20, 17, 23, seed=13)
+    grid = (1, 2, 9, 0, 2, 9)
+    kw = dict(KW, receivers=grid)
+    snap = 0 if method == "boundary" else 4
+    mig_o, ill_o, rec_o = orc.rtm3d(v, e, d, mode=1, snap_every=snap, **kw)
+    mig, ill = geo.rtm3d(v, e, d, mode="fast", method=method, snap_every=4, laplace=False, illum=True, **kw)
+    assert rec_o.shape == (9, 9, KW["nt"]) and np.abs(mig_o).max() > 0
+    assert np.array_equal(ill, ill_o), rel_l2(ill, ill_o)
+    assert np.array_equal(mig, mig_o), rel_l2(mig, mig_o)
+    full = geo.rtm3d(v, e, d, mode="fast", method=method, snap_every=4, laplace=False, **KW)
+    assert not np.array_equal(full, mig)
+    if method == "checkpoint":
+        th, ph = smooth_angles(v.shape, seed=3)
+        mig_o, _, _ = orc.rtm3d(v, e, d, snap_every=4, theta=th, phi=ph, **kw)
+        mig = geo.rtm3d(v, e, d, mode="fast", method=method, snap_every=4, laplace=False, theta=th, phi=ph, **kw)
+        assert np.array_equal(mig, mig_o), rel_l2(mig, mig_o)
