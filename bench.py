@@ -39,6 +39,13 @@ CFG = {"workload": "3D VTI FD shot 400^3 (+40 sponge), 2500 steps, dt=0.8 ms, 10
        "stress_form": "fast (unsplit interior)", "l2": "inputs larger than L2 (no flush)"}
 
 
+# DRAM bytes (read + write) of one launch of the fused step at 400^3 + 40,
+# from ncu on the 200^3 + 20 case (same sponge fraction, 240^3 padded, a
+# few GB on the device) scaled by the updated points (472/232)^3; command and
+# figures in profiles/fd3d_fused_200cube_traffic.md.
+TRAFFIC_BYTES_PER_STEP = 8665488602
+
+
 def updates_per_step():
     return (NX + 2 * NPD - 8) * (NY + 2 * NPD - 8) * (NZ + 2 * NPD - 8)
 
@@ -230,12 +237,7 @@ def run_ours(args, rank, world):
     step_ms = plan.time_steps(nsteps, stream=torch.cuda.current_stream().cuda_stream) / nsteps
     peak, peak_kind = measured_peak()
     achieved = algorithmic_bytes_per_step() / (step_ms / 1000) / 1e9
-    traffic = None
-    tf = os.path.join(ROOT, "profiles", "fd3d_fused_400cube_traffic.md")
-    if os.path.exists(tf):
-        for line in open(tf):
-            if line.startswith("bytes_per_step:"):
-                traffic = int(line.split(":")[1])
+    traffic = TRAFFIC_BYTES_PER_STEP
 
     # end to end through the C ABI with host buffers: the model from pinned
     # host memory, the record read back into pinned host memory
@@ -290,11 +292,14 @@ def run_ours(args, rank, world):
             "cpu_baseline": cpu,
             "exact_form": {"step_ms": exact_ms, "value": updates_per_step() / (exact_ms / 1000) / 1e9,
                            "unit": "Gpt/s",
-                           # split stresses everywhere: 84 algorithmic bytes at every updated point
-                           "roofline_frac": updates_per_step() * 84 / (exact_ms / 1000) / 1e9 / peak,
-                           "note": "bare steps of the reference-arithmetic form (84 B per update: split "
-                           "stresses everywhere); the headline fast form's record is 1.08e-5 rel-L2 from it "
-                           "after 2500 steps"}}
+                           # the same algorithmic bytes as the headline (52 B interior,
+                           # 84 B sponge): what the step must move, not what this form moves
+                           "roofline_frac": algorithmic_bytes_per_step() / (exact_ms / 1000) / 1e9 / peak,
+                           "note": "bare steps of the reference-arithmetic form, bit-identical to the reference "
+                           "program built without FMA contraction; it keeps the split stresses everywhere "
+                           "(84 B moved per update); the headline fast form's record is 1.08e-5 rel-L2 from it "
+                           "after 2500 steps, and the reference program's own default and no-FMA builds are "
+                           "2.25e-5 apart on this shot"}}
     print(json.dumps(line), flush=True)
 
 
@@ -403,9 +408,9 @@ def run_rtm_learned_case(args):
     """3D VTI RTM, one shot, 512x512x384 at 10 m (+40 sponge), dt 0.8 ms,
     15 Hz: the plain recomputes (the program's boundary re-propagation and
     the exact checkpoint recompute) against snapshots every 4 steps through
-    the learned codec (shots/hour), and the codec's image error against
-    stored fp32 snapshots (on the first err_nt steps: all 3000 steps of fp32
-    snapshots would need 302 GB; the checkpoint image equals them)."""
+    the learned codec (shots/hour), and the codec's image error over the
+    whole run against the exact checkpoint recompute's image (bit for bit
+    the image of stored fp32 snapshots, which would need 302 GB here)."""
     import numpy as np
     import torch
 
@@ -426,21 +431,14 @@ def run_rtm_learned_case(args):
         return out, time.perf_counter() - t0
 
     res = {}
-    _, res["boundary"] = timed(nt=args.nt, method="boundary")
-    _, res["checkpoint"] = timed(nt=args.nt, method="checkpoint", snap_every=4)
+    bnd, res["boundary"] = timed(nt=args.nt, method="boundary")
+    ref, res["checkpoint"] = timed(nt=args.nt, method="checkpoint", snap_every=4)
     codec.set_escape(0.02, 0.0)
-    _, res["learned16"] = timed(nt=args.nt, method="learned", snap_every=4, codec=codec)
+    l16, res["learned16"] = timed(nt=args.nt, method="learned", snap_every=4, codec=codec)
     codec.set_escape(0.02, args.escape)
     b0, e0 = codec.stats()
-    _, res["learned_esc"] = timed(nt=args.nt, method="learned", snap_every=4, codec=codec)
+    les, res["learned_esc"] = timed(nt=args.nt, method="learned", snap_every=4, codec=codec)
     b1, e1 = codec.stats()
-    # image error on err_nt steps
-    ref, _ = timed(nt=args.err_nt, method="snapshot", snap_every=4)
-    codec.set_escape(0.02, 0.0)
-    l16, _ = timed(nt=args.err_nt, method="learned", snap_every=4, codec=codec)
-    codec.set_escape(0.02, args.escape)
-    les, _ = timed(nt=args.err_nt, method="learned", snap_every=4, codec=codec)
-    bnd, _ = timed(nt=args.err_nt, method="boundary")
 
     def rel(a, b):
         a, b = a[0].double(), b[0].double()
@@ -457,9 +455,10 @@ def run_rtm_learned_case(args):
                                     "learned_esc": res["boundary"] / res["learned_esc"]},
             "speedup_vs_checkpoint": {"learned16": res["checkpoint"] / res["learned16"],
                                       "learned_esc": res["checkpoint"] / res["learned_esc"]},
-            "image_rel_l2_vs_fp32_snapshots": {"learned16": rel(l16, ref), "learned_esc": rel(les, ref),
-                                               "boundary": rel(bnd, ref), "err_nt": args.err_nt,
-                                               "image": "Laplacian-filtered, illumination-divided"},
+            "image_rel_l2_vs_plain": {"learned16": rel(l16, ref), "learned_esc": rel(les, ref),
+                                      "boundary": rel(bnd, ref), "steps": args.nt,
+                                      "plain": "checkpoint recompute (= stored fp32 snapshots bit for bit)",
+                                      "image": "Laplacian-filtered, illumination-divided"},
             "compression": {"learned16": 16384 / per_block(0.0),
                             "learned_esc": 16384 / per_block(esc_frac), "escaped_block_frac": esc_frac,
                             "escape_budget": args.escape},
@@ -521,8 +520,9 @@ def run_tti_case(args):
 
 def run_tti_rtm_case(args):
     """3D TTI RTM on the 600x600x400 (+40 sponge) medium at 12.5 m, 3500
-    steps, 12 Hz, every surface node recorded (the 3D RTM program's
-    receivers; the 300x300 2-node grid is a subset): plain checkpoint
+    steps, 12 Hz, a 300x300 receiver grid at 2-node spacing recording and
+    taking the record back (--all-nodes: every surface node, the 3D RTM
+    program's receivers): plain checkpoint
     recompute (full wavefield every K steps, segments re-propagated; the
     stored-snapshot image bit for bit) against snapshots every 4 steps
     through the learned codec trained on TTI snapshots from the solver.
@@ -540,7 +540,8 @@ def run_tti_rtm_case(args):
     codec, tinfo = train_codec(geo, args.train_iters, tti=True)
     rk = dict(npd=NPD, dx=TTI_DX, dy=TTI_DX, dz=TTI_DX, dt=TTI_DT, favg=TTI_FAVG, fsx=nx // 2 - 100, fsy=ny // 2,
               dsx=200 // max(1, args.shots - 1) if args.shots > 1 else 0, fsz=1, mute_tt=70, laplace=True,
-              mode="fast", theta=th, phi=ph, nt=args.nt, ns=args.shots, snap_every=4)
+              mode="fast", theta=th, phi=ph, nt=args.nt, ns=args.shots, snap_every=4,
+              receivers=None if args.all_nodes else (0, 2, nx // 2, 0, 2, ny // 2))
 
     def timed(**kw):
         torch.cuda.synchronize()
@@ -566,6 +567,8 @@ def run_tti_rtm_case(args):
     print(json.dumps({"case": "tti-rtm", "metric": "3D TTI RTM shots/hr, learned snapshot codec vs plain "
                                                    "checkpoint recompute", "grid": [nx, ny, nz], "sponge": NPD,
                       "nt": args.nt, "shots": args.shots, "snap_every": 4,
+                      "receivers": "every surface node" if args.all_nodes else
+                      "%dx%d grid at 2-node spacing" % (nx // 2, ny // 2),
                       "shots_per_hr": dict({"checkpoint": args.shots * 3600.0 / tp},
                                            **{k: args.shots * 3600.0 / o[1] for k, o in out.items()}),
                       "seconds": dict({"checkpoint": tp}, **{k: o[1] for k, o in out.items()}),
@@ -734,7 +737,8 @@ def main():
     ap.add_argument("--nt", type=int, default=3000, help="rtm-learned, rtm2d, tti-rtm (3500 there): time steps")
     ap.add_argument("--shots", type=int, default=128, help="rtm2d: shots in the batch (the workload has 128); "
                                                            "tti-rtm: shots back to back (the workload has 8)")
-    ap.add_argument("--err-nt", type=int, default=1200, help="rtm-learned: steps of the image-error comparison")
+    ap.add_argument("--all-nodes", action="store_true", help="tti-rtm: every surface node records (default: the "
+                    "300x300 grid at 2-node spacing)")
     ap.add_argument("--train-iters", type=int, default=16000, help="rtm-learned: codec training steps")
     ap.add_argument("--escape", type=float, default=0.03, help="rtm-learned: escaped-block budget")
     ap.add_argument("--methods", default="boundary,learned", help="rtm-methods: methods to run")
