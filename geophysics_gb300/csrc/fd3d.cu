@@ -307,6 +307,7 @@ static int step3d(geo_fd3d_plan *p, int f, const StepArgs3D &st, cudaStream_t s)
         const float *tl = p->tilt.as<float>();
         t.ct = tl; t.st = tl + p->nalloc; t.cp = tl + 2 * p->nalloc; t.sp = tl + 3 * p->nalloc;
         t.save = p->save.as<float>();
+        t.err = p->err.as<int>();
         GEO_TRY(launch_tti3d(t, st, s));
     } else {
         const Fused3D r = make_fused(p, f);

@@ -41,6 +41,7 @@ struct Tti3DStep {
     float *u1, *v1, *w1, *P1, *Q1;
     const float *ct, *st, *cp, *sp;
     float *save;
+    int *err;                   // device error word (pipeline wait timeouts)
 };
 int launch_tti3d(const Tti3DStep &t, const StepArgs3D &st, cudaStream_t s);
 
