@@ -734,9 +734,10 @@ def main():
     ap.add_argument("--grid", type=int, default=None, help="small (192 by default), tti (600x600x400 by "
                                                            "default): cube edge, for profiling cases")
     ap.add_argument("--sponge", type=int, default=40, help="small: sponge width")
-    ap.add_argument("--nt", type=int, default=3000, help="rtm-learned, rtm2d, tti-rtm (3500 there): time steps")
-    ap.add_argument("--shots", type=int, default=128, help="rtm2d: shots in the batch (the workload has 128); "
-                                                           "tti-rtm: shots back to back (the workload has 8)")
+    ap.add_argument("--nt", type=int, default=None, help="rtm-learned, rtm2d (default 3000), tti-rtm (default "
+                    "3500): time steps")
+    ap.add_argument("--shots", type=int, default=None, help="rtm2d: shots in the batch (default 128, the "
+                    "workload's); tti-rtm: shots back to back (default 8, the workload's)")
     ap.add_argument("--all-nodes", action="store_true", help="tti-rtm: every surface node records (default: the "
                     "300x300 grid at 2-node spacing)")
     ap.add_argument("--train-iters", type=int, default=16000, help="rtm-learned: codec training steps")
@@ -746,6 +747,10 @@ def main():
     if args.case == "fd2d":
         run_fd2d_case(args)
         return
+    if args.shots is None:
+        args.shots = {"rtm2d": 128, "tti-rtm": 8}.get(args.case, 1)
+    if args.nt is None:
+        args.nt = TTI_NT if args.case == "tti-rtm" else 3000
     if args.case == "rtm2d":
         run_rtm2d_case(args)
         return

@@ -229,6 +229,70 @@ struct Batch2D {
     int stress(int phase, Step2D st, cudaStream_t s) {
         return launch_stress2d(variant, phase, d_S.as<Shot2D>(), d_items.as<int>(), (int)items.size(), by, grid, st, s);
     }
+
+    // Skewed schedule (MPI form, two or more shots): the shots are split
+    // into groups A = [0, split) and B = [split, ns) of about equal tiles,
+    // B half a step behind A, so that every launch pairs one group's stress
+    // tiles with the other's velocity tiles (launch_mix2d).  Every shot
+    // still runs velocity then stress of each step in order.  Tables, as
+    // (shot | kind << 30, tile) items with the kinds interleaved:
+    //   VA: velocity of A;  MX: stress of A + velocity of B;
+    //   MY: velocity of A + stress of B;  SB: stress of B.
+    enum { VA = 0, MX = 1, MY = 2, SB = 3 };
+    DevBuf d_mix;
+    int split = 0, mix_n[4] = {0, 0, 0, 0};
+    size_t mix_o[4] = {0, 0, 0, 0};
+    int build_mix(cudaStream_t s) {
+        const int ns = (int)S.size();
+        std::vector<long> tiles(ns);
+        long total = 0;
+        for (int k = 0; k < ns; k++) {
+            tiles[k] = (long)S[k].ntz * ((S[k].nnx + by - 1) / by);
+            total += tiles[k];
+        }
+        long acc = 0;
+        split = 1;
+        for (int k = 0; k < ns - 1; k++) {
+            acc += tiles[k];
+            split = k + 1;
+            if (2 * acc >= total) break;
+        }
+        auto list = [&](int k0, int k1, int kind) {
+            std::vector<int2> v;
+            for (int k = k0; k < k1; k++)
+                for (long t = 0; t < tiles[k]; t++) v.push_back(make_int2(k | (kind << 30), (int)t));
+            return v;
+        };
+        auto merge = [](const std::vector<int2> &a, const std::vector<int2> &b) {
+            std::vector<int2> v;
+            v.reserve(a.size() + b.size());
+            size_t i = 0, j = 0;
+            while (i < a.size() || j < b.size()) {
+                if (j >= b.size() || (i < a.size() && i * b.size() <= j * a.size())) v.push_back(a[i++]);
+                else v.push_back(b[j++]);
+            }
+            return v;
+        };
+        const std::vector<int2> vA = list(0, split, 0), sA = list(0, split, 1), vB = list(split, ns, 0),
+                                sB = list(split, ns, 1);
+        const std::vector<int2> tab[4] = {vA, merge(sA, vB), merge(vA, sB), sB};
+        size_t off = 0;
+        for (int t = 0; t < 4; t++) {
+            mix_o[t] = off;
+            mix_n[t] = (int)tab[t].size();
+            off += tab[t].size();
+        }
+        GEO_TRY(d_mix.alloc(off * sizeof(int2)));
+        for (int t = 0; t < 4; t++)
+            GEO_CUDA(cudaMemcpyAsync(d_mix.as<int2>() + mix_o[t], tab[t].data(), tab[t].size() * sizeof(int2),
+                                     cudaMemcpyHostToDevice, s));
+        GEO_CUDA(cudaStreamSynchronize(s));
+        return GEO_OK;
+    }
+    int mix(int table, int phase, int fast, Step2D sv, Step2D ss, cudaStream_t s) {
+        return launch_mix2d(phase, fast, d_S.as<Shot2D>(), d_mix.as<int2>() + mix_o[table], mix_n[table], by, grid,
+                            sv, ss, s);
+    }
 };
 
 // Graph of a range of steps; capture on a private stream.
@@ -562,13 +626,30 @@ extern "C" int geo_rtm2d_batch_adcig(const geo_rtm2d_desc *desc, const float *v,
         if (wd.every <= 0 || ((k + 1) % wd.every && !last)) return GEO_OK;
         return launch_watch_shots(B.d_S.as<Shot2D>(), D.ns, nf, wd.d, k + 1, ss.cs);
     };
-    // forward: source side only, with records and edge lines
+    // forward: source side only, with records and edge lines; with two or
+    // more shots on the skewed schedule (Batch2D::build_mix)
+    const bool skew = D.ns >= 2;
+    if (skew) GEO_TRY(B.build_mix(ss.cs));
+    auto fwd_st = [&](int it) {
+        Step2D st{};
+        st.it = it; st.amp = amp[it]; st.src_on = on[it]; st.taper = 1; st.nf = 1; st.fast = fast;
+        return st;
+    };
     {
         Graph G;
         GEO_TRY(capture(G, ss.cs, [&]() -> int {
+            if (skew) {
+                GEO_TRY(B.mix(Batch2D::VA, PH_FWD, fast, fwd_st(0), fwd_st(0), ss.cs));
+                for (int it = 0; it < nt; it++) {
+                    GEO_TRY(B.mix(Batch2D::MX, PH_FWD, fast, fwd_st(it), fwd_st(it), ss.cs));
+                    if (it + 1 < nt) GEO_TRY(B.mix(Batch2D::MY, PH_FWD, fast, fwd_st(it + 1), fwd_st(it), ss.cs));
+                    else GEO_TRY(B.mix(Batch2D::SB, PH_FWD, fast, fwd_st(it), fwd_st(it), ss.cs));
+                    GEO_TRY(watch(it, it == nt - 1, 1));
+                }
+                return GEO_OK;
+            }
             for (int it = 0; it < nt; it++) {
-                Step2D st{};
-                st.it = it; st.amp = amp[it]; st.src_on = on[it]; st.taper = 1; st.nf = 1; st.fast = fast;
+                const Step2D st = fwd_st(it);
                 GEO_TRY(B.vel(st, ss.cs));
                 GEO_TRY(B.stress(PH_FWD, st, ss.cs));
                 GEO_TRY(watch(it, it == nt - 1, 1));
@@ -594,11 +675,33 @@ extern "C" int geo_rtm2d_batch_adcig(const geo_rtm2d_desc *desc, const float *v,
     // backward: inject, both propagations, fused imaging
     {
         Graph G;
+        auto bwd_st = [&](int it) {
+            Step2D st{};
+            st.it = it; st.nf = 2; st.fast = fast;
+            return st;
+        };
+        const Shot2D *dA = B.d_S.as<Shot2D>(), *dB = dA + B.split;
+        const int nA = B.split, nB = D.ns - B.split;
         GEO_TRY(capture(G, ss.cs, [&]() -> int {
+            if (skew) {
+                GEO_TRY(launch_inject2d(dA, nA, maxline, nt - 1, ss.cs));
+                GEO_TRY(B.mix(Batch2D::VA, PH_BWD, fast, bwd_st(nt - 1), bwd_st(nt - 1), ss.cs));
+                for (int it = nt - 1; it >= 0; it--) {
+                    GEO_TRY(launch_inject2d(dB, nB, maxline, it, ss.cs));
+                    GEO_TRY(B.mix(Batch2D::MX, PH_BWD, fast, bwd_st(it), bwd_st(it), ss.cs));
+                    if (it > 0) {
+                        GEO_TRY(launch_inject2d(dA, nA, maxline, it - 1, ss.cs));
+                        GEO_TRY(B.mix(Batch2D::MY, PH_BWD, fast, bwd_st(it - 1), bwd_st(it), ss.cs));
+                    } else {
+                        GEO_TRY(B.mix(Batch2D::SB, PH_BWD, fast, bwd_st(it), bwd_st(it), ss.cs));
+                    }
+                    GEO_TRY(watch(nt - 1 - it, it == 0, 2));
+                }
+                return GEO_OK;
+            }
             for (int it = nt - 1; it >= 0; it--) {
                 GEO_TRY(launch_inject2d(B.d_S.as<Shot2D>(), D.ns, maxline, it, ss.cs));
-                Step2D st{};
-                st.it = it; st.nf = 2; st.fast = fast;
+                const Step2D st = bwd_st(it);
                 GEO_TRY(B.vel(st, ss.cs));
                 GEO_TRY(B.stress(PH_BWD, st, ss.cs));
                 GEO_TRY(watch(nt - 1 - it, it == 0, 2));

@@ -453,6 +453,43 @@ int launch_inject2d(const Shot2D *d_shots, int nshots, int maxline, int it, cuda
     return check_launch("inject2d");
 }
 
+// One launch that runs velocity tiles of some shots and stress tiles of
+// others (the MPI form of the batched RTM).  Each item is (shot | kind << 30,
+// tile): kind 0 a velocity tile at step st_v, kind 1 a stress tile at st_s.
+// The caller keeps the two kinds on disjoint shots, so the read-only path
+// stays valid for both.  The exact form's stress tiles are bound by the FP64
+// pipe and the velocity tiles by memory, so a launch that holds both keeps
+// both busy on every SM.
+template <int PHASE, bool FAST>
+__global__ void __launch_bounds__(256) k_mix2d(const Shot2D *__restrict__ shots, const int2 *__restrict__ items,
+                                               int nitems, Step2D st_v, Step2D st_s) {
+    for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
+        const int2 e = items[item];
+        const int kind = e.x >> 30;
+        const Shot2D &sh = shots[e.x & ((1 << 30) - 1)];
+        const int tz = e.y % sh.ntz, tx = e.y / sh.ntz;
+        const int iz = tz * 32 + threadIdx.x, ix = tx * blockDim.y + threadIdx.y;
+        if (ix < 4 || ix >= sh.nnx - 4 || iz < 4 || iz >= sh.nnz - 4) continue;
+        if (kind == 0) vel_point<V_MPI, true>(sh, ix, iz, st_v);
+        else stress_point<V_MPI, PHASE, true, FAST>(sh, ix, iz, st_s);
+    }
+}
+
+int launch_mix2d(int phase, int fast, const Shot2D *d_shots, const int2 *d_items, int nitems, int by, int grid,
+                 Step2D st_v, Step2D st_s, cudaStream_t s) {
+    if (nitems < 1) return GEO_OK;
+    GEO_TRY(ensure_gauss());
+    dim3 block(32, by), g(grid < nitems ? grid : nitems);
+    if (phase == PH_FWD) {
+        if (fast) k_mix2d<PH_FWD, true><<<g, block, 0, s>>>(d_shots, d_items, nitems, st_v, st_s);
+        else k_mix2d<PH_FWD, false><<<g, block, 0, s>>>(d_shots, d_items, nitems, st_v, st_s);
+    } else {
+        if (fast) k_mix2d<PH_BWD, true><<<g, block, 0, s>>>(d_shots, d_items, nitems, st_v, st_s);
+        else k_mix2d<PH_BWD, false><<<g, block, 0, s>>>(d_shots, d_items, nitems, st_v, st_s);
+    }
+    return check_launch("mix2d");
+}
+
 // The MPI program's bin of one cosine a1 (before its 90 -> 89 clamp).
 static int ref_adcig_bin(float a1) {
     const float a2 = (float)(0.5 * std::acos(a1) * 180 / kPiMpi);

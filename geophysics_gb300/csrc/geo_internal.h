@@ -189,6 +189,10 @@ int launch_vel2d(int variant, const Shot2D *d_shots, const int *d_item_shot, int
 int launch_stress2d(int variant, int phase, const Shot2D *d_shots, const int *d_item_shot, int nitems,
                     int by, int grid, Step2D st, cudaStream_t s);
 int launch_inject2d(const Shot2D *d_shots, int nshots, int maxline, int it, cudaStream_t s);
+// Velocity tiles (kind 0, step st_v) and stress tiles (kind 1, step st_s)
+// of disjoint shots in one launch, MPI form (fd2d.cu, k_mix2d).
+int launch_mix2d(int phase, int fast, const Shot2D *d_shots, const int2 *d_items, int nitems, int by, int grid,
+                 Step2D st_v, Step2D st_s, cudaStream_t s);
 int launch_mute_records(float *rec, int nx, int nt, const int *lo, const int *hi, cudaStream_t s);
 // cos and sin of n tilt angles in radians on the device, as the 2D TTI
 // programs form them (in place: th_cos holds the angles, then the cosines).
