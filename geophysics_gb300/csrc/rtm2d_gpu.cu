@@ -38,6 +38,7 @@
 #include "geo_internal.h"
 #include "adcig.cuh"
 #include "tti2d.cuh"
+#include "gridsync.cuh"
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -75,128 +76,224 @@ static TtiField tti_field(const GField &f) {
     return t;
 }
 
-__global__ void k_g_src(GField f, long id, float amp) {
-    f.P[id] += amp;
-    f.Q[id] += amp;
-}
+// Everything one persistent launch of a pass needs.
+struct GCoop {
+    GRtm g;
+    TtiGrid tg;
+    GField S, R;                 // source-side and receiver-side fields
+    TtiField tS, tR;
+    const float *e2, *d2;        // stress model of the pass (SV taper forward)
+    const float *amp;            // pfac*w(t) of every step
+    const unsigned char *on;     // source active at every step
+    long src;                    // source cell
+    int ixs, izs;
+    float *rec;                  // nt*nx, time-major
+    float *bp, *bq;              // ring of P and Q, nt*L each
+    float *ill, *mig, *adcig;
+    int L;
+    int it0, it1;                // forward: steps it0..it1-1; backward: it0 down to it1
+    unsigned *bar;               // grid-barrier arrival counter, zeroed before the launch
+    int *err;                    // set when a barrier wait gave up
+};
 
-__global__ void k_g_vel(GRtm g, GField f) {
-    const long n = (long)g.nnx * g.nnz;
-    for (long id = blockIdx.x * (long)blockDim.x + threadIdx.x; id < n; id += (long)gridDim.x * blockDim.x) {
-        const int ix = (int)(id / g.nnz), iz = (int)(id % g.nnz);
-        if (ix < 4 || ix >= g.nnx - 4 || iz < 4 || iz >= g.nnz - 4) continue;
-        float xx = 0.0f, zz = 0.0f;
+// The VTI program's update_vel (Toa_gpu2DvtiFdRtmAdcigsLaplace.cu:256-289)
+// at one point; SRC folds the step's point source (add_source :204, P,Q +=
+// amp at the source cell before the update) into the taps that read it.
+template <bool SRC>
+__device__ __forceinline__ void g_vel_at(const GRtm &g, const GField &f, long id, int ix, int iz, long src, float amp) {
+    const long s = g.nnz;
+    float xx = 0.0f, zz = 0.0f;
 #pragma unroll
-        for (int im = 0; im < 4; im++) {
-            xx += c_grtm[im] * (f.P[id + (im + 1) * (long)g.nnz] - f.P[id - im * (long)g.nnz]);
-            zz += c_grtm[im] * (f.Q[id + im + 1] - f.Q[id - im]);
-        }
-        f.u[id] = g.cx2[ix] * f.u[id] - g.cx1[ix] * g.dtx * xx;
-        f.w[id] = g.cz2[iz] * f.w[id] - g.cz1[iz] * g.dtz * zz;
+    for (int im = 0; im < 4; im++) {
+        xx += c_grtm[im] * (tti_tap<true, SRC>(f.P, id + (im + 1) * s, src, amp) - tti_tap<true, SRC>(f.P, id - im * s, src, amp));
+        zz += c_grtm[im] * (tti_tap<true, SRC>(f.Q, id + im + 1, src, amp) - tti_tap<true, SRC>(f.Q, id - im, src, amp));
     }
+    f.u[id] = g.cx2[ix] * __ldcg(f.u + id) - g.cx1[ix] * g.dtx * xx;
+    f.w[id] = g.cz2[iz] * __ldcg(f.w + id) - g.cz1[iz] * g.dtz * zz;
 }
 
-__global__ void k_g_stress(GRtm g, GField f, const float *e2, const float *d2) {
-    const long n = (long)g.nnx * g.nnz;
-    for (long id = blockIdx.x * (long)blockDim.x + threadIdx.x; id < n; id += (long)gridDim.x * blockDim.x) {
-        const int ix = (int)(id / g.nnz), iz = (int)(id % g.nnz);
-        if (ix < 4 || ix >= g.nnx - 4 || iz < 4 || iz >= g.nnz - 4) continue;
-        float xx = 0.0f, zz = 0.0f;
+// The VTI program's update_stress (:303-404) at one point; returns P and Q.
+__device__ __forceinline__ float2 g_stress_at(const GRtm &g, const GField &f, const float *e2, const float *d2,
+                                              long id, int ix, int iz) {
+    const long s = g.nnz;
+    float xx = 0.0f, zz = 0.0f;
 #pragma unroll
-        for (int im = 0; im < 4; im++) {
-            xx += c_grtm[im] * (f.u[id + im * (long)g.nnz] - f.u[id - (im + 1) * (long)g.nnz]);
-            zz += c_grtm[im] * (f.w[id + im] - f.w[id - im - 1]);
+    for (int im = 0; im < 4; im++) {
+        xx += c_grtm[im] * (__ldcg(f.u + id + im * s) - __ldcg(f.u + id - (im + 1) * s));
+        zz += c_grtm[im] * (__ldcg(f.w + id + im) - __ldcg(f.w + id - im - 1));
+    }
+    const float vp = g.vp[id];
+    const float px = g.ax2[ix] * __ldcg(f.px + id) - g.ax1[ix] * vp * vp * e2[id] * g.dtx * xx;
+    const float pz = g.az2[iz] * __ldcg(f.pz + id) - g.az1[iz] * vp * vp * d2[id] * g.dtz * zz;
+    const float qx = g.ax2[ix] * __ldcg(f.qx + id) - g.ax1[ix] * vp * vp * d2[id] * g.dtx * xx;
+    const float qz = g.az2[iz] * __ldcg(f.qz + id) - g.az1[iz] * vp * vp * g.dtz * zz;
+    f.px[id] = px; f.pz[id] = pz; f.qx[id] = qx; f.qz[id] = qz;
+    const float P = px + pz, Q = qx + qz;
+    f.P[id] = P;
+    f.Q[id] = Q;
+    return make_float2(P, Q);
+}
+
+// One program's velocity / stress update: the TTI program's
+// (Toa_gpu_2dtti_rtm_adcigs_iorderfunciton.cu:126-228) over the tilt field,
+// or the VTI program's.
+template <bool TTI, bool SRC>
+__device__ __forceinline__ void vel_at(const GCoop &a, const GField &f, const TtiField &tf, long id, int ix, int iz,
+                                       float amp) {
+    if constexpr (TTI) tti_vel_at<true, SRC>(a.tg, tf, c_grtm, id, ix, iz, a.src, amp);
+    else g_vel_at<SRC>(a.g, f, id, ix, iz, a.src, amp);
+}
+
+template <bool TTI>
+__device__ __forceinline__ float2 stress_at(const GCoop &a, const GField &f, const TtiField &tf, long id, int ix,
+                                            int iz) {
+    if constexpr (TTI) return tti_stress_at<true>(a.tg, tf, a.e2, a.d2, c_grtm, id, ix, iz);
+    else return g_stress_at(a.g, f, a.e2, a.d2, id, ix, iz);
+}
+
+// Position of (ix, iz) in the ring of wavefield_bndr (:532): rows npml-1
+// (top) and npml+nz+1 (bottom) over the nx interior columns, then columns
+// npml-1 (left) and npml+nx+1 (right) over the nz interior rows; -1 off it.
+__device__ __forceinline__ int ring_index(const GRtm &g, int ix, int iz) {
+    const int npml = g.npml, nx = g.nx, nz = g.nz;
+    if (ix >= npml && ix < npml + nx) {
+        if (iz == npml - 1) return ix - npml;
+        if (iz == npml + nz + 1) return nx + ix - npml;
+    }
+    if (iz >= npml && iz < npml + nz) {
+        if (ix == npml - 1) return 2 * nx + iz - npml;
+        if (ix == npml + nx + 1) return 2 * nx + nz + iz - npml;
+    }
+    return -1;
+}
+
+__device__ __forceinline__ bool g_updated(const GRtm &g, int ix, int iz) {
+    return ix >= 4 && ix < g.nnx - 4 && iz >= 4 && iz < g.nnz - 4;
+}
+
+// Forward pass, steps it0..it1-1, one cooperative launch: per step the
+// velocity half-step (source folded in), a grid barrier, the stress
+// half-step with the SV taper and, per point, the surface record
+// (shot_record :498), the ring save (wavefield_bndr :532) and the source
+// illumination (cal_illumination :654: ill += P*P + Q*Q, <= 0 -> 1), a grid
+// barrier.  The ring covers cells outside the updated band too (their
+// unchanged values).
+template <bool TTI>
+__global__ void __launch_bounds__(256) k_grtm_fwd(const GCoop a) {
+    if (ld_acquire_u32(reinterpret_cast<const unsigned *>(a.err))) return;   // an earlier run gave up
+    const GRtm &g = a.g;
+    const long n = (long)g.nnx * g.nnz, stride = (long)gridDim.x * blockDim.x;
+    const long first = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    unsigned k = 0;
+    for (int it = a.it0; it < a.it1; it++) {
+        const bool on = a.on[it] != 0;
+        const float amp = a.amp[it];
+        for (long id = first; id < n; id += stride) {
+            const int ix = (int)(id / g.nnz), iz = (int)(id % g.nnz);
+            if (!g_updated(g, ix, iz)) continue;
+            const bool near = on && ((iz == a.izs && abs(ix - a.ixs) <= 4) || (ix == a.ixs && abs(iz - a.izs) <= 4));
+            if (near) vel_at<TTI, true>(a, a.S, a.tS, id, ix, iz, amp);
+            else vel_at<TTI, false>(a, a.S, a.tS, id, ix, iz, 0.0f);
         }
-        const float vp = g.vp[id];
-        const float px = g.ax2[ix] * f.px[id] - g.ax1[ix] * vp * vp * e2[id] * g.dtx * xx;
-        const float pz = g.az2[iz] * f.pz[id] - g.az1[iz] * vp * vp * d2[id] * g.dtz * zz;
-        const float qx = g.ax2[ix] * f.qx[id] - g.ax1[ix] * vp * vp * d2[id] * g.dtx * xx;
-        const float qz = g.az2[iz] * f.qz[id] - g.az1[iz] * vp * vp * g.dtz * zz;
-        f.px[id] = px; f.pz[id] = pz; f.qx[id] = qx; f.qz[id] = qz;
-        f.P[id] = px + pz;
-        f.Q[id] = qx + qz;
+        if (!grid_barrier(a.bar, ++k * gridDim.x, a.err)) return;
+        for (long id = first; id < n; id += stride) {
+            const int ix = (int)(id / g.nnz), iz = (int)(id % g.nnz);
+            const int r = ring_index(g, ix, iz), gx = ix - g.npml, gz = iz - g.npml;
+            const bool inner = gx >= 0 && gx < g.nx && gz >= 0 && gz < g.nz;
+            if (!g_updated(g, ix, iz)) {
+                if (r >= 0) {
+                    a.bp[(long)it * a.L + r] = __ldcg(a.S.P + id);
+                    a.bq[(long)it * a.L + r] = __ldcg(a.S.Q + id);
+                }
+                continue;
+            }
+            const float2 pq = stress_at<TTI>(a, a.S, a.tS, id, ix, iz);
+            if (gz == 0 && inner) a.rec[(long)it * g.nx + gx] = pq.x;
+            if (r >= 0) {
+                a.bp[(long)it * a.L + r] = pq.x;
+                a.bq[(long)it * a.L + r] = pq.y;
+            }
+            if (inner) {
+                const long o = (long)gx * g.nz + gz;
+                float v = a.ill[o] + (pq.x * pq.x + pq.y * pq.y);
+                if (v <= 0.0f) v = 1.0f;
+                a.ill[o] = v;
+            }
+        }
+        if (it + 1 < a.it1 && !grid_barrier(a.bar, ++k * gridDim.x, a.err)) return;
     }
 }
 
-// The TTI program's update_vel / update_stress (Toa_gpu_2dtti_rtm_adcigs_iorderfunciton.cu:126-228).
-__global__ void k_g_vel_tti(TtiGrid g, TtiField f) {
-    const long n = (long)g.nnx * g.nnz;
-    for (long id = blockIdx.x * (long)blockDim.x + threadIdx.x; id < n; id += (long)gridDim.x * blockDim.x) {
-        const int ix = (int)(id / g.nnz), iz = (int)(id % g.nnz);
-        if (ix < 4 || ix >= g.nnx - 4 || iz < 4 || iz >= g.nnz - 4) continue;
-        tti_vel_at(g, f, c_grtm, id, ix, iz);
+// Before backward step it: the saved ring into the source-side P,Q and the
+// muted record into the receiver-side P,Q at row npml (shot_record with
+// record = false).
+__device__ __forceinline__ void restore_inject(const GCoop &a, long id, int ix, int iz, int it) {
+    const GRtm &g = a.g;
+    const int r = ring_index(g, ix, iz);
+    if (r >= 0) {
+        a.S.P[id] = a.bp[(long)it * a.L + r];
+        a.S.Q[id] = a.bq[(long)it * a.L + r];
+    }
+    const int gx = ix - g.npml;
+    if (iz == g.npml && gx >= 0 && gx < g.nx) {
+        const float v = a.rec[(long)it * g.nx + gx];
+        a.R.P[id] = v;
+        a.R.Q[id] = v;
     }
 }
 
-__global__ void k_g_stress_tti(TtiGrid g, TtiField f, const float *e2, const float *d2) {
-    const long n = (long)g.nnx * g.nnz;
-    for (long id = blockIdx.x * (long)blockDim.x + threadIdx.x; id < n; id += (long)gridDim.x * blockDim.x) {
-        const int ix = (int)(id / g.nnz), iz = (int)(id % g.nnz);
-        if (ix < 4 || ix >= g.nnx - 4 || iz < 4 || iz >= g.nnz - 4) continue;
-        tti_stress_at(g, f, e2, d2, c_grtm, id, ix, iz);
-    }
-}
-
-// record P at row npml (time-major), or with inject write it into P and Q
-__global__ void k_g_surface(GRtm g, GField f, float *rec, int it, int inject) {
-    const int ix = blockIdx.x * blockDim.x + threadIdx.x;
-    if (ix >= g.nx) return;
-    const long id = g.npml + (long)g.nnz * (ix + g.npml), r = (long)it * g.nx + ix;
-    if (inject) {
-        f.P[id] = rec[r];
-        f.Q[id] = rec[r];
-    } else {
-        rec[r] = f.P[id];
-    }
-}
-
-// ring of wavefield_bndr: up, bottom (row npml+nz+1), left, right (column npml+nx+1)
-__global__ void k_g_ring(GRtm g, GField f, float *bp, float *bq, int it, int save) {
-    const int L = 2 * g.nx + 2 * g.nz;
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= L) return;
-    long id;
-    if (k < g.nx) id = g.npml - 1 + (long)g.nnz * (k + g.npml);
-    else if (k < 2 * g.nx) id = g.npml + g.nz + 1 + (long)g.nnz * (k - g.nx + g.npml);
-    else if (k < 2 * g.nx + g.nz) id = k - 2 * g.nx + g.npml + (long)g.nnz * (g.npml - 1);
-    else id = k - 2 * g.nx - g.nz + g.npml + (long)g.nnz * (g.npml + g.nx + 1);
-    const long b = (long)it * L + k;
-    if (save) {
-        bp[b] = f.P[id];
-        bq[b] = f.Q[id];
-    } else {
-        f.P[id] = bp[b];
-        f.Q[id] = bq[b];
-    }
-}
-
-__global__ void k_g_illum(GRtm g, GField f, float *ill) {
-    const long n = (long)g.nx * g.nz;
-    for (long o = blockIdx.x * (long)blockDim.x + threadIdx.x; o < n; o += (long)gridDim.x * blockDim.x) {
-        const int ix = (int)(o / g.nz), iz = (int)(o % g.nz);
-        const long id = iz + g.npml + (long)g.nnz * (ix + g.npml);
-        float v = ill[o] + (f.P[id] * f.P[id] + f.Q[id] * f.Q[id]);
-        if (v <= 0.0f) v = 1.0f;
-        ill[o] = v;
-    }
-}
-
-__global__ void k_g_image(GRtm g, GField s, GField r, float *mig, float *adcig) {
-    const long n = (long)g.nx * g.nz;
-    for (long o = blockIdx.x * (long)blockDim.x + threadIdx.x; o < n; o += (long)gridDim.x * blockDim.x) {
-        const int ix = (int)(o / g.nz), iz = (int)(o % g.nz);
-        const long id = iz + g.npml + (long)g.nnz * (ix + g.npml);
-        const float sP = s.P[id], gP = r.P[id];
-        mig[o] = mig[o] + sP * gP;
-        if (!adcig || ix % g.dcdp != 0) continue;
-        const float Ssx = -sP * s.u[id], Ssz = -s.Q[id] * s.w[id];
-        const float Sgx = gP * r.u[id], Sgz = r.Q[id] * r.w[id];
-        const float b1 = Ssx * Ssx + Ssz * Ssz, b2 = Sgx * Sgx + Sgz * Sgz;
-        const int ia = poynting_bin(Ssx * Sgx + Ssz * Sgz, b1, b2, c_gthr, g.nangle);
-        if (ia < 0) continue;
-        const float c = c_gcos[ia];
-        float *ag = adcig + iz + (long)g.nz * ia + (long)g.nz * g.nangle * (ix / g.dcdp);
-        *ag = *ag + sP * gP * c * c * c;
+// Backward pass, steps it0 down to it1, one cooperative launch: the ring
+// restore and record injection of step it0, a grid barrier, then per step
+// both fields' velocity half-steps, a grid barrier, both stress half-steps
+// with, per image point, the cross-correlation image (cal_migration :679)
+// and the Poynting gathers (:718-766), then the restore and injection of
+// the next step at the same point, a grid barrier.  A ring or surface cell
+// is read by no other point of the phase that writes it.
+template <bool TTI>
+__global__ void __launch_bounds__(256) k_grtm_bwd(const GCoop a) {
+    if (ld_acquire_u32(reinterpret_cast<const unsigned *>(a.err))) return;
+    const GRtm &g = a.g;
+    const long n = (long)g.nnx * g.nnz, stride = (long)gridDim.x * blockDim.x;
+    const long first = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    unsigned k = 0;
+    for (long id = first; id < n; id += stride) restore_inject(a, id, (int)(id / g.nnz), (int)(id % g.nnz), a.it0);
+    if (!grid_barrier(a.bar, ++k * gridDim.x, a.err)) return;
+    for (int it = a.it0; it >= a.it1; it--) {
+        for (long id = first; id < n; id += stride) {
+            const int ix = (int)(id / g.nnz), iz = (int)(id % g.nnz);
+            if (!g_updated(g, ix, iz)) continue;
+            vel_at<TTI, false>(a, a.S, a.tS, id, ix, iz, 0.0f);
+            vel_at<TTI, false>(a, a.R, a.tR, id, ix, iz, 0.0f);
+        }
+        if (!grid_barrier(a.bar, ++k * gridDim.x, a.err)) return;
+        for (long id = first; id < n; id += stride) {
+            const int ix = (int)(id / g.nnz), iz = (int)(id % g.nnz);
+            if (g_updated(g, ix, iz)) {
+                const float2 s = stress_at<TTI>(a, a.S, a.tS, id, ix, iz);
+                const float2 r = stress_at<TTI>(a, a.R, a.tR, id, ix, iz);
+                const int gx = ix - g.npml, gz = iz - g.npml;
+                if (gx >= 0 && gx < g.nx && gz >= 0 && gz < g.nz) {
+                    const long o = (long)gx * g.nz + gz;
+                    const float sP = s.x, gP = r.x;
+                    a.mig[o] = a.mig[o] + sP * gP;
+                    // gathers at ix = 0, dcdp, ... below nx / dcdp * dcdp (Poynting_Adcigs
+                    // :473 runs id < nx/dcdp*nz; the array holds nx/dcdp gathers)
+                    if (a.adcig && gx % g.dcdp == 0 && gx / g.dcdp < g.nx / g.dcdp) {
+                        const float Ssx = -sP * __ldcg(a.S.u + id), Ssz = -s.y * __ldcg(a.S.w + id);
+                        const float Sgx = gP * __ldcg(a.R.u + id), Sgz = r.y * __ldcg(a.R.w + id);
+                        const float b1 = Ssx * Ssx + Ssz * Ssz, b2 = Sgx * Sgx + Sgz * Sgz;
+                        const int ia = poynting_bin(Ssx * Sgx + Ssz * Sgz, b1, b2, c_gthr, g.nangle);
+                        if (ia >= 0) {
+                            const float c = c_gcos[ia];
+                            float *ag = a.adcig + gz + (long)g.nz * ia + (long)g.nz * g.nangle * (gx / g.dcdp);
+                            *ag = *ag + sP * gP * c * c * c;
+                        }
+                    }
+                }
+            }
+            if (it > a.it1) restore_inject(a, id, ix, iz, it - 1);
+        }
+        if (it > a.it1 && !grid_barrier(a.bar, ++k * gridDim.x, a.err)) return;
     }
 }
 
@@ -423,22 +520,60 @@ static int gpu_rtm_run(const GpuRtmProgram &prog, const geo_rtm2d_gpu_desc &D, c
     };
     const GField S = fields(fs_), R = fields(fr_);
     float *bp = ring.as<float>(), *bq = bp + (size_t)nt * L;
-    const int gb = grid_of_n((long)n), gi = grid_of_n((long)n0);
+    const int gi = grid_of_n((long)n0);
     const cudaMemcpyKind kout = mem == GEO_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
     const cudaMemcpyKind kin = mem == GEO_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
     if (shots || obs) GEO_TRY(trs.alloc((size_t)nt * nx * 4));
-    const TtiGrid tg = tti_grid(g);
-    auto step = [&](const GField &f, const float *e2p, const float *d2p) -> int {
-        if (prog.tti) {
-            k_g_vel_tti<<<gb, 256, 0, s>>>(tg, tti_field(f));
-            GEO_TRY(check_launch("grtm_vel_tti"));
-            k_g_stress_tti<<<gb, 256, 0, s>>>(tg, tti_field(f), e2p, d2p);
-            return check_launch("grtm_stress_tti");
-        }
-        k_g_vel<<<gb, 256, 0, s>>>(g, f);
-        GEO_TRY(check_launch("grtm_vel"));
-        k_g_stress<<<gb, 256, 0, s>>>(g, f, e2p, d2p);
-        return check_launch("grtm_stress");
+    DevBuf d_amp, d_on, d_sync;
+    GEO_TRY(d_amp.alloc((size_t)nt * 4));
+    GEO_TRY(d_on.alloc((size_t)nt));
+    GEO_TRY(d_sync.alloc(8));
+    GEO_TRY(d_sync.zero(s));
+    GEO_CUDA(cudaMemcpyAsync(d_amp.p, amp.data(), (size_t)nt * 4, cudaMemcpyHostToDevice, s));
+    GEO_CUDA(cudaMemcpyAsync(d_on.p, on.data(), (size_t)nt, cudaMemcpyHostToDevice, s));
+    GCoop a{};
+    a.g = g;
+    a.tg = tti_grid(g);
+    a.S = S;
+    a.R = R;
+    a.tS = tti_field(S);
+    a.tR = tti_field(R);
+    a.amp = d_amp.as<float>();
+    a.on = d_on.as<unsigned char>();
+    a.rec = rec.as<float>();
+    a.bp = bp;
+    a.bq = bq;
+    a.ill = ill.as<float>();
+    a.mig = mig.as<float>();
+    a.adcig = ag.p ? ag.as<float>() : nullptr;
+    a.L = L;
+    a.bar = d_sync.as<unsigned>();
+    a.err = d_sync.as<int>() + 1;
+    // every block resident at once (the grid barrier needs it; the
+    // cooperative launch checks it), threads striding over the points
+    const void *kf = prog.tti ? (const void *)k_grtm_fwd<true> : (const void *)k_grtm_fwd<false>;
+    const void *kb = prog.tti ? (const void *)k_grtm_bwd<true> : (const void *)k_grtm_bwd<false>;
+    int grid_f = 0, grid_b = 0;
+    {
+        int dev = 0, sms = 0, occ_f = 0, occ_b = 0, coop = 0;
+        GEO_CUDA(cudaGetDevice(&dev));
+        GEO_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        GEO_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
+        GEO_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_f, kf, 256, 0));
+        GEO_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_b, kb, 256, 0));
+        if (!coop || occ_f < 1 || occ_b < 1) return fail(GEO_ERR_CUDA, "cooperative launch unavailable");
+        grid_f = (int)std::min<size_t>((n + 255) / 256, (size_t)occ_f * sms);
+        grid_b = (int)std::min<size_t>((n + 255) / 256, (size_t)occ_b * sms);
+        if ((long long)std::max(grid_f, grid_b) * (2LL * nt + 2) >= 4000000000LL)
+            return fail(GEO_ERR_ARG, "too many steps for one launch");
+    }
+    auto launch = [&](const void *fn, int grid, int it0, int it1) -> int {
+        a.it0 = it0;
+        a.it1 = it1;
+        GEO_CUDA(cudaMemsetAsync(a.bar, 0, 4, s));
+        void *args[] = {(void *)&a};
+        GEO_CUDA(cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(256), args, 0, s));
+        return check_launch("grtm_pass");
     };
     Watchdog wd;
     GEO_TRY(wd.open());
@@ -469,22 +604,20 @@ static int gpu_rtm_run(const GpuRtmProgram &prog, const geo_rtm2d_gpu_desc &D, c
         GEO_TRY(fr_.zero(s));
         GEO_TRY(rec.zero(s));
         GEO_TRY(ring.zero(s));
-        const long src = (long)(D.fs + (is - 1) * D.ds + npml - 1) * nnz + (D.zs + npml - 1);
-        for (int it = 0; it < nt; it++) {
-            if (on[it]) {
-                k_g_src<<<1, 1, 0, s>>>(S, src, amp[it]);
-                GEO_TRY(check_launch("grtm_src"));
-            }
-            GEO_TRY(step(S, dte2.as<float>(), dtd2.as<float>()));
-            k_g_surface<<<(nx + 255) / 256, 256, 0, s>>>(g, S, rec.as<float>(), it, 0);
-            GEO_TRY(check_launch("grtm_record"));
-            k_g_ring<<<(L + 255) / 256, 256, 0, s>>>(g, S, bp, bq, it, 1);
-            GEO_TRY(check_launch("grtm_ring"));
-            k_g_illum<<<gi, 256, 0, s>>>(g, S, ill.as<float>());
-            GEO_TRY(check_launch("grtm_illum"));
-            const int w = wd.check(S.P, n, it, it == nt - 1, s);
+        a.ixs = D.fs + (is - 1) * D.ds + npml - 1;
+        a.izs = D.zs + npml - 1;
+        a.src = (long)a.ixs * nnz + a.izs;
+        a.e2 = dte2.as<float>();
+        a.d2 = dtd2.as<float>();
+        // runs of steps between the watchdog's scans, one launch each
+        for (int it0 = 0; it0 < nt;) {
+            int it1 = it0 + 1;
+            while (it1 < nt && !(wd.every > 0 && it1 % wd.every == 0)) it1++;
+            GEO_TRY(launch(kf, grid_f, it0, it1));
+            const int w = wd.check(S.P, n, it1 - 1, it1 == nt, s);
             if (w == GEO_ERR_NAN) break;
             GEO_TRY(w);
+            it0 = it1;
         }
         GEO_TRY(wd.verdict(s, "2D RTM forward pass"));
         // direct-wave mute (GPU form, tt), exactly as the program's kernel
@@ -521,20 +654,26 @@ static int gpu_rtm_run(const GpuRtmProgram &prog, const geo_rtm2d_gpu_desc &D, c
             GEO_CUDA(cudaMemcpyAsync(trs.p, obs + (size_t)(is - 1) * nx * nt, (size_t)nx * nt * 4, kin, s));
             GEO_TRY(launch_transpose_records(trs.as<float>(), rec.as<float>(), nt, nx, s));
         }
-        for (int it = nt - 1; it >= 0; it--) {
-            k_g_ring<<<(L + 255) / 256, 256, 0, s>>>(g, S, bp, bq, it, 0);
-            GEO_TRY(check_launch("grtm_ring"));
-            GEO_TRY(step(S, de2.as<float>(), dd2.as<float>()));
-            k_g_surface<<<(nx + 255) / 256, 256, 0, s>>>(g, R, rec.as<float>(), it, 1);
-            GEO_TRY(check_launch("grtm_inject"));
-            GEO_TRY(step(R, de2.as<float>(), dd2.as<float>()));
-            k_g_image<<<gi, 256, 0, s>>>(g, S, R, mig.as<float>(), ag.p ? ag.as<float>() : nullptr);
-            GEO_TRY(check_launch("grtm_image"));
-            const int w = wd.check(R.P, n, nt - 1 - it, it == 0, s);
+        a.e2 = de2.as<float>();
+        a.d2 = dd2.as<float>();
+        // runs of steps between the watchdog's scans (after backward step
+        // it when (nt - it) is a multiple of the interval), one launch each
+        for (int hi = nt - 1; hi >= 0;) {
+            int lo = hi;
+            while (lo > 0 && !(wd.every > 0 && (nt - lo) % wd.every == 0)) lo--;
+            GEO_TRY(launch(kb, grid_b, hi, lo));
+            const int w = wd.check(R.P, n, nt - 1 - lo, lo == 0, s);
             if (w == GEO_ERR_NAN) break;
             GEO_TRY(w);
+            hi = lo - 1;
         }
         GEO_TRY(wd.verdict(s, "2D RTM backward pass"));
+    }
+    {
+        int err = 0;
+        GEO_CUDA(cudaMemcpyAsync(&err, a.err, 4, cudaMemcpyDeviceToHost, s));
+        GEO_CUDA(cudaStreamSynchronize(s));
+        if (err) return fail(GEO_ERR_CUDA, "2D RTM: a grid barrier wait timed out");
     }
     GEO_TRY(launch_normalize_image(mig.as<float>(), ill.as<float>(), n0, s));
     GEO_TRY(lap.alloc(n0 * 4));

@@ -11,11 +11,17 @@
 // snap_every on (:451-456).  The program swaps its old/new pointers without
 // keeping two buffers (u0 = u1 after the first step), so every field is
 // updated in place; this file does that directly.
-// cos and sin of the tilt are formed once on the host (cosf/sinf of the
+// cos and sin of the tilt are formed once on the device (cosf/sinf of the
 // angle in radians, theta * pi/180 as the program converts it).
+// The program launches four kernels per step; here the steps between two
+// host events (a snapshot, a watchdog scan) run as one cooperative launch
+// with grid barriers between the half-steps, the source folded into the
+// velocity taps that read its cell and the record written by the stress
+// phase.
 #include "geo_internal.h"
 #include <algorithm>
 #include "tti2d.cuh"
+#include "gridsync.cuh"
 #include <cmath>
 #include <vector>
 
@@ -44,32 +50,53 @@ int launch_tilt_trig(float *th_cos, float *sn, size_t n, cudaStream_t s) {
 
 __constant__ float c_tti[4] = {1.196289f, -0.0797526f, 0.009570313f, -0.0006975447f};
 
-__global__ void k_tti_src(TtiField f, long id, float amp) {
-    f.P[id] += amp;
-    f.Q[id] += amp;
-}
+// A whole 2D TTI shot (or a run of its steps) in one cooperative launch:
+// per step the velocity half-step over every updated point (the step's
+// point source folded into the taps that read the source cell), a grid
+// barrier, the stress half-step with the surface record of P, a grid
+// barrier.  The per-point arithmetic is tti_vel_at / tti_stress_at's; field
+// values other blocks wrote are read through L2.
+struct TtiShot {
+    TtiGrid g;
+    TtiField f;
+    const float *e2, *d2;
+    const float *amp;            // pfac*w(t) of every step
+    const unsigned char *on;     // source active at every step
+    long src;                    // source cell
+    int ixs, izs;
+    float *rec;                  // nx*nt, trace-major
+    int nx, npd, rec_iz, nt;
+    int it0, it1;                // steps of this launch
+    unsigned *bar;               // grid-barrier arrival counter, zeroed before the launch
+    int *err;                    // set when a barrier wait gave up
+};
 
-__global__ void k_tti_vel(TtiGrid g, TtiField f) {
-    const long n = (long)g.nnx * g.nnz;
-    for (long id = blockIdx.x * (long)blockDim.x + threadIdx.x; id < n; id += (long)gridDim.x * blockDim.x) {
-        const int ix = (int)(id / g.nnz), iz = (int)(id % g.nnz);
-        if (ix < 4 || ix >= g.nnx - 4 || iz < 4 || iz >= g.nnz - 4) continue;
-        tti_vel_at(g, f, c_tti, id, ix, iz);
+__global__ void __launch_bounds__(256) k_tti_shot(const TtiShot a) {
+    if (ld_acquire_u32(reinterpret_cast<const unsigned *>(a.err))) return;   // an earlier run gave up
+    const TtiGrid &g = a.g;
+    const long n = (long)g.nnx * g.nnz, stride = (long)gridDim.x * blockDim.x;
+    const long first = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    unsigned k = 0;
+    for (int it = a.it0; it < a.it1; it++) {
+        const bool on = a.on[it] != 0;
+        const float amp = a.amp[it];
+        for (long id = first; id < n; id += stride) {
+            const int ix = (int)(id / g.nnz), iz = (int)(id % g.nnz);
+            if (ix < 4 || ix >= g.nnx - 4 || iz < 4 || iz >= g.nnz - 4) continue;
+            const bool near = on && ((iz == a.izs && abs(ix - a.ixs) <= 4) || (ix == a.ixs && abs(iz - a.izs) <= 4));
+            if (near) tti_vel_at<true, true>(g, a.f, c_tti, id, ix, iz, a.src, amp);
+            else tti_vel_at<true, false>(g, a.f, c_tti, id, ix, iz);
+        }
+        if (!grid_barrier(a.bar, ++k * gridDim.x, a.err)) return;
+        for (long id = first; id < n; id += stride) {
+            const int ix = (int)(id / g.nnz), iz = (int)(id % g.nnz);
+            if (ix < 4 || ix >= g.nnx - 4 || iz < 4 || iz >= g.nnz - 4) continue;
+            const float P = tti_stress_at<true>(g, a.f, a.e2, a.d2, c_tti, id, ix, iz).x;
+            // shot_record (:273-283): P at the receiver row, after the step
+            if (iz == a.rec_iz && ix >= a.npd && ix < a.npd + a.nx) a.rec[it + (long)a.nt * (ix - a.npd)] = P;
+        }
+        if (it + 1 < a.it1 && !grid_barrier(a.bar, ++k * gridDim.x, a.err)) return;
     }
-}
-
-__global__ void k_tti_stress(TtiGrid g, TtiField f, const float *e2, const float *d2) {
-    const long n = (long)g.nnx * g.nnz;
-    for (long id = blockIdx.x * (long)blockDim.x + threadIdx.x; id < n; id += (long)gridDim.x * blockDim.x) {
-        const int ix = (int)(id / g.nnz), iz = (int)(id % g.nnz);
-        if (ix < 4 || ix >= g.nnx - 4 || iz < 4 || iz >= g.nnz - 4) continue;
-        tti_stress_at(g, f, e2, d2, c_tti, id, ix, iz);
-    }
-}
-
-__global__ void k_tti_rec(const float *P, float *shot, int nnz, int nx, int npd, int rec_iz, int it, int nt) {
-    const int ix = blockIdx.x * blockDim.x + threadIdx.x;
-    if (ix < nx) shot[it + (long)nt * ix] = P[rec_iz + (long)nnz * (ix + npd)];
 }
 
 }  // namespace geo
@@ -172,28 +199,71 @@ extern "C" int geo_tti2d_shot(const geo_fd2d_desc *desc, const float *v, const f
     TtiField f;
     f.u = fb; f.w = fb + n; f.px = fb + 2 * n; f.pz = fb + 3 * n; f.qx = fb + 4 * n; f.qz = fb + 5 * n;
     f.P = fb + 6 * n; f.Q = fb + 7 * n;
-    const int blocks = (int)std::min<size_t>((n + 255) / 256, 152 * 16);
-    const long src_id = (long)ixs * nnz + izs;
     const cudaMemcpyKind kout = mem == GEO_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+    DevBuf d_amp, d_on, d_sync;
+    GEO_TRY(d_amp.alloc((size_t)nt * 4));
+    GEO_TRY(d_on.alloc((size_t)nt));
+    GEO_TRY(d_sync.alloc(8));
+    GEO_TRY(d_sync.zero(s));
+    GEO_CUDA(cudaMemcpyAsync(d_amp.p, amp.data(), (size_t)nt * 4, cudaMemcpyHostToDevice, s));
+    GEO_CUDA(cudaMemcpyAsync(d_on.p, on.data(), (size_t)nt, cudaMemcpyHostToDevice, s));
+    TtiShot a{};
+    a.g = g;
+    a.f = f;
+    a.e2 = e2;
+    a.d2 = d2;
+    a.amp = d_amp.as<float>();
+    a.on = d_on.as<unsigned char>();
+    a.src = (long)ixs * nnz + izs;
+    a.ixs = ixs;
+    a.izs = izs;
+    a.rec = drec.as<float>();
+    a.nx = nx;
+    a.npd = npd;
+    a.rec_iz = D.rec_iz;
+    a.nt = nt;
+    a.bar = d_sync.as<unsigned>();
+    a.err = d_sync.as<int>() + 1;
+    // every block resident at once (the grid barrier needs it; the
+    // cooperative launch checks it), threads striding over the points
+    int dev = 0, sms = 0, occ = 0, coop = 0;
+    GEO_CUDA(cudaGetDevice(&dev));
+    GEO_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    GEO_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
+    GEO_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_tti_shot, 256, 0));
+    if (!coop || occ < 1) return fail(GEO_ERR_CUDA, "cooperative launch unavailable");
+    const int grid = (int)std::min<size_t>((n + 255) / 256, (size_t)occ * sms);
     Watchdog wd;
     GEO_TRY(wd.open());
-    for (int it = 0; it < nt; it++) {
-        if (on[it]) {
-            k_tti_src<<<1, 1, 0, s>>>(f, src_id, amp[it]);
-            GEO_TRY(check_launch("tti_src"));
+    // runs of steps between the host's work: a snapshot after step it
+    // (it % snap_every == 0, it > 0) and the watchdog's scan end a run
+    for (int it0 = 0; it0 < nt;) {
+        int it1 = it0;
+        while (true) {
+            const int it = it1++;
+            const bool snap_due = snap && it % snap_every == 0 && it != 0;
+            const bool watch_due = wd.every > 0 && (it + 1) % wd.every == 0;
+            if (snap_due || watch_due || it1 == nt) break;
         }
-        k_tti_vel<<<blocks, 256, 0, s>>>(g, f);
-        GEO_TRY(check_launch("tti_vel"));
-        k_tti_stress<<<blocks, 256, 0, s>>>(g, f, e2, d2);
-        GEO_TRY(check_launch("tti_stress"));
-        k_tti_rec<<<(nx + 255) / 256, 256, 0, s>>>(f.P, drec.as<float>(), nnz, nx, npd, D.rec_iz, it, nt);
-        GEO_TRY(check_launch("tti_rec"));
+        if ((long long)grid * 2 * (it1 - it0) >= 4000000000LL) it1 = it0 + (int)(1900000000LL / grid);
+        a.it0 = it0;
+        a.it1 = it1;
+        GEO_CUDA(cudaMemsetAsync(a.bar, 0, 4, s));
+        void *args[] = {(void *)&a};
+        GEO_CUDA(cudaLaunchCooperativeKernel((const void *)k_tti_shot, dim3(grid), dim3(256), args, 0, s));
+        GEO_TRY(check_launch("tti_shot"));
+        const int it = it1 - 1;
         if (snap && it % snap_every == 0 && it != 0)
             GEO_CUDA(cudaMemcpyAsync(snap + (size_t)(it / snap_every - 1) * n, f.P, n * 4, kout, s));
         const int w = wd.check(f.P, n, it, it == nt - 1, s);
         if (w == GEO_ERR_NAN) break;
         GEO_TRY(w);
+        it0 = it1;
     }
+    int err = 0;
+    GEO_CUDA(cudaMemcpyAsync(&err, a.err, 4, cudaMemcpyDeviceToHost, s));
+    GEO_CUDA(cudaStreamSynchronize(s));
+    if (err) return fail(GEO_ERR_CUDA, "2D TTI shot: a grid barrier wait timed out");
     GEO_TRY(wd.verdict(s, "2D TTI shot"));
     GEO_CUDA(cudaMemcpyAsync(shot, drec.p, (size_t)nx * nt * 4, kout, s));
     GEO_CUDA(cudaStreamSynchronize(s));

@@ -137,6 +137,22 @@ def test_rtm2d_gpu_program_observed_shots(geo, orc):
     assert np.array_equal(out["adcigs"], ag)
 
 
+def test_rtm2d_gpu_program_thin_sponge_large_grid(geo, orc):
+    """npml = 5 puts the ring's bottom row and right column outside the
+    updated band (they carry saved and restored values only), and a grid of
+    more points than one wave of resident threads makes each thread of the
+    persistent passes stride over several points."""
+    v, e, d = model(nx=700, nz=400)
+    kw = dict(GKW, npml=5, ns=1, nt=150, fs=350)
+    mig, ill, ag, shots = orc.rtm2d_gpu(v, e, d, **kw)
+    out = geo.rtm2d_gpu(v, e, d, **kw)
+    assert np.abs(ill).max() > 0
+    assert np.array_equal(out["shots"], shots)
+    assert np.array_equal(out["illum"], ill)
+    assert np.array_equal(out["mig_lap"], orc.laplace2d_adj(mig))
+    assert np.array_equal(out["adcigs"], ag)
+
+
 def test_rtm2d_gpu_program_stability_check(geo):
     v, e, d = model(nx=96, nz=60)
     with pytest.raises(geo.GeoError) as ei:

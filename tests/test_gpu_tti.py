@@ -41,6 +41,30 @@ def test_tti2d_device_buffers_and_second_shot(geo, orc):
     assert np.array_equal(out.cpu().numpy(), ref)
 
 
+def test_tti2d_source_on_receiver_row_large_grid(geo, orc):
+    """The record row through the source cell (the step's source reaches the
+    velocity taps only, never the recorded P), snapshots every 7 steps, and
+    a grid of more points than one wave of resident threads, so each thread
+    of the persistent launch strides over several points."""
+    v, e, d, th = _model(nx=1100, nz=1000, seed=5)
+    kw = dict(KW, nt=60, rec_iz=29)          # source cell row: (int)(zs + 0.5) + npd - 1
+    ref, rs = orc.tti2d(v, e, d, th, snap_every=7, trig=cuda_trig(th), **kw)
+    out, snaps = geo.tti2d_shot(v, e, d, th, snap_every=7, **kw)
+    assert np.abs(ref).max() > 0
+    assert np.array_equal(out, ref), rel_l2(out, ref)
+    assert snaps.shape == rs.shape == (8, 1140, 1040)
+    assert np.array_equal(snaps, rs)
+
+
+def test_tti2d_receiver_row_outside_updated_band(geo, orc):
+    v, e, d, th = _model(seed=6)
+    kw = dict(KW, nt=40, rec_iz=2)
+    ref = orc.tti2d(v, e, d, th, trig=cuda_trig(th), **kw)
+    out = geo.tti2d_shot(v, e, d, th, **kw)
+    assert np.array_equal(out, ref)
+    assert not out.any()
+
+
 def test_tti2d_rejects_bad_input(geo):
     v, e, d, th = _model()
     th[3, 4] = np.nan
@@ -63,6 +87,20 @@ def test_rtm2d_tti_program_bit_exact(geo, orc, dcdp):
     out = geo.rtm2d_tti(v, e, d, th, dcdp=dcdp, **TKW)
     assert np.abs(ill).max() > 0 and np.abs(ag).max() > 0
     assert out["adcigs"].shape == (91 // dcdp, 65, 60)
+    assert np.array_equal(out["shots"], shots)
+    assert np.array_equal(out["illum"], ill)
+    assert np.array_equal(out["mig_lap"], orc.laplace2d_adj(mig))
+    assert np.array_equal(out["adcigs"], ag), rel_l2(out["adcigs"], ag)
+
+
+def test_rtm2d_tti_program_thin_sponge_large_grid(geo, orc):
+    """As the VTI program's case: npml = 5 (ring cells outside the updated
+    band) on a grid larger than one wave of resident threads."""
+    v, e, d, th = _model(nx=700, nz=400, seed=8)
+    kw = dict(TKW, npml=5, ns=1, nt=150, fs=350)
+    mig, ill, ag, shots = orc.rtm2d_tti(v, e, d, th, trig=cuda_trig(th), **kw)
+    out = geo.rtm2d_tti(v, e, d, th, **kw)
+    assert np.abs(ill).max() > 0
     assert np.array_equal(out["shots"], shots)
     assert np.array_equal(out["illum"], ill)
     assert np.array_equal(out["mig_lap"], orc.laplace2d_adj(mig))
