@@ -113,15 +113,21 @@ __global__ void __launch_bounds__(256) k_ae_e1(const E1Args a) {
     if (b < a.nb && a.vol.src) {
         const AeVolume &v = a.vol;
         const int bz = b % v.nbz, bx = (b / v.nbz) % v.nbx, by = b / (v.nbz * v.nbx);
-#pragma unroll 4
+        // all sixteen loads of the thread in flight before the first use
+        float vals[16];
+#pragma unroll
         for (int p = 0; p < 16; p++) {
             const int idx = p * 256 + t, z = idx & 15, x = (idx >> 4) & 15, y = idx >> 8;
             const int iz = bz * 16 + z, ix = bx * 16 + x, iy = by * 16 + y;
-            float val = 0.0f;
+            vals[p] = 0.0f;
             if (iz < v.nz && ix < v.nx && iy < v.ny)
-                val = v.src[(long)(v.oz + iz) + v.ldz * (v.ox + ix) + v.sxy * (v.oy + iy)];
-            xs[morton_of(z, x, y)] = val;
-            mx = fmaxf(mx, fabsf(val));
+                vals[p] = __ldg(v.src + (long)(v.oz + iz) + v.ldz * (v.ox + ix) + v.sxy * (v.oy + iy));
+        }
+#pragma unroll
+        for (int p = 0; p < 16; p++) {
+            const int idx = p * 256 + t;
+            xs[morton_of(idx & 15, (idx >> 4) & 15, idx >> 8)] = vals[p];
+            mx = fmaxf(mx, fabsf(vals[p]));
         }
     } else if (b < a.nb) {
         const float *src;
@@ -326,7 +332,7 @@ __global__ void __launch_bounds__(256) k_ae_d1(const D1Args a) {
     }
     const int slot = a.esc ? a.esc[b] : -1;
     const __nv_bfloat16 *res = slot >= 0 ? a.res + (long)slot * kAePts : nullptr;
-#pragma unroll 4
+#pragma unroll 8
     for (int p = 0; p < 16; p++) {
         const int idx = p * 256 + t, z = idx & 15, x = (idx >> 4) & 15, y = idx >> 8;
         const int iz = bz * 16 + z, ix = bx * 16 + x, iy = by * 16 + y;

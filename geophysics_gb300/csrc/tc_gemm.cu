@@ -24,26 +24,40 @@ using namespace tc;
 constexpr int kGM = 128, kGK = 64;
 
 // Stage ring sized so two CTAs fit on an SM (one's epilogue overlaps the
-// other's main loop): 2 stages for BN 256, 3 for 128, 4 for 64.
-template <int BN>
+// other's main loop): 2 stages for BN 256, 3 for 128, 4 for 64.  A GEMM
+// with fewer K slices than that gets as many stages as slices (ST), so that
+// more CTAs share an SM and more tiles are in flight: the skinny codec
+// levels (K = 64, 128) have one or two slices per tile.  The shared memory
+// is then padded so that no more CTAs fit than tensor memory holds
+// accumulators for (512 columns per SM), so no allocation ever waits.
+constexpr int default_stages(int bn) { return bn >= 256 ? 2 : (bn >= 128 ? 3 : 4); }
+constexpr size_t kSmSmem = 233472;      // shared memory per SM
+constexpr size_t kCtaReserve = 1024;    // reserved per resident CTA
+
+template <int BN, int ST = default_stages(BN)>
 struct GemmShape {
     static constexpr int kA = kGM * kGK * 2;
     static constexpr int kB = BN * kGK * 2;
     static constexpr int kStage = kA + kB;
-    static constexpr int kStages = BN >= 256 ? 2 : (BN >= 128 ? 3 : 4);
-    static constexpr size_t kSmem = (size_t)kStages * kStage + 1024 + 256;
+    static constexpr int kStages = ST;
     static constexpr uint32_t kCols = BN < 32 ? 32 : BN;
+    static constexpr size_t kRing = (size_t)kStages * kStage + 1024 + 256;
+    // fewest bytes with which at most 512 / kCols CTAs fit on an SM
+    static constexpr size_t kFloor = kSmSmem / (512 / kCols + 1) + 1 - kCtaReserve;
+    static constexpr size_t kSmem = kRing > kFloor ? kRing : kFloor;
     static_assert(kA % 1024 == 0 && kB % 1024 == 0, "swizzle atoms stay 1024-byte aligned");
     static_assert(BN % 16 == 0 && BN >= 16 && BN <= 256, "UMMA N for M = 128");
+    static_assert(ST >= 1 && ST <= default_stages(BN), "stage count");
     static_assert(2 * kSmem <= 232448, "two CTAs per SM");
+    static_assert((kSmSmem / (kSmem + kCtaReserve)) * kCols <= 512, "resident CTAs' accumulators fit in TMEM");
 };
 
 __device__ __forceinline__ float leaky(float v) { return v > 0.0f ? v : kLeak * v; }
 
-template <int BN>
+template <int BN, int ST>
 __global__ void __launch_bounds__(128, 2)
     k_tc_gemm(const __grid_constant__ CUtensorMap ta, const __grid_constant__ CUtensorMap tb, const TcGemm g) {
-    using S = GemmShape<BN>;
+    using S = GemmShape<BN, ST>;
     extern __shared__ unsigned char smem_raw[];
     uint8_t *sm = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     constexpr int kGStages = S::kStages;
@@ -184,20 +198,32 @@ static int encode_bf16_2d(CUtensorMap *map, const void *base, int rows, int cols
     return GEO_OK;
 }
 
-template <int BN>
+template <int BN, int ST>
 static int launch_bn(const TcGemm &g, cudaStream_t s) {
-    using S = GemmShape<BN>;
+    using S = GemmShape<BN, ST>;
     static bool attr = false;
     if (!attr) {
-        GEO_CUDA(cudaFuncSetAttribute(k_tc_gemm<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::kSmem));
+        GEO_CUDA(cudaFuncSetAttribute(k_tc_gemm<BN, ST>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::kSmem));
         attr = true;
     }
     CUtensorMap ta, tb;
     GEO_TRY(encode_bf16_2d(&ta, g.A, g.M, g.K, kGM));
     GEO_TRY(encode_bf16_2d(&tb, g.B, g.N, g.K, BN));
     dim3 grid(g.M / kGM, g.N / BN);
-    k_tc_gemm<BN><<<grid, 128, S::kSmem, s>>>(ta, tb, g);
+    k_tc_gemm<BN, ST><<<grid, 128, S::kSmem, s>>>(ta, tb, g);
     return check_launch("tc_gemm");
+}
+
+// stages = K slices, up to the tile width's default
+template <int BN>
+static int launch_bn_k(const TcGemm &g, cudaStream_t s) {
+    const int nk = g.K / kGK;
+    if constexpr (default_stages(BN) >= 4)
+        if (nk >= 4) return launch_bn<BN, 4>(g, s);
+    if constexpr (default_stages(BN) >= 3)
+        if (nk >= 3) return launch_bn<BN, (default_stages(BN) >= 3 ? 3 : 1)>(g, s);
+    if (nk >= 2) return launch_bn<BN, 2>(g, s);
+    return launch_bn<BN, 1>(g, s);
 }
 
 int tc_gemm(const TcGemm &g, cudaStream_t s) {
@@ -207,9 +233,9 @@ int tc_gemm(const TcGemm &g, cudaStream_t s) {
     const uintptr_t al = reinterpret_cast<uintptr_t>(g.A) | reinterpret_cast<uintptr_t>(g.B) |
                          reinterpret_cast<uintptr_t>(g.out) | reinterpret_cast<uintptr_t>(g.gate);
     if (al & 15) return fail(GEO_ERR_ARG, "tc_gemm: operands must be 16-byte aligned");
-    if (g.N % 256 == 0) return launch_bn<256>(g, s);
-    if (g.N % 128 == 0) return launch_bn<128>(g, s);
-    return launch_bn<64>(g, s);
+    if (g.N % 256 == 0) return launch_bn_k<256>(g, s);
+    if (g.N % 128 == 0) return launch_bn_k<128>(g, s);
+    return launch_bn_k<64>(g, s);
 }
 
 }  // namespace geo
