@@ -470,6 +470,39 @@ TTI_SHAPE, TTI_DX, TTI_DT, TTI_FAVG, TTI_NT = (600, 600, 400), 12.5, 0.0008, 12.
 TTI_BYTES_PER_PT = 104   # velocity kernel 12 floats (P,Q,u,v,w,4 trig in; u,v,w out), stress 14
 
 
+def run_codec_case(args):
+    """The learned snapshot codec alone: encode + decode of one 512x512x384
+    snapshot (24 576 blocks of 16^3, the 3D RTM comparison's grid) as
+    Codec.roundtrip runs it (E1 gather, six tcgen05 GEMM levels, D1
+    scatter).  Input: seeded Gaussian noise smoothed by a 5^3 box filter;
+    untrained weights (the codec's speed does not depend on them).  Each
+    call allocates its code buffers, so the time includes those
+    allocations."""
+    import torch
+
+    import geophysics_gb300 as geo
+    from geophysics_gb300 import build as B
+    B.build()
+    g = torch.Generator(device="cuda").manual_seed(3)
+    vol = torch.randn((512, 512, 384), device="cuda", generator=g)
+    vol = torch.nn.functional.avg_pool3d(vol[None, None], 5, stride=1, padding=2)[0, 0].contiguous()
+    cd = geo.Codec(seed=1)
+    for _ in range(max(args.warmup, 3)):
+        cd.roundtrip(vol)
+    torch.cuda.synchronize()
+    times = []
+    for _ in range(max(args.steps, 5)):
+        t0 = time.perf_counter()
+        cd.roundtrip(vol)
+        torch.cuda.synchronize()
+        times.append(time.perf_counter() - t0)
+    print(json.dumps({"case": "codec", "metric": "codec encode+decode ms per snapshot",
+                      "value": 1000 * statistics.median(times), "unit": "ms", "min_ms": 1000 * min(times),
+                      "blocks": 24576, "grid": [512, 512, 384], "dtype": "bf16 codec", "data": "synthetic"}),
+          flush=True)
+    cd.close()
+
+
 def run_tti_case(args):
     """Bare 3D TTI time steps on the 600x600x400 (+40 sponge) medium at
     12.5 m, dt 0.8 ms (tti_model): updates/s and the two kernels' roofline
@@ -731,7 +764,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--case", default="full", choices=["full", "small", "traffic", "rtm-learned", "rtm-methods", "fd2d", "rtm2d",
-                                                      "tti", "tti-rtm"],
+                                                      "tti", "tti-rtm", "codec"],
                     help="small / traffic: ncu profiling cases; rtm-learned: the learned-codec RTM comparison")
     ap.add_argument("--grid", type=int, default=None, help="small (192 by default), tti (600x600x400 by "
                                                            "default): cube edge, for profiling cases")
@@ -748,6 +781,9 @@ def main():
     args = ap.parse_args()
     if args.case == "fd2d":
         run_fd2d_case(args)
+        return
+    if args.case == "codec":
+        run_codec_case(args)
         return
     if args.shots is None:
         args.shots = {"rtm2d": 128, "tti-rtm": 8}.get(args.case, 1)

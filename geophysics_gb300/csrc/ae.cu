@@ -2,15 +2,19 @@
 //
 // Inference (snapshot encode in the forward pass of RTM, decode + imaging in
 // the backward pass):
-//   k_ae_e1      gather one 16^3 block of the wavefield into Morton order,
+//   k_ae_e1_vol  gather one 16^3 block of the wavefield into Morton order,
 //                scale by its max |value|, level E1 (8 -> 16) on CUDA cores;
 //   tc_gemm x3   E2, E3, E4 on tcgen05 (the last one writes the bf16 code);
 //   tc_gemm x3   D4, D3, D2 on tcgen05;
-//   k_ae_d1      level D1 (16 -> 8), unscale, scatter back to the field order
+//   k_ae_d1_vol  level D1 (16 -> 8), unscale, scatter back to the field order
 //                and either store the snapshot or add its product with the
-//                receiver wavefield to the image.
+//                receiver wavefield to the image (or, for the escape check,
+//                compare it with the field).
+// The snapshot kernels take E1's and D1's weights by value (a host copy kept
+// per weight version), so every weight is an operand of its multiply-add.
 // Training (one CUDA graph per iteration): the same forward on blocks drawn
-// from a store of solver snapshots, the loss and the D1 backward fused into
+// from a store of solver snapshots (k_ae_e1, weights read from the device
+// copy that Adam updates inside the graph), the loss and the D1 backward in
 // k_ae_d1, per level the weight gradient (k_ae_wgrad, CUDA cores, fp32), the
 // bias gradient (k_ae_colsum) and the input gradient (tc_gemm against the
 // transposed weights, the activation derivative fused as a gate), E1's
@@ -71,9 +75,49 @@ static AeOffsets ae_offsets() {
     return o;
 }
 
+// Weights of the two CUDA-core levels, passed by value to the snapshot
+// kernels (the host keeps a copy of the current ones).
+struct AeSmallW {
+    float w1[128], b1[16];   // E1: W [16 x 8] (bf16 values), b [16]
+    float v1[128], c1[8];    // D1: W [8 x 16] (bf16 values), b [8]
+};
+
+// E1 of one level-1 node: h = leaky(W1 x + b1) as 16 bf16 (32 bytes).
+__device__ __forceinline__ void e1_node(const float *w1, const float *b1, const float *x8, __nv_bfloat16 *out) {
+    uint4 q[2];
+    __nv_bfloat16 *qb = reinterpret_cast<__nv_bfloat16 *>(q);
+#pragma unroll
+    for (int c = 0; c < 16; c++) {
+        float acc = 0.0f;
+#pragma unroll
+        for (int j = 0; j < 8; j++) acc = __fmaf_rn(w1[c * 8 + j], x8[j], acc);
+        acc += b1[c];
+        qb[c] = __float2bfloat16_rn(leaky_d(acc));
+    }
+    uint4 *dst = reinterpret_cast<uint4 *>(out);
+    dst[0] = q[0];
+    dst[1] = q[1];
+}
+
+// D1 of one level-1 node: y = V1 g + c1 from its 16 bf16 inputs.
+__device__ __forceinline__ void d1_node(const float *v1, const float *c1, const __nv_bfloat16 *in, float *g,
+                                        float *y) {
+    const uint4 *src = reinterpret_cast<const uint4 *>(in);
+    uint4 q[2] = {src[0], src[1]};
+    const __nv_bfloat16 *qb = reinterpret_cast<const __nv_bfloat16 *>(q);
+#pragma unroll
+    for (int j = 0; j < 16; j++) g[j] = __bfloat162float(qb[j]);
+#pragma unroll
+    for (int c = 0; c < 8; c++) {
+        float acc = 0.0f;
+#pragma unroll
+        for (int j = 0; j < 16; j++) acc = __fmaf_rn(v1[c * 16 + j], g[j], acc);
+        y[c] = acc + c1[c];
+    }
+}
+
 // ---------------------------------------------------------------- kernels
 struct E1Args {
-    AeVolume vol;                 // volume mode when vol.src
     const float *direct;          // given blocks (Morton, nb x 4096), or null
     const float *store;           // training store (Morton), sampled by hash
     long nstore;
@@ -105,31 +149,14 @@ __device__ __forceinline__ float block_max(float v, float *red) {
     return m;
 }
 
+// E1 on blocks given in Morton order (evaluation) or drawn from the training
+// store: scale by the block max, W1 x + b1, leaky ReLU, bf16 out.
 __global__ void __launch_bounds__(256) k_ae_e1(const E1Args a) {
     __shared__ float xs[kAePts];
     __shared__ float red[8];
     const int b = blockIdx.x, t = threadIdx.x;
     float mx = 0.0f;
-    if (b < a.nb && a.vol.src) {
-        const AeVolume &v = a.vol;
-        const int bz = b % v.nbz, bx = (b / v.nbz) % v.nbx, by = b / (v.nbz * v.nbx);
-        // all sixteen loads of the thread in flight before the first use
-        float vals[16];
-#pragma unroll
-        for (int p = 0; p < 16; p++) {
-            const int idx = p * 256 + t, z = idx & 15, x = (idx >> 4) & 15, y = idx >> 8;
-            const int iz = bz * 16 + z, ix = bx * 16 + x, iy = by * 16 + y;
-            vals[p] = 0.0f;
-            if (iz < v.nz && ix < v.nx && iy < v.ny)
-                vals[p] = __ldg(v.src + (long)(v.oz + iz) + v.ldz * (v.ox + ix) + v.sxy * (v.oy + iy));
-        }
-#pragma unroll
-        for (int p = 0; p < 16; p++) {
-            const int idx = p * 256 + t;
-            xs[morton_of(idx & 15, (idx >> 4) & 15, idx >> 8)] = vals[p];
-            mx = fmaxf(mx, fabsf(vals[p]));
-        }
-    } else if (b < a.nb) {
+    if (b < a.nb) {
         const float *src;
         if (a.direct) {
             src = a.direct + (long)b * kAePts;
@@ -165,89 +192,93 @@ __global__ void __launch_bounds__(256) k_ae_e1(const E1Args a) {
             if (a.xn) a.xn[(long)b * kAePts + p * 8 + j] = xv;
             x8[j] = bf16r(xv);
         }
-        uint4 q[2];
-        __nv_bfloat16 *qb = reinterpret_cast<__nv_bfloat16 *>(q);
+        e1_node(a.w1, a.b1, x8, a.h1 + ((long)b * 512 + p) * 16);
+    }
+}
+
+// Interior-box gather of a snapshot, E1 with the weights passed by value
+// (each weight a constant-bank operand of its multiply-add, no load).
+// Thread t owns depth z = t & 15 of row x = t >> 4 of the block on all
+// sixteen planes y, so its Morton slot is fixed up to the y bits.
+struct E1Vol {
+    AeVolume vol;
+    int nb;
+    __nv_bfloat16 *h1;            // [nbp*512 x 16]
+    float *scale;                 // [nbp]
+    AeSmallW w;
+};
+
+__global__ void __launch_bounds__(256) k_ae_e1_vol(const E1Vol a) {
+    __shared__ float xs[kAePts];
+    __shared__ float red[8];
+    const int b = blockIdx.x, t = threadIdx.x;
+    float mx = 0.0f;
+    if (b < a.nb) {
+        const AeVolume &v = a.vol;
+        const int bz = b % v.nbz, bx = (b / v.nbz) % v.nbx, by = b / (v.nbz * v.nbx);
+        const int z = t & 15, x = t >> 4, iz = bz * 16 + z, ix = bx * 16 + x, iy0 = by * 16;
+        const bool zx = iz < v.nz && ix < v.nx;
+        const float *col = v.src + (long)(v.oz + iz) + v.ldz * (v.ox + ix) + v.sxy * (v.oy + iy0);
+        // all sixteen loads in flight before the first use
+        float vals[16];
 #pragma unroll
-        for (int c = 0; c < 16; c++) {
-            float acc = 0.0f;
+        for (int y = 0; y < 16; y++) vals[y] = zx && iy0 + y < v.ny ? __ldg(col + v.sxy * y) : 0.0f;
+        const int m = morton_of(z, x, 0);
 #pragma unroll
-            for (int j = 0; j < 8; j++) acc += a.w1[c * 8 + j] * x8[j];
-            acc += a.b1[c];
-            qb[c] = __float2bfloat16_rn(leaky_d(acc));
+        for (int y = 0; y < 16; y++) {
+            xs[m + morton_of(0, 0, y)] = vals[y];
+            mx = fmaxf(mx, fabsf(vals[y]));
         }
-        uint4 *dst = reinterpret_cast<uint4 *>(a.h1 + ((long)b * 512 + p) * 16);
-        dst[0] = q[0];
-        dst[1] = q[1];
+    } else {
+        for (int p = 0; p < 16; p++) xs[p * 256 + t] = 0.0f;
+    }
+    const float s = block_max(mx, red);
+    const float inv = s >= kAeTiny ? 1.0f / s : 0.0f;
+    if (t == 0) a.scale[b] = s >= kAeTiny ? s : 0.0f;
+#pragma unroll
+    for (int r = 0; r < 2; r++) {
+        const int p = t + 256 * r;
+        float x8[8];
+#pragma unroll
+        for (int j = 0; j < 8; j++) x8[j] = bf16r(xs[p * 8 + j] * inv);
+        e1_node(a.w.w1, a.w.b1, x8, a.h1 + ((long)b * 512 + p) * 16);
     }
 }
 
 struct D1Args {
-    AeVolume vol;                 // geometry of the output / receiver field
-    int nb, mode;                 // 0 store the snapshot in vol (as dst), 1 image, 2 train,
-                                  // 3 escape check against the field vol.src
+    int nb;
     const __nv_bfloat16 *g1;      // [nbp*512 x 16]
     const float *v1, *c1;         // D1: W [8 x 16] (bf16 values), b [8]
-    const float *scale;           // [nbp]
-    float *dst;                   // mode 0: field with vol's strides
-    const float *gP;              // mode 1: receiver field (vol's strides)
-    float *mig;                   // mode 1: image, iz + nz*(ix + nx*iy)
-    float wimg;                   // mode 1: weight of this snapshot
-    const float *xn;              // mode 2: normalized target
-    float *recon;                 // mode 2: normalized reconstruction, or null
-    __nv_bfloat16 *dg1;           // mode 2: gradient at D2's output (gated)
-    float *gd1;                   // mode 2: D1 gradient (W then b, 136 floats)
-    double *loss;                 // mode 2: sum of squared errors, slot *step - step0
+    const float *xn;              // normalized target
+    float *recon;                 // normalized reconstruction, or null
+    __nv_bfloat16 *dg1;           // gradient at D2's output (gated)
+    float *gd1;                   // D1 gradient (W then b, 136 floats)
+    double *loss;                 // sum of squared errors, slot *step - step0
     const int *step;
     int step0;
-    const float *wrow;            // mode 2: block weights (null: all 1)
-    const float *wsum;            // mode 2: batch weight sum slot base (null: block count)
-    const int *esc;               // modes 0/1: escaped-block slot per row (-1: none), or null
-    const __nv_bfloat16 *res;     // modes 0/1: residual pool (4096 per slot, natural order)
-    __nv_bfloat16 *resall;        // mode 3: residual of every row (natural order)
-    float *err2, *norm2;          // mode 3: per-row squared error and squared norm
+    const float *wrow;            // block weights (null: all 1)
+    const float *wsum;            // batch weight sum slot base (null: block count)
 };
 
+// D1 in training / evaluation: reconstruction, weighted loss, D1's weight
+// and bias gradients and the gated gradient at D2's output.
+// loss = sum_b w_b |e_b|^2 / (W * 4096), W = sum_b w_b.
 __global__ void __launch_bounds__(256) k_ae_d1(const D1Args a) {
-    __shared__ float ys[kAePts];
     __shared__ float sg[136];
     __shared__ float red[8];
     const int b = blockIdx.x, t = threadIdx.x;
     if (b >= a.nb) return;
-    if (a.mode == 2) {
-        for (int i = t; i < 136; i += 256) sg[i] = 0.0f;
-        __syncthreads();
-    }
-    const float s = a.scale[b];
+    for (int i = t; i < 136; i += 256) sg[i] = 0.0f;
+    __syncthreads();
     float lsum = 0.0f;
-    // mode 2: loss = sum_b w_b |e_b|^2 / (W * 4096), W = sum_b w_b
-    float wb = 1.0f, gsc = 0.0f;
-    if (a.mode == 2) {
-        const float W = a.wsum ? a.wsum[*a.step - a.step0] : (float)gridDim.x;
-        wb = a.wrow ? a.wrow[b] : 1.0f;
-        gsc = wb / (W * (float)kAePts);
-    }
+    const float W = a.wsum ? a.wsum[*a.step - a.step0] : (float)gridDim.x;
+    const float wb = a.wrow ? a.wrow[b] : 1.0f;
+    const float gsc = wb / (W * (float)kAePts);
 #pragma unroll 1
     for (int r = 0; r < 2; r++) {
         const int p = t + 256 * r;
-        const uint4 *src = reinterpret_cast<const uint4 *>(a.g1 + ((long)b * 512 + p) * 16);
-        uint4 q[2] = {src[0], src[1]};
-        const __nv_bfloat16 *qb = reinterpret_cast<const __nv_bfloat16 *>(q);
-        float g[16];
-#pragma unroll
-        for (int j = 0; j < 16; j++) g[j] = __bfloat162float(qb[j]);
-        float y[8];
-#pragma unroll
-        for (int c = 0; c < 8; c++) {
-            float acc = 0.0f;
-#pragma unroll
-            for (int j = 0; j < 16; j++) acc += a.v1[c * 16 + j] * g[j];
-            y[c] = acc + a.c1[c];
-        }
-        if (a.mode != 2) {
-#pragma unroll
-            for (int c = 0; c < 8; c++) ys[p * 8 + c] = y[c] * s;
-            continue;
-        }
+        float g[16], y[8];
+        d1_node(a.v1, a.c1, a.g1 + ((long)b * 512 + p) * 16, g, y);
         float dy[8];
 #pragma unroll
         for (int c = 0; c < 8; c++) {
@@ -276,44 +307,81 @@ __global__ void __launch_bounds__(256) k_ae_d1(const D1Args a) {
         dst[0] = o4[0];
         dst[1] = o4[1];
     }
-    if (a.mode == 2) {
 #pragma unroll
-        for (int o = 16; o; o >>= 1) lsum += __shfl_xor_sync(0xffffffffu, lsum, o);
-        if ((t & 31) == 0) red[t >> 5] = lsum;
-        __syncthreads();
-        if (t == 0) {
-            double tot = 0.0;
-            for (int w = 0; w < 8; w++) tot += red[w];
-            const double W = a.wsum ? (double)a.wsum[*a.step - a.step0] : (double)gridDim.x;
-            atomicAdd(a.loss + (*a.step - a.step0), tot * wb / W);
-        }
-        for (int i = t; i < 136; i += 256) atomicAdd(&a.gd1[i], sg[i]);
-        return;
+    for (int o = 16; o; o >>= 1) lsum += __shfl_xor_sync(0xffffffffu, lsum, o);
+    if ((t & 31) == 0) red[t >> 5] = lsum;
+    __syncthreads();
+    if (t == 0) {
+        double tot = 0.0;
+        for (int w = 0; w < 8; w++) tot += red[w];
+        const double Wd = a.wsum ? (double)a.wsum[*a.step - a.step0] : (double)gridDim.x;
+        atomicAdd(a.loss + (*a.step - a.step0), tot * wb / Wd);
+    }
+    for (int i = t; i < 136; i += 256) atomicAdd(&a.gd1[i], sg[i]);
+}
+
+// D1 of a snapshot's blocks with the weights passed by value, unscaled and
+// scattered to the interior box: mode 0 stores the snapshot (dst, the box's
+// strides), mode 1 adds wimg * snapshot * gP to the image, mode 3 compares
+// with the field vol.src and keeps every block's residual (bf16, natural
+// order) and its squared error and norm (the escape check).  Escaped blocks
+// (esc) add their residual in modes 0 and 1.  Thread t owns depth
+// z = t & 15 of row x = t >> 4 on all sixteen planes, as in k_ae_e1_vol.
+struct D1Vol {
+    AeVolume vol;
+    int nb, mode;
+    const __nv_bfloat16 *g1;      // [nbp*512 x 16]
+    const float *scale;           // [nbp]
+    float *dst;                   // mode 0
+    const float *gP;              // mode 1: receiver field (vol's strides)
+    float *mig;                   // mode 1: image, iz + nz*(ix + nx*iy)
+    float wimg;                   // mode 1: weight of this snapshot
+    const int *esc;               // modes 0/1: escaped-block slot per row (-1: none), or null
+    const __nv_bfloat16 *res;     // modes 0/1: residual pool (4096 per slot, natural order)
+    __nv_bfloat16 *resall;        // mode 3: residual of every row (natural order)
+    float *err2, *norm2;          // mode 3: per-row squared error and squared norm
+    AeSmallW w;
+};
+
+__global__ void __launch_bounds__(256) k_ae_d1_vol(const D1Vol a) {
+    __shared__ float ys[kAePts];
+    __shared__ float red2[2][8];
+    const int b = blockIdx.x, t = threadIdx.x;
+    if (b >= a.nb) return;
+    const float s = a.scale[b];
+#pragma unroll
+    for (int r = 0; r < 2; r++) {
+        const int p = t + 256 * r;
+        float g[16], y[8];
+        d1_node(a.w.v1, a.w.c1, a.g1 + ((long)b * 512 + p) * 16, g, y);
+#pragma unroll
+        for (int c = 0; c < 8; c++) ys[p * 8 + c] = y[c] * s;
     }
     __syncthreads();
     const AeVolume &v = a.vol;
     const int bz = b % v.nbz, bx = (b / v.nbz) % v.nbx, by = b / (v.nbz * v.nbx);
+    const int z = t & 15, x = t >> 4, iz = bz * 16 + z, ix = bx * 16 + x, iy0 = by * 16;
+    const bool zx = iz < v.nz && ix < v.nx;
+    const long col = (long)(v.oz + iz) + v.ldz * (v.ox + ix) + v.sxy * (v.oy + iy0);
+    const int m = morton_of(z, x, 0);
     if (a.mode == 3) {
         float e2 = 0.0f, x2 = 0.0f;
         __nv_bfloat16 *rb = a.resall + (long)b * kAePts;
-#pragma unroll 4
-        for (int p = 0; p < 16; p++) {
-            const int idx = p * 256 + t, z = idx & 15, x = (idx >> 4) & 15, y = idx >> 8;
-            const int iz = bz * 16 + z, ix = bx * 16 + x, iy = by * 16 + y;
-            float val = 0.0f;
-            if (iz < v.nz && ix < v.nx && iy < v.ny)
-                val = v.src[(long)(v.oz + iz) + v.ldz * (v.ox + ix) + v.sxy * (v.oy + iy)];
-            const float d = val - ys[morton_of(z, x, y)];
-            rb[idx] = __float2bfloat16_rn(d);
+        float vals[16];
+#pragma unroll
+        for (int y = 0; y < 16; y++) vals[y] = zx && iy0 + y < v.ny ? __ldg(v.src + col + v.sxy * y) : 0.0f;
+#pragma unroll
+        for (int y = 0; y < 16; y++) {
+            const float d = vals[y] - ys[m + morton_of(0, 0, y)];
+            rb[y * 256 + t] = __float2bfloat16_rn(d);
             e2 += d * d;
-            x2 += val * val;
+            x2 += vals[y] * vals[y];
         }
 #pragma unroll
         for (int o = 16; o; o >>= 1) {
             e2 += __shfl_xor_sync(0xffffffffu, e2, o);
             x2 += __shfl_xor_sync(0xffffffffu, x2, o);
         }
-        __shared__ float red2[2][8];
         if ((t & 31) == 0) {
             red2[0][t >> 5] = e2;
             red2[1][t >> 5] = x2;
@@ -330,22 +398,34 @@ __global__ void __launch_bounds__(256) k_ae_d1(const D1Args a) {
         }
         return;
     }
+    if (!zx) return;
     const int slot = a.esc ? a.esc[b] : -1;
     const __nv_bfloat16 *res = slot >= 0 ? a.res + (long)slot * kAePts : nullptr;
-#pragma unroll 8
-    for (int p = 0; p < 16; p++) {
-        const int idx = p * 256 + t, z = idx & 15, x = (idx >> 4) & 15, y = idx >> 8;
-        const int iz = bz * 16 + z, ix = bx * 16 + x, iy = by * 16 + y;
-        if (iz >= v.nz || ix >= v.nx || iy >= v.ny) continue;
-        float val = ys[morton_of(z, x, y)];
-        if (res) val += __bfloat162float(res[idx]);   // escaped block: decoded + residual
-        const long id = (long)(v.oz + iz) + v.ldz * (v.ox + ix) + v.sxy * (v.oy + iy);
-        if (a.mode == 0) {
-            a.dst[id] = val;
-        } else {
-            const long o = iz + (long)v.nz * (ix + (long)v.nx * iy);
-            a.mig[o] = a.mig[o] + a.wimg * val * a.gP[id];
+    if (a.mode == 0) {
+#pragma unroll
+        for (int y = 0; y < 16; y++) {
+            if (iy0 + y >= v.ny) break;
+            float val = ys[m + morton_of(0, 0, y)];
+            if (res) val += __bfloat162float(res[y * 256 + t]);   // escaped block: decoded + residual
+            a.dst[col + v.sxy * y] = val;
         }
+        return;
+    }
+    // mode 1: all image and receiver-field loads in flight first
+    const long o0 = iz + (long)v.nz * (ix + (long)v.nx * iy0), so = (long)v.nz * v.nx;
+    float gp[16], mg[16];
+#pragma unroll
+    for (int y = 0; y < 16; y++) {
+        const bool in = iy0 + y < v.ny;
+        gp[y] = in ? __ldg(a.gP + col + v.sxy * y) : 0.0f;
+        mg[y] = in ? a.mig[o0 + so * y] : 0.0f;
+    }
+#pragma unroll
+    for (int y = 0; y < 16; y++) {
+        if (iy0 + y >= v.ny) break;
+        float val = ys[m + morton_of(0, 0, y)];
+        if (res) val += __bfloat162float(res[y * 256 + t]);
+        a.mig[o0 + so * y] = mg[y] + a.wimg * val * gp[y];
     }
 }
 
@@ -589,6 +669,10 @@ struct geo_ae {
     DevBuf resall, err2, norm2;
     int erows = 0;
     long long st_blocks = 0, st_escaped = 0;   // totals over RTM shots
+    // host copy of the CUDA-core levels' weights for the snapshot kernels:
+    // wver counts weight updates (packs), hver the version copied
+    geo::AeSmallW hw{};
+    long wver = 1, hver = 0;
 };
 
 namespace geo {
@@ -609,6 +693,7 @@ static int ae_pack(geo_ae *ae, int inc, cudaStream_t s) {
     }
     a.step = ae->step.as<int>();
     a.inc = inc;
+    ae->wver++;
     k_ae_pack<<<152 * 4, 256, 0, s>>>(a);
     return check_launch("ae_pack");
 }
@@ -728,16 +813,29 @@ static E1Args e1_args(geo_ae *ae, int nb) {
     return a;
 }
 
-static D1Args d1_args(geo_ae *ae, int nb, int mode) {
+static D1Args d1_args(geo_ae *ae, int nb) {
     D1Args a{};
     a.nb = nb;
-    a.mode = mode;
     a.g1 = bf(ae->g1);
     a.v1 = ae->small.as<float>() + 128;
     a.c1 = ae->params.as<float>() + ae->off.b[7];
-    a.scale = ae->scale.as<float>();
     a.step = ae->step.as<int>();
     return a;
+}
+
+// The host copy of the E1/D1 weights, refreshed when a pack changed them
+// (a 1 KB read and a wait on the stream, once per weight version).
+static int ae_mirror(geo_ae *ae, cudaStream_t s) {
+    if (ae->hver == ae->wver) return GEO_OK;
+    AeSmallW &h = ae->hw;
+    const float *sm = ae->small.as<float>(), *pr = ae->params.as<float>();
+    GEO_CUDA(cudaMemcpyAsync(h.w1, sm, sizeof h.w1, cudaMemcpyDeviceToHost, s));
+    GEO_CUDA(cudaMemcpyAsync(h.v1, sm + 128, sizeof h.v1, cudaMemcpyDeviceToHost, s));
+    GEO_CUDA(cudaMemcpyAsync(h.b1, pr + ae->off.b[0], sizeof h.b1, cudaMemcpyDeviceToHost, s));
+    GEO_CUDA(cudaMemcpyAsync(h.c1, pr + ae->off.b[7], sizeof h.c1, cudaMemcpyDeviceToHost, s));
+    GEO_CUDA(cudaStreamSynchronize(s));
+    ae->hver = ae->wver;
+    return GEO_OK;
 }
 
 int ae_check_err(geo_ae *ae, cudaStream_t s) {
@@ -777,10 +875,14 @@ int ae_encode_volume(geo_ae *ae, const AeVolume &v, void *code, float *scale, in
                      cudaStream_t s) {
     const int nb = blocks_of(v), rows = pad128(nb);
     GEO_TRY(ensure_rows(ae, rows));
-    E1Args a = e1_args(ae, nb);
+    GEO_TRY(ae_mirror(ae, s));
+    E1Vol a{};
     a.vol = v;
+    a.nb = nb;
+    a.h1 = bf(ae->h1);
     a.scale = scale;
-    k_ae_e1<<<rows, 256, 0, s>>>(a);
+    a.w = ae->hw;
+    k_ae_e1_vol<<<rows, 256, 0, s>>>(a);
     GEO_TRY(check_launch("ae_e1"));
     GEO_TRY(encode_rows(ae, rows, static_cast<__nv_bfloat16 *>(code), s));
     if (!esc) return GEO_OK;
@@ -796,13 +898,17 @@ int ae_encode_volume(geo_ae *ae, const AeVolume &v, void *code, float *scale, in
         ae->erows = rows;
     }
     GEO_TRY(decode_rows(ae, rows, static_cast<const __nv_bfloat16 *>(code), s));
-    D1Args c = d1_args(ae, nb, 3);
+    D1Vol c{};
     c.vol = v;
+    c.nb = nb;
+    c.mode = 3;
+    c.g1 = bf(ae->g1);
     c.scale = scale;
     c.resall = bf(ae->resall);
     c.err2 = ae->err2.as<float>();
     c.norm2 = ae->norm2.as<float>();
-    k_ae_d1<<<rows, 256, 0, s>>>(c);
+    c.w = ae->hw;
+    k_ae_d1_vol<<<rows, 256, 0, s>>>(c);
     GEO_TRY(check_launch("ae_check"));
     k_ae_select<<<1, 1024, 0, s>>>(ae->err2.as<float>(), ae->norm2.as<float>(), nb, ae->tau * ae->tau,
                                    ae_escape_cap(ae, v), esc, count);
@@ -819,8 +925,12 @@ int ae_decode_volume(geo_ae *ae, const AeVolume &v, const void *code, const floa
     const int nb = blocks_of(v), rows = pad128(nb);
     GEO_TRY(ensure_rows(ae, rows));
     GEO_TRY(decode_rows(ae, rows, static_cast<const __nv_bfloat16 *>(code), s));
-    D1Args a = d1_args(ae, nb, mode);
+    GEO_TRY(ae_mirror(ae, s));
+    D1Vol a{};
     a.vol = v;
+    a.nb = nb;
+    a.mode = mode;
+    a.g1 = bf(ae->g1);
     a.scale = scale;
     a.dst = dst;
     a.gP = gP;
@@ -828,7 +938,8 @@ int ae_decode_volume(geo_ae *ae, const AeVolume &v, const void *code, const floa
     a.wimg = w;
     a.esc = esc;
     a.res = static_cast<const __nv_bfloat16 *>(res);
-    k_ae_d1<<<rows, 256, 0, s>>>(a);
+    a.w = ae->hw;
+    k_ae_d1_vol<<<rows, 256, 0, s>>>(a);
     return check_launch("ae_d1");
 }
 
@@ -838,7 +949,7 @@ static int train_pass(geo_ae *ae, int rows, double *loss, const float *wsum, int
                       cudaStream_t s) {
     GEO_TRY(encode_rows(ae, rows, bf(ae->z), s));
     GEO_TRY(decode_rows(ae, rows, bf(ae->z), s));
-    D1Args a = d1_args(ae, rows, 2);
+    D1Args a = d1_args(ae, rows);
     a.xn = ae->xn.as<float>();
     a.recon = recon;
     a.dg1 = bf(ae->dg1);
@@ -1119,6 +1230,7 @@ extern "C" int geo_ae_train(geo_ae *ae, int iters, int batch, float lr, float *l
         cudaGraphExecDestroy(exec);
         if (ce != cudaSuccess) return fail(GEO_ERR_CUDA, "graph launch: %s", cudaGetErrorString(ce));
     }
+    ae->wver++;   // the graph's packs changed the weights
     GEO_TRY(ae_check_err(ae, s));
     std::vector<double> l(iters);
     GEO_CUDA(cudaMemcpyAsync(l.data(), dloss.p, (size_t)iters * 8, cudaMemcpyDeviceToHost, s));
