@@ -47,7 +47,10 @@ __host__ __device__ inline unsigned long long splitmix(unsigned long long x) {
 }
 
 __device__ __forceinline__ float bf16r(float v) { return __bfloat162float(__float2bfloat16_rn(v)); }
-__device__ __forceinline__ float leaky_d(float v) { return v > 0.0f ? v : kLeak * v; }
+// leaky ReLU as max(v, kLeak v): the same value as v > 0 ? v : kLeak v for
+// 0 < kLeak < 1 (signed zeros, infinities and NaN included), one
+// instruction fewer
+__device__ __forceinline__ float leaky_d(float v) { return fmaxf(v, kLeak * v); }
 
 // ---------------------------------------------------------------- layout
 struct AeOffsets {
@@ -86,14 +89,18 @@ struct AeSmallW {
 __device__ __forceinline__ void e1_node(const float *w1, const float *b1, const float *x8, __nv_bfloat16 *out) {
     uint4 q[2];
     __nv_bfloat16 *qb = reinterpret_cast<__nv_bfloat16 *>(q);
+    float h[16];
 #pragma unroll
     for (int c = 0; c < 16; c++) {
         float acc = 0.0f;
 #pragma unroll
         for (int j = 0; j < 8; j++) acc = __fmaf_rn(w1[c * 8 + j], x8[j], acc);
-        acc += b1[c];
-        qb[c] = __float2bfloat16_rn(leaky_d(acc));
+        h[c] = leaky_d(acc + b1[c]);
     }
+    // two channels per conversion (low half = even channel)
+    __nv_bfloat162 *q2 = reinterpret_cast<__nv_bfloat162 *>(qb);
+#pragma unroll
+    for (int c = 0; c < 8; c++) q2[c] = __floats2bfloat162_rn(h[2 * c], h[2 * c + 1]);
     uint4 *dst = reinterpret_cast<uint4 *>(out);
     dst[0] = q[0];
     dst[1] = q[1];

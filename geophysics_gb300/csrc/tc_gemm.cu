@@ -10,7 +10,8 @@
 //                  producer, a final commit signals the epilogue;
 //   all 4 warps    epilogue: warp w reads TMEM lanes 32w..32w+31 (rows) with
 //                  tcgen05.ld, adds the bias, applies the activation or the
-//                  activation-derivative gate, and stores fp32 or bf16.
+//                  activation-derivative gate, and stores fp32, or bf16
+//                  staged in the freed ring and written back as whole rows.
 // Every wait is bounded (2 s): on timeout the CTA sets the error word, lets
 // its copies in flight land (bounded), frees its TMEM and returns.
 #include "geo_internal.h"
@@ -41,7 +42,10 @@ struct GemmShape {
     static constexpr int kStage = kA + kB;
     static constexpr int kStages = ST;
     static constexpr uint32_t kCols = BN < 32 ? 32 : BN;
-    static constexpr size_t kRing = (size_t)kStages * kStage + 1024 + 256;
+    // the ring, reused after the last MMA as the bf16 output tile
+    static constexpr size_t kOut = (size_t)kGM * BN * 2;
+    static constexpr size_t kData = (size_t)kStages * kStage > kOut ? (size_t)kStages * kStage : kOut;
+    static constexpr size_t kRing = kData + 1024 + 256;
     // fewest bytes with which at most 512 / kCols CTAs fit on an SM
     static constexpr size_t kFloor = kSmSmem / (512 / kCols + 1) + 1 - kCtaReserve;
     static constexpr size_t kSmem = kRing > kFloor ? kRing : kFloor;
@@ -52,7 +56,8 @@ struct GemmShape {
     static_assert((kSmSmem / (kSmem + kCtaReserve)) * kCols <= 512, "resident CTAs' accumulators fit in TMEM");
 };
 
-__device__ __forceinline__ float leaky(float v) { return v > 0.0f ? v : kLeak * v; }
+// max(v, kLeak v) = (v > 0 ? v : kLeak v) for 0 < kLeak < 1, one instruction fewer
+__device__ __forceinline__ float leaky(float v) { return fmaxf(v, kLeak * v); }
 
 template <int BN, int ST>
 __global__ void __launch_bounds__(128, 2)
@@ -61,13 +66,15 @@ __global__ void __launch_bounds__(128, 2)
     extern __shared__ unsigned char smem_raw[];
     uint8_t *sm = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     constexpr int kGStages = S::kStages;
-    uint64_t *full = reinterpret_cast<uint64_t *>(sm + kGStages * S::kStage);
+    uint64_t *full = reinterpret_cast<uint64_t *>(sm + S::kData);
     uint64_t *empty = full + kGStages;
     uint64_t *done = empty + kGStages;
     uint32_t *tslot = reinterpret_cast<uint32_t *>(done + 1);
     __shared__ int s_abort;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int m0 = blockIdx.x * kGM, n0 = blockIdx.y * BN;
+    // consecutive CTAs share a row tile of A (its second and later reads hit L2)
+    const int ntn = g.N / BN;
+    const int m0 = (int)(blockIdx.x / ntn) * kGM, n0 = (int)(blockIdx.x % ntn) * BN;
     const int nk = g.K / kGK;
 
     if (threadIdx.x == 0) {
@@ -125,11 +132,17 @@ __global__ void __launch_bounds__(128, 2)
     }
     __syncwarp();
 
-    // epilogue
+    // epilogue.  bf16 output goes through shared memory (the ring is free
+    // once every MMA has completed): each warp stages its 32 rows with the
+    // 16-byte chunks of a row XOR-swizzled by the row (conflict-free in both
+    // directions), then writes them back as whole rows, consecutive lanes on
+    // consecutive 16-byte chunks.
     if (!mbar_wait(done, 0)) s_abort = 1;
     tc_fence_after();
     const int row = m0 + warp * 32 + lane;
     const bool ok = !*(volatile int *)&s_abort;
+    uint4 *stg = reinterpret_cast<uint4 *>(sm + (size_t)warp * 32 * BN * 2);
+    constexpr int CPR = BN / 8;   // 16-byte chunks per output row
 #pragma unroll 1
     for (int c0 = 0; c0 < BN; c0 += 16) {
         uint32_t r[16];
@@ -161,12 +174,21 @@ __global__ void __launch_bounds__(128, 2)
             for (int j = 0; j < 4; j++) op[j] = make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
         } else {
             uint4 q[2];
-            __nv_bfloat16 *qb = reinterpret_cast<__nv_bfloat16 *>(q);
+            __nv_bfloat162 *q2 = reinterpret_cast<__nv_bfloat162 *>(q);
 #pragma unroll
-            for (int j = 0; j < 16; j++) qb[j] = __float2bfloat16_rn(v[j]);
-            uint4 *op = reinterpret_cast<uint4 *>(static_cast<__nv_bfloat16 *>(g.out) + o);
-            op[0] = q[0];
-            op[1] = q[1];
+            for (int j = 0; j < 8; j++) q2[j] = __floats2bfloat162_rn(v[2 * j], v[2 * j + 1]);
+            const int q0 = c0 / 8;
+            stg[lane * CPR + (q0 ^ (lane & 7))] = q[0];
+            stg[lane * CPR + ((q0 + 1) ^ (lane & 7))] = q[1];
+        }
+    }
+    if (ok && !g.out_f32) {
+        __syncwarp();
+        __nv_bfloat16 *out = static_cast<__nv_bfloat16 *>(g.out) + (long)(m0 + warp * 32) * g.N + n0;
+#pragma unroll 4
+        for (int it = 0; it < CPR; it++) {
+            const int idx = it * 32 + lane, rl = idx / CPR, q = idx % CPR;
+            reinterpret_cast<uint4 *>(out + (long)rl * g.N)[q] = stg[rl * CPR + (q ^ (rl & 7))];
         }
     }
     tc_fence_before();
@@ -209,7 +231,7 @@ static int launch_bn(const TcGemm &g, cudaStream_t s) {
     CUtensorMap ta, tb;
     GEO_TRY(encode_bf16_2d(&ta, g.A, g.M, g.K, kGM));
     GEO_TRY(encode_bf16_2d(&tb, g.B, g.N, g.K, BN));
-    dim3 grid(g.M / kGM, g.N / BN);
+    const dim3 grid((unsigned)(g.M / kGM) * (unsigned)(g.N / BN));
     k_tc_gemm<BN, ST><<<grid, 128, S::kSmem, s>>>(ta, tb, g);
     return check_launch("tc_gemm");
 }

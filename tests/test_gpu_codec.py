@@ -9,8 +9,12 @@ from tests.util import random_model_3d, rel_l2, wave_blocks
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("M,N,K", [(128, 64, 64), (256, 128, 128), (384, 256, 512), (128, 512, 2048),
-                                   (256, 2048, 512)])
+# tile widths 64/128/256 with every stage count (stages = K/64 up to the
+# width's ring: 4/3/2), including one-slice tiles whose bf16 output tile is
+# larger than their ring
+@pytest.mark.parametrize("M,N,K", [(128, 64, 64), (128, 64, 128), (256, 64, 192), (128, 64, 256),
+                                   (128, 128, 64), (256, 128, 128), (128, 128, 192),
+                                   (256, 256, 64), (384, 256, 512), (128, 512, 2048), (256, 2048, 512)])
 def test_tc_gemm_matches_torch(geo, M, N, K):
     import torch
     g = torch.Generator(device="cpu").manual_seed(M + N + K)
