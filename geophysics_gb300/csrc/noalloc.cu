@@ -47,9 +47,8 @@ static float h_box[2 * kTB * kTB], h_taper[2 * kTB * kTB];
 static int h_mute[2 * kMaxN];
 static std::mutex g_host_mu;
 
-// Device address of the scratch array on the current device.  The first
-// call on a device resolves it; that first call must come before any stream
-// capture on that device.
+// Device address of the scratch array on the current device, resolved by the
+// first call on that device and kept.
 int scratch_address(void **out) {
     int dev = 0;
     GEO_CUDA(cudaGetDevice(&dev));

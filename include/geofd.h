@@ -122,10 +122,9 @@ int geo_fd2d_shot(const geo_fd2d_desc *desc, const float *v, const float *e, con
  *     library keeps until exit; larger shots fail with GEO_ERR_ARG;
  *   - CPU and GPU variants (SV taper and GPU-form mute included), no
  *     snapshots;
- *   - the first call on a device resolves the array's device address, so
- *     make that first call before any stream capture on that device;
- *   - the device address of the array is kept for the life of the
- *     process: do not call this on a device after cudaDeviceReset;
+ *   - the first call on a device resolves the array's device address,
+ *     which is kept for the life of the process: do not call this on a
+ *     device after cudaDeviceReset;
  *   - the host-side set-up is one fixed set of static arrays guarded by a
  *     mutex: calls from several host threads (on one or several devices)
  *     take turns for it;
