@@ -470,6 +470,49 @@ TTI_SHAPE, TTI_DX, TTI_DT, TTI_FAVG, TTI_NT = (600, 600, 400), 12.5, 0.0008, 12.
 TTI_BYTES_PER_PT = 104   # velocity kernel 12 floats (P,Q,u,v,w,4 trig in; u,v,w out), stress 14
 
 
+def run_prog2d_case(args):
+    """The 2D GPU programs at their own sizes, device buffers: the 2D TTI
+    forward shot at the TTI program's 600x300 (5 m, npml 50, 801 steps,
+    40 Hz, dt 0.5 ms, source (200, 140)) and one shot of each 2D GPU RTM
+    program on the TTI RTM program's 1700x601 (5 m, npml 50, 2000 of its
+    9001 steps, 20 Hz); seeded layered VTI media, tilt 25 +- 20 deg as a
+    smooth field.  Median wall time per call."""
+    import numpy as np
+    import torch
+
+    import geophysics_gb300 as geo
+    from geophysics_gb300 import build as B
+    from geophysics_gb300 import media
+    B.build()
+
+    def tilt(nx, nz):
+        x, z = np.meshgrid(np.arange(nx), np.arange(nz), indexing="ij")
+        return (25 + 20 * np.sin(x / 40.0) * np.cos(z / 30.0)).astype(np.float32)
+
+    def timed(fn, reps):
+        for _ in range(max(args.warmup, 1)):
+            fn()
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            fn()
+            torch.cuda.synchronize()
+            ts.append(time.perf_counter() - t0)
+        return 1000 * statistics.median(ts)
+
+    v, e, d = media.layered_vti(600, 300, seed=1)
+    t = [torch.from_numpy(a).cuda() for a in (v, e, d, tilt(600, 300))]
+    kw = dict(npd=50, nt=801, dx=5.0, dz=5.0, dt=5e-4, favg=40.0, fs=200, zs=140)
+    res = {"tti2d_shot_600x300_801_ms": timed(lambda: geo.tti2d_shot(*t, **kw), max(args.steps, 5))}
+    v, e, d = media.layered_vti(1700, 601, seed=2)
+    t = [torch.from_numpy(a).cuda() for a in (v, e, d, tilt(1700, 601))]
+    kr = dict(npml=50, nt=2000, dx=5.0, dz=5.0, dt=5e-4, favg=20.0, ns=1, fs=850, zs=1)
+    res["rtm2d_tti_1700x601_2000_ms"] = timed(lambda: geo.rtm2d_tti(*t, **kr), max(args.steps, 3))
+    res["rtm2d_gpu_1700x601_2000_ms"] = timed(lambda: geo.rtm2d_gpu(*t[:3], **kr), max(args.steps, 3))
+    print(json.dumps({"case": "prog2d", "unit": "ms", **res, "dtype": "f32", "data": "synthetic"}), flush=True)
+
+
 def run_codec_case(args):
     """The learned snapshot codec alone: encode + decode of one 512x512x384
     snapshot (24 576 blocks of 16^3, the 3D RTM comparison's grid) as
@@ -764,7 +807,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--case", default="full", choices=["full", "small", "traffic", "rtm-learned", "rtm-methods", "fd2d", "rtm2d",
-                                                      "tti", "tti-rtm", "codec"],
+                                                      "tti", "tti-rtm", "codec", "prog2d"],
                     help="small / traffic: ncu profiling cases; rtm-learned: the learned-codec RTM comparison")
     ap.add_argument("--grid", type=int, default=None, help="small (192 by default), tti (600x600x400 by "
                                                            "default): cube edge, for profiling cases")
@@ -784,6 +827,9 @@ def main():
         return
     if args.case == "codec":
         run_codec_case(args)
+        return
+    if args.case == "prog2d":
+        run_prog2d_case(args)
         return
     if args.shots is None:
         args.shots = {"rtm2d": 128, "tti-rtm": 8}.get(args.case, 1)

@@ -153,6 +153,19 @@ def test_rtm2d_gpu_program_thin_sponge_large_grid(geo, orc):
     assert np.array_equal(out["adcigs"], ag)
 
 
+@pytest.mark.parametrize("every", ["0", "7"])
+def test_rtm2d_gpu_program_independent_of_launch_segments(geo, orc, monkeypatch, every):
+    monkeypatch.setenv("GEO_WATCH_EVERY", every)
+    v, e, d = model(nx=80, nz=50)
+    kw = dict(GKW, ns=1, nt=130)
+    mig, ill, ag, shots = orc.rtm2d_gpu(v, e, d, **kw)
+    out = geo.rtm2d_gpu(v, e, d, **kw)
+    assert np.array_equal(out["shots"], shots)
+    assert np.array_equal(out["illum"], ill)
+    assert np.array_equal(out["mig_lap"], orc.laplace2d_adj(mig))
+    assert np.array_equal(out["adcigs"], ag)
+
+
 def test_rtm2d_gpu_program_stability_check(geo):
     v, e, d = model(nx=96, nz=60)
     with pytest.raises(geo.GeoError) as ei:

@@ -107,6 +107,25 @@ def test_rtm2d_tti_program_thin_sponge_large_grid(geo, orc):
     assert np.array_equal(out["adcigs"], ag), rel_l2(out["adcigs"], ag)
 
 
+@pytest.mark.parametrize("every", ["0", "7", "1"])
+def test_2d_programs_independent_of_launch_segments(geo, orc, monkeypatch, every):
+    """The persistent launches end at every watchdog scan (GEO_WATCH_EVERY
+    steps; 0: one launch per pass, 1: one launch per step), and a backward
+    launch opens with the ring restore and record injection of its first
+    step: the results are the oracle's whatever the segmentation."""
+    monkeypatch.setenv("GEO_WATCH_EVERY", every)
+    v, e, d, th = _model(nx=70, nz=50, seed=9)
+    kw = dict(TKW, ns=1, nt=120)
+    mig, ill, ag, shots = orc.rtm2d_tti(v, e, d, th, trig=cuda_trig(th), **kw)
+    out = geo.rtm2d_tti(v, e, d, th, **kw)
+    assert np.array_equal(out["shots"], shots)
+    assert np.array_equal(out["mig_lap"], orc.laplace2d_adj(mig))
+    assert np.array_equal(out["adcigs"], ag)
+    ref, rs = orc.tti2d(v, e, d, th, snap_every=9, trig=cuda_trig(th), **dict(KW, nt=100))
+    got, gs = geo.tti2d_shot(v, e, d, th, snap_every=9, **dict(KW, nt=100))
+    assert np.array_equal(got, ref) and np.array_equal(gs, rs)
+
+
 def test_rtm2d_tti_program_observed_shots_device(geo, orc):
     import torch
     v, e, d, th = _model(nx=80, nz=50, seed=6)
