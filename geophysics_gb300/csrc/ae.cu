@@ -436,7 +436,7 @@ __global__ void __launch_bounds__(256) k_ae_d1_vol(const D1Vol a) {
     }
 }
 
-// Escape pass 1 is k_ae_d1 in mode 3: decode, compare with the field, keep
+// Escape pass 1 is k_ae_d1_vol in mode 3: decode, compare with the field, keep
 // every block's residual (bf16, natural order) and its squared error and norm.
 
 // Escape pass 2 (one block of 1024 threads): the cap blocks with the
