@@ -472,20 +472,65 @@ extern "C" int geo_fd2d_shot(const geo_fd2d_desc *desc, const float *v, const fl
     const size_t nn = (size_t)nnx * nnz;
     Watchdog wd;
     GEO_TRY(wd.open());
-    if (snap && snap_every > 0) {
+    const cudaMemcpyKind ksnap = mem == GEO_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+    // CPU and GPU forms: every block keeps its tile of the fields in shared
+    // memory for the run (launch_fd2d_tile), one launch per run of steps
+    // between snapshots, when the grid fits on the device that way
+    bool tiled = false;
+    if (var == V_CPU || var == V_GPU) {
+        DevBuf xch, d_amp, d_on, d_sync;
+        GEO_TRY(xch.alloc(8 * nn * 4));
+        GEO_TRY(xch.zero(ss.cs));
+        GEO_TRY(d_amp.alloc((size_t)D.nt * 4));
+        GEO_TRY(d_on.alloc((size_t)D.nt));
+        GEO_TRY(d_sync.alloc(8));
+        GEO_TRY(d_sync.zero(ss.cs));
+        GEO_CUDA(cudaMemcpyAsync(d_amp.p, amp.data(), (size_t)D.nt * 4, cudaMemcpyHostToDevice, ss.cs));
+        GEO_CUDA(cudaMemcpyAsync(d_on.p, on.data(), (size_t)D.nt, cudaMemcpyHostToDevice, ss.cs));
+        unsigned *bar = d_sync.as<unsigned>();
+        int *errw = d_sync.as<int>() + 1;
+        for (int it0 = 0; it0 < D.nt;) {
+            int it1 = it0 + 1;
+            if (snap && snap_every > 0)
+                while (it1 < D.nt && (it1 - 1) % snap_every != 0) it1++;
+            else
+                it1 = D.nt;
+            bool fits = false;
+            GEO_TRY(launch_fd2d_tile(var, B.S[0], xch.as<float>(), d_amp.as<float>(), d_on.as<unsigned char>(),
+                                     taper ? 1 : 0, it0, it1, bar, errw, &fits, ss.cs));
+            if (!fits) {   // decided by the grid alone, so on the first run of steps
+                if (tiled) return fail(GEO_ERR_CUDA, "2D shot: tile-resident launch refused mid-run");
+                break;
+            }
+            tiled = true;
+            const int it = it1 - 1;
+            if (snap && snap_every > 0 && it % snap_every == 0)
+                GEO_CUDA(cudaMemcpyAsync(snap + (size_t)(it / snap_every) * nn, B.S[0].P[0], nn * 4, ksnap, ss.cs));
+            if (wd.every > 0) {
+                GEO_TRY(launch_watch_shots(B.d_S.as<Shot2D>(), 1, 1, wd.d, it + 1, ss.cs));
+                if (wd.tripped()) break;
+            }
+            it0 = it1;
+        }
+        if (tiled) {
+            int err = 0;
+            GEO_CUDA(cudaMemcpyAsync(&err, errw, 4, cudaMemcpyDeviceToHost, ss.cs));
+            GEO_CUDA(cudaStreamSynchronize(ss.cs));
+            if (err) return fail(GEO_ERR_CUDA, "2D shot: a grid barrier wait timed out");
+            if (wd.every > 0) GEO_TRY(wd.scan(B.S[0].rec_p, (size_t)D.nx * D.nt, D.nt, ss.cs));
+        }
+    }
+    if (!tiled && snap && snap_every > 0) {
         for (int it = 0; it < D.nt; it++) {
             GEO_TRY(step(it));
-            if (it % snap_every == 0) {
-                float *dst = snap + (size_t)(it / snap_every) * nn;
-                GEO_CUDA(cudaMemcpyAsync(dst, B.S[0].P[0], nn * 4,
-                                         mem == GEO_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, ss.cs));
-            }
+            if (it % snap_every == 0)
+                GEO_CUDA(cudaMemcpyAsync(snap + (size_t)(it / snap_every) * nn, B.S[0].P[0], nn * 4, ksnap, ss.cs));
             if (wd.every > 0 && ((it + 1) % wd.every == 0 || it == D.nt - 1)) {
                 GEO_TRY(launch_watch_shots(B.d_S.as<Shot2D>(), 1, 1, wd.d, it + 1, ss.cs));
                 if (wd.tripped()) break;
             }
         }
-    } else {
+    } else if (!tiled) {
         // the whole shot in one cooperative launch (grid barriers between the
         // half-steps, bounded waits reported through an error word)
         DevBuf d_amp, d_on, d_sync;

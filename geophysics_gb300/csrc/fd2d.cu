@@ -19,6 +19,8 @@
 #include <cfloat>
 #include <cmath>
 #include <cstring>
+#include <cstdio>
+#include <cstdlib>
 
 namespace geo {
 
@@ -318,6 +320,293 @@ int launch_fd2d_shot(int variant, const Shot2D *d_shots, const int *d_item_shot,
     void *args[] = {(void *)&d_shots, (void *)&d_item_shot, (void *)&nitems, (void *)&a};
     GEO_CUDA(cudaLaunchCooperativeKernel(fn, dim3(grid), block, args, 0, s));
     return check_launch("fd2d_shot");
+}
+
+// ------------------------------------------------------ tile-resident shot
+// A single shot (CPU or GPU form) whose fields stay in shared memory for the
+// whole run: block b owns a TZ(z) x TX(x) tile of every field and of the
+// model.  Per step it loads only halos from the previous step's exchange
+// copy of P, Q, u, w (x halos of P and u, z halos of Q and w), recomputes
+// the velocities on its tile and on the 4-cell halos the stress update
+// reads (the same arithmetic as the neighbour's own update), updates its
+// stresses, writes its P, Q, u, w to the other exchange copy and meets the
+// other blocks at one grid barrier.  The per-point arithmetic is
+// vel_point's and stress_point's (CPU/GPU forms, forward phase, receivers);
+// the GPU form's point source (P,Q += amp at one cell before the velocity
+// update) is added to every copy of that cell's P,Q the step reads.
+struct TileShot2D {
+    Shot2D sh;                         // fields: state at the launch's start and end
+    float *xP[2], *xQ[2], *xu[2], *xw[2];  // exchange copies, by step parity
+    const float *amp;
+    const unsigned char *on;
+    int lz_shift, TX, ntz, taper;      // TZ = 1 << lz_shift
+    int it0, it1;                      // steps of this launch
+    unsigned *bar;
+    int *err;
+};
+
+// Shared floats of one tile: P with its x halo (7 each side), Q with its z
+// halo (7), u with x halo (4 left, 3 right), w with z halo (4 above, 3
+// below), the four split stresses and the three model arrays.
+__host__ __device__ constexpr long tile2d_floats(int TZ, int TX) {
+    return 11L * TX * TZ + 21L * (TX + TZ);
+}
+
+template <int VARIANT>
+__global__ void __launch_bounds__(512) k_fd2d_tile(const TileShot2D a) {
+    extern __shared__ float sm[];
+    if (ld_acquire_u32(reinterpret_cast<const unsigned *>(a.err))) return;   // an earlier run gave up
+    const Shot2D &sh = a.sh;
+    const int TZ = 1 << a.lz_shift, TX = a.TX, nnx = sh.nnx, nnz = sh.nnz;
+    const int z0 = (blockIdx.x % a.ntz) * TZ, x0 = (blockIdx.x / a.ntz) * TX;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    float *PH = sm, *QH = PH + (TX + 14) * TZ, *UH = QH + TX * (TZ + 14), *WH = UH + (TX + 7) * TZ;
+    float *PX = WH + TX * (TZ + 7), *PZ = PX + TX * TZ, *QX = PZ + TX * TZ, *QZ = QX + TX * TZ;
+    float *VP = QZ + TX * TZ, *E2 = VP + TX * TZ, *D2 = E2 + TX * TZ;
+    // tile-local views: cx, lz relative to (x0, z0)
+    auto ph = [&](int cx, int lz) -> float & { return PH[(cx + 7) * TZ + lz]; };          // cx in [-7, TX+7)
+    auto qh = [&](int cx, int lz) -> float & { return QH[cx * (TZ + 14) + lz + 7]; };    // lz in [-7, TZ+7)
+    auto uh = [&](int cx, int lz) -> float & { return UH[(cx + 4) * TZ + lz]; };          // cx in [-4, TX+3)
+    auto wh = [&](int cx, int lz) -> float & { return WH[cx * (TZ + 7) + lz + 4]; };     // lz in [-4, TZ+3)
+    auto upd = [&](int ix, int iz) { return ix >= 4 && ix < nnx - 4 && iz >= 4 && iz < nnz - 4; };
+
+    // own state and model (SV taper applied to 1+2eps, sqrtf(1+2del))
+    for (int cx = warp; cx < TX; cx += nw)
+        for (int lz = lane; lz < TZ; lz += 32) {
+            const int ix = x0 + cx, iz = z0 + lz, o = cx * TZ + lz;
+            const bool in = ix < nnx && iz < nnz;
+            const long id = (long)ix * nnz + iz;
+            ph(cx, lz) = in ? sh.P[0][id] : 0.0f;
+            qh(cx, lz) = in ? sh.Q[0][id] : 0.0f;
+            uh(cx, lz) = in ? sh.u[0][id] : 0.0f;
+            wh(cx, lz) = in ? sh.w[0][id] : 0.0f;
+            PX[o] = in ? sh.px[0][id] : 0.0f;
+            PZ[o] = in ? sh.pz[0][id] : 0.0f;
+            QX[o] = in ? sh.qx[0][id] : 0.0f;
+            QZ[o] = in ? sh.qz[0][id] : 0.0f;
+            float e2 = in ? sh.e2[id] : 0.0f, d2 = in ? sh.d2[id] : 0.0f;
+            if (a.taper) {
+                const int bx = ix - sh.tx0, bz = iz - sh.tz0;
+                if (bx >= 0 && bx < kTB && bz >= 0 && bz < kTB) {
+                    e2 = sh.te2[bx * kTB + bz];
+                    d2 = sh.td2[bx * kTB + bz];
+                }
+            }
+            VP[o] = in ? sh.vp[id] : 0.0f;
+            E2[o] = e2;
+            D2[o] = d2;
+        }
+    unsigned k = 0;
+    for (int it = a.it0; it < a.it1; it++) {
+        const int b = it & 1;
+        const bool on = a.on[it] != 0;
+        const float amp = a.amp[it];
+        const bool pt_src = VARIANT == V_GPU && on;
+        // halos of the previous step (another block's values: through L2)
+        auto halo = [&](const float *x, int ix, int iz) {
+            if (ix < 0 || ix >= nnx || iz < 0 || iz >= nnz) return 0.0f;
+            float v = __ldcg(x + (long)ix * nnz + iz);
+            if (pt_src && ix == sh.ixs && iz == sh.izs) v = v + amp;
+            return v;
+        };
+        for (int c = warp; c < 14; c += nw) {
+            const int cx = c < 7 ? c - 7 : TX + c - 7;
+            for (int lz = lane; lz < TZ; lz += 32) ph(cx, lz) = halo(a.xP[b], x0 + cx, z0 + lz);
+        }
+        for (int c = warp; c < 7; c += nw) {
+            const int cx = c < 4 ? c - 4 : TX + c - 4;
+            for (int lz = lane; lz < TZ; lz += 32) {
+                const int ix = x0 + cx, iz = z0 + lz;
+                uh(cx, lz) = ix >= 0 && ix < nnx && iz < nnz ? __ldcg(a.xu[b] + (long)ix * nnz + iz) : 0.0f;
+            }
+        }
+        for (int t = threadIdx.x; t < TX * 14; t += blockDim.x) {
+            const int cx = t / 14, r = t % 14, lz = r < 7 ? r - 7 : TZ + r - 7;
+            qh(cx, lz) = halo(a.xQ[b], x0 + cx, z0 + lz);
+        }
+        for (int t = threadIdx.x; t < TX * 7; t += blockDim.x) {
+            const int cx = t / 7, r = t % 7, lz = r < 4 ? r - 4 : TZ + r - 4;
+            const int ix = x0 + cx, iz = z0 + lz;
+            wh(cx, lz) = ix < nnx && iz >= 0 && iz < nnz ? __ldcg(a.xw[b] + (long)ix * nnz + iz) : 0.0f;
+        }
+        // the source cell inside the tile (its own copy)
+        if (pt_src && threadIdx.x == 0) {
+            const int cx = sh.ixs - x0, lz = sh.izs - z0;
+            if (cx >= 0 && cx < TX && lz >= 0 && lz < TZ) {
+                ph(cx, lz) = ph(cx, lz) + amp;
+                qh(cx, lz) = qh(cx, lz) + amp;
+            }
+        }
+        __syncthreads();
+        // velocities on the tile and its halos (vel_point)
+        for (int cx = warp - 4; cx < TX + 3; cx += nw)
+            for (int lz = lane; lz < TZ; lz += 32) {
+                const int ix = x0 + cx, iz = z0 + lz;
+                if (!upd(ix, iz)) continue;
+                float xx = 0.0f;
+#pragma unroll
+                for (int im = 0; im < 4; im++) xx += c_fd[im] * (ph(cx + im + 1, lz) - ph(cx - im, lz));
+                uh(cx, lz) = sh.cx2[ix] * uh(cx, lz) - sh.cx1[ix] * sh.dtx * xx;
+            }
+        for (int cx = warp; cx < TX; cx += nw)
+            for (int lz = lane - 4; lz < TZ + 3; lz += 32) {
+                const int ix = x0 + cx, iz = z0 + lz;
+                if (!upd(ix, iz)) continue;
+                float zz = 0.0f;
+#pragma unroll
+                for (int im = 0; im < 4; im++) zz += c_fd[im] * (qh(cx, lz + im + 1) - qh(cx, lz - im));
+                wh(cx, lz) = sh.cz2[iz] * wh(cx, lz) - sh.cz1[iz] * sh.dtz * zz;
+            }
+        __syncthreads();
+        // stresses of the tile (stress_point, forward), receivers, exchange
+        float *yP = a.xP[b ^ 1], *yQ = a.xQ[b ^ 1], *yu = a.xu[b ^ 1], *yw = a.xw[b ^ 1];
+        for (int cx = warp; cx < TX; cx += nw)
+            for (int lz = lane; lz < TZ; lz += 32) {
+                const int ix = x0 + cx, iz = z0 + lz;
+                if (!upd(ix, iz)) continue;
+                float xx = 0.0f, zz = 0.0f;
+#pragma unroll
+                for (int im = 0; im < 4; im++) {
+                    xx += c_fd[im] * (uh(cx + im, lz) - uh(cx - im - 1, lz));
+                    zz += c_fd[im] * (wh(cx, lz + im) - wh(cx, lz - im - 1));
+                }
+                const int o = cx * TZ + lz;
+                const float vp = VP[o], e2 = E2[o], d2 = D2[o];
+                const float ax1 = sh.ax1[ix], ax2 = sh.ax2[ix], az1 = sh.az1[iz], az2 = sh.az2[iz];
+                const float px = ax2 * PX[o] - ax1 * vp * vp * e2 * sh.dtx * xx;
+                const float pz = az2 * PZ[o] - az1 * vp * vp * d2 * sh.dtz * zz;
+                const float qx = ax2 * QX[o] - ax1 * vp * vp * d2 * sh.dtx * xx;
+                const float qz = az2 * QZ[o] - az1 * vp * vp * sh.dtz * zz;
+                PX[o] = px; PZ[o] = pz; QX[o] = qx; QZ[o] = qz;
+                float P, Q;
+                if (VARIANT == V_CPU) {
+                    // 7x7 Gaussian source window, added after the split sum
+                    float s = 0.0f;
+                    const int rx = ix - sh.ixs, rz = iz - sh.izs;
+                    if (on && rx >= -3 && rx <= 3 && rz >= -3 && rz <= 3)
+                        s = (float)((double)amp * c_gauss[(rx + 3) * 7 + (rz + 3)]);
+                    P = px + pz + s;
+                    Q = qx + qz + s;
+                } else {
+                    P = px + pz;
+                    Q = qx + qz;
+                }
+                ph(cx, lz) = P;
+                qh(cx, lz) = Q;
+                const long id = (long)ix * nnz + iz;
+                yP[id] = P;
+                yQ[id] = Q;
+                yu[id] = uh(cx, lz);
+                yw[id] = wh(cx, lz);
+                const int gx = ix - sh.npd;
+                if (iz == sh.rec_iz && gx >= 0 && gx < sh.nx)
+                    sh.rec_p[(long)it * sh.nx + gx] = sh.rec_scale == 2.0f ? P + P : P * sh.rec_scale;
+            }
+        if (it + 1 < a.it1 && !grid_barrier(a.bar, ++k * gridDim.x, a.err)) return;
+    }
+    __syncthreads();
+    // state back to the shot's fields
+    for (int cx = warp; cx < TX; cx += nw)
+        for (int lz = lane; lz < TZ; lz += 32) {
+            const int ix = x0 + cx, iz = z0 + lz, o = cx * TZ + lz;
+            if (ix >= nnx || iz >= nnz) continue;
+            const long id = (long)ix * nnz + iz;
+            sh.P[0][id] = ph(cx, lz);
+            sh.Q[0][id] = qh(cx, lz);
+            sh.u[0][id] = uh(cx, lz);
+            sh.w[0][id] = wh(cx, lz);
+            sh.px[0][id] = PX[o];
+            sh.pz[0][id] = PZ[o];
+            sh.qx[0][id] = QX[o];
+            sh.qz[0][id] = QZ[o];
+        }
+}
+
+constexpr size_t kTileSmemMax = 220 * 1024;
+
+// Tile shape of the tile-resident shot: every tile's block resident at once
+// (cooperative launch).  The half-steps are bound by shared-memory and L2
+// latency chains, so more resident warps per SM beat less halo work: at
+// 401^2 + 50 (2000 steps) 64x16 tiles (two blocks per SM) take 17.7 ms,
+// 128x16 and 64x32 (one per SM) 18.0 and 18.2 ms, 32x32 18.7 ms, 32x64
+// 20.5 ms.  So: TZ 64 first (then 128, 32, 256), the narrowest TX that
+// fits.  Returns false when the grid does not fit on the device this way.
+static bool tile2d_shape(const void *fn, int nnx, int nnz, int sms, int &lz_shift, int &TX, size_t &smem) {
+    static const int kLz[] = {6, 7, 5, 8};
+    static const int kTX[] = {8, 12, 16, 24, 32, 48, 64};
+    for (int ls : kLz) {
+        const int TZ = 1 << ls;
+        for (int tx : kTX) {
+            const size_t bytes = (size_t)tile2d_floats(TZ, tx) * 4;
+            if (bytes > kTileSmemMax) continue;
+            int per_sm = 0;
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 512, bytes) != cudaSuccess) return false;
+            const long tiles = (long)((nnz + TZ - 1) / TZ) * ((nnx + tx - 1) / tx);
+            if (per_sm < 1 || tiles > (long)per_sm * sms) continue;
+            lz_shift = ls;
+            TX = tx;
+            smem = bytes;
+            return true;
+        }
+    }
+    return false;
+}
+
+int launch_fd2d_tile(int variant, const Shot2D &sh, float *xch, const float *amp, const unsigned char *on,
+                     int taper, int it0, int it1, unsigned *bar, int *err, bool *fits, cudaStream_t s) {
+    *fits = false;
+    if (variant != V_CPU && variant != V_GPU) return GEO_OK;
+    int dev = 0, sms = 0, coop = 0;
+    GEO_CUDA(cudaGetDevice(&dev));
+    GEO_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    GEO_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
+    const void *fn = variant == V_CPU ? (const void *)k_fd2d_tile<V_CPU> : (const void *)k_fd2d_tile<V_GPU>;
+    GEO_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTileSmemMax));
+    int ls = 0, TX = 0;
+    size_t smem = 0;
+    if (!coop || !tile2d_shape(fn, sh.nnx, sh.nnz, sms, ls, TX, smem)) return GEO_OK;
+    // GEO_FD2D_TILE=TZxTX fixes the tile instead (TZ a power of two 32..256)
+    if (const char *e = getenv("GEO_FD2D_TILE")) {
+        int tz = 0, tx = 0;
+        if (sscanf(e, "%dx%d", &tz, &tx) == 2 && tx >= 4 && tx <= 128)
+            for (int l = 5; l <= 8; l++)
+                if (tz == (1 << l)) {
+                    ls = l;
+                    TX = tx;
+                    smem = (size_t)tile2d_floats(tz, tx) * 4;
+                }
+        if (smem > kTileSmemMax) return fail(GEO_ERR_ARG, "GEO_FD2D_TILE %s: tile too large", e);
+    }
+    int occ = 0;
+    GEO_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, 512, smem));
+    const int TZ = 1 << ls, ntz = (sh.nnz + TZ - 1) / TZ, ntx = (sh.nnx + TX - 1) / TX;
+    if (occ < 1 || (long)ntz * ntx > (long)occ * sms) return GEO_OK;
+    if ((long long)ntz * ntx * (it1 - it0) >= 4000000000LL) return GEO_OK;
+    GEO_TRY(ensure_gauss());
+    *fits = true;
+    const size_t n = (size_t)sh.nnx * sh.nnz;
+    TileShot2D a{};
+    a.sh = sh;
+    for (int p = 0; p < 2; p++) {
+        a.xP[p] = xch + (size_t)(4 * p) * n;
+        a.xQ[p] = xch + (size_t)(4 * p + 1) * n;
+        a.xu[p] = xch + (size_t)(4 * p + 2) * n;
+        a.xw[p] = xch + (size_t)(4 * p + 3) * n;
+    }
+    a.amp = amp;
+    a.on = on;
+    a.lz_shift = ls;
+    a.TX = TX;
+    a.ntz = ntz;
+    a.taper = taper;
+    a.it0 = it0;
+    a.it1 = it1;
+    a.bar = bar;
+    a.err = err;
+    GEO_CUDA(cudaMemsetAsync(bar, 0, 4, s));
+    void *args[] = {(void *)&a};
+    GEO_CUDA(cudaLaunchCooperativeKernel(fn, dim3(ntz * ntx), dim3(512), args, smem, s));
+    return check_launch("fd2d_tile");
 }
 
 // Boundary-driven reconstruction and receiver injection before step it of

@@ -183,6 +183,12 @@ struct Persist2D {
 };
 int launch_fd2d_shot(int variant, const Shot2D *d_shots, const int *d_item_shot, int nitems, int by, Persist2D a,
                      cudaStream_t s);
+// The same shot with each block's tile of the fields resident in shared
+// memory (CPU and GPU forms), steps it0..it1-1; *fits is false (and nothing
+// runs) when the grid does not fit on the device that way.  xch: 8 exchange
+// fields of nnx*nnz floats, zeroed before the first run.
+int launch_fd2d_tile(int variant, const Shot2D &sh, float *xch, const float *amp, const unsigned char *on,
+                     int taper, int it0, int it1, unsigned *bar, int *err, bool *fits, cudaStream_t s);
 
 int launch_vel2d(int variant, const Shot2D *d_shots, const int *d_item_shot, int nitems, int by,
                  int grid, Step2D st, cudaStream_t s);

@@ -47,6 +47,30 @@ def test_fd2d_ragged_sizes(geo, orc):
         assert np.array_equal(geo.fd2d_shot(v, e, d, variant=variant, **kw), orc.fd2d(v, e, d, variant=var, **kw))
 
 
+@pytest.mark.parametrize("variant", ["cpu", "gpu"])
+def test_fd2d_source_at_tile_seams(geo, orc, variant):
+    """The CPU and GPU forms keep each block's tile of the fields in shared
+    memory and exchange halos; sources on and next to the seams between
+    tiles (x every 8 or more cells, z every 32 or more) reach every copy of
+    the source cell the step reads."""
+    v, e, d = layered_model(70, 60, seed=5)
+    var = {"cpu": orc.V_CPU, "gpu": orc.V_GPU}[variant]
+    for fs, zs in ((13.0, 13.0), (14.0, 14.0), (21.0, 12.0), (29.0, 45.0), (30.0, 44.0)):
+        kw = dict(KW, fs=fs, zs=zs, nt=120)
+        ref = orc.fd2d(v, e, d, variant=var, **kw)
+        out = geo.fd2d_shot(v, e, d, variant=variant, **kw)
+        assert np.array_equal(out, ref), (fs, zs, rel_l2(out, ref))
+
+
+def test_fd2d_grid_beyond_resident_tiles(geo, orc):
+    """A grid too large for every tile to stay in shared memory at once
+    takes the launch that reads the fields through L2: same results."""
+    v, e, d = layered_model(1250, 820, seed=6)
+    kw = dict(KW, fs=600.0, zs=5.0, nt=30)
+    for variant, var in (("cpu", orc.V_CPU), ("gpu", orc.V_GPU)):
+        assert np.array_equal(geo.fd2d_shot(v, e, d, variant=variant, **kw), orc.fd2d(v, e, d, variant=var, **kw))
+
+
 def test_dropin_files_match_oracle(geo, orc, tmp_path):
     v, e, d = layered_model(50, 45, seed=4)
     for name, arr in (("v", v), ("e", e), ("d", d)):
