@@ -396,6 +396,9 @@ __global__ void __launch_bounds__(512) k_fd2d_tile(const TileShot2D a) {
             E2[o] = e2;
             D2[o] = d2;
         }
+    // the own tile is read by other threads from here on (the source cell's
+    // update below, the first step's taps)
+    __syncthreads();
     unsigned k = 0;
     for (int it = a.it0; it < a.it1; it++) {
         const int b = it & 1;

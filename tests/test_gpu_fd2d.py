@@ -62,6 +62,18 @@ def test_fd2d_source_at_tile_seams(geo, orc, variant):
         assert np.array_equal(out, ref), (fs, zs, rel_l2(out, ref))
 
 
+def test_fd2d_gpu_form_snapshots_while_source_on(geo, orc):
+    """Snapshots every 3 steps end a launch every 3 steps while the GPU
+    form's point source is still on: each launch reloads the tiles and adds
+    the source to the reloaded cell."""
+    v, e, d = layered_model(70, 60, seed=8)
+    kw = dict(KW, fs=29.0, zs=13.0, nt=61)
+    ref, rs = orc.fd2d(v, e, d, variant=orc.V_GPU, snap_every=3, **kw)
+    out, os_ = geo.fd2d_shot(v, e, d, variant="gpu", snap_every=3, **kw)
+    assert np.array_equal(out, ref), rel_l2(out, ref)
+    assert np.array_equal(os_, rs)
+
+
 def test_fd2d_grid_beyond_resident_tiles(geo, orc):
     """A grid too large for every tile to stay in shared memory at once
     takes the launch that reads the fields through L2: same results."""
