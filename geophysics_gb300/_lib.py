@@ -130,6 +130,8 @@ def lib():
         "geo_par_get_string": (_i, [_vp, C.c_char_p, C.c_char_p, _i]),
         "geo_par_free": (None, [_vp]),
         "geo_selftest_bounded_wait": (_i, [_i, C.POINTER(_i), _vp]),
+        "geo_selftest_conversions": (_i, [C.c_longlong, C.c_ulonglong, C.POINTER(C.c_longlong),
+                                          C.POINTER(C.c_longlong), _vp]),
         "geo_fd2d": (_i, [_vp, _i, _vp, _vp]),
         "geo_fd3d": (_i, [_vp, _i, _vp, _vp]),
         "geo_rtm2d": (_i, [_vp, _i, _vp, _vp]),

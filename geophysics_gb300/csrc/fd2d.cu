@@ -15,6 +15,7 @@
 #include "geo_internal.h"
 #include "tc_util.cuh"
 #include "gridsync.cuh"
+#include "softcvt.cuh"
 #include <algorithm>
 #include <cfloat>
 #include <cmath>
@@ -192,8 +193,9 @@ __device__ __forceinline__ void stress_point(const Shot2D &sh, int ix, int iz, c
         if (VARIANT == V_MPI) {
             px = ax2 * px - ax1 * vp * e2 * sh.dtx * xx;
             if (dpw) {
-                pz = (float)((double)(az2 * pz) - kz * (double)zz);
-                qx = (float)((double)(ax2 * qx) - kx * (double)xx);
+                // the conversions on the integer pipe (softcvt.cuh): same bits
+                pz = d2f_rn(f2d_exact(az2 * pz) - kz * f2d_exact(zz));
+                qx = d2f_rn(f2d_exact(ax2 * qx) - kx * f2d_exact(xx));
             } else {
                 pz = az2 * pz - az1 * vp * d2 * sh.dtz * zz;
                 qx = ax2 * qx - ax1 * vp * d2 * sh.dtx * xx;
@@ -243,7 +245,10 @@ __device__ __forceinline__ void stress_point(const Shot2D &sh, int ix, int iz, c
         const float sv = Pn[0];
         float ill;
         if (FAST) ill = sh.ill[o] + sv * sv;
-        else ill = (float)((double)sh.ill[o] + (double)sv * (double)sv);
+        else {
+            const double svd = f2d_exact(sv);
+            ill = d2f_rn(f2d_exact(sh.ill[o]) + svd * svd);
+        }
         if (ill == 0.0f) ill = 1.0f;
         sh.ill[o] = ill;
         sh.mig[o] = sh.mig[o] + Pn[1] * sv;
@@ -255,7 +260,7 @@ __device__ __forceinline__ void stress_point(const Shot2D &sh, int ix, int iz, c
             const float a1 = (float)((double)a / ((double)sqrtf(b1 * b2) + 0.0000000000001));
             const int ia = adcig_bin(a1);
             float *ag = sh.adcig + (long)ia * sh.nx * sh.nz + o;
-            *ag = (float)((double)*ag + (double)(Pn[1] * sv) * c_adw[ia]);
+            *ag = d2f_rn(f2d_exact(*ag) + f2d_exact(Pn[1] * sv) * c_adw[ia]);
         }
     }
 }

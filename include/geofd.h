@@ -487,6 +487,14 @@ void geo_par_free(geo_par *par);
  * and the context is usable -- what a stuck pipeline stage looks like to a
  * caller of the 3D step or the codec (GEO_ERR_CUDA, "... timed out"). */
 int geo_selftest_bounded_wait(int limit_ms, int *gave_up, void *stream);
+/* Diagnostic without a reference counterpart: the library's integer-pipe
+ * float <-> double conversions (used in the MPI program's double chains)
+ * against the hardware conversions on the device -- the widening over all
+ * 2^32 binary32 patterns, the narrowing (round to nearest even) over
+ * n_random binary64 values spanning underflow to overflow, exact ties and
+ * binary32 images.  Mismatch counts in *f2d_bad, *d2f_bad. */
+int geo_selftest_conversions(long long n_random, unsigned long long seed, long long *f2d_bad, long long *d2f_bad,
+                             void *stream);
 
 int geo_fd2d(const geo_par *par, int device, float *d_shots, void *stream);
 int geo_fd3d(const geo_par *par, int device, float *d_shots, void *stream);
