@@ -253,18 +253,20 @@ def run_ours(args, rank, world):
     plan.run_shot(0, out=rec)
     barrier()
     e2e_steps = max(1, args.steps)
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        plan.set_model(hv, he, hd)
-        plan.run_shot(0, out=rec)
-    barrier()
-    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    with Clocks(dev) as clk_e2e:
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            plan.set_model(hv, he, hd)
+            plan.run_shot(0, out=rec)
+        barrier()
+        e2e_s = (time.perf_counter() - t0) / e2e_steps
     if world > 1:
         t = torch.tensor([e2e_s], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         e2e_s = float(t.item())
     e2e = {"value": world * updates_per_step() * NT / e2e_s / 1e9, "unit": "Gpt/s",
-           "h2d_bytes_per_step": int(hv.nbytes + he.nbytes + hd.nbytes), "d2h_bytes_per_step": int(rec.nbytes)}
+           "h2d_bytes_per_step": int(hv.nbytes + he.nbytes + hd.nbytes), "d2h_bytes_per_step": int(rec.nbytes),
+           "clocks": clk_e2e.summary()}
     plan.close()
     # the exact stress form (the reference's FP32 arithmetic, bit-identical to
     # the oracle) on the same grid, bare steps, for callers that need it
