@@ -19,11 +19,64 @@
 #pragma once
 
 #include <cstdint>
+#include <cstring>
+
+#if defined(__CUDACC__)
+#define GEO_SC_FN __host__ __device__ __forceinline__
+#else
+#define GEO_SC_FN inline
+#endif
 
 namespace geo {
 
-__device__ __forceinline__ double f2d_exact(float f) {
-    const uint32_t u = __float_as_uint(f);
+// bit casts and the leading-zero count on either side (the host build is
+// the CPU check of the same code)
+GEO_SC_FN uint32_t sc_f2u(float f) {
+#if defined(__CUDA_ARCH__)
+    return __float_as_uint(f);
+#else
+    uint32_t u;
+    memcpy(&u, &f, 4);
+    return u;
+#endif
+}
+GEO_SC_FN float sc_u2f(uint32_t u) {
+#if defined(__CUDA_ARCH__)
+    return __uint_as_float(u);
+#else
+    float f;
+    memcpy(&f, &u, 4);
+    return f;
+#endif
+}
+GEO_SC_FN uint64_t sc_d2u(double d) {
+#if defined(__CUDA_ARCH__)
+    return (uint64_t)__double_as_longlong(d);
+#else
+    uint64_t u;
+    memcpy(&u, &d, 8);
+    return u;
+#endif
+}
+GEO_SC_FN double sc_u2d(uint64_t u) {
+#if defined(__CUDA_ARCH__)
+    return __longlong_as_double((long long)u);
+#else
+    double d;
+    memcpy(&d, &u, 8);
+    return d;
+#endif
+}
+GEO_SC_FN int sc_clz(uint32_t x) {   // x != 0
+#if defined(__CUDA_ARCH__)
+    return __clz(x);
+#else
+    return __builtin_clz(x);
+#endif
+}
+
+GEO_SC_FN double f2d_exact(float f) {
+    const uint32_t u = sc_f2u(f);
     const uint64_t sign = (uint64_t)(u & 0x80000000u) << 32;
     const uint32_t ex = (u >> 23) & 0xffu, man = u & 0x7fffffu;
     uint64_t bits;
@@ -36,20 +89,20 @@ __device__ __forceinline__ double f2d_exact(float f) {
         bits = sign;
     } else {
         // subnormal: man * 2^-149 = 1.f * 2^(p - 149), p the leading one's position
-        const int p = 31 - __clz(man);
+        const int p = 31 - sc_clz(man);
         bits = sign | ((uint64_t)(p - 149 + 1023) << 52) | (((uint64_t)man << (52 - p)) & 0xfffffffffffffull);
     }
-    return __longlong_as_double((long long)bits);
+    return sc_u2d(bits);
 }
 
-__device__ __forceinline__ float d2f_rn(double d) {
-    const uint64_t b = (uint64_t)__double_as_longlong(d);
+GEO_SC_FN float d2f_rn(double d) {
+    const uint64_t b = sc_d2u(d);
     const uint32_t sign = (uint32_t)(b >> 32) & 0x80000000u;
     const int ex = (int)((b >> 52) & 0x7ffu);
     const uint64_t m = b & 0xfffffffffffffull;
     if (ex == 0x7ff) {
         if (m) return (float)d;   // NaN: the hardware's own quieting (never on a finite run)
-        return __uint_as_float(sign | 0x7f800000u);
+        return sc_u2f(sign | 0x7f800000u);
     }
     const uint64_t sig = ex ? (m | (1ull << 52)) : m;   // 53-bit significand (value = sig * 2^(ex-1075))
     const int e = ex - 1023 + 127;                       // binary32 biased exponent of a normal result
@@ -62,7 +115,7 @@ __device__ __forceinline__ float d2f_rn(double d) {
     } else {
         // subnormal or zero result: units of 2^-149, sig * 2^(ex-1075) / 2^-149 = sig >> s
         const int s = 926 - ex;   // >= 29 + (1 - e)
-        if (s >= 64) return __uint_as_float(sign);
+        if (s >= 64) return sc_u2f(sign);
         q = (uint32_t)(sig >> s);
         rem = sig & ((1ull << s) - 1);
         half = 1ull << (s - 1);
@@ -75,12 +128,12 @@ __device__ __forceinline__ float d2f_rn(double d) {
             q >>= 1;
             E++;
         }
-        if (E >= 0xffu) return __uint_as_float(sign | 0x7f800000u);
-        return __uint_as_float(sign | (E << 23) | (q & 0x7fffffu));
+        if (E >= 0xffu) return sc_u2f(sign | 0x7f800000u);
+        return sc_u2f(sign | (E << 23) | (q & 0x7fffffu));
     }
     // q <= 2^23: a carry into bit 23 is the smallest normal, which the
     // bit pattern already encodes
-    return __uint_as_float(sign | q);
+    return sc_u2f(sign | q);
 }
 
 }  // namespace geo
