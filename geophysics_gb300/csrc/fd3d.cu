@@ -925,13 +925,10 @@ extern "C" int geo_rtm3d_adcig(const geo_rtm3d_desc *desc, const float *v, const
     const long nag = (long)D.nz * na * nxa * nya;
     DevBuf ag, atab;
     if (adcig_out) {
-        std::vector<float> tab(2 * kMaxAngles);
-        adcig_angle_tables(na, da, tab.data(), tab.data() + kMaxAngles);
         GEO_TRY(ag.alloc(nag * 4));
         GEO_TRY(ag.zero(s));
-        GEO_TRY(atab.alloc(tab.size() * 4));
-        GEO_CUDA(cudaMemcpyAsync(atab.p, tab.data(), tab.size() * 4, cudaMemcpyHostToDevice, s));
-        GEO_CUDA(cudaStreamSynchronize(s));
+        GEO_TRY(atab.alloc(2 * kMaxAngles * 4));
+        GEO_TRY(adcig_angle_tables(na, da, atab.as<float>(), atab.as<float>() + kMaxAngles, s));
     }
     float *bp = ring.as<float>(), *bq = bp + (size_t)D.nt * L;
     const int ntr = D.nrx * D.nry;

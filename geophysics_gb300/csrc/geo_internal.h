@@ -123,10 +123,11 @@ void mute_window_3d_band(int nx, int ny, int nt, float dt, float favg, float dx,
                          int fsx, int fsy, int dsx, int dsy, int fsz, int is, float vp1, float eps1, int tt,
                          std::vector<int> &lo, std::vector<int> &hi);
 
-// Angle-gather tables of the GPU RTM programs' Poynting bin: thresholds
-// (largest cosine of bins >= k, -2 where none) and cosf(ia*pi/180), 128
-// entries each.
-void adcig_angle_tables(int nangle, int dangle, float *thr, float *cs);
+// Angle-gather tables of the GPU RTM programs' Poynting bin, built on the
+// device into device arrays of 128 floats each: thresholds (largest cosine
+// of bins >= k, -2 where none) and cosf(ia*pi/180), from the device's acosf
+// and cosf.
+int adcig_angle_tables(int nangle, int dangle, float *thr, float *cs, cudaStream_t s);
 
 // Raw float32 files: read exactly n values; write n values at a byte offset.
 int read_floats(const char *fn, size_t n, std::vector<float> &out);

@@ -326,49 +326,59 @@ __global__ void k_g_stack_angles(const float *adcig, float *stk, int nx, int nz,
     }
 }
 
-// The programs' bin of a cosine a: (int)((float)(0.5*acosf(a)*180.0/pi) / (dangle*1.0)).
-static int ref_gpu_bin(float a, int dangle) {
-    const float deg = (float)(0.5 * std::acos(a) * 180.0 / kPiGui);
+// The programs' bin of a cosine a: (int)((float)(0.5*acosf(a)*180.0/pi) / (dangle*1.0)),
+// with the device's acosf, as their Poynting_Adcigs kernels evaluate it.
+__device__ int ref_gpu_bin(float a, int dangle) {
+    const float deg = (float)(0.5 * acosf(a) * 180.0 / kPiGui);
     return (int)(deg / (dangle * 1.0));
 }
 
-static uint32_t okey(float f) {
-    uint32_t b;
-    memcpy(&b, &f, 4);
+// Float keys ordered like the floats they encode.
+__device__ uint32_t okey(float f) {
+    const uint32_t b = __float_as_uint(f);
     return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
 }
 
-static float kfloat(uint32_t k) {
-    const uint32_t b = (k & 0x80000000u) ? (k & 0x7fffffffu) : ~k;
-    float f;
-    memcpy(&f, &b, 4);
-    return f;
+__device__ float kfloat(uint32_t k) {
+    return __uint_as_float((k & 0x80000000u) ? (k & 0x7fffffffu) : ~k);
 }
 
-// thr[k-1] = largest float a in [-1,1] with bin(a) >= k (binary search over
-// the ordered float keys; bin is non-increasing in a), -2 where none is;
-// cs[ia] = cosf(ia*pi/180).  Both arrays hold kMaxAngles entries.
-void adcig_angle_tables(int nangle, int dangle, float *thr, float *cs) {
-    const uint32_t lo = okey(-1.0f), hi = okey(1.0f);
-    for (int k = 0; k < kMaxAngles; k++) { thr[k] = -2.0f; cs[k] = 0.0f; }
-    for (int k = 1; k <= nangle; k++) {
-        if (ref_gpu_bin(-1.0f, dangle) < k) continue;
-        uint32_t a = lo, b = hi;
+// One thread per bin k < kMaxAngles: thr[k] = largest float a in [-1,1]
+// with bin(a) >= k+1 (binary search over the ordered float keys; bin is
+// non-increasing in a), -2 where none is; cs[k] = cosf(k*pi/180).  Both
+// come from the device's acosf and cosf, the functions the programs'
+// kernels call, so the tables give their bins and weights bit for bit.
+__global__ void k_angle_tables(float *thr, float *cs, int nangle, int dangle) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= kMaxAngles) return;
+    cs[k] = k < nangle ? cosf((float)(k * kPiGui / 180.0)) : 0.0f;
+    float t = -2.0f;
+    if (k < nangle && ref_gpu_bin(-1.0f, dangle) >= k + 1) {
+        uint32_t a = okey(-1.0f), b = okey(1.0f);
         while (a < b) {
             const uint32_t m = a + (b - a + 1) / 2;
-            if (ref_gpu_bin(kfloat(m), dangle) >= k) a = m;
+            if (ref_gpu_bin(kfloat(m), dangle) >= k + 1) a = m;
             else b = m - 1;
         }
-        thr[k - 1] = kfloat(a);
+        t = kfloat(a);
     }
-    for (int ia = 0; ia < nangle; ia++) cs[ia] = std::cos((float)(ia * kPiGui / 180.0));
+    thr[k] = t;
 }
 
+int adcig_angle_tables(int nangle, int dangle, float *thr, float *cs, cudaStream_t s) {
+    k_angle_tables<<<1, kMaxAngles, 0, s>>>(thr, cs, nangle, dangle);
+    return check_launch("angle_tables");
+}
+
+__device__ float g_angle_stage[2 * kMaxAngles];
+
 static int gpu_adcig_tables(int nangle, int dangle, cudaStream_t s) {
-    std::vector<float> thr(kMaxAngles), cs(kMaxAngles);
-    adcig_angle_tables(nangle, dangle, thr.data(), cs.data());
-    GEO_CUDA(cudaMemcpyToSymbolAsync(c_gthr, thr.data(), kMaxAngles * 4, 0, cudaMemcpyHostToDevice, s));
-    GEO_CUDA(cudaMemcpyToSymbolAsync(c_gcos, cs.data(), kMaxAngles * 4, 0, cudaMemcpyHostToDevice, s));
+    void *stage = nullptr;
+    GEO_CUDA(cudaGetSymbolAddress(&stage, g_angle_stage));
+    float *st = static_cast<float *>(stage);
+    GEO_TRY(adcig_angle_tables(nangle, dangle, st, st + kMaxAngles, s));
+    GEO_CUDA(cudaMemcpyToSymbolAsync(c_gthr, st, kMaxAngles * 4, 0, cudaMemcpyDeviceToDevice, s));
+    GEO_CUDA(cudaMemcpyToSymbolAsync(c_gcos, st + kMaxAngles, kMaxAngles * 4, 0, cudaMemcpyDeviceToDevice, s));
     return GEO_OK;
 }
 

@@ -506,6 +506,47 @@ void orc_set_tilt_trig(const float *ct, const float *st)
     g_tilt_sin = st;
 }
 
+/* The GPU RTM programs' angle-gather weight cosf(ia*pi/180) (pi =
+ * 3.141592653), which their Poynting_Adcigs kernels evaluate with the
+ * device's cosf: for some bins it differs from the host's cosf in the last
+ * place, so the caller may hand over the device's values (ia < 128);
+ * without them the host's cosf. */
+static const float *g_angle_cos;
+
+void orc_set_angle_cos(const float *tab)
+{
+    g_angle_cos = tab;
+}
+
+static float gpu_angle_cos(int ia)
+{
+    return g_angle_cos ? g_angle_cos[ia] : cosf(ia * PI_GUI / 180.0);
+}
+
+/* Their angle bin (int)((float)(0.5*acosf(a)*180/pi) / (da*1.0)) of a
+ * cosine a in [-1, 1], likewise with the device's acosf: the host's acosf
+ * can put a cosine next to a bin edge in the neighbouring bin, so the
+ * caller may hand over the device's bin edges for the call's da (thr[k] =
+ * largest float whose device bin is >= k+1, -2 where none, k < 128); the
+ * bin is then the number of edges at or above a. */
+static const float *g_angle_thr;
+
+void orc_set_angle_thresholds(const float *thr)
+{
+    g_angle_thr = thr;
+}
+
+static int gpu_angle_bin(float a, int da)
+{
+    if (g_angle_thr) {
+        int c = 0;
+        while (c < 128 && a <= g_angle_thr[c]) c++;
+        return c;
+    }
+    a = 0.5 * acosf(a) * 180.0 / PI_GUI;
+    return (int)(a / (da * 1.0));
+}
+
 /* taper_R, taper_r: SV taper of e2t/d2t centred (fs+(is-1)ds+npd, zs+npd) (0: none) */
 static void ttim_init(orc_ttim *m, const orc_fd2d_desc *d, const float *v, const float *e, const float *dl,
                       const float *theta, int rtm_sponge, int taper_R, int taper_r)
@@ -956,10 +997,9 @@ int orc_rtm2d_gpu(int nx, int nz, int npml, int nt, float dx, float dz, float dt
                         float a = (Ssx * Sgx + Ssz * Sgz) / (sqrtf(b1 * b2) * (1 - 0.1));
                         if (a >= -1 && a <= 1) {
                             int ia;
-                            a = 0.5 * acosf(a) * 180.0 / PI_GUI;
-                            ia = (int)(a / (dangle * 1.0));
+                            ia = gpu_angle_bin(a, dangle);
                             if (ia < nangle) {
-                                float c = cosf(ia * PI_GUI / 180.0);
+                                float c = gpu_angle_cos(ia);
                                 adcigs[iz + (size_t)nz * ia + (size_t)nz * nangle * ix] += sP * gP * c * c * c;
                             }
                         }
@@ -1076,10 +1116,9 @@ int orc_rtm2d_tti(int nx, int nz, int npml, int nt, float dx, float dz, float dt
                         float a = (Ssx * Sgx + Ssz * Sgz) / (sqrtf(b1 * b2) * (1 - 0.1));
                         if (a >= -1 && a <= 1) {
                             int ia;
-                            a = 0.5 * acosf(a) * 180.0 / PI_GUI;
-                            ia = (int)(a / (dangle * 1.0));
+                            ia = gpu_angle_bin(a, dangle);
                             if (ia < nangle) {
-                                float c = cosf(ia * PI_GUI / 180.0);
+                                float c = gpu_angle_cos(ia);
                                 adcigs[iz + (size_t)nz * ia + (size_t)nz * nangle * (ix / dcdp)] += sP * gP * c * c * c;
                             }
                         }
@@ -1620,10 +1659,9 @@ static int rtm3d_shot_run(const orc_fd3d_desc *d, int mute_tt, const float *v, c
                 float a = (Ssx * Sgx + Ssy * Sgy + Ssz * Sgz) / (sqrtf(b1 * b2) * (1 - 0.1));
                 if (a >= -1 && a <= 1) {
                     int ia;
-                    a = 0.5 * acosf(a) * 180.0 / PI_GUI;
-                    ia = (int)(a / (da * 1.0));
+                    ia = gpu_angle_bin(a, da);
                     if (ia < na) {
-                        float c = cosf(ia * PI_GUI / 180.0);
+                        float c = gpu_angle_cos(ia);
                         adcigs[iz + (long)nz * (ia + (long)na * (ix + (long)nxa * iy))] += sP * gP * c * c * c;
                     }
                 }

@@ -55,6 +55,8 @@ def lib(prec=32):
         L.orc_fd2d.argtypes = [C.POINTER(FD2DDesc)] + [C.POINTER(C.c_float)] * 5 + [C.c_int]
         L.orc_tti2d.argtypes = [C.POINTER(FD2DDesc)] + [C.POINTER(C.c_float)] * 6 + [C.c_int]
         L.orc_set_tilt_trig.argtypes = [C.POINTER(C.c_float)] * 2
+        L.orc_set_angle_cos.argtypes = [C.POINTER(C.c_float)]
+        L.orc_set_angle_thresholds.argtypes = [C.POINTER(C.c_float)]
         L.orc_fd3d.argtypes = [C.POINTER(FD3DDesc)] + [C.POINTER(C.c_float)] * 6
         L.orc_tti3d.argtypes = [C.POINTER(FD3DDesc)] + [C.POINTER(C.c_float)] * 8
         L.orc_rtm3d_tti_shot.argtypes = [C.POINTER(FD3DDesc), C.c_int] + [C.POINTER(C.c_float)] * 8
@@ -118,6 +120,32 @@ class _TiltTrig:
         self.L.orc_set_tilt_trig(None, None)
 
 
+class _AngleTables:
+    """Hand the device's angle-gather weights cosf(ia*pi/180) and bin edges
+    (128 entries each; refgpu.cuda_angle_cos, refgpu.cuda_angle_thresholds)
+    to the oracle for one call (orc_set_angle_cos, orc_set_angle_thresholds);
+    None keeps the host's cosf / acosf."""
+
+    def __init__(self, prec, cos, thr):
+        self.L = lib(prec)
+        self.cos = None if cos is None else c32(cos)
+        self.thr = None if thr is None else c32(thr)
+        for t in (self.cos, self.thr):
+            if t is not None and t.size < 128:
+                raise ValueError("angle tables need 128 entries")
+
+    def __enter__(self):
+        if self.cos is not None:
+            self.L.orc_set_angle_cos(_fp(self.cos))
+        if self.thr is not None:
+            self.L.orc_set_angle_thresholds(_fp(self.thr))
+        return self
+
+    def __exit__(self, *a):
+        self.L.orc_set_angle_cos(None)
+        self.L.orc_set_angle_thresholds(None)
+
+
 def tti2d(v, e, d, theta, *, npd, nt, dx, dz, dt, favg, pfac, fs, zs, ds=0.0, is_=1, sv=0, wtype=1, rec_iz=None,
           snap_every=0, prec=32, trig=None):
     """2D TTI forward modelling (GPU TTI program semantics); theta in degrees.
@@ -163,14 +191,17 @@ def fd3d(v, e, d, *, npd, nt, dx, dy, dz, dt, favg, pfac, fsx, fsy, fsz, dsx=0, 
 
 def rtm3d(v, e, d, *, npd, nt, dx, dy, dz, dt, favg, pfac, fsx, fsy, fsz, dsx=0, dsy=0, dsz=0,
           ns=1, sv=0, wtype=1, mode=0, mute_tt=70, snap_every=0, prec=32, adcig=None, theta=None, phi=None,
-          receivers=None):
+          receivers=None, angle_cos=None, angle_thr=None):
     """3D boundary-saving RTM over shots 0..ns-1 (3D GPU RTM program
     semantics; with snap_every > 0 the stored-snapshot method instead);
     v,e,d shaped (ny, nx, nz).  Returns (mig divided by the illumination,
     illum, last shot's muted record (ny, nx, nt); zeros for snap_every > 0)
     [+ the Poynting angle gathers (ny/dcdp, nx/dcdp, na, nz) divided by the
     illumination, when adcig = (na, da, dcdp)].  theta/phi (degrees): the
-    3D TTI medium (no angle gathers)."""
+    3D TTI medium (no angle gathers).  angle_cos, angle_thr: the device's
+    gather weights cosf(ia*pi/180) and angle-bin edges for da
+    (refgpu.cuda_angle_cos, cuda_angle_thresholds); without them the host's
+    cosf and acosf."""
     v, e, d = c32(v), c32(e), c32(d)
     tti = theta is not None
     if tti:
@@ -204,8 +235,9 @@ def rtm3d(v, e, d, *, npd, nt, dx, dy, dz, dt, favg, pfac, fsx, fsy, fsz, dsx=0,
             lib(prec).orc_rtm3d_snap_shot(C.byref(desc), mute_tt, snap_every, _fp(v), _fp(e), _fp(d), _fp(mig),
                                           _fp(ill))
         else:
-            lib(prec).orc_rtm3d_shot(C.byref(desc), mute_tt, _fp(v), _fp(e), _fp(d), _fp(mig), _fp(ill), _fp(rec),
-                                     na, da, dcdp, _fp(ag))
+            with _AngleTables(prec, angle_cos, angle_thr):
+                lib(prec).orc_rtm3d_shot(C.byref(desc), mute_tt, _fp(v), _fp(e), _fp(d), _fp(mig), _fp(ill),
+                                         _fp(rec), na, da, dcdp, _fp(ag))
     lib(prec).orc_image_illum(mig.size, _fp(mig), _fp(ill))
     if ag is None:
         return mig, ill, rec
@@ -229,9 +261,9 @@ def rtm2d_mpi_shot(v, e, d, *, npd, nt, dx, dz, dt_ms, favg, pfac, fs_sxd, ds_sx
 
 
 def rtm2d_gpu(v, e, d, *, npml, nt, dx, dz, dt, favg, pfac, wtype=1, ns=1, fs=1, ds=0, zs=1, mute_tt=20,
-              nangle=70, dangle=1, obs=None, prec=32):
+              nangle=70, dangle=1, obs=None, prec=32, angle_cos=None, angle_thr=None):
     """The 2D GPU RTM program; returns (mig/ill (nx,nz), ill, adcigs (nx,nangle,nz),
-    muted modelled shots (ns,nx,nt))."""
+    muted modelled shots (ns,nx,nt)).  angle_cos, angle_thr: as for rtm3d."""
     v, e, d = c32(v), c32(e), c32(d)
     nx, nz = v.shape
     mig = np.zeros((nx, nz), _f)
@@ -239,16 +271,18 @@ def rtm2d_gpu(v, e, d, *, npml, nt, dx, dz, dt, favg, pfac, wtype=1, ns=1, fs=1,
     ag = np.zeros((nx, nangle, nz), _f)
     shots = np.zeros((ns, nx, nt), _f)
     ob = c32(obs) if obs is not None else None
-    lib(prec).orc_rtm2d_gpu(nx, nz, npml, nt, dx, dz, dt, favg, pfac, wtype, ns, fs, ds, zs, mute_tt, nangle,
-                            dangle, _fp(v), _fp(e), _fp(d), _fp(ob), _fp(mig), _fp(ill), _fp(ag), _fp(shots))
+    with _AngleTables(prec, angle_cos, angle_thr):
+        lib(prec).orc_rtm2d_gpu(nx, nz, npml, nt, dx, dz, dt, favg, pfac, wtype, ns, fs, ds, zs, mute_tt, nangle,
+                                dangle, _fp(v), _fp(e), _fp(d), _fp(ob), _fp(mig), _fp(ill), _fp(ag), _fp(shots))
     return mig, ill, ag, shots
 
 
 def rtm2d_tti(v, e, d, theta, *, npml, nt, dx, dz, dt, favg, pfac, wtype=1, ns=1, fs=1, ds=0, zs=1, mute_tt=30,
-              nangle=65, dangle=1, dcdp=1, obs=None, prec=32, trig=None):
+              nangle=65, dangle=1, dcdp=1, obs=None, prec=32, trig=None, angle_cos=None,
+              angle_thr=None):
     """The 2D TTI GPU RTM program; theta in degrees.  Returns (mig/ill (nx,nz),
     ill, adcigs (nx//dcdp,nangle,nz), muted modelled shots (ns,nx,nt)).
-    trig: as for tti2d."""
+    trig: as for tti2d; angle_cos, angle_thr: as for rtm3d."""
     v, e, d, theta = c32(v), c32(e), c32(d), c32(theta)
     nx, nz = v.shape
     mig = np.zeros((nx, nz), _f)
@@ -256,7 +290,7 @@ def rtm2d_tti(v, e, d, theta, *, npml, nt, dx, dz, dt, favg, pfac, wtype=1, ns=1
     ag = np.zeros((nx // dcdp, nangle, nz), _f)
     shots = np.zeros((ns, nx, nt), _f)
     ob = c32(obs) if obs is not None else None
-    with _TiltTrig(prec, trig):
+    with _TiltTrig(prec, trig), _AngleTables(prec, angle_cos, angle_thr):
         lib(prec).orc_rtm2d_tti(nx, nz, npml, nt, dx, dz, dt, favg, pfac, wtype, ns, fs, ds, zs, mute_tt, nangle,
                                 dangle, dcdp, _fp(v), _fp(e), _fp(d), _fp(theta), _fp(ob), _fp(mig), _fp(ill),
                                 _fp(ag), _fp(shots))

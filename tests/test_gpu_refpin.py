@@ -1,11 +1,14 @@
-"""The library's drop-ins GPU_vti3dfd and GPU_vti2dfd and its 2D TTI shot
-against the reference's own GPU programs
+"""The library's drop-ins GPU_vti3dfd and GPU_vti2dfd, its 2D TTI shot and
+its three GPU-program RTMs against the reference's own GPU programs
 (2D-3D-vti-fd-cuda-gtk-GUI/GPU_vti3dfd_kernels.cu, GPU_vti2dfd_kernels.cu,
-2D-tti-fd+rtm-cuda/Toa_gpu_2dtti_fd_1orderfunction.cu), whose device code
-was compiled unmodified and run
-on a GPU: the golden records of tests/golden/make_golden_refgpu.py, and, where
-the cubins are present (oracle/_ref), the 400^3 headline shot run through the
-reference program itself.
+2D-tti-fd+rtm-cuda/Toa_gpu_2dtti_fd_1orderfunction.cu,
+2D-vti-fd+rtm-cuda/Toa_gpu2DvtiFdRtmAdcigsLaplace.cu,
+2D-tti-fd+rtm-cuda/Toa_gpu_2dtti_rtm_adcigs_iorderfunciton.cu,
+3D-vti-fd+rtm-cuda/Toa_gpu_3dvti_rtm_adcigs_1orderfunction.cu), whose device
+code was compiled unmodified and run on a GPU: the golden outputs of
+tests/golden/make_golden_refgpu.py, and, where the cubins are present
+(oracle/_ref), the 400^3 headline shot run through the reference program
+itself.
 
 Tolerances: the exact 3D form and the 2D GPU-program form are bit-identical
 to the program built with contraction to FMA off.  The fast 3D form (FMAs at
@@ -106,6 +109,98 @@ def test_tti2d_shot_bit_exact_vs_reference_program(geo, case):
         assert np.array_equal(shot, ref), rel_l2(shot, ref)
         if snaps is not None and is_ == 1:
             assert np.array_equal(snaps, g["snap_%s_nofma" % case])
+
+
+def _rtm_case(name):
+    """The RTM fixture's case `name` as (library kwargs, golden tag)."""
+    kw = dict(M.RTM_VTI)
+    kw["dt"] = np.float32(kw["dt"])
+    if name == "vti_b":
+        kw.update(ns=1, fs=31)
+    return kw, name + "_nofma"
+
+
+@pytest.mark.parametrize("name", ["vti_a", "vti_b"])
+def test_rtm2d_gpu_program_bit_exact_vs_reference_program(geo, orc, name):
+    """geo_rtm2d_gpu against the 2D GPU RTM program's RTM()
+    (Toa_gpu2DvtiFdRtmAdcigsLaplace.cu:1184-1566): muted records, image,
+    illumination and Poynting gathers (both divided by the illumination),
+    with modelled (a) and observed (b, readShot) records.  The program
+    filters its image on the host with its own Laplacian; the library's is
+    compared through the oracle's, which is pinned to laplace.c."""
+    g = _load("golden_rtm2d_gpu.npz")
+    kw, t = _rtm_case(name)
+    obs = g["obs"] if name == "vti_b" else None
+    out = geo.rtm2d_gpu(g["v"], g["e"], g["d"], mute_tt=20, obs=obs, **kw)
+    assert np.abs(g["ag_" + t]).max() > 0
+    assert np.array_equal(out["shots"], g["shots_" + t])
+    assert np.array_equal(out["illum"], g["ill_" + t])
+    assert np.array_equal(out["adcigs"], g["ag_" + t]), rel_l2(out["adcigs"], g["ag_" + t])
+    assert np.array_equal(out["mig_lap"], orc.laplace2d_adj(g["mig_" + t]))
+
+
+@pytest.mark.parametrize("name,dcdp", [("tti_a", 1), ("tti_b", 3)])
+def test_rtm2d_tti_program_bit_exact_vs_reference_program(geo, orc, name, dcdp):
+    """geo_rtm2d_tti against the 2D TTI GPU RTM program
+    (Toa_gpu_2dtti_rtm_adcigs_iorderfunciton.cu:500-800), gathers at every
+    CDP and at every third (64 traces: not a multiple of 3)."""
+    g = _load("golden_rtm2d_gpu.npz")
+    kw = dict(M.RTM_TTI)
+    kw["dt"] = np.float32(kw["dt"])
+    t = name + "_nofma"
+    out = geo.rtm2d_tti(g["tv"], g["te"], g["td"], g["theta"], dcdp=dcdp, mute_tt=30, **kw)
+    assert np.abs(g["ag_" + t]).max() > 0
+    assert np.array_equal(out["shots"], g["shots_tti_a_nofma"])
+    assert np.array_equal(out["illum"], g["ill_" + t])
+    assert np.array_equal(out["adcigs"], g["ag_" + t]), rel_l2(out["adcigs"], g["ag_" + t])
+    assert np.array_equal(out["mig_lap"], orc.laplace2d_adj(g["mig_" + t]))
+
+
+def rtm3d_kwargs(kw):
+    """The library's / oracle's arguments for a 3D RTM program case: the
+    program runs the SV taper on every propagation and mutes with tt = 70."""
+    return dict(npd=kw["npml"], nt=kw["nt"], dx=kw["dx"], dy=kw["dy"], dz=kw["dz"], dt=np.float32(kw["dt"]),
+                favg=kw["favg"], pfac=kw["pfac"], fsx=kw["fsx"], fsy=kw["fsy"], fsz=kw["zs"], dsx=kw["dsx"],
+                dsy=kw["dsy"], ns=kw["ns"], sv=1, mute_tt=70)
+
+
+@pytest.mark.parametrize("case", sorted(M.CASES_RTM3))
+def test_rtm3d_program_bit_exact_vs_reference_program(geo, case):
+    """geo_rtm3d (boundary method, exact form) against the 3D GPU RTM
+    program (Toa_gpu_3dvti_rtm_adcigs_1orderfunction.cu:686-981): image and
+    gathers divided by the illumination, and the illumination; the fast
+    form within the distance between the program's two builds (x1.5)."""
+    g = _load("golden_rtm3d_gpu.npz")
+    kw = M.CASES_RTM3[case]
+    k = rtm3d_kwargs(kw)
+    ad = (kw["na"], kw["da"], kw["dcdp"])
+    t = case + "_nofma"
+    mig, ill, ag = geo.rtm3d(g["v"], g["e"], g["d"], mode="exact", laplace=False, illum=True, adcig=ad, **k)
+    assert np.abs(g["ag_" + t]).max() > 0
+    assert np.array_equal(mig, g["mig_" + t]), rel_l2(mig, g["mig_" + t])
+    assert np.array_equal(ill, g["ill_" + t])
+    assert np.array_equal(ag, g["ag_" + t]), rel_l2(ag, g["ag_" + t])
+    if "mig_%s_fma" % case in g:
+        own = rel_l2(g["mig_%s_fma" % case], g["mig_" + t])
+        fast = geo.rtm3d(g["v"], g["e"], g["d"], mode="fast", laplace=False, **k)
+        assert rel_l2(fast, g["mig_" + t]) <= 1.5 * own and rel_l2(fast, g["mig_%s_fma" % case]) <= 1.5 * own
+
+
+@pytest.mark.parametrize("da", [1, 2, 3])
+def test_poynting_bin_edges_reproduce_device_bins(da):
+    """The GPU RTM programs' angle bin (int)((float)(0.5*acosf(a)*180/pi)/da)
+    with the device's acosf is, for every float a in [-1, 1] (2.1e9 values,
+    on the GPU), the number of the device's bin edges at or above a -- the
+    form the CPU oracle is given and the library's gathers use.  The host's
+    acosf puts a few cosines next to an edge in the neighbouring bin
+    (printed)."""
+    from oracle import refgpu
+    thr = refgpu.cuda_angle_thresholds(da, 128)
+    assert (np.diff(thr[thr > -2]) < 0).all()
+    assert refgpu.bin_check(128, da, thr) == 0
+    host = refgpu.host_bin_thresholds(128, da)
+    print("POYNTING_BINS da=%d: edges differing host/device %d, floats binned differently by the host's acosf %d"
+          % (da, int((host != thr).sum()), refgpu.bin_check(128, da)))
 
 
 def test_headline_shot_against_reference_program(geo):

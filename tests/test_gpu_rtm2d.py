@@ -3,6 +3,7 @@ images, the shot-ordered stack and the Laplacian are bit-exact."""
 import numpy as np
 import pytest
 
+from oracle.refgpu import cuda_angle_tables
 from tests.util import layered_model
 
 pytestmark = pytest.mark.gpu
@@ -114,7 +115,7 @@ def test_rtm2d_gpu_program_bit_exact(geo, orc):
     Poynting gathers): image, illumination, gathers, angle stack and
     records equal the oracle's."""
     v, e, d = model(nx=96, nz=60)
-    mig, ill, ag, shots = orc.rtm2d_gpu(v, e, d, **GKW)
+    mig, ill, ag, shots = orc.rtm2d_gpu(v, e, d, **cuda_angle_tables(GKW["dangle"]), **GKW)
     out = geo.rtm2d_gpu(v, e, d, **GKW)
     assert np.abs(ill).max() > 0 and np.abs(ag).max() > 0
     assert np.array_equal(out["shots"], shots)
@@ -131,7 +132,7 @@ def test_rtm2d_gpu_program_observed_shots(geo, orc):
     v, e, d = model(nx=96, nz=60)
     kw = dict(GKW, ns=1, nt=520)          # nt < 512 rounding: the mute's surplus threads span traces
     obs = np.random.default_rng(5).standard_normal((1, 96, 520)).astype(np.float32) * 1e-3
-    mig, ill, ag, _ = orc.rtm2d_gpu(v, e, d, obs=obs, **kw)
+    mig, ill, ag, _ = orc.rtm2d_gpu(v, e, d, obs=obs, **cuda_angle_tables(kw["dangle"]), **kw)
     out = geo.rtm2d_gpu(v, e, d, obs=obs, **kw)
     assert np.array_equal(out["mig_lap"], orc.laplace2d_adj(mig))
     assert np.array_equal(out["adcigs"], ag)
@@ -144,7 +145,7 @@ def test_rtm2d_gpu_program_thin_sponge_large_grid(geo, orc):
     persistent passes stride over several points."""
     v, e, d = model(nx=700, nz=400)
     kw = dict(GKW, npml=5, ns=1, nt=150, fs=350)
-    mig, ill, ag, shots = orc.rtm2d_gpu(v, e, d, **kw)
+    mig, ill, ag, shots = orc.rtm2d_gpu(v, e, d, **cuda_angle_tables(kw["dangle"]), **kw)
     out = geo.rtm2d_gpu(v, e, d, **kw)
     assert np.abs(ill).max() > 0
     assert np.array_equal(out["shots"], shots)
@@ -158,7 +159,7 @@ def test_rtm2d_gpu_program_independent_of_launch_segments(geo, orc, monkeypatch,
     monkeypatch.setenv("GEO_WATCH_EVERY", every)
     v, e, d = model(nx=80, nz=50)
     kw = dict(GKW, ns=1, nt=130)
-    mig, ill, ag, shots = orc.rtm2d_gpu(v, e, d, **kw)
+    mig, ill, ag, shots = orc.rtm2d_gpu(v, e, d, **cuda_angle_tables(kw["dangle"]), **kw)
     out = geo.rtm2d_gpu(v, e, d, **kw)
     assert np.array_equal(out["shots"], shots)
     assert np.array_equal(out["illum"], ill)

@@ -2,6 +2,7 @@
 import numpy as np
 import pytest
 
+from oracle.refgpu import cuda_angle_tables
 from tests.util import random_model_3d, rel_l2
 
 pytestmark = pytest.mark.gpu
@@ -64,7 +65,7 @@ def test_rtm3d_adcig_bit_exact(geo, orc, mode, adcig):
     """Poynting angle gathers (Poynting_Adcigs + adcigs_illum) bit-exact,
     together with the image and the illumination of the same run."""
     v, e, d = random_model_3d(20, 17, 23, seed=14)
-    mig_o, ill_o, _, ag_o = orc.rtm3d(v, e, d, mode=mode, adcig=adcig, **KW)
+    mig_o, ill_o, _, ag_o = orc.rtm3d(v, e, d, mode=mode, adcig=adcig, **cuda_angle_tables(adcig[1]), **KW)
     mig, ill, ag = geo.rtm3d(v, e, d, mode=mode, laplace=False, illum=True, adcig=adcig, **KW)
     na, _, dcdp = adcig
     assert ag.shape == (17 // dcdp, 20 // dcdp, na, 23)

@@ -4,7 +4,7 @@ device's values (oracle.refgpu.cuda_trig) and restates the rest."""
 import numpy as np
 import pytest
 
-from oracle.refgpu import cuda_trig
+from oracle.refgpu import cuda_angle_tables, cuda_trig
 from tests.util import layered_model, rel_l2
 
 pytestmark = pytest.mark.gpu
@@ -83,7 +83,8 @@ def test_rtm2d_tti_program_bit_exact(geo, orc, dcdp):
     multiple of 3): image, illumination, gathers and records equal the
     oracle's."""
     v, e, d, th = _model(nx=91, nz=60, seed=5)
-    mig, ill, ag, shots = orc.rtm2d_tti(v, e, d, th, dcdp=dcdp, trig=cuda_trig(th), **TKW)
+    mig, ill, ag, shots = orc.rtm2d_tti(v, e, d, th, dcdp=dcdp, trig=cuda_trig(th),
+                                        **cuda_angle_tables(TKW["dangle"]), **TKW)
     out = geo.rtm2d_tti(v, e, d, th, dcdp=dcdp, **TKW)
     assert np.abs(ill).max() > 0 and np.abs(ag).max() > 0
     assert out["adcigs"].shape == (91 // dcdp, 65, 60)
@@ -98,7 +99,7 @@ def test_rtm2d_tti_program_thin_sponge_large_grid(geo, orc):
     band) on a grid larger than one wave of resident threads."""
     v, e, d, th = _model(nx=700, nz=400, seed=8)
     kw = dict(TKW, npml=5, ns=1, nt=150, fs=350)
-    mig, ill, ag, shots = orc.rtm2d_tti(v, e, d, th, trig=cuda_trig(th), **kw)
+    mig, ill, ag, shots = orc.rtm2d_tti(v, e, d, th, trig=cuda_trig(th), **cuda_angle_tables(kw["dangle"]), **kw)
     out = geo.rtm2d_tti(v, e, d, th, **kw)
     assert np.abs(ill).max() > 0
     assert np.array_equal(out["shots"], shots)
@@ -116,7 +117,7 @@ def test_2d_programs_independent_of_launch_segments(geo, orc, monkeypatch, every
     monkeypatch.setenv("GEO_WATCH_EVERY", every)
     v, e, d, th = _model(nx=70, nz=50, seed=9)
     kw = dict(TKW, ns=1, nt=120)
-    mig, ill, ag, shots = orc.rtm2d_tti(v, e, d, th, trig=cuda_trig(th), **kw)
+    mig, ill, ag, shots = orc.rtm2d_tti(v, e, d, th, trig=cuda_trig(th), **cuda_angle_tables(kw["dangle"]), **kw)
     out = geo.rtm2d_tti(v, e, d, th, **kw)
     assert np.array_equal(out["shots"], shots)
     assert np.array_equal(out["mig_lap"], orc.laplace2d_adj(mig))
@@ -131,7 +132,7 @@ def test_rtm2d_tti_program_observed_shots_device(geo, orc):
     v, e, d, th = _model(nx=80, nz=50, seed=6)
     kw = dict(TKW, ns=1, nt=400)
     obs = np.random.default_rng(7).standard_normal((1, 80, 400)).astype(np.float32) * 1e-3
-    mig, ill, ag, _ = orc.rtm2d_tti(v, e, d, th, obs=obs, trig=cuda_trig(th), **kw)
+    mig, ill, ag, _ = orc.rtm2d_tti(v, e, d, th, obs=obs, trig=cuda_trig(th), **cuda_angle_tables(kw["dangle"]), **kw)
     t = [torch.from_numpy(a).cuda() for a in (v, e, d, th, obs)]
     out = geo.rtm2d_tti(*t[:4], obs=t[4], **kw)
     assert out["mig_lap"].is_cuda

@@ -1,10 +1,16 @@
 """The oracle's GPU-program restatements against the reference's own GPU
-programs: golden records made by running GPU_vti3dfd and GPU_vti2dfd
+programs: golden outputs made by running GPU_vti3dfd and GPU_vti2dfd
 (2D-3D-vti-fd-cuda-gtk-GUI/GPU_vti3dfd_kernels.cu:371,
-GPU_vti2dfd_kernels.cu:301) and the 2D TTI forward program
-(2D-tti-fd+rtm-cuda/Toa_gpu_2dtti_fd_1orderfunction.cu:312), their device
-code compiled unmodified, on a GPU (tests/golden/make_golden_refgpu.py).
-CPU only.
+GPU_vti2dfd_kernels.cu:301), the 2D TTI forward program
+(2D-tti-fd+rtm-cuda/Toa_gpu_2dtti_fd_1orderfunction.cu:312) and the three
+GPU RTM programs (2D-vti-fd+rtm-cuda/Toa_gpu2DvtiFdRtmAdcigsLaplace.cu:1184,
+2D-tti-fd+rtm-cuda/Toa_gpu_2dtti_rtm_adcigs_iorderfunciton.cu:500,
+3D-vti-fd+rtm-cuda/Toa_gpu_3dvti_rtm_adcigs_1orderfunction.cu:686), their
+device code compiled unmodified, on a GPU
+(tests/golden/make_golden_refgpu.py).  CPU only.  Where the programs call
+cosf on the device (the TTI tilt, the angle-gather weights) and acosf (the
+angle-gather bins), the fixtures carry the device's values and bin edges,
+and the oracle is given them.
 
 The programs were built twice: with contraction to FMA off ("nofma"), which
 the oracle reproduces bit for bit, and with the compiler's defaults ("fma",
@@ -121,3 +127,75 @@ def test_reference_builds_differ_by_rounding_only():
             a, b = g["shot_%s_fma" % c], g["shot_%s_nofma" % c]
             assert not np.array_equal(a, b)
             assert rel_l2(a, b) < 1e-4
+
+
+def _rtm2d_kw(name):
+    kw = dict(M.RTM_VTI)
+    kw["dt"] = np.float32(kw["dt"])
+    if name == "vti_b":
+        kw.update(ns=1, fs=31)
+    return kw
+
+
+@pytest.mark.parametrize("name", ["vti_a", "vti_b"])
+def test_rtm2d_gpu_oracle_bit_exact_vs_reference_program(orc, name):
+    """orc_rtm2d_gpu against the 2D GPU RTM program's RTM() (ring saving,
+    forward-stepped reconstruction, illumination, Poynting gathers; b reads
+    observed records): image and gathers divided by the illumination, the
+    illumination and the muted records, bit for bit."""
+    g = _load("golden_rtm2d_gpu.npz")
+    t = name + "_nofma"
+    obs = g["obs"] if name == "vti_b" else None
+    mig, ill, ag, shots = orc.rtm2d_gpu(g["v"], g["e"], g["d"], mute_tt=20, obs=obs,
+                                        angle_cos=g["angle_cos_dev"], angle_thr=g["angle_thr_dev"],
+                                        **_rtm2d_kw(name))
+    assert np.abs(ag).max() > 0 and (np.abs(ag).max(axis=(0, 2)) > 0).all()
+    assert np.array_equal(shots, g["shots_" + t])
+    assert np.array_equal(ill, g["ill_" + t])
+    assert np.array_equal(mig, g["mig_" + t])
+    assert np.array_equal(ag, g["ag_" + t]), rel_l2(ag, g["ag_" + t])
+    if "mig_%s_fma" % name in g:
+        assert rel_l2(mig, g["mig_%s_fma" % name]) < 1e-4
+
+
+@pytest.mark.parametrize("name,dcdp", [("tti_a", 1), ("tti_b", 3)])
+def test_rtm2d_tti_oracle_bit_exact_vs_reference_program(orc, name, dcdp):
+    """orc_rtm2d_tti against the 2D TTI GPU RTM program, gathers at every CDP
+    and every third (64 traces: not a multiple of 3)."""
+    g = _load("golden_rtm2d_gpu.npz")
+    kw = dict(M.RTM_TTI)
+    kw["dt"] = np.float32(kw["dt"])
+    t = name + "_nofma"
+    mig, ill, ag, shots = orc.rtm2d_tti(g["tv"], g["te"], g["td"], g["theta"], dcdp=dcdp, mute_tt=30,
+                                        trig=(g["tcos_dev"], g["tsin_dev"]), angle_cos=g["angle_cos_dev"],
+                                        angle_thr=g["angle_thr_dev"], **kw)
+    assert np.abs(ag).max() > 0
+    assert np.array_equal(shots, g["shots_tti_a_nofma"])
+    assert np.array_equal(ill, g["ill_" + t])
+    assert np.array_equal(mig, g["mig_" + t])
+    assert np.array_equal(ag, g["ag_" + t]), rel_l2(ag, g["ag_" + t])
+    if "mig_%s_fma" % name in g:
+        assert rel_l2(mig, g["mig_%s_fma" % name]) < 1e-4
+
+
+@pytest.mark.parametrize("case", sorted(M.CASES_RTM3))
+def test_rtm3d_oracle_bit_exact_vs_reference_program(orc, case):
+    """orc_rtm3d_shot (boundary-saving RTM, exact form, SV taper on every
+    propagation as the program runs it) against the 3D GPU RTM program:
+    image and gathers divided by the illumination, the illumination and the
+    last shot's muted record, bit for bit."""
+    g = _load("golden_rtm3d_gpu.npz")
+    kw = M.CASES_RTM3[case]
+    k = dict(npd=kw["npml"], nt=kw["nt"], dx=kw["dx"], dy=kw["dy"], dz=kw["dz"], dt=np.float32(kw["dt"]),
+             favg=kw["favg"], pfac=kw["pfac"], fsx=kw["fsx"], fsy=kw["fsy"], fsz=kw["zs"], dsx=kw["dsx"],
+             dsy=kw["dsy"], ns=kw["ns"], sv=1, mute_tt=70)
+    t = case + "_nofma"
+    mig, ill, rec, ag = orc.rtm3d(g["v"], g["e"], g["d"], mode=0, adcig=(kw["na"], kw["da"], kw["dcdp"]),
+                                  angle_cos=g["angle_cos_dev"], angle_thr=g["angle_thr_dev"], **k)
+    assert np.abs(ag).max() > 0
+    assert np.array_equal(rec, g["shots_a_nofma"][kw["ns"] - 1])
+    assert np.array_equal(ill, g["ill_" + t])
+    assert np.array_equal(mig, g["mig_" + t])
+    assert np.array_equal(ag, g["ag_" + t]), rel_l2(ag, g["ag_" + t])
+    if "mig_%s_fma" % case in g:
+        assert rel_l2(mig, g["mig_%s_fma" % case]) < 1e-4
