@@ -3,10 +3,12 @@
 // the 2D program's Poynting_Adcigs, 2D-vti-fd+rtm-cuda/Toa_gpu2DvtiFdRtmAdcigsLaplace.cu):
 //   a = (S.G) / (sqrtf(b1*b2) * (1 - 0.1))   -- a double quotient stored as float
 //   if -1 <= a <= 1:  ia = (int)((float)(0.5*acosf(a)*180/pi) / (da*1.0)),  kept if ia < na.
-// The host turns the acosf expression into thresholds: thr[k-1] is the
-// largest float a with bin(a) >= k (non-increasing in k, -2 where no float
-// in [-1,1] reaches bin k), so the bin of a is the number of thresholds at or
-// above a and no acosf runs on the device.
+// The acosf expression becomes thresholds, found once per run on the device
+// with the device's acosf (k_angle_tables): thr[k-1] is the largest float a
+// with bin(a) >= k (non-increasing in k, -2 where no float in [-1,1]
+// reaches bin k), so the bin of a is the number of thresholds at or above a
+// and no acosf runs per point.  The host's acosf would not do: it bins a
+// few dozen of the floats in [-1,1] next to a bin edge differently.
 //
 // The quotient is first formed in float.  Against the exact quotient its
 // relative error is below 2.1e-7 (0.9f against 0.9, one product and one
