@@ -62,6 +62,21 @@ def test_fd2d_source_at_tile_seams(geo, orc, variant):
         assert np.array_equal(out, ref), (fs, zs, rel_l2(out, ref))
 
 
+@pytest.mark.parametrize("tile", ["32x8", "64x12", "128x24", "256x8"])
+def test_fd2d_tile_shapes(geo, orc, monkeypatch, tile):
+    """Tile shapes other than the automatic one (GEO_FD2D_TILE): many small
+    tiles (up to 4 per SM), wide and narrow ones, ragged edges, 400 steps of
+    halo exchange and grid barriers, both forms bit-exact."""
+    monkeypatch.setenv("GEO_FD2D_TILE", tile)
+    v, e, d = layered_model(157, 131, seed=12)
+    kw = dict(KW, fs=77.0, zs=9.0, nt=400)
+    for variant, var in (("cpu", orc.V_CPU), ("gpu", orc.V_GPU)):
+        ref = orc.fd2d(v, e, d, variant=var, **kw)
+        out = geo.fd2d_shot(v, e, d, variant=variant, **kw)
+        assert np.abs(ref).max() > 0
+        assert np.array_equal(out, ref), (tile, variant, rel_l2(out, ref))
+
+
 def test_fd2d_gpu_form_snapshots_while_source_on(geo, orc):
     """Snapshots every 3 steps end a launch every 3 steps while the GPU
     form's point source is still on: each launch reloads the tiles and adds
